@@ -1,0 +1,1191 @@
+// oxg_engine.cu - host side of the GB300 oxDNA force engine and its C ABI
+// (include/oxdna_gb300.h).
+//
+// oxg_context  holds the per-term, per-type-pair parameters (the reference's
+//              param_type PODs, src/EvaluatorPairOxDNA*.h, src/OxDNABondedParams.h)
+//              and their FP32 device block.
+// oxg_system   is the resident-state engine that stands in for the HOOMD runtime:
+//              SoA float4 state in HBM, a cell neighbour list with bond exclusions
+//              and a buffer (HOOMD Cell nlist semantics, oxdna/model/dna1.py:307-309),
+//              one fused force kernel per step and the Langevin / NO_SQUISH
+//              integrator, replayed from a captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/oxdna_gb300.h"
+#include "oxg_kernels.cuh"
+
+using namespace oxg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_err(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define OXG_CUDA(call)                                                                  \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            return set_err(OXG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int dalloc(T** p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) n = 1;
+    OXG_CUDA(cudaMalloc((void**)p, n * sizeof(T)));
+    return OXG_OK;
+}
+template <class T>
+void dfree(T*& p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// f4 set (A, B, T0, TS, TC) -> device form with the cosine support interval, widened
+// by 1e-5 so the zero-factor test stays conservative under FP32 rounding.
+F4 mk_f4(const double* t)
+{
+    F4 f;
+    f.a = (float)t[0];
+    f.b = (float)t[1];
+    f.t0 = (float)t[2];
+    f.ts = (float)t[3];
+    f.tc = (float)t[4];
+    const double lo = t[2] - t[4], hi = t[2] + t[4];
+    f.cmax = lo > 0.0 ? (float)(std::cos(lo) + 1e-5) : 2.f;
+    f.cmin = hi < M_PI ? (float)(std::cos(hi) - 1e-5) : -2.f;
+    f.pad = 0.f;
+    return f;
+}
+void cp3(float* d, const double* s) { d[0] = (float)s[0]; d[1] = (float)s[1]; d[2] = (float)s[2]; }
+void cpn(float* d, const double* s, int n) { for (int k = 0; k < n; ++k) d[k] = (float)s[k]; }
+float sq(double r) { return (float)(r * r); }
+
+DExcVol to_dev(const oxg_excvol_params& s, double rcut)
+{
+    DExcVol d;
+    std::memset(&d, 0, sizeof(d));
+    d.eps = (float)s.eps;
+    cp3(d.base, s.base_site);
+    cp3(d.back, s.back_site);
+    for (int k = 0; k < 4; ++k) {
+        d.sigma2[k] = sq(s.sigma[k]);
+        d.rstar2[k] = sq(s.rstar[k]);
+        d.b[k] = (float)s.b[k];
+        d.rc[k] = (float)s.rc[k];
+        d.rc2[k] = sq(s.rc[k]);
+    }
+    d.rcutsq = sq(rcut);
+    return d;
+}
+DHBond to_dev(const oxg_hbond_params& s, double rcut)
+{
+    DHBond d;
+    std::memset(&d, 0, sizeof(d));
+    d.shift_factor = (float)s.shift_factor;
+    cp3(d.base, s.base_site);
+    cpn(d.f1, s.f1, 8);
+    d.t1 = mk_f4(s.t1);
+    d.t23 = mk_f4(s.t23);
+    d.t4 = mk_f4(s.t4);
+    d.t78 = mk_f4(s.t78);
+    d.rcutsq = sq(rcut);
+    return d;
+}
+DCross to_dev(const oxg_cross_params& s, double rcut)
+{
+    DCross d;
+    std::memset(&d, 0, sizeof(d));
+    cp3(d.base, s.base_site);
+    cpn(d.f2, s.f2, 9);
+    d.t1 = mk_f4(s.t1);
+    d.t23 = mk_f4(s.t23);
+    d.t4 = mk_f4(s.t4);
+    d.t78 = mk_f4(s.t78);
+    d.rcutsq = sq(rcut);
+    d.t4_enabled = s.t4_enabled;
+    return d;
+}
+DHBCross to_dev(const oxg_hbondcross_params& s, double rcut)
+{
+    DHBCross d;
+    std::memset(&d, 0, sizeof(d));
+    cp3(d.base, s.base_site);
+    d.shift_factor = (float)s.shift_factor;
+    cpn(d.f1, s.f1, 8);
+    d.hb_t1 = mk_f4(s.hb_t1);
+    d.hb_t23 = mk_f4(s.hb_t23);
+    d.hb_t4 = mk_f4(s.hb_t4);
+    d.hb_t78 = mk_f4(s.hb_t78);
+    cpn(d.f2, s.f2, 9);
+    d.cs_t1 = mk_f4(s.cs_t1);
+    d.cs_t23 = mk_f4(s.cs_t23);
+    d.cs_t4 = mk_f4(s.cs_t4);
+    d.cs_t78 = mk_f4(s.cs_t78);
+    d.rcutsq = sq(rcut);
+    return d;
+}
+DCoax to_dev(const oxg_coax_params& s, double rcut)
+{
+    DCoax d;
+    std::memset(&d, 0, sizeof(d));
+    cp3(d.stack, s.stack_site);
+    cp3(d.bref, s.stack_back_ref);
+    d.gamma = (float)s.gamma;
+    cpn(d.f2, s.f2, 9);
+    d.t1 = mk_f4(s.t1);
+    d.t4 = mk_f4(s.t4);
+    d.t56 = mk_f4(s.t56);
+    cpn(d.phi3, s.phi3, 4);
+    cpn(d.phi4, s.phi4, 4);
+    d.t1_mode = s.t1_mode;
+    d.phi3_enabled = s.phi3_enabled;
+    d.rna_coax = s.rna_coax;
+    d.t1_sa = (float)s.t1_sa;
+    d.t1_sb = (float)s.t1_sb;
+    d.rcutsq = sq(rcut);
+    return d;
+}
+DDebye to_dev(const oxg_debye_params& s, double rcut)
+{
+    DDebye d;
+    std::memset(&d, 0, sizeof(d));
+    cp3(d.back, s.back_site);
+    d.minus_kappa = (float)s.minus_kappa;
+    d.prefactor = (float)s.prefactor;
+    d.b_smooth = (float)s.b_smooth;
+    d.rc = (float)s.rc;
+    d.rhigh = (float)s.rhigh;
+    d.rcutsq = sq(rcut);
+    return d;
+}
+DBonded to_dev(const oxg_bonded_params& s)
+{
+    DBonded d;
+    std::memset(&d, 0, sizeof(d));
+    d.eps_backbone = s.eps_backbone;
+    d.r0_backbone = s.r0_backbone;
+    d.delta_backbone = s.delta_backbone;
+    d.delta2 = s.delta2;
+    for (int k = 0; k < 3; ++k) d.back_site[k] = s.back_site[k];
+    cp3(d.back, s.back_site);
+    cp3(d.base, s.base_site);
+    d.excl_eps = (float)s.excl_eps;
+    for (int k = 0; k < 3; ++k) {
+        d.bx_sigma2[k] = sq(s.bx_sigma[k]);
+        d.bx_rstar2[k] = sq(s.bx_rstar[k]);
+        d.bx_b[k] = (float)s.bx_b[k];
+        d.bx_rc[k] = (float)s.bx_rc[k];
+    }
+    d.stacking_enabled = s.stacking_enabled;
+    d.rna_stacking = s.rna_stacking;
+    cp3(d.stack, s.stack_site);
+    cp3(d.bref, s.stack_back_ref);
+    d.gamma = (float)s.st_gamma;
+    cpn(d.f1, s.st_f1, 8);
+    d.shift_factor = (float)s.st_f1[8];
+    for (int i = 0; i < kMaxTypes; ++i)
+        for (int j = 0; j < kMaxTypes; ++j) d.st_eps[i][j] = (float)s.st_eps[i][j];
+    d.t4 = mk_f4(s.t4);
+    d.t5 = mk_f4(s.t5);
+    d.tB1 = mk_f4(s.tB1);
+    d.tB2 = mk_f4(s.tB2);
+    cpn(d.p1, s.p1, 4);
+    cp3(d.stack3, s.stack_3_site);
+    cp3(d.stack5, s.stack_5_site);
+    cp3(d.bbv3, s.bbvector_3);
+    cp3(d.bbv5, s.bbvector_5);
+    return d;
+}
+
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+int num_sms()
+{
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+}  // namespace
+
+// ======================================================================== context
+template <class POD>
+struct TermTable {
+    bool any = false;
+    POD p[kMaxPairs];
+    double rcut[kMaxPairs];
+    bool set[kMaxPairs];
+    TermTable()
+    {
+        std::memset(p, 0, sizeof(p));
+        for (int k = 0; k < kMaxPairs; ++k) {
+            rcut[k] = 0.0;
+            set[k] = false;
+        }
+    }
+};
+
+struct oxg_context {
+    int device = 0;
+    int n_types = 0;
+    int n_bond_types = 0;
+    TermTable<oxg_excvol_params> excvol;
+    TermTable<oxg_hbond_params> hbond;
+    TermTable<oxg_cross_params> cross;
+    TermTable<oxg_hbondcross_params> hbx;
+    TermTable<oxg_coax_params> coax;
+    TermTable<oxg_debye_params> debye;
+    std::vector<oxg_bonded_params> bonded;
+    std::vector<bool> bonded_set;
+    std::vector<unsigned char> block;  // host image of the device block
+    unsigned char* d_block = nullptr;
+    int block_bytes = 0;
+    bool dirty = true;
+    uint64_t version = 0;
+    uint32_t* d_status = nullptr;
+    cudaStream_t last_stream = nullptr;
+    int first_error = OXG_OK;
+};
+
+namespace {
+
+template <class POD, class D>
+bool add_term(const oxg_context* c, const TermTable<POD>& tt, int tid, ParamHeader& H,
+              std::vector<unsigned char>& blk, float& rmax2, float& rshort2, bool is_short)
+{
+    if (!tt.any) return true;
+    const int nt = c->n_types;
+    for (int a = 0; a < nt; ++a)
+        for (int b = 0; b < nt; ++b)
+            if (!tt.set[a * kMaxTypes + b]) return false;
+    std::vector<D> d(kMaxPairs);
+    std::memset(d.data(), 0, sizeof(D) * kMaxPairs);
+    for (int a = 0; a < nt; ++a)
+        for (int b = 0; b < nt; ++b) {
+            const int k = a * kMaxTypes + b;
+            d[k] = to_dev(tt.p[k], tt.rcut[k]);
+            rmax2 = std::max(rmax2, sq(tt.rcut[k]));
+            if (is_short) rshort2 = std::max(rshort2, sq(tt.rcut[k]));
+        }
+    bool uniform = true;
+    for (int a = 0; a < nt && uniform; ++a)
+        for (int b = 0; b < nt; ++b)
+            if (std::memcmp(&d[a * kMaxTypes + b], &d[0], sizeof(D)) != 0) {
+                uniform = false;
+                break;
+            }
+    const size_t off = align16(blk.size());
+    const int count = uniform ? 1 : kMaxPairs;
+    blk.resize(off + align16(sizeof(D) * count), 0);
+    std::memcpy(blk.data() + off, d.data(), sizeof(D) * count);
+    H.off[tid] = (int)off;
+    H.stride[tid] = uniform ? 0 : (int)sizeof(D);
+    H.present |= 1u << tid;
+    return true;
+}
+
+int build_block(oxg_context* c)
+{
+    if (!c->dirty) return OXG_OK;
+    ParamHeader H;
+    std::memset(&H, 0, sizeof(H));
+    H.n_types = c->n_types;
+    H.n_bond_types = c->n_bond_types;
+    std::vector<unsigned char> blk(align16(sizeof(ParamHeader)), 0);
+    float rmax2 = 0.f, rshort2 = 0.f;
+    bool ok = add_term<oxg_excvol_params, DExcVol>(c, c->excvol, kExcVol, H, blk, rmax2, rshort2, true) &&
+              add_term<oxg_hbond_params, DHBond>(c, c->hbond, kHBond, H, blk, rmax2, rshort2, true) &&
+              add_term<oxg_cross_params, DCross>(c, c->cross, kCross, H, blk, rmax2, rshort2, true) &&
+              add_term<oxg_hbondcross_params, DHBCross>(c, c->hbx, kHBCross, H, blk, rmax2, rshort2, true) &&
+              add_term<oxg_coax_params, DCoax>(c, c->coax, kCoax, H, blk, rmax2, rshort2, true) &&
+              add_term<oxg_debye_params, DDebye>(c, c->debye, kDebye, H, blk, rmax2, rshort2, false);
+    if (!ok) return set_err(OXG_ERR_NO_PARAMS, "a term has parameters for some but not all type pairs");
+    for (int k = 0; k < kMaxPairs; ++k) {
+        if (c->hbond.any) {
+            H.hb_eps[k] = (float)c->hbond.p[k].eps;
+            H.hb_shift[k] = (float)(c->hbond.p[k].eps * c->hbond.p[k].shift_factor);
+        }
+        if (c->hbx.any) {
+            H.hbx_eps[k] = (float)c->hbx.p[k].eps;
+            H.hbx_shift[k] = (float)(c->hbx.p[k].eps * c->hbx.p[k].shift_factor);
+        }
+    }
+    H.hb_cs_same_site = 0;
+    if (c->hbond.any && c->cross.any) {
+        bool same = true;
+        for (int k = 0; k < kMaxPairs; ++k)
+            for (int d = 0; d < 3; ++d)
+                if (c->hbond.p[k].base_site[d] != c->cross.p[k].base_site[d]) same = false;
+        H.hb_cs_same_site = same ? 1 : 0;
+    }
+    H.rcutsq_max = rmax2;
+    H.rcutsq_short = rshort2;
+    const size_t offb = align16(blk.size());
+    std::vector<DBonded> bd(std::max(1, c->n_bond_types));
+    for (int t = 0; t < c->n_bond_types; ++t)
+        if (c->bonded_set[t]) bd[t] = to_dev(c->bonded[t]);
+        else std::memset(&bd[t], 0, sizeof(DBonded));
+    blk.resize(offb + align16(sizeof(DBonded) * bd.size()), 0);
+    std::memcpy(blk.data() + offb, bd.data(), sizeof(DBonded) * bd.size());
+    H.off_bonded = (int)offb;
+    H.total_bytes = (int)blk.size();
+    std::memcpy(blk.data(), &H, sizeof(H));
+    if (blk.size() > (size_t)kParamBlockMax)
+        return set_err(OXG_ERR_CAPACITY, "parameter block larger than the shared-memory budget");
+    if ((int)blk.size() > c->block_bytes) {
+        dfree(c->d_block);
+        int rc = dalloc(&c->d_block, kParamBlockMax);
+        if (rc) return rc;
+    }
+    OXG_CUDA(cudaMemcpy(c->d_block, blk.data(), blk.size(), cudaMemcpyHostToDevice));
+    c->block = blk;
+    c->block_bytes = (int)blk.size();
+    c->dirty = false;
+    c->version++;
+    return OXG_OK;
+}
+
+const ParamHeader& header(const oxg_context* c) { return *reinterpret_cast<const ParamHeader*>(c->block.data()); }
+
+template <class POD>
+int set_pair(oxg_context* c, TermTable<POD>& tt, int ti, int tj, const POD* p, double rcut)
+{
+    if (!c || !p) return set_err(OXG_ERR_INVALID_ARG, "null context or parameters");
+    if (ti < 0 || tj < 0 || ti >= c->n_types || tj >= c->n_types)
+        return set_err(OXG_ERR_INVALID_ARG, "type index out of range");
+    if (!(rcut >= 0.0)) return set_err(OXG_ERR_INVALID_ARG, "negative r_cut");
+    for (int k : {ti * kMaxTypes + tj, tj * kMaxTypes + ti}) {
+        tt.p[k] = *p;
+        tt.rcut[k] = rcut;
+        tt.set[k] = true;
+    }
+    tt.any = true;
+    c->dirty = true;
+    return OXG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* oxg_version(void) { return "oxdna_gb300 1.0 (sm_103a)"; }
+const char* oxg_last_error(void) { return g_last_error.c_str(); }
+
+const char* oxg_status_string(int s)
+{
+    switch (s) {
+    case OXG_OK: return "ok";
+    case OXG_ERR_INVALID_ARG: return "invalid argument";
+    case OXG_ERR_CUDA: return "CUDA error";
+    case OXG_ERR_NLIST_OVERFLOW: return "neighbour list overflow";
+    case OXG_ERR_BAD_INDEX: return "index out of range";
+    case OXG_ERR_TIMEOUT: return "device wait timed out";
+    case OXG_ERR_NO_PARAMS: return "missing parameters";
+    case OXG_ERR_CAPACITY: return "capacity exceeded";
+    case OXG_ERR_NONFINITE: return "non-finite state";
+    }
+    return "unknown status";
+}
+
+int oxg_create(oxg_context** out, int n_types, int n_bond_types)
+{
+    if (!out) return set_err(OXG_ERR_INVALID_ARG, "null output");
+    *out = nullptr;
+    if (n_types < 1 || n_types > kMaxTypes || n_bond_types < 0 || n_bond_types > kMaxBondTypes)
+        return set_err(OXG_ERR_INVALID_ARG, "n_types must be 1..4 and n_bond_types 0..4");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return set_err(OXG_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    oxg_context* c = new oxg_context();
+    cudaGetDevice(&c->device);
+    c->n_types = n_types;
+    c->n_bond_types = n_bond_types;
+    c->bonded.assign(std::max(1, n_bond_types), oxg_bonded_params());
+    std::memset(c->bonded.data(), 0, sizeof(oxg_bonded_params) * c->bonded.size());
+    c->bonded_set.assign(std::max(1, n_bond_types), false);
+    int rc = dalloc(&c->d_status, 1);
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    cudaMemset(c->d_status, 0, sizeof(uint32_t));
+    *out = c;
+    return OXG_OK;
+}
+
+int oxg_destroy(oxg_context* c)
+{
+    if (!c) return OXG_OK;
+    dfree(c->d_block);
+    dfree(c->d_status);
+    delete c;
+    return OXG_OK;
+}
+
+int oxg_set_excvol_params(oxg_context* c, int ti, int tj, const oxg_excvol_params* p, double r)
+{ return set_pair(c, c->excvol, ti, tj, p, r); }
+int oxg_set_hbond_params(oxg_context* c, int ti, int tj, const oxg_hbond_params* p, double r)
+{ return set_pair(c, c->hbond, ti, tj, p, r); }
+int oxg_set_cross_params(oxg_context* c, int ti, int tj, const oxg_cross_params* p, double r)
+{ return set_pair(c, c->cross, ti, tj, p, r); }
+int oxg_set_hbondcross_params(oxg_context* c, int ti, int tj, const oxg_hbondcross_params* p, double r)
+{ return set_pair(c, c->hbx, ti, tj, p, r); }
+int oxg_set_coax_params(oxg_context* c, int ti, int tj, const oxg_coax_params* p, double r)
+{ return set_pair(c, c->coax, ti, tj, p, r); }
+int oxg_set_debye_params(oxg_context* c, int ti, int tj, const oxg_debye_params* p, double r)
+{ return set_pair(c, c->debye, ti, tj, p, r); }
+
+int oxg_set_bonded_params(oxg_context* c, int bt, const oxg_bonded_params* p)
+{
+    if (!c || !p) return set_err(OXG_ERR_INVALID_ARG, "null context or parameters");
+    if (bt < 0 || bt >= c->n_bond_types) return set_err(OXG_ERR_INVALID_ARG, "invalid bond type");
+    c->bonded[bt] = *p;
+    c->bonded_set[bt] = true;
+    c->dirty = true;
+    return OXG_OK;
+}
+
+static uint32_t present_mask(const oxg_context* c)
+{
+    uint32_t m = 0;
+    if (c->excvol.any) m |= 1u << kExcVol;
+    if (c->hbond.any) m |= 1u << kHBond;
+    if (c->cross.any) m |= 1u << kCross;
+    if (c->hbx.any) m |= 1u << kHBCross;
+    if (c->coax.any) m |= 1u << kCoax;
+    if (c->debye.any) m |= 1u << kDebye;
+    return m;
+}
+
+int oxg_pair_forces(oxg_context* c, uint32_t mask, int N, const double* pos_type,
+                    const double* quat, const double* charge, const float box[3],
+                    const uint32_t* n_neigh, const uint32_t* nlist, const uint64_t* head_list,
+                    float* force, float* torque, float* virial, double* term_energy, void* stream)
+{
+    if (!c || N < 0 || !box) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (mask & ~present_mask(c)) return set_err(OXG_ERR_NO_PARAMS, "a requested term has no parameters");
+    if (N == 0 || mask == 0) return OXG_OK;
+    if (!pos_type || !quat || !n_neigh || !nlist || !head_list || !force || !torque)
+        return set_err(OXG_ERR_INVALID_ARG, "null device array");
+    if (!(box[0] > 0.f && box[1] > 0.f && box[2] > 0.f)) return set_err(OXG_ERR_INVALID_ARG, "bad box");
+    int rc = build_block(c);
+    if (rc) return rc;
+    HoomdPairArgs a;
+    a.params = c->d_block;
+    a.param_bytes = c->block_bytes;
+    a.mask = mask;
+    a.N = N;
+    a.pos = reinterpret_cast<const double4_32a*>(pos_type);
+    a.quat = reinterpret_cast<const double4_32a*>(quat);
+    a.charge = charge;
+    a.n_neigh = n_neigh;
+    a.nlist = nlist;
+    a.head_list = reinterpret_cast<const unsigned long long*>(head_list);
+    a.L = make_double3(box[0], box[1], box[2]);
+    a.force = reinterpret_cast<float4*>(force);
+    a.torque = reinterpret_cast<float4*>(torque);
+    a.virial = virial;
+    a.energy = term_energy;
+    a.status = c->d_status;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int threads = 256;
+    const int blocks = (int)(((long long)N * 32 + threads - 1) / threads);
+    if (term_energy) k_pairs_hoomd<true><<<blocks, threads, c->block_bytes, s>>>(a);
+    else k_pairs_hoomd<false><<<blocks, threads, c->block_bytes, s>>>(a);
+    OXG_CUDA(cudaGetLastError());
+    c->last_stream = s;
+    return OXG_OK;
+}
+
+int oxg_bonded_forces(oxg_context* c, int N, const double* pos_type, const double* quat,
+                      const float box[3], int n_bonds, const int32_t* bonds, float* force,
+                      float* torque, float* virial, double* split_energy, void* stream)
+{
+    if (!c || N < 0 || n_bonds < 0 || !box) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (n_bonds == 0) return OXG_OK;
+    if (!pos_type || !quat || !bonds || !force || !torque)
+        return set_err(OXG_ERR_INVALID_ARG, "null device array");
+    for (int t = 0; t < c->n_bond_types; ++t)
+        if (!c->bonded_set[t]) return set_err(OXG_ERR_NO_PARAMS, "bond type without parameters");
+    int rc = build_block(c);
+    if (rc) return rc;
+    BondDropinArgs a;
+    a.params = c->d_block;
+    a.param_bytes = c->block_bytes;
+    a.N = N;
+    a.n_bonds = n_bonds;
+    a.pos = reinterpret_cast<const double4_32a*>(pos_type);
+    a.quat = reinterpret_cast<const double4_32a*>(quat);
+    a.bonds = bonds;
+    a.L = make_double3(box[0], box[1], box[2]);
+    a.force = reinterpret_cast<float4*>(force);
+    a.torque = reinterpret_cast<float4*>(torque);
+    a.virial = virial;
+    a.energy = split_energy;
+    a.status = c->d_status;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int threads = 256;
+    k_bonds_dropin<<<(n_bonds + threads - 1) / threads, threads, c->block_bytes, s>>>(a);
+    OXG_CUDA(cudaGetLastError());
+    c->last_stream = s;
+    return OXG_OK;
+}
+
+int oxg_context_status(oxg_context* c, int clear)
+{
+    if (!c) return set_err(OXG_ERR_INVALID_ARG, "null context");
+    OXG_CUDA(cudaStreamSynchronize(c->last_stream));
+    uint32_t f = 0;
+    OXG_CUDA(cudaMemcpy(&f, c->d_status, sizeof(f), cudaMemcpyDeviceToHost));
+    if (clear) OXG_CUDA(cudaMemset(c->d_status, 0, sizeof(uint32_t)));
+    if (f & kStBadIndex) return set_err(OXG_ERR_BAD_INDEX, "a neighbour or bond index was out of range");
+    return OXG_OK;
+}
+
+}  // extern "C"
+
+// ========================================================================= system
+struct oxg_system {
+    oxg_context* ctx = nullptr;
+    int N = 0;
+    int n_bonds = 0;
+    float3 L, invL;
+    cudaStream_t stream = nullptr;
+    // resident state
+    float4 *pos = nullptr, *quat = nullptr, *vel = nullptr, *angmom = nullptr;
+    float4 *accel = nullptr, *tnet = nullptr, *pos_ref = nullptr;
+    float4 *force = nullptr, *torque = nullptr;
+    float* charge = nullptr;
+    int4* bonds = nullptr;
+    int4* excl = nullptr;
+    // neighbour list
+    double buffer = 0.4;
+    int3 nc = make_int3(1, 1, 1);
+    int use_cells = 0;
+    int cell_cap = 64;
+    int n_cells = 1;
+    uint32_t* cell_count = nullptr;
+    int* cell_list = nullptr;
+    int2 *pairs_short = nullptr, *pairs_long = nullptr;
+    long long cap_short = 0, cap_long = 0;
+    float rlist2 = 0.f, rshort2 = 0.f;
+    uint32_t nlist_mask = 0xffffffffu;  // term mask the current sizing was made for
+    uint64_t nlist_version = ~0ull;
+    DevStatus* st = nullptr;
+    DevStatus* st_host = nullptr;  // pinned
+    double* energy = nullptr;      // 9 doubles
+    // integrator
+    double dt = 0.003, kT = 0.1, gamma = 1.0, gamma_r = 1.0;
+    uint64_t seed = 1;
+    uint32_t run_mask = 0;
+    int run_bonded = 1;
+    bool integ_set = false;
+    unsigned long long timestep = 0;
+    // checkpoint of the state at the start of a graph chunk
+    float4 *ck_pos = nullptr, *ck_quat = nullptr, *ck_vel = nullptr, *ck_angmom = nullptr;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    uint64_t graph_key = ~0ull;
+    int grid_forces = 0;
+    // stats
+    long long steps_run = 0;
+};
+
+namespace {
+
+int sys_alloc_nlist(oxg_system* s)
+{
+    dfree(s->cell_count);
+    dfree(s->cell_list);
+    dfree(s->pairs_short);
+    dfree(s->pairs_long);
+    int rc;
+    if ((rc = dalloc(&s->cell_count, (size_t)2 * s->n_cells))) return rc;
+    OXG_CUDA(cudaMemset(s->cell_count, 0, sizeof(uint32_t) * 2 * s->n_cells));
+    if ((rc = dalloc(&s->cell_list, (size_t)s->n_cells * s->cell_cap))) return rc;
+    if ((rc = dalloc(&s->pairs_short, (size_t)s->cap_short))) return rc;
+    if ((rc = dalloc(&s->pairs_long, (size_t)s->cap_long))) return rc;
+    return OXG_OK;
+}
+
+// Size the cell grid and pair lists for the current parameters and mask.
+int sys_setup_nlist(oxg_system* s, uint32_t mask, bool bonded_only)
+{
+    int rc = build_block(s->ctx);
+    if (rc) return rc;
+    if (s->nlist_mask == mask && s->nlist_version == s->ctx->version && s->cell_count) return OXG_OK;
+    double rmax = 0.0, rshort = 0.0;
+    // per-term maxima over type pairs
+    auto upd = [&](bool any, const double* rc, bool is_short, int t) {
+        if (!any || !((mask >> t) & 1u)) return;
+        for (int k = 0; k < kMaxPairs; ++k) {
+            rmax = std::max(rmax, rc[k]);
+            if (is_short) rshort = std::max(rshort, rc[k]);
+        }
+    };
+    oxg_context* c = s->ctx;
+    upd(c->excvol.any, c->excvol.rcut, true, kExcVol);
+    upd(c->hbond.any, c->hbond.rcut, true, kHBond);
+    upd(c->cross.any, c->cross.rcut, true, kCross);
+    upd(c->hbx.any, c->hbx.rcut, true, kHBCross);
+    upd(c->coax.any, c->coax.rcut, true, kCoax);
+    upd(c->debye.any, c->debye.rcut, false, kDebye);
+    (void)bonded_only;
+    const double rlist = (rmax > 0.0 ? rmax + s->buffer : 0.0);
+    s->rlist2 = (float)(rlist * rlist);
+    const double rsh = rshort > 0.0 ? rshort + s->buffer : 0.0;
+    s->rshort2 = (float)(rsh * rsh);
+    const double Ls[3] = {s->L.x, s->L.y, s->L.z};
+    int n[3];
+    s->use_cells = rlist > 0.0;
+    for (int d = 0; d < 3; ++d) {
+        n[d] = rlist > 0.0 ? (int)std::floor(Ls[d] / rlist) : 1;
+        if (n[d] < 3) s->use_cells = 0;
+        n[d] = std::max(1, std::min(n[d], 1024));
+    }
+    if (!s->use_cells) n[0] = n[1] = n[2] = 1;
+    s->nc = make_int3(n[0], n[1], n[2]);
+    s->n_cells = n[0] * n[1] * n[2];
+    if (s->cap_short == 0) {
+        s->cap_short = 32LL * s->N + 1024;
+        s->cap_long = 64LL * s->N + 1024;
+    }
+    if ((rc = sys_alloc_nlist(s))) return rc;
+    s->nlist_mask = mask;
+    s->nlist_version = c->version;
+    s->graph_key = ~0ull;  // capacities or sizes changed
+    return OXG_OK;
+}
+
+NlistArgs nlist_args(oxg_system* s)
+{
+    NlistArgs a;
+    a.N = s->N;
+    a.pos = s->pos;
+    a.pos_ref = s->pos_ref;
+    a.excl = s->excl;
+    a.nc = s->nc;
+    a.use_cells = s->use_cells;
+    a.cell_cap = s->cell_cap;
+    a.n_cells = s->n_cells;
+    a.cell_count = s->cell_count;
+    a.cell_list = s->cell_list;
+    a.L = s->L;
+    a.invL = s->invL;
+    a.rlist2 = s->rlist2;
+    a.rshort2 = s->rshort2;
+    a.pairs_short = s->pairs_short;
+    a.pairs_long = s->pairs_long;
+    a.cap_short = (int)std::min<long long>(s->cap_short, 0x7fffffff);
+    a.cap_long = (int)std::min<long long>(s->cap_long, 0x7fffffff);
+    a.st = s->st;
+    return a;
+}
+
+ForceArgs force_args(oxg_system* s, uint32_t mask, int bonded)
+{
+    ForceArgs a;
+    a.params = s->ctx->d_block;
+    a.param_bytes = s->ctx->block_bytes;
+    a.mask = mask;
+    a.bonded = bonded && s->n_bonds > 0;
+    a.N = s->N;
+    a.n_bonds = s->n_bonds;
+    a.pos = s->pos;
+    a.quat = s->quat;
+    a.charge = s->charge;
+    a.bonds = s->bonds;
+    a.pairs_short = s->pairs_short;
+    a.pairs_long = s->pairs_long;
+    a.st = s->st;
+    a.st_rw = s->st;
+    a.L = s->L;
+    a.invL = s->invL;
+    a.force = s->force;
+    a.torque = s->torque;
+    a.energy = s->energy;
+    a.virial = nullptr;
+    return a;
+}
+
+IntegArgs integ_args(oxg_system* s)
+{
+    IntegArgs a;
+    a.N = s->N;
+    a.pos = s->pos;
+    a.quat = s->quat;
+    a.vel = s->vel;
+    a.angmom = s->angmom;
+    a.accel = s->accel;
+    a.tnet = s->tnet;
+    a.pos_ref = s->pos_ref;
+    a.force = s->force;
+    a.torque = s->torque;
+    a.st = s->st;
+    a.L = s->L;
+    a.invL = s->invL;
+    a.dt = (float)s->dt;
+    a.kT = (float)s->kT;
+    a.gamma = (float)s->gamma;
+    a.gamma_r = (float)s->gamma_r;
+    a.half_buf2 = (float)(0.25 * s->buffer * s->buffer);
+    a.inertia = make_float3(1.f, 1.f, 1.f);
+    a.seed_lo = (uint32_t)s->seed;
+    a.seed_hi = (uint32_t)(s->seed >> 32);
+    return a;
+}
+
+int forces_grid(oxg_system* s)
+{
+    if (s->grid_forces == 0) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces<false>, 256, s->ctx->block_bytes);
+        if (per_sm < 1) per_sm = 1;
+        s->grid_forces = num_sms() * per_sm;
+    }
+    return s->grid_forces;
+}
+
+// Launch nlist (if flagged) + forces on s->stream.
+int launch_nlist_forces(oxg_system* s, uint32_t mask, int bonded, bool energy)
+{
+    const NlistArgs na = nlist_args(s);
+    const int threads = 256;
+    const int nb = std::max(1, (std::max(s->N, s->n_cells) + threads - 1) / threads);
+    k_nlist_bin<<<nb, threads, 0, s->stream>>>(na);
+    k_nlist_pairs<<<std::max(1, (s->N + threads - 1) / threads), threads, 0, s->stream>>>(na);
+    const ForceArgs fa = force_args(s, mask, bonded);
+    const int grid = forces_grid(s);
+    if (energy) k_forces<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    else k_forces<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    OXG_CUDA(cudaGetLastError());
+    return OXG_OK;
+}
+
+int set_rebuild(oxg_system* s)
+{
+    const uint32_t one = 1u;
+    OXG_CUDA(cudaMemcpyAsync(&s->st->rebuild, &one, sizeof(one), cudaMemcpyHostToDevice, s->stream));
+    return OXG_OK;
+}
+
+int read_status(oxg_system* s, DevStatus* out)
+{
+    OXG_CUDA(cudaMemcpyAsync(s->st_host, s->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s->stream));
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    *out = *s->st_host;
+    return OXG_OK;
+}
+
+int clear_flags(oxg_system* s)
+{
+    OXG_CUDA(cudaMemsetAsync(&s->st->flags, 0, sizeof(uint32_t), s->stream));
+    return OXG_OK;
+}
+
+// Grow whatever overflowed; returns true if something grew.
+int grow_for(oxg_system* s, const DevStatus& d, bool* grew)
+{
+    *grew = false;
+    if (d.flags & kStCellOverflow) {
+        s->cell_cap = std::max<int>(s->cell_cap * 2, (int)d.max_cell + 16);
+        *grew = true;
+    }
+    if (d.flags & kStPairOverflow) {
+        s->cap_short = std::max<long long>(s->cap_short * 3 / 2, (long long)d.n_short * 5 / 4 + 1024);
+        s->cap_long = std::max<long long>(s->cap_long * 3 / 2, (long long)d.n_long * 5 / 4 + 1024);
+        *grew = true;
+    }
+    if (*grew) {
+        int rc = sys_alloc_nlist(s);
+        if (rc) return rc;
+        s->graph_key = ~0ull;
+    }
+    return OXG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box[3], int n_bonds,
+                      const int32_t* bonds_host)
+{
+    if (!out || !ctx || N <= 0 || n_bonds < 0 || !box || (n_bonds > 0 && !bonds_host))
+        return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (!(box[0] > 0.f && box[1] > 0.f && box[2] > 0.f)) return set_err(OXG_ERR_INVALID_ARG, "bad box");
+    *out = nullptr;
+    // validate bonds and build the exclusion table on the host
+    std::vector<int4> excl(N, make_int4(-1, -1, -1, -1));
+    std::vector<int4> bnd(std::max(1, n_bonds));
+    for (int b = 0; b < n_bonds; ++b) {
+        const int A = bonds_host[3 * b], B = bonds_host[3 * b + 1], t = bonds_host[3 * b + 2];
+        if (A < 0 || B < 0 || A >= N || B >= N || A == B || t < 0 || t >= ctx->n_bond_types)
+            return set_err(OXG_ERR_BAD_INDEX, "bond " + std::to_string(b) + " has an invalid index or type");
+        bnd[b] = make_int4(A, B, t, 0);
+        for (int pass = 0; pass < 2; ++pass) {
+            const int x = pass ? B : A, y = pass ? A : B;
+            int4& e = excl[x];
+            if (e.x < 0) e.x = y;
+            else if (e.y < 0) e.y = y;
+            else if (e.z < 0) e.z = y;
+            else if (e.w < 0) e.w = y;
+            else return set_err(OXG_ERR_CAPACITY, "a particle has more than 4 bonds");
+        }
+    }
+    oxg_system* s = new oxg_system();
+    s->ctx = ctx;
+    s->N = N;
+    s->n_bonds = n_bonds;
+    s->L = make_float3(box[0], box[1], box[2]);
+    s->invL = make_float3(1.f / box[0], 1.f / box[1], 1.f / box[2]);
+    int rc = OXG_OK;
+    auto fail = [&](int code) {
+        oxg_system_destroy(s);
+        return code;
+    };
+    if ((rc = dalloc(&s->pos, N)) || (rc = dalloc(&s->quat, N)) || (rc = dalloc(&s->vel, N)) ||
+        (rc = dalloc(&s->angmom, N)) || (rc = dalloc(&s->accel, N)) || (rc = dalloc(&s->tnet, N)) ||
+        (rc = dalloc(&s->pos_ref, N)) || (rc = dalloc(&s->force, N)) || (rc = dalloc(&s->torque, N)) ||
+        (rc = dalloc(&s->charge, N)) || (rc = dalloc(&s->bonds, std::max(1, n_bonds))) ||
+        (rc = dalloc(&s->excl, N)) || (rc = dalloc(&s->st, 1)) || (rc = dalloc(&s->energy, 9)) ||
+        (rc = dalloc(&s->ck_pos, N)) || (rc = dalloc(&s->ck_quat, N)) || (rc = dalloc(&s->ck_vel, N)) ||
+        (rc = dalloc(&s->ck_angmom, N)))
+        return fail(rc);
+    if (cudaMallocHost((void**)&s->st_host, sizeof(DevStatus)) != cudaSuccess)
+        return fail(set_err(OXG_ERR_CUDA, "cudaMallocHost failed"));
+    cudaMemcpy(s->bonds, bnd.data(), sizeof(int4) * bnd.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(s->excl, excl.data(), sizeof(int4) * N, cudaMemcpyHostToDevice);
+    cudaMemset(s->st, 0, sizeof(DevStatus));
+    cudaMemset(s->energy, 0, 9 * sizeof(double));
+    // defaults: unit mass, identity orientation, zero momenta, unit charge
+    std::vector<float4> v(N, make_float4(0.f, 0.f, 0.f, 1.f));
+    std::vector<float4> q(N, make_float4(1.f, 0.f, 0.f, 0.f));
+    std::vector<float4> z(N, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<float> ch(N, 1.f);
+    cudaMemcpy(s->vel, v.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->quat, q.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->pos, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->angmom, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->accel, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->tnet, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->charge, ch.data(), sizeof(float) * N, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(set_err(OXG_ERR_CUDA, cudaGetErrorString(e)));
+    *out = s;
+    return OXG_OK;
+}
+
+int oxg_system_destroy(oxg_system* s)
+{
+    if (!s) return OXG_OK;
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    dfree(s->pos); dfree(s->quat); dfree(s->vel); dfree(s->angmom); dfree(s->accel);
+    dfree(s->tnet); dfree(s->pos_ref); dfree(s->force); dfree(s->torque); dfree(s->charge);
+    dfree(s->bonds); dfree(s->excl); dfree(s->st); dfree(s->energy);
+    dfree(s->cell_count); dfree(s->cell_list); dfree(s->pairs_short); dfree(s->pairs_long);
+    dfree(s->ck_pos); dfree(s->ck_quat); dfree(s->ck_vel); dfree(s->ck_angmom);
+    if (s->st_host) cudaFreeHost(s->st_host);
+    delete s;
+    return OXG_OK;
+}
+
+int oxg_system_set_stream(oxg_system* s, void* stream)
+{
+    if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    s->stream = (cudaStream_t)stream;
+    s->graph_key = ~0ull;
+    return OXG_OK;
+}
+
+int oxg_system_set_state(oxg_system* s, const float* pos_type, const float* quat, const float* vel,
+                         const float* angmom, const float* charge)
+{
+    if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    const size_t b4 = sizeof(float4) * s->N;
+    if (pos_type) OXG_CUDA(cudaMemcpyAsync(s->pos, pos_type, b4, cudaMemcpyHostToDevice, s->stream));
+    if (quat) OXG_CUDA(cudaMemcpyAsync(s->quat, quat, b4, cudaMemcpyHostToDevice, s->stream));
+    if (vel) OXG_CUDA(cudaMemcpyAsync(s->vel, vel, b4, cudaMemcpyHostToDevice, s->stream));
+    if (angmom) OXG_CUDA(cudaMemcpyAsync(s->angmom, angmom, b4, cudaMemcpyHostToDevice, s->stream));
+    if (charge) OXG_CUDA(cudaMemcpyAsync(s->charge, charge, sizeof(float) * s->N, cudaMemcpyHostToDevice, s->stream));
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    return OXG_OK;
+}
+
+int oxg_system_get_state(oxg_system* s, float* pos_type, float* quat, float* vel, float* angmom)
+{
+    if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    const size_t b4 = sizeof(float4) * s->N;
+    if (pos_type) OXG_CUDA(cudaMemcpyAsync(pos_type, s->pos, b4, cudaMemcpyDeviceToHost, s->stream));
+    if (quat) OXG_CUDA(cudaMemcpyAsync(quat, s->quat, b4, cudaMemcpyDeviceToHost, s->stream));
+    if (vel) OXG_CUDA(cudaMemcpyAsync(vel, s->vel, b4, cudaMemcpyDeviceToHost, s->stream));
+    if (angmom) OXG_CUDA(cudaMemcpyAsync(angmom, s->angmom, b4, cudaMemcpyDeviceToHost, s->stream));
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    return OXG_OK;
+}
+
+int oxg_system_device_state(oxg_system* s, float** pos_type, float** quat, float** vel,
+                            float** angmom, float** charge)
+{
+    if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (pos_type) *pos_type = reinterpret_cast<float*>(s->pos);
+    if (quat) *quat = reinterpret_cast<float*>(s->quat);
+    if (vel) *vel = reinterpret_cast<float*>(s->vel);
+    if (angmom) *angmom = reinterpret_cast<float*>(s->angmom);
+    if (charge) *charge = s->charge;
+    return OXG_OK;
+}
+
+int oxg_system_set_nlist_buffer(oxg_system* s, double buffer)
+{
+    if (!s || !(buffer >= 0.0)) return set_err(OXG_ERR_INVALID_ARG, "bad buffer");
+    s->buffer = buffer;
+    s->nlist_version = ~0ull;
+    return OXG_OK;
+}
+
+static int system_compute_impl(oxg_system* s, uint32_t mask, int bonded)
+{
+    int rc = sys_setup_nlist(s, mask, false);
+    if (rc) return rc;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        OXG_CUDA(cudaMemsetAsync(s->force, 0, sizeof(float4) * s->N, s->stream));
+        OXG_CUDA(cudaMemsetAsync(s->torque, 0, sizeof(float4) * s->N, s->stream));
+        OXG_CUDA(cudaMemsetAsync(s->energy, 0, sizeof(double) * 9, s->stream));
+        if ((rc = clear_flags(s)) || (rc = set_rebuild(s))) return rc;
+        if ((rc = launch_nlist_forces(s, mask, bonded, true))) return rc;
+        DevStatus d;
+        if ((rc = read_status(s, &d))) return rc;
+        bool grew = false;
+        if ((rc = grow_for(s, d, &grew))) return rc;
+        if (!grew) return OXG_OK;
+    }
+    return set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
+}
+
+int oxg_system_compute(oxg_system* s, uint32_t mask, int bonded, float* force, float* torque,
+                       double* pair_energy, double* bonded_energy)
+{
+    if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (mask & ~present_mask(s->ctx)) return set_err(OXG_ERR_NO_PARAMS, "a requested term has no parameters");
+    if (bonded)
+        for (int t = 0; t < s->ctx->n_bond_types; ++t)
+            if (!s->ctx->bonded_set[t]) return set_err(OXG_ERR_NO_PARAMS, "bond type without parameters");
+    int rc = system_compute_impl(s, mask, bonded);
+    if (rc) return rc;
+    const size_t b4 = sizeof(float4) * s->N;
+    if (force) OXG_CUDA(cudaMemcpyAsync(force, s->force, b4, cudaMemcpyDeviceToHost, s->stream));
+    if (torque) OXG_CUDA(cudaMemcpyAsync(torque, s->torque, b4, cudaMemcpyDeviceToHost, s->stream));
+    double e[9];
+    OXG_CUDA(cudaMemcpyAsync(e, s->energy, sizeof(e), cudaMemcpyDeviceToHost, s->stream));
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    if (pair_energy) std::memcpy(pair_energy, e, sizeof(double) * kNTerms);
+    if (bonded_energy) std::memcpy(bonded_energy, e + kNTerms, sizeof(double) * 3);
+    return OXG_OK;
+}
+
+int oxg_system_set_integrator(oxg_system* s, double dt, double kT, double gamma, double gamma_r,
+                              uint64_t seed, uint32_t mask, int bonded)
+{
+    if (!s || !(dt > 0.0) || !(kT >= 0.0) || !(gamma >= 0.0) || !(gamma_r >= 0.0))
+        return set_err(OXG_ERR_INVALID_ARG, "bad integrator parameters");
+    if (mask & ~present_mask(s->ctx)) return set_err(OXG_ERR_NO_PARAMS, "a requested term has no parameters");
+    s->dt = dt;
+    s->kT = kT;
+    s->gamma = gamma;
+    s->gamma_r = gamma_r;
+    s->seed = seed;
+    s->run_mask = mask;
+    s->run_bonded = bonded;
+    s->integ_set = true;
+    s->graph_key = ~0ull;
+    return OXG_OK;
+}
+
+// One MD step as kernel launches on s->stream.
+static int enqueue_step(oxg_system* s)
+{
+    const IntegArgs ia = integ_args(s);
+    const int threads = 256;
+    const int nb = (s->N + threads - 1) / threads;
+    k_step_one<<<nb, threads, 0, s->stream>>>(ia);
+    int rc = launch_nlist_forces(s, s->run_mask, s->run_bonded, false);
+    if (rc) return rc;
+    k_step_two<<<nb, threads, 0, s->stream>>>(ia);
+    OXG_CUDA(cudaGetLastError());
+    return OXG_OK;
+}
+
+static int build_graph(oxg_system* s, int steps)
+{
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    cudaStream_t cap = s->stream;
+    bool own = false;
+    if (cap == nullptr) {  // the legacy stream cannot be captured
+        OXG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        own = true;
+    }
+    forces_grid(s);  // occupancy query outside the capture
+    cudaStream_t saved = s->stream;
+    s->stream = cap;
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        s->stream = saved;
+        if (own) cudaStreamDestroy(cap);
+        return set_err(OXG_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
+    }
+    int rc = OXG_OK;
+    for (int k = 0; k < steps && rc == OXG_OK; ++k) rc = enqueue_step(s);
+    e = cudaStreamEndCapture(cap, &g);
+    s->stream = saved;
+    if (own) cudaStreamDestroy(cap);
+    if (rc) return rc;
+    if (e != cudaSuccess) return set_err(OXG_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return set_err(OXG_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+    s->graph_steps = steps;
+    return OXG_OK;
+}
+
+static int checkpoint(oxg_system* s, bool restore)
+{
+    const size_t b4 = sizeof(float4) * s->N;
+    float4* src[4] = {s->pos, s->quat, s->vel, s->angmom};
+    float4* dst[4] = {s->ck_pos, s->ck_quat, s->ck_vel, s->ck_angmom};
+    for (int k = 0; k < 4; ++k) {
+        if (restore) OXG_CUDA(cudaMemcpyAsync(src[k], dst[k], b4, cudaMemcpyDeviceToDevice, s->stream));
+        else OXG_CUDA(cudaMemcpyAsync(dst[k], src[k], b4, cudaMemcpyDeviceToDevice, s->stream));
+    }
+    return OXG_OK;
+}
+
+// prepRun: fresh neighbour list, forces, a = F/m (HOOMD computes the net force at
+// the start of every run() call).
+static int prep_run(oxg_system* s)
+{
+    int rc;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        OXG_CUDA(cudaMemsetAsync(s->force, 0, sizeof(float4) * s->N, s->stream));
+        OXG_CUDA(cudaMemsetAsync(s->torque, 0, sizeof(float4) * s->N, s->stream));
+        if ((rc = clear_flags(s)) || (rc = set_rebuild(s))) return rc;
+        if ((rc = launch_nlist_forces(s, s->run_mask, s->run_bonded, false))) return rc;
+        DevStatus d;
+        if ((rc = read_status(s, &d))) return rc;
+        bool grew = false;
+        if ((rc = grow_for(s, d, &grew))) return rc;
+        if (!grew) break;
+        if (attempt == 7) return set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
+    }
+    const IntegArgs ia = integ_args(s);
+    k_prep_accel<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
+    OXG_CUDA(cudaGetLastError());
+    return OXG_OK;
+}
+
+int oxg_system_run(oxg_system* s, long nsteps)
+{
+    if (!s || nsteps < 0) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (!s->integ_set) return set_err(OXG_ERR_INVALID_ARG, "integrator not set");
+    for (int t = 0; t < s->ctx->n_bond_types && s->run_bonded; ++t)
+        if (!s->ctx->bonded_set[t]) return set_err(OXG_ERR_NO_PARAMS, "bond type without parameters");
+    int rc = sys_setup_nlist(s, s->run_mask, false);
+    if (rc) return rc;
+    // the RNG counter continues from the system's timestep
+    OXG_CUDA(cudaMemcpyAsync(&s->st->step, &s->timestep, sizeof(unsigned long long),
+                             cudaMemcpyHostToDevice, s->stream));
+    if ((rc = prep_run(s))) return rc;
+    if (nsteps == 0) {
+        OXG_CUDA(cudaStreamSynchronize(s->stream));
+        return OXG_OK;
+    }
+    const int chunk = (int)std::min<long>(nsteps, 100);
+    long done = 0;
+    int retries = 0;
+    while (done < nsteps) {
+        const int todo = (int)std::min<long>(chunk, nsteps - done);
+        const uint64_t key = ((uint64_t)todo << 32) ^ s->ctx->version ^ ((uint64_t)(uintptr_t)s->stream << 8);
+        if (todo == chunk) {
+            if (s->graph_key != key || !s->graph) {
+                if ((rc = build_graph(s, todo))) return rc;
+                s->graph_key = key;
+            }
+        }
+        if ((rc = checkpoint(s, false))) return rc;
+        DevStatus before;
+        if ((rc = read_status(s, &before))) return rc;
+        if (todo == chunk) {
+            OXG_CUDA(cudaGraphLaunch(s->graph, s->stream));
+        } else {
+            for (int k = 0; k < todo && rc == OXG_OK; ++k) rc = enqueue_step(s);
+            if (rc) return rc;
+        }
+        DevStatus d;
+        if ((rc = read_status(s, &d))) return rc;
+        if (d.flags & kStNonFinite) return set_err(OXG_ERR_NONFINITE, "non-finite positions or orientations");
+        if (d.flags & (kStCellOverflow | kStPairOverflow)) {
+            if (++retries > 8) return set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
+            bool grew = false;
+            if ((rc = grow_for(s, d, &grew))) return rc;
+            if ((rc = checkpoint(s, true))) return rc;
+            // restore the RNG counter and redo this chunk with a fresh prepRun
+            OXG_CUDA(cudaMemcpyAsync(&s->st->step, &before.step, sizeof(unsigned long long),
+                                     cudaMemcpyHostToDevice, s->stream));
+            if ((rc = prep_run(s))) return rc;
+            s->graph_key = ~0ull;
+            continue;
+        }
+        done += todo;
+        s->timestep = d.step;
+        s->steps_run += todo;
+    }
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    return OXG_OK;
+}
+
+int oxg_system_energies(oxg_system* s, double* pair_energy, double* bonded_energy)
+{
+    if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    uint32_t mask = s->integ_set ? s->run_mask : present_mask(s->ctx);
+    int bonded = s->integ_set ? s->run_bonded : 1;
+    return oxg_system_compute(s, mask, bonded, nullptr, nullptr, pair_energy, bonded_energy);
+}
+
+int oxg_system_stats(oxg_system* s, int64_t* out, int n)
+{
+    if (!s || !out) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    DevStatus d;
+    int rc = read_status(s, &d);
+    if (rc) return rc;
+    const int64_t v[5] = {s->steps_run, (int64_t)d.builds, (int64_t)d.n_short, (int64_t)d.n_long, 5};
+    for (int k = 0; k < n && k < 5; ++k) out[k] = v[k];
+    return OXG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,791 @@
+// oxg_kernels.cuh - sm_103a kernels of the oxDNA force engine.
+//
+//  k_forces          one launch per step for every force: a grid-stride loop over
+//                    [short-range pairs | bonds | long-range (Debye-only) pairs],
+//                    parameters staged in shared memory, float4 vector atomics
+//                    (red.global.add.v4.f32) for both ends, FP64 per-term energies
+//                    reduced by warp shuffles and one atomic per warp.
+//  k_pairs_hoomd     the evaluator-level drop-in over a HOOMD full neighbour list:
+//                    one warp per particle, lanes over neighbours, warp-shuffle
+//                    force/torque reductions (no atomics), FP64 energies.
+//  k_bonds_dropin    the bonded drop-in: one thread per bond, FENE in FP64.
+//  k_nlist_bin / k_nlist_pairs   cell list + half pair lists split by range.
+//  k_step_one / k_step_two       Langevin + NO_SQUISH (Miller et al. 2002).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "oxg_device.cuh"
+#include "oxg_params.h"
+
+namespace oxg {
+
+// device status bits (OR-ed into Status::flags)
+enum : uint32_t {
+    kStCellOverflow = 1u,
+    kStPairOverflow = 2u,
+    kStBadIndex = 4u,
+    kStNonFinite = 8u,
+};
+
+// device-resident bookkeeping of one system
+struct DevStatus {
+    uint32_t flags;        // kSt* bits
+    uint32_t rebuild;      // neighbour list must be rebuilt this step
+    uint32_t gen;          // neighbour list generation (parity selects the cell buffer)
+    uint32_t n_short;      // short-range pair count
+    uint32_t n_long;       // long-range pair count
+    uint32_t builds;       // neighbour list builds so far
+    uint32_t max_cell;     // largest cell occupancy seen
+    uint32_t pad;
+    unsigned long long step;  // current timestep (RNG counter)
+};
+
+// ------------------------------------------------------------ parameter view
+struct ParamView {
+    const unsigned char* b;
+    __device__ __forceinline__ const ParamHeader& h() const { return *reinterpret_cast<const ParamHeader*>(b); }
+    template <class T>
+    __device__ __forceinline__ const T& term(int t, int pidx) const
+    {
+        const ParamHeader& H = h();
+        return *reinterpret_cast<const T*>(b + H.off[t] + pidx * H.stride[t]);
+    }
+    __device__ __forceinline__ const DBonded& bonded(int bt) const
+    {
+        return reinterpret_cast<const DBonded*>(b + h().off_bonded)[bt];
+    }
+};
+
+// Copy the parameter block into dynamic shared memory (16-byte vectors).
+__device__ __forceinline__ ParamView stage_params(const unsigned char* g, int bytes)
+{
+    extern __shared__ float4 smem_params[];
+    const float4* src = reinterpret_cast<const float4*>(g);
+    for (int k = threadIdx.x; k < bytes / 16; k += blockDim.x) smem_params[k] = src[k];
+    __syncthreads();
+    ParamView v;
+    v.b = reinterpret_cast<const unsigned char*>(smem_params);
+    return v;
+}
+
+// ------------------------------------------------------------ pair evaluation
+// All selected nonbonded terms for one pair. dr = r_i - r_j (minimum image), E[t]
+// receives each term's pair energy. Returns true if anything was non-zero.
+__device__ __forceinline__ bool eval_pair(const ParamView& P, uint32_t mask, int pidx,
+                                          float3 dr, float rsq, float4 qi, float4 qj,
+                                          float ci, float cj, PairAcc& acc, float* E)
+{
+    const ParamHeader& H = P.h();
+    if (!(rsq < H.rcutsq_max)) return false;
+    const Frame fi = quat_frame(qi), fj = quat_frame(qj);
+    const float3 rc = -dr;
+    bool any = false;
+    if (mask & (1u << kExcVol)) {
+        const DExcVol& p = P.term<DExcVol>(kExcVol, pidx);
+        if (rsq < p.rcutsq) {
+            const float e = excvol_term(p, rc, fi, fj, acc);
+            E[kExcVol] += e;
+            any = true;
+        }
+    }
+    if (mask & ((1u << kHBond) | (1u << kCross))) {
+        const bool use_hb = (mask >> kHBond) & 1u, use_cs = (mask >> kCross) & 1u;
+        const DHBond* ph = use_hb ? &P.term<DHBond>(kHBond, pidx) : nullptr;
+        const DCross* pc = use_cs ? &P.term<DCross>(kCross, pidx) : nullptr;
+        const bool in_hb = use_hb && rsq < ph->rcutsq;
+        const bool in_cs = use_cs && rsq < pc->rcutsq;
+        BBGeom g;
+        bool gv = false;
+        if (in_hb) {
+            gv = bb_geometry(rc, fi, fj, ph->base, g);
+            if (gv) {
+                RadialF1 R{ph->f1, H.hb_eps[pidx], H.hb_shift[pidx]};
+                E[kHBond] += bb_term<false>(g, fi, fj, ph->t1, ph->t23, ph->t4, ph->t78, true, R, acc);
+            }
+            any = true;
+        }
+        if (in_cs) {
+            if (!in_hb || !H.hb_cs_same_site) gv = bb_geometry(rc, fi, fj, pc->base, g);
+            if (gv) {
+                RadialF2 R{pc->f2};
+                E[kCross] += bb_term<true>(g, fi, fj, pc->t1, pc->t23, pc->t4, pc->t78,
+                                           pc->t4_enabled != 0, R, acc);
+            }
+            any = true;
+        }
+    }
+    if (mask & (1u << kHBCross)) {
+        const DHBCross& p = P.term<DHBCross>(kHBCross, pidx);
+        if (rsq < p.rcutsq) {
+            BBGeom g;
+            if (bb_geometry(rc, fi, fj, p.base, g)) {
+                RadialF1 R1{p.f1, H.hbx_eps[pidx], H.hbx_shift[pidx]};
+                float e = bb_term<false>(g, fi, fj, p.hb_t1, p.hb_t23, p.hb_t4, p.hb_t78, true, R1, acc);
+                RadialF2 R2{p.f2};
+                e += bb_term<true>(g, fi, fj, p.cs_t1, p.cs_t23, p.cs_t4, p.cs_t78, true, R2, acc);
+                E[kHBCross] += e;
+            }
+            any = true;
+        }
+    }
+    if (mask & (1u << kCoax)) {
+        const DCoax& p = P.term<DCoax>(kCoax, pidx);
+        if (rsq < p.rcutsq) {
+            E[kCoax] += coax_term(p, rc, fi, fj, acc);
+            any = true;
+        }
+    }
+    if (mask & (1u << kDebye)) {
+        const DDebye& p = P.term<DDebye>(kDebye, pidx);
+        if (rsq < p.rcutsq) {
+            E[kDebye] += debye_term(p, rc, fi, fj, ci, cj, acc);
+            any = true;
+        }
+    }
+    return any;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float3 min_image(float3 d, float3 L, float3 invL)
+{
+    d.x -= L.x * rintf(d.x * invL.x);
+    d.y -= L.y * rintf(d.y * invL.y);
+    d.z -= L.z * rintf(d.z * invL.z);
+    return d;
+}
+
+__device__ __forceinline__ int type_of(float4 p) { return __float_as_int(p.w); }
+
+// ----------------------------------------------------------- engine force kernel
+struct ForceArgs {
+    const unsigned char* params;
+    int param_bytes;
+    uint32_t mask;        // nonbonded terms
+    int bonded;           // evaluate bonds
+    int N;
+    int n_bonds;
+    const float4* pos;    // x, y, z, type bits
+    const float4* quat;
+    const float* charge;
+    const int4* bonds;    // A, B, type, unused
+    const int2* pairs_short;
+    const int2* pairs_long;
+    const DevStatus* st;  // n_short / n_long
+    DevStatus* st_rw;     // rebuild flag cleared here
+    float3 L, invL;
+    float4* force;        // accumulated (pre-zeroed)
+    float4* torque;
+    double* energy;       // [6 pair terms][3 bonded] (ENERGY only)
+    float* virial;        // unused by the engine
+};
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(256) k_forces(ForceArgs a)
+{
+    const ParamView P = stage_params(a.params, a.param_bytes);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && a.st_rw->rebuild) {
+        a.st_rw->rebuild = 0u;
+        a.st_rw->gen += 1u;
+    }
+    const int n_short = (int)a.st->n_short;
+    const int n_long = (int)a.st->n_long;
+    const int n_bonds = a.bonded ? a.n_bonds : 0;
+    const int total = n_short + n_bonds + n_long;
+    double eacc[kNTerms + 3];
+#pragma unroll
+    for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
+    const uint32_t long_mask = a.mask & (1u << kDebye);
+
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
+        if (w < n_short || w >= n_short + n_bonds) {
+            const bool is_short = w < n_short;
+            const int2 pr = is_short ? a.pairs_short[w] : a.pairs_long[w - n_short - n_bonds];
+            const int i = pr.x, j = pr.y;
+            const float4 pi = a.pos[i], pj = a.pos[j];
+            const float3 dr = min_image(mk3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z), a.L, a.invL);
+            const float rsq = dot(dr, dr);
+            const int pidx = type_of(pi) * kMaxTypes + type_of(pj);
+            PairAcc acc;
+            acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+            float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
+            const bool any = eval_pair(P, is_short ? a.mask : long_mask, pidx, dr, rsq, a.quat[i],
+                                       a.quat[j], ci, cj, acc, E);
+            if (any) {
+                float eh = 0.f;
+                if (ENERGY) {
+#pragma unroll
+                    for (int t = 0; t < kNTerms; ++t) {
+                        eacc[t] += (double)E[t];
+                        eh += E[t];
+                    }
+                    eh *= 0.5f;
+                }
+                atomicAdd(a.force + i, make_float4(acc.fi.x, acc.fi.y, acc.fi.z, eh));
+                atomicAdd(a.force + j, make_float4(-acc.fi.x, -acc.fi.y, -acc.fi.z, eh));
+                atomicAdd(a.torque + i, make_float4(acc.ti.x, acc.ti.y, acc.ti.z, 0.f));
+                atomicAdd(a.torque + j, make_float4(acc.tj.x, acc.tj.y, acc.tj.z, 0.f));
+            }
+        } else {
+            const int4 bd = a.bonds[w - n_short];
+            const int A = bd.x, B = bd.y;
+            const float4 pA = a.pos[A], pB = a.pos[B];
+            const float3 Rcf = min_image(mk3(pB.x - pA.x, pB.y - pA.y, pB.z - pA.z), a.L, a.invL);
+            const float4 qA = a.quat[A], qB = a.quat[B];
+            BondAcc acc;
+            bonded_pair(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
+                        make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
+                        type_of(pA), type_of(pB), acc);
+            float eh = 0.f;
+            if (ENERGY) {
+                eacc[kNTerms + 0] += acc.e[0];
+                eacc[kNTerms + 1] += acc.e[1];
+                eacc[kNTerms + 2] += acc.e[2];
+                eh = (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2]));
+            }
+            atomicAdd(a.force + A, make_float4(-acc.fB.x, -acc.fB.y, -acc.fB.z, eh));
+            atomicAdd(a.force + B, make_float4(acc.fB.x, acc.fB.y, acc.fB.z, eh));
+            atomicAdd(a.torque + A, make_float4(acc.tA.x, acc.tA.y, acc.tA.z, 0.f));
+            atomicAdd(a.torque + B, make_float4(acc.tB.x, acc.tB.y, acc.tB.z, 0.f));
+        }
+    }
+    if (ENERGY) {
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int t = 0; t < kNTerms + 3; ++t) {
+            const double s = warp_sum(eacc[t]);
+            if (lane == 0 && s != 0.0) atomicAdd(a.energy + t, s);
+        }
+    }
+}
+
+// --------------------------------------------------- drop-in: HOOMD full nlist
+struct HoomdPairArgs {
+    const unsigned char* params;
+    int param_bytes;
+    uint32_t mask;
+    int N;
+    const double4_32a* pos;
+    const double4_32a* quat;
+    const double* charge;
+    const uint32_t* n_neigh;
+    const uint32_t* nlist;
+    const unsigned long long* head_list;
+    double3 L;
+    float4* force;
+    float4* torque;
+    float* virial;  // 6 * N, component-major pitch N (may be null)
+    double* energy; // kNTerms (may be null)
+    uint32_t* status;
+};
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(256) k_pairs_hoomd(HoomdPairArgs a)
+{
+    const ParamView P = stage_params(a.params, a.param_bytes);
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= a.N) return;  // whole warp exits together
+    const double4_32a pi = a.pos[i];
+    const double4_32a qid = a.quat[i];
+    const float4 qi = make_float4((float)qid.x, (float)qid.y, (float)qid.z, (float)qid.w);
+    const int ti = (int)(__double_as_longlong(pi.w) & 0xffffffffLL);
+    const float ci = a.charge ? (float)a.charge[i] : 1.f;
+    const int nn = (int)a.n_neigh[i];
+    const unsigned long long head = a.head_list[i];
+    float3 f = mk3(0.f, 0.f, 0.f), tq = mk3(0.f, 0.f, 0.f);
+    float e_half = 0.f;
+    float vir[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double eacc[kNTerms] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    bool bad = false;
+    for (int k = lane; k < nn; k += 32) {
+        const uint32_t j = a.nlist[head + k];
+        if (j >= (uint32_t)a.N) {
+            bad = true;
+            continue;
+        }
+        const double4_32a pj = a.pos[j];
+        double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        dx -= a.L.x * rint(dx / a.L.x);
+        dy -= a.L.y * rint(dy / a.L.y);
+        dz -= a.L.z * rint(dz / a.L.z);
+        const float3 dr = mk3((float)dx, (float)dy, (float)dz);
+        const float rsq = dot(dr, dr);
+        const double4_32a qjd = a.quat[j];
+        const float4 qj = make_float4((float)qjd.x, (float)qjd.y, (float)qjd.z, (float)qjd.w);
+        const int tj = (int)(__double_as_longlong(pj.w) & 0xffffffffLL);
+        const float cj = a.charge ? (float)a.charge[j] : 1.f;
+        PairAcc acc;
+        acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+        float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (!eval_pair(P, a.mask, ti * kMaxTypes + tj, dr, rsq, qi, qj, ci, cj, acc, E)) continue;
+        f += acc.fi;
+        tq += acc.ti;
+        if (ENERGY) {
+#pragma unroll
+            for (int t = 0; t < kNTerms; ++t) {
+                eacc[t] += 0.5 * (double)E[t];
+                e_half += 0.5f * E[t];
+            }
+        }
+        if (a.virial) {  // HOOMD pair virial: 0.5 * dr (x) F_i
+            vir[0] += 0.5f * dr.x * acc.fi.x;
+            vir[1] += 0.5f * dr.x * acc.fi.y;
+            vir[2] += 0.5f * dr.x * acc.fi.z;
+            vir[3] += 0.5f * dr.y * acc.fi.y;
+            vir[4] += 0.5f * dr.y * acc.fi.z;
+            vir[5] += 0.5f * dr.z * acc.fi.z;
+        }
+    }
+    f.x = warp_sum(f.x);
+    f.y = warp_sum(f.y);
+    f.z = warp_sum(f.z);
+    tq.x = warp_sum(tq.x);
+    tq.y = warp_sum(tq.y);
+    tq.z = warp_sum(tq.z);
+    if (ENERGY) e_half = warp_sum(e_half);
+    if (a.virial)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) vir[c] = warp_sum(vir[c]);
+    if (lane == 0) {
+        float4 F = a.force[i];
+        F.x += f.x;
+        F.y += f.y;
+        F.z += f.z;
+        F.w += e_half;
+        a.force[i] = F;
+        float4 T = a.torque[i];
+        T.x += tq.x;
+        T.y += tq.y;
+        T.z += tq.z;
+        a.torque[i] = T;
+        if (a.virial)
+            for (int c = 0; c < 6; ++c) a.virial[(size_t)c * a.N + i] += vir[c];
+    }
+    if (ENERGY && a.energy) {
+#pragma unroll
+        for (int t = 0; t < kNTerms; ++t) {
+            const double s = warp_sum(eacc[t]);
+            if (lane == 0 && s != 0.0) atomicAdd(a.energy + t, s);
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(a.status, kStBadIndex);
+}
+
+// ------------------------------------------------------------- drop-in: bonds
+struct BondDropinArgs {
+    const unsigned char* params;
+    int param_bytes;
+    int N, n_bonds;
+    const double4_32a* pos;
+    const double4_32a* quat;
+    const int* bonds;  // 3 per bond
+    double3 L;
+    float4* force;
+    float4* torque;
+    float* virial;
+    double* energy;    // 3 (fene, bexc, stack), may be null
+    uint32_t* status;
+};
+
+__global__ void __launch_bounds__(256) k_bonds_dropin(BondDropinArgs a)
+{
+    const ParamView P = stage_params(a.params, a.param_bytes);
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+    bool bad = false;
+    if (b < a.n_bonds) {
+        const int A = a.bonds[3 * b], B = a.bonds[3 * b + 1], bt = a.bonds[3 * b + 2];
+        const int nbt = P.h().n_bond_types;
+        if (A < 0 || B < 0 || A >= a.N || B >= a.N || bt < 0 || bt >= nbt) {
+            bad = true;
+        } else {
+            const double4_32a pA = a.pos[A], pB = a.pos[B];
+            double dx = pB.x - pA.x, dy = pB.y - pA.y, dz = pB.z - pA.z;
+            dx -= a.L.x * rint(dx / a.L.x);
+            dy -= a.L.y * rint(dy / a.L.y);
+            dz -= a.L.z * rint(dz / a.L.z);
+            const int tA = (int)(__double_as_longlong(pA.w) & 0xffffffffLL);
+            const int tB = (int)(__double_as_longlong(pB.w) & 0xffffffffLL);
+            BondAcc acc;
+            bonded_pair(P.bonded(bt), make_double3(dx, dy, dz), a.quat[A], a.quat[B], tA, tB, acc);
+            const float eh = (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2]));
+            atomicAdd(a.force + A, make_float4(-acc.fB.x, -acc.fB.y, -acc.fB.z, eh));
+            atomicAdd(a.force + B, make_float4(acc.fB.x, acc.fB.y, acc.fB.z, eh));
+            atomicAdd(a.torque + A, make_float4(acc.tA.x, acc.tA.y, acc.tA.z, 0.f));
+            atomicAdd(a.torque + B, make_float4(acc.tB.x, acc.tB.y, acc.tB.z, 0.f));
+            if (a.virial) {
+                for (int c = 0; c < 6; ++c) {  // the half virial goes to both ends
+                    atomicAdd(a.virial + (size_t)c * a.N + A, acc.vir[c]);
+                    atomicAdd(a.virial + (size_t)c * a.N + B, acc.vir[c]);
+                }
+            }
+            e0 = acc.e[0];
+            e1 = acc.e[1];
+            e2 = acc.e[2];
+        }
+    }
+    if (a.energy) {
+        e0 = warp_sum(e0);
+        e1 = warp_sum(e1);
+        e2 = warp_sum(e2);
+        if ((threadIdx.x & 31) == 0) {
+            if (e0 != 0.0) atomicAdd(a.energy + 0, e0);
+            if (e1 != 0.0) atomicAdd(a.energy + 1, e1);
+            if (e2 != 0.0) atomicAdd(a.energy + 2, e2);
+        }
+    }
+    if (bad) atomicOr(a.status, kStBadIndex);
+}
+
+// ------------------------------------------------------------ neighbour list
+struct NlistArgs {
+    int N;
+    const float4* pos;
+    float4* pos_ref;
+    const int4* excl;      // up to 4 bonded partners per particle (-1 = none)
+    int3 nc;               // cells per dimension (>= 3 each when use_cells)
+    int use_cells;
+    int cell_cap;
+    int n_cells;
+    uint32_t* cell_count;  // 2 * n_cells (double-buffered by generation parity)
+    int* cell_list;        // n_cells * cell_cap
+    float3 L, invL;
+    float rlist2, rshort2;
+    int2* pairs_short;
+    int2* pairs_long;
+    int cap_short, cap_long;
+    DevStatus* st;
+};
+
+__device__ __forceinline__ int cell_coord(float x, float invL, int n)
+{
+    float u = x * invL + 0.5f;
+    u -= floorf(u);
+    int c = (int)(u * (float)n);
+    return c >= n ? n - 1 : (c < 0 ? 0 : c);
+}
+
+__global__ void k_nlist_bin(NlistArgs a)
+{
+    if (!a.st->rebuild) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t par = a.st->gen & 1u;
+    // zero the other generation's counts for the next rebuild
+    uint32_t* other = a.cell_count + (size_t)(par ^ 1u) * a.n_cells;
+    for (int c = i; c < a.n_cells; c += gridDim.x * blockDim.x) other[c] = 0u;
+    if (i == 0) {
+        a.st->n_short = 0u;
+        a.st->n_long = 0u;
+    }
+    if (i >= a.N) return;
+    const float4 p = a.pos[i];
+    a.pos_ref[i] = p;
+    if (!a.use_cells) return;
+    const int cx = cell_coord(p.x, a.invL.x, a.nc.x), cy = cell_coord(p.y, a.invL.y, a.nc.y),
+              cz = cell_coord(p.z, a.invL.z, a.nc.z);
+    const int c = (cz * a.nc.y + cy) * a.nc.x + cx;
+    const uint32_t slot = atomicAdd(a.cell_count + (size_t)par * a.n_cells + c, 1u);
+    if (slot < (uint32_t)a.cell_cap) a.cell_list[(size_t)c * a.cell_cap + slot] = i;
+    else atomicOr(&a.st->flags, kStCellOverflow);
+    atomicMax(&a.st->max_cell, slot + 1u);
+}
+
+__device__ __forceinline__ bool is_excluded(int4 e, int j) { return e.x == j || e.y == j || e.z == j || e.w == j; }
+
+// Visit every candidate j > i (bond-excluded, within rlist) of particle i.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const NlistArgs& a, int i, float4 p,
+                                                   const uint32_t* counts, F&& fn)
+{
+    const int4 ex = a.excl[i];
+    if (a.use_cells) {
+        const int cx = cell_coord(p.x, a.invL.x, a.nc.x), cy = cell_coord(p.y, a.invL.y, a.nc.y),
+                  cz = cell_coord(p.z, a.invL.z, a.nc.z);
+        for (int dz = -1; dz <= 1; ++dz) {
+            const int z = (cz + dz + a.nc.z) % a.nc.z;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int y = (cy + dy + a.nc.y) % a.nc.y;
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int x = (cx + dx + a.nc.x) % a.nc.x;
+                    const int c = (z * a.nc.y + y) * a.nc.x + x;
+                    const int n = min((int)counts[c], a.cell_cap);
+                    const int* lst = a.cell_list + (size_t)c * a.cell_cap;
+                    for (int q = 0; q < n; ++q) {
+                        const int j = lst[q];
+                        if (j <= i || is_excluded(ex, j)) continue;
+                        const float4 pj = a.pos[j];
+                        const float3 d = min_image(mk3(p.x - pj.x, p.y - pj.y, p.z - pj.z), a.L, a.invL);
+                        const float r2 = dot(d, d);
+                        if (r2 < a.rlist2) fn(j, r2);
+                    }
+                }
+            }
+        }
+    } else {
+        for (int j = i + 1; j < a.N; ++j) {
+            if (is_excluded(ex, j)) continue;
+            const float4 pj = a.pos[j];
+            const float3 d = min_image(mk3(p.x - pj.x, p.y - pj.y, p.z - pj.z), a.L, a.invL);
+            const float r2 = dot(d, d);
+            if (r2 < a.rlist2) fn(j, r2);
+        }
+    }
+}
+
+// warp-aggregated reservation of n slots in a global list
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t n)
+{
+    const int lane = threadIdx.x & 31;
+    uint32_t incl = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(counter, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + incl - n;
+}
+
+__global__ void k_nlist_pairs(NlistArgs a)
+{
+    if (!a.st->rebuild) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < a.N;
+    const uint32_t* counts = a.cell_count + (size_t)(a.st->gen & 1u) * a.n_cells;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t ns = 0, nl = 0;
+    if (active) {
+        p = a.pos[i];
+        for_each_candidate(a, i, p, counts, [&](int, float r2) {
+            if (r2 < a.rshort2) ++ns;
+            else ++nl;
+        });
+    }
+    const uint32_t bs = warp_reserve(&a.st->n_short, ns);
+    const uint32_t bl = warp_reserve(&a.st->n_long, nl);
+    if (!active) return;
+    uint32_t ks = bs, kl = bl;
+    bool over = false;
+    for_each_candidate(a, i, p, counts, [&](int j, float r2) {
+        if (r2 < a.rshort2) {
+            if (ks < (uint32_t)a.cap_short) a.pairs_short[ks] = make_int2(i, j);
+            else over = true;
+            ++ks;
+        } else {
+            if (kl < (uint32_t)a.cap_long) a.pairs_long[kl] = make_int2(i, j);
+            else over = true;
+            ++kl;
+        }
+    });
+    if (over) atomicOr(&a.st->flags, kStPairOverflow);
+    if (i == 0) atomicAdd(&a.st->builds, 1u);
+}
+
+// ------------------------------------------------------------------ integrator
+__device__ __forceinline__ void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+    // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), written from the paper
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+struct IntegArgs {
+    int N;
+    float4* pos;       // x, y, z, type
+    float4* quat;
+    float4* vel;       // vx, vy, vz, mass
+    float4* angmom;
+    float4* accel;     // (F + F_bath) / m from the last step two
+    float4* tnet;      // T + T_bath (lab) from the last step two
+    const float4* pos_ref;
+    float4* force;
+    float4* torque;
+    DevStatus* st;
+    float3 L, invL;
+    float dt, kT, gamma, gamma_r;
+    float half_buf2;   // (buffer / 2)^2
+    float3 inertia;
+    uint32_t seed_lo, seed_hi;
+};
+
+__device__ __forceinline__ float4 qmul_vec(float4 q, float3 t)
+{
+    // q * (0, t) with q = (s, x, y, z) in (.x, .y, .z, .w)
+    return make_float4(-(q.y * t.x + q.z * t.y + q.w * t.z), q.x * t.x + q.z * t.z - q.w * t.y,
+                       q.x * t.y + q.w * t.x - q.y * t.z, q.x * t.z + q.y * t.y - q.z * t.x);
+}
+__device__ __forceinline__ float3 rot_conj(float4 q, float3 v)
+{
+    const float4 c = make_float4(q.x, -q.y, -q.z, -q.w);
+    const Frame f = quat_frame(c);
+    return f.a1 * v.x + f.a2 * v.y + f.a3 * v.z;
+}
+__device__ __forceinline__ float4 perm(int k, float4 a)
+{
+    if (k == 1) return make_float4(-a.y, a.x, a.w, -a.z);
+    if (k == 2) return make_float4(-a.z, -a.w, a.x, a.y);
+    return make_float4(-a.w, a.z, -a.y, a.x);
+}
+__device__ __forceinline__ void free_rotor(int k, float h, float I, float4& p, float4& q)
+{
+    const float4 pq = perm(k, q);
+    const float phi = (p.x * pq.x + p.y * pq.y + p.z * pq.z + p.w * pq.w) / (4.f * I);
+    float s, c;
+    sincosf(h * phi, &s, &c);
+    const float4 pp = perm(k, p);
+    p = make_float4(c * p.x + s * pp.x, c * p.y + s * pp.y, c * p.z + s * pp.z, c * p.w + s * pp.w);
+    q = make_float4(c * q.x + s * pq.x, c * q.y + s * pq.y, c * q.z + s * pq.z, c * q.w + s * pq.w);
+}
+
+// Step one: v += dt/2 a; x += dt v (wrapped); p += dt q*(0, t_body); NO_SQUISH free
+// rotor (axes 3, 2 at dt/2, 1 at dt, 2, 3 at dt/2); renormalise q. Zeroes the force
+// accumulators and flags a neighbour-list rebuild when a particle moved more than
+// half the buffer since the last build.
+__global__ void k_step_one(IntegArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) a.st->step += 1ull;
+    bool far = false, bad = false;
+    if (i < a.N) {
+        float4 v = a.vel[i];
+        const float4 ac = a.accel[i];
+        float4 x = a.pos[i];
+        v.x += 0.5f * a.dt * ac.x;
+        v.y += 0.5f * a.dt * ac.y;
+        v.z += 0.5f * a.dt * ac.z;
+        x.x += a.dt * v.x;
+        x.y += a.dt * v.y;
+        x.z += a.dt * v.z;
+        x.x -= a.L.x * rintf(x.x * a.invL.x);
+        x.y -= a.L.y * rintf(x.y * a.invL.y);
+        x.z -= a.L.z * rintf(x.z * a.invL.z);
+        float4 q = a.quat[i], p = a.angmom[i];
+        const float4 tn = a.tnet[i];
+        const float3 tb = rot_conj(q, mk3(tn.x, tn.y, tn.z));
+        const float4 dq = qmul_vec(q, tb);
+        p.x += a.dt * dq.x;
+        p.y += a.dt * dq.y;
+        p.z += a.dt * dq.z;
+        p.w += a.dt * dq.w;
+        free_rotor(3, 0.5f * a.dt, a.inertia.z, p, q);
+        free_rotor(2, 0.5f * a.dt, a.inertia.y, p, q);
+        free_rotor(1, a.dt, a.inertia.x, p, q);
+        free_rotor(2, 0.5f * a.dt, a.inertia.y, p, q);
+        free_rotor(3, 0.5f * a.dt, a.inertia.z, p, q);
+        const float nq = rsqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+        q = make_float4(q.x * nq, q.y * nq, q.z * nq, q.w * nq);
+        bad = !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(q.x));
+        a.pos[i] = x;
+        a.vel[i] = v;
+        a.quat[i] = q;
+        a.angmom[i] = p;
+        a.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        a.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 r = a.pos_ref[i];
+        const float3 d = min_image(mk3(x.x - r.x, x.y - r.y, x.z - r.z), a.L, a.invL);
+        far = dot(d, d) > a.half_buf2;
+    }
+    if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&a.st->rebuild, 1u);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&a.st->flags, kStNonFinite);
+}
+
+// Step two (HOOMD TwoStepLangevin semantics): bath force u*sqrt(6 gamma kT/dt) -
+// gamma v with u uniform in [-1, 1); bath torque (body frame) n*sqrt(2 gamma_r kT/dt)
+// - gamma_r L/I with n standard normal; a = (F + F_bath)/m; v += dt/2 a;
+// tnet = T + R(q) T_bath; p += dt q*(0, t_body). RNG counter (tag, step, stream).
+__global__ void k_step_two(IntegArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const unsigned long long step = a.st->step;
+    uint32_t r0[4] = {(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 0u};
+    uint32_t r1[4] = {(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 1u};
+    philox4x32(r0, a.seed_lo, a.seed_hi);
+    philox4x32(r1, a.seed_lo, a.seed_hi);
+    const float ct = sqrtf(6.f * a.gamma * a.kT / a.dt);
+    const float cr = sqrtf(2.f * a.gamma_r * a.kT / a.dt);
+    float4 v = a.vel[i];
+    const float minv = 1.f / v.w;
+    const float4 F = a.force[i];
+    const float inv31 = 1.f / 2147483648.f;
+    float4 ac;
+    ac.x = (F.x + (float)(int32_t)r0[0] * inv31 * ct - a.gamma * v.x) * minv;
+    ac.y = (F.y + (float)(int32_t)r0[1] * inv31 * ct - a.gamma * v.y) * minv;
+    ac.z = (F.z + (float)(int32_t)r0[2] * inv31 * ct - a.gamma * v.z) * minv;
+    ac.w = 0.f;
+    const float4 q = a.quat[i];
+    float4 p = a.angmom[i];
+    // s = (1/2 conj(q) p).v : body-frame angular momentum
+    const float sx = 0.5f * (q.x * p.y - p.x * q.y - (q.z * p.w - q.w * p.z));
+    const float sy = 0.5f * (q.x * p.z - p.x * q.z - (q.w * p.y - q.y * p.w));
+    const float sz = 0.5f * (q.x * p.w - p.x * q.w - (q.y * p.z - q.z * p.y));
+    // Box-Muller on two word pairs
+    const float u1 = ((float)r1[0] + 1.f) * 2.3283064365386963e-10f;
+    const float u2 = (float)r1[1] * 2.3283064365386963e-10f;
+    const float u3 = ((float)r1[2] + 1.f) * 2.3283064365386963e-10f;
+    const float u4 = (float)r1[3] * 2.3283064365386963e-10f;
+    const float ra = sqrtf(-2.f * logf(fminf(u1, 1.f))), rb = sqrtf(-2.f * logf(fminf(u3, 1.f)));
+    float s2a, c2a, s2b, c2b;
+    sincosf(2.f * kPi * u2, &s2a, &c2a);
+    sincosf(2.f * kPi * u4, &s2b, &c2b);
+    const float3 bt = mk3(ra * c2a * cr - a.gamma_r * sx / a.inertia.x,
+                          ra * s2a * cr - a.gamma_r * sy / a.inertia.y,
+                          rb * c2b * cr - a.gamma_r * sz / a.inertia.z);
+    const Frame fq = quat_frame(q);
+    const float3 btl = fq.a1 * bt.x + fq.a2 * bt.y + fq.a3 * bt.z;
+    const float4 T = a.torque[i];
+    const float4 tn = make_float4(T.x + btl.x, T.y + btl.y, T.z + btl.z, 0.f);
+    v.x += 0.5f * a.dt * ac.x;
+    v.y += 0.5f * a.dt * ac.y;
+    v.z += 0.5f * a.dt * ac.z;
+    const float3 tb = rot_conj(q, mk3(tn.x, tn.y, tn.z));
+    const float4 dq = qmul_vec(q, tb);
+    p.x += a.dt * dq.x;
+    p.y += a.dt * dq.y;
+    p.z += a.dt * dq.z;
+    p.w += a.dt * dq.w;
+    a.vel[i] = v;
+    a.angmom[i] = p;
+    a.accel[i] = ac;
+    a.tnet[i] = tn;
+}
+
+// prepRun: accelerations from the forces alone (no bath), as HOOMD does at run start.
+__global__ void k_prep_accel(IntegArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const float4 F = a.force[i], T = a.torque[i], v = a.vel[i];
+    const float minv = 1.f / v.w;
+    a.accel[i] = make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f);
+    a.tnet[i] = make_float4(T.x, T.y, T.z, 0.f);
+}
+
+}  // namespace oxg

@@ -1,0 +1,336 @@
+"""oxDNA topology / configuration I/O and seeded synthetic system builders.
+
+Readers and the orientation conversion have the reference's names and conventions
+(``oxdna/io.py``): bases map to type ids A=0, G=1, C=2, T=3 (U aliases T);
+quaternions are (w, x, y, z) with rotate(q, e_x) = a1 and rotate(q, e_z) = a3;
+backbone bonds are (i, n5[i]); charges are 1, or 0.5 at strand ends when asked.
+
+The builders produce the benchmark systems from ideal B-form helices (rise 0.3897,
+twist 34.8 deg, centre of mass 0.6 from the axis): duplexes and hairpins placed with
+uniform-random centre and orientation without overlap in a periodic cubic box.
+"""
+
+import math
+
+import numpy as np
+
+DNA_BASES = ["A", "G", "C", "T"]
+BASE_ALIAS = {"U": "T"}
+
+RISE = 0.3897
+TWIST = math.radians(34.8)
+COM_RADIUS = 0.6
+
+
+def base_typeid(letter):
+    return DNA_BASES.index(BASE_ALIAS.get(letter, letter))
+
+
+def read_topology(top_path):
+    """Parse an oxDNA .top file: n, n_strands, strand, base, n3, n5."""
+    with open(top_path) as fh:
+        n, n_strands = (int(x) for x in fh.readline().split()[:2])
+        strand = np.empty(n, dtype=int)
+        n3 = np.empty(n, dtype=int)
+        n5 = np.empty(n, dtype=int)
+        base = []
+        for i in range(n):
+            parts = fh.readline().split()
+            strand[i] = int(parts[0])
+            base.append(parts[1])
+            n3[i] = int(parts[2])
+            n5[i] = int(parts[3])
+    return dict(n=n, n_strands=n_strands, strand=strand, base=base, n3=n3, n5=n5)
+
+
+def iter_conf_frames(conf_path):
+    """Yield (t, box, arr) per frame; arr rows are com(3) a1(3) a3(3) v(3) L(3)."""
+    with open(conf_path) as fh:
+        lines = fh.readlines()
+    i = 0
+    while i < len(lines):
+        if not lines[i].startswith("t ="):
+            i += 1
+            continue
+        t = float(lines[i].split("=")[1])
+        box = np.array(lines[i + 1].split("=")[1].split(), dtype=float)
+        i += 3
+        rows = []
+        while i < len(lines) and not lines[i].startswith("t ="):
+            s = lines[i].split()
+            if len(s) >= 9:
+                rows.append([float(x) for x in s[:15]])
+            i += 1
+        yield t, box, np.array(rows, dtype=float)
+
+
+def quat_to_matrix(q):
+    """Rotation matrices (..., 3, 3) of (w, x, y, z) quaternions (HOOMD rotate)."""
+    q = np.asarray(q, dtype=float)
+    w, x, y, z = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
+    R = np.empty(q.shape[:-1] + (3, 3))
+    R[..., 0, 0] = w * w + x * x - y * y - z * z
+    R[..., 0, 1] = 2 * (x * y - w * z)
+    R[..., 0, 2] = 2 * (x * z + w * y)
+    R[..., 1, 0] = 2 * (x * y + w * z)
+    R[..., 1, 1] = w * w - x * x + y * y - z * z
+    R[..., 1, 2] = 2 * (y * z - w * x)
+    R[..., 2, 0] = 2 * (x * z - w * y)
+    R[..., 2, 1] = 2 * (y * z + w * x)
+    R[..., 2, 2] = w * w - x * x - y * y + z * z
+    return R
+
+
+def matrix_to_quaternion(R):
+    """Rotation matrices (..., 3, 3) -> unit (w, x, y, z), Shepperd's branch choice."""
+    R = np.asarray(R, dtype=float)
+    flat = R.reshape(-1, 3, 3)
+    out = np.empty((flat.shape[0], 4))
+    for k, M in enumerate(flat):
+        tr = M[0, 0] + M[1, 1] + M[2, 2]
+        if tr > 0.0:
+            s = 2.0 * math.sqrt(tr + 1.0)
+            q = (0.25 * s, (M[2, 1] - M[1, 2]) / s, (M[0, 2] - M[2, 0]) / s, (M[1, 0] - M[0, 1]) / s)
+        elif M[0, 0] > M[1, 1] and M[0, 0] > M[2, 2]:
+            s = 2.0 * math.sqrt(1.0 + M[0, 0] - M[1, 1] - M[2, 2])
+            q = ((M[2, 1] - M[1, 2]) / s, 0.25 * s, (M[0, 1] + M[1, 0]) / s, (M[0, 2] + M[2, 0]) / s)
+        elif M[1, 1] > M[2, 2]:
+            s = 2.0 * math.sqrt(1.0 + M[1, 1] - M[0, 0] - M[2, 2])
+            q = ((M[0, 2] - M[2, 0]) / s, (M[0, 1] + M[1, 0]) / s, 0.25 * s, (M[1, 2] + M[2, 1]) / s)
+        else:
+            s = 2.0 * math.sqrt(1.0 + M[2, 2] - M[0, 0] - M[1, 1])
+            q = ((M[1, 0] - M[0, 1]) / s, (M[0, 2] + M[2, 0]) / s, (M[1, 2] + M[2, 1]) / s, 0.25 * s)
+        q = np.array(q)
+        out[k] = q / np.linalg.norm(q)
+    return out.reshape(R.shape[:-2] + (4,))
+
+
+def orientations_to_quaternions(a1, a3, check=True):
+    """Per-nucleotide (a1, a3) -> (w, x, y, z) with rotate(q, e_x) = a1 (io.py:117-136)."""
+    a1 = np.asarray(a1, float)
+    a3 = np.asarray(a3, float)
+    e1 = a1 / np.linalg.norm(a1, axis=1, keepdims=True)
+    e3 = a3 / np.linalg.norm(a3, axis=1, keepdims=True)
+    e2 = np.cross(e3, e1)
+    R = np.stack([e1, e2, e3], axis=-1)
+    q = matrix_to_quaternion(R)
+    if check:
+        err = np.linalg.norm(quat_to_matrix(q)[..., :, 0] - e1, axis=1)
+        if len(err) and err.max() > 1e-6:
+            i = int(np.argmax(err))
+            raise ValueError(f"quaternion convention check failed at nucleotide {i}: {err[i]:.2e}")
+    return q
+
+
+def terminal_charges(top, end_charge=0.5, interior_charge=1.0):
+    charges = np.full(top["n"], interior_charge)
+    charges[(np.asarray(top["n3"]) < 0) | (np.asarray(top["n5"]) < 0)] = end_charge
+    return charges
+
+
+class SystemArrays(dict):
+    """pos (N,3), quat (N,4), typeid (N,), box (3,), bonds [(A,B)], charge (N,),
+    plus strand/n3/n5 bookkeeping. Convert with :func:`snapshot_from_arrays`."""
+
+
+def snapshot_from_arrays(positions, quaternions, typeids, box, bonds=None, types=DNA_BASES,
+                         bond_type="backbone", charges=None):
+    """Snapshot from arrays (positions box-centred). Unit charge by default."""
+    from .runtime import Snapshot
+    n = len(positions)
+    snap = Snapshot()
+    p = snap.particles
+    p.N = n
+    p.types = list(types)
+    p.position[:] = np.asarray(positions, float)
+    p.typeid[:] = np.asarray(typeids, int)
+    p.mass[:] = 1.0
+    p.moment_inertia[:] = 1.0
+    p.orientation[:] = np.asarray(quaternions, float)
+    p.charge[:] = np.ones(n) if charges is None else np.asarray(charges, float)
+    snap.configuration.box = [float(box[0]), float(box[1]), float(box[2]), 0, 0, 0]
+    bonds = list(bonds or [])
+    snap.bonds.N = len(bonds)
+    snap.bonds.types = [bond_type]
+    if bonds:
+        snap.bonds.group[:] = np.asarray(bonds, int)
+        snap.bonds.typeid[:] = 0
+    return snap
+
+
+def build_snapshot(top_path, conf_path, frame=0, bond_type="backbone", half_charged_ends=False):
+    """Snapshot from an oxDNA topology + configuration frame (io.py:196-241)."""
+    top = read_topology(top_path)
+    _, box, arr = list(iter_conf_frames(conf_path))[frame]
+    q = orientations_to_quaternions(arr[:, 3:6], arr[:, 6:9])
+    typeids = [base_typeid(b) for b in top["base"]]
+    bonds = [(i, int(top["n5"][i])) for i in range(top["n"]) if top["n5"][i] >= 0]
+    charges = terminal_charges(top) if half_charged_ends else np.ones(top["n"])
+    return snapshot_from_arrays(arr[:, 0:3] - box / 2.0, q, typeids, box, bonds=bonds,
+                                bond_type=bond_type, charges=charges)
+
+
+# ------------------------------------------------------------------ synthetic builders
+def ideal_strand(n, start=0, direction=+1):
+    """Ideal B-form helix positions and frames for n nucleotides of one strand.
+
+    Strand nucleotide k sits at height (start + direction*k)*RISE, azimuth
+    phi = (start + direction*k)*TWIST, centre of mass COM_RADIUS from the axis; a1
+    points at the axis, a3 along the strand towards its 5' neighbour (the next
+    index). Returns pos (n,3), a1 (n,3), a3 (n,3) in the helix frame (axis = z).
+    """
+    k = start + direction * np.arange(n)
+    phi = k * TWIST
+    radial = np.stack([np.cos(phi), np.sin(phi), np.zeros(n)], axis=1)
+    pos = COM_RADIUS * radial + np.outer(k * RISE, [0.0, 0.0, 1.0])
+    a1 = -radial
+    a3 = np.tile([0.0, 0.0, float(direction)], (n, 1))
+    return pos, a1, a3
+
+
+def duplex(seq):
+    """Ideal duplex: strand 1 (bases seq, 3'->5' along +z) then its complement.
+
+    Strand-2 nucleotide m pairs with strand-1 nucleotide n-1-m and sits on the far
+    side of the axis with a1 and a3 reversed. Returns pos, a1, a3, types, bonds
+    (local indices, (i, i+1) within each strand) and strand-end flags.
+    """
+    n = len(seq)
+    comp = {"A": "T", "T": "A", "G": "C", "C": "G"}
+    p1, a11, a31 = ideal_strand(n)
+    # strand 2: nucleotide m pairs with n-1-m (same height, opposite side)
+    k = np.arange(n)[::-1]
+    phi = k * TWIST
+    radial = np.stack([np.cos(phi), np.sin(phi), np.zeros(n)], axis=1)
+    p2 = -COM_RADIUS * radial + np.outer(k * RISE, [0.0, 0.0, 1.0])
+    a12 = radial
+    a32 = np.tile([0.0, 0.0, -1.0], (n, 1))
+    seq2 = [comp[seq[n - 1 - m]] for m in range(n)]
+    pos = np.vstack([p1, p2])
+    a1 = np.vstack([a11, a12])
+    a3 = np.vstack([a31, a32])
+    types = np.array([base_typeid(b) for b in list(seq) + seq2])
+    bonds = [(i, i + 1) for i in range(n - 1)] + [(n + i, n + i + 1) for i in range(n - 1)]
+    ends = np.zeros(2 * n, bool)
+    ends[[0, n - 1, n, 2 * n - 1]] = True
+    return pos, a1, a3, types, bonds, ends
+
+
+def hairpin_strand(seq):
+    """One strand as an extended ideal helix (hairpins start unfolded)."""
+    n = len(seq)
+    pos, a1, a3 = ideal_strand(n)
+    types = np.array([base_typeid(b) for b in seq])
+    bonds = [(i, i + 1) for i in range(n - 1)]
+    ends = np.zeros(n, bool)
+    ends[[0, n - 1]] = True
+    return pos, a1, a3, types, bonds, ends
+
+
+def random_rotation(rng):
+    """Uniform random rotation matrix (from a uniform random unit quaternion)."""
+    u1, u2, u3 = rng.random(3)
+    q = np.array([math.sqrt(1 - u1) * math.sin(2 * math.pi * u2),
+                  math.sqrt(1 - u1) * math.cos(2 * math.pi * u2),
+                  math.sqrt(u1) * math.sin(2 * math.pi * u3),
+                  math.sqrt(u1) * math.cos(2 * math.pi * u3)])
+    return quat_to_matrix(q)
+
+
+def random_sequence(rng, n, alphabet="ACGT"):
+    return "".join(alphabet[i] for i in rng.integers(0, len(alphabet), n))
+
+
+def pack_molecules(molecules, box_len, rng, min_dist=1.5, max_tries=2000):
+    """Place molecules (pos, a1, a3, types, bonds, ends) with random centre and
+    orientation in a periodic cube without any inter-molecule COM pair closer than
+    min_dist. Returns the concatenated system arrays."""
+    L = float(box_len)
+    cell = max(min_dist, 1e-3)
+    ncell = max(1, int(L // cell))
+    grid = {}
+
+    def cell_of(p):
+        return tuple(((np.floor((p + L / 2) / L * ncell)).astype(int)) % ncell)
+
+    out_pos, out_a1, out_a3, out_t, out_b, out_ends, out_mol = [], [], [], [], [], [], []
+    offset = 0
+    for mid, (pos, a1, a3, types, bonds, ends) in enumerate(molecules):
+        centred = pos - pos.mean(axis=0)
+        placed = False
+        for _ in range(max_tries):
+            R = random_rotation(rng)
+            c = (rng.random(3) - 0.5) * L
+            p = centred @ R.T + c
+            p = p - L * np.round(p / L)
+            ok = True
+            for x in p:
+                ci = cell_of(x)
+                for dx in (-1, 0, 1):
+                    for dy in (-1, 0, 1):
+                        for dz in (-1, 0, 1):
+                            key = ((ci[0] + dx) % ncell, (ci[1] + dy) % ncell, (ci[2] + dz) % ncell)
+                            for y in grid.get(key, ()):
+                                d = x - y
+                                d -= L * np.round(d / L)
+                                if d @ d < min_dist * min_dist:
+                                    ok = False
+                                    break
+                            if not ok:
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                placed = True
+                break
+        if not placed:
+            raise RuntimeError(f"could not place molecule {mid} without overlap")
+        for x in p:
+            grid.setdefault(cell_of(x), []).append(x)
+        out_pos.append(p)
+        out_a1.append(a1 @ R.T)
+        out_a3.append(a3 @ R.T)
+        out_t.append(types)
+        out_b += [(a + offset, b + offset) for a, b in bonds]
+        out_ends.append(ends)
+        out_mol.append(np.full(len(p), mid))
+        offset += len(p)
+    pos = np.vstack(out_pos)
+    a1 = np.vstack(out_a1)
+    a3 = np.vstack(out_a3)
+    return SystemArrays(pos=pos, quat=orientations_to_quaternions(a1, a3),
+                        typeid=np.concatenate(out_t), box=np.array([L, L, L]), bonds=out_b,
+                        ends=np.concatenate(out_ends), molecule=np.concatenate(out_mol),
+                        charge=np.ones(len(pos)))
+
+
+def duplex_system(n_duplexes, n_bp, box_len, seed=1, min_dist=1.5):
+    """n_duplexes random-sequence B-form duplexes of n_bp base pairs (or a list of
+    lengths) in a periodic cube of side box_len (seeded PCG64)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lengths = n_bp if hasattr(n_bp, "__len__") else [n_bp] * n_duplexes
+    mols = [duplex(random_sequence(rng, int(n))) for n in lengths]
+    return pack_molecules(mols, box_len, rng, min_dist=min_dist)
+
+
+def hairpin_system(n_hairpins, stem=16, loop=16, box_len=80.0, seed=1, min_dist=1.5):
+    """Single strands 5'-stem, loop, complementary stem-3' started as extended helices."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    comp = {"A": "T", "T": "A", "G": "C", "C": "G"}
+    mols = []
+    for _ in range(n_hairpins):
+        s = random_sequence(rng, stem)
+        lp = random_sequence(rng, loop)
+        seq = s + lp + "".join(comp[b] for b in reversed(s))
+        mols.append(hairpin_strand(seq))
+    return pack_molecules(mols, box_len, rng, min_dist=min_dist)
+
+
+def system_snapshot(sysarr, half_charged_ends=False):
+    charges = np.where(sysarr["ends"], 0.5, 1.0) if half_charged_ends else sysarr["charge"]
+    return snapshot_from_arrays(sysarr["pos"], sysarr["quat"], sysarr["typeid"], sysarr["box"],
+                                bonds=sysarr["bonds"], charges=charges)

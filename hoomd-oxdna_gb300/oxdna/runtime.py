@@ -1,0 +1,416 @@
+"""Minimal simulation runtime with HOOMD-blue's Python surface.
+
+The reference plugin runs inside HOOMD-blue; this package stands that runtime in
+with the subset the reference's model files, tests and benchmark use
+(``hoomd.Simulation``, ``Snapshot``, ``md.Integrator``, ``md.methods.Langevin``,
+``md.nlist.Cell``, ``filter.All``, ``device.GPU``). Everything it runs goes through
+the native library: the state lives on the GPU, and each step (neighbour list,
+every attached force in one fused kernel, Langevin + NO_SQUISH) is replayed from a
+captured CUDA graph.
+"""
+
+import ctypes as C
+import types as _types
+
+import numpy as np
+
+from . import _abi
+from .forces import OxDNABonded, _PairForce
+
+
+# --------------------------------------------------------------------- snapshot
+class _Particles:
+    def __init__(self):
+        self._n = 0
+        self.types = []
+        self._alloc(0)
+
+    def _alloc(self, n):
+        self.position = np.zeros((n, 3))
+        self.typeid = np.zeros(n, dtype=np.int64)
+        self.mass = np.ones(n)
+        self.moment_inertia = np.ones((n, 3))
+        self.orientation = np.tile([1.0, 0.0, 0.0, 0.0], (n, 1))
+        self.charge = np.zeros(n)
+        self.velocity = np.zeros((n, 3))
+        self.angmom = np.zeros((n, 4))
+        self.image = np.zeros((n, 3), dtype=np.int64)
+
+    @property
+    def N(self):
+        return self._n
+
+    @N.setter
+    def N(self, n):
+        self._n = int(n)
+        self._alloc(self._n)
+
+
+class _Bonds:
+    def __init__(self):
+        self._n = 0
+        self.types = []
+        self.group = np.zeros((0, 2), dtype=np.int64)
+        self.typeid = np.zeros(0, dtype=np.int64)
+
+    @property
+    def N(self):
+        return self._n
+
+    @N.setter
+    def N(self, n):
+        self._n = int(n)
+        self.group = np.zeros((self._n, 2), dtype=np.int64)
+        self.typeid = np.zeros(self._n, dtype=np.int64)
+
+
+class _Configuration:
+    def __init__(self):
+        self.box = [1.0, 1.0, 1.0, 0.0, 0.0, 0.0]
+
+
+class _Communicator:
+    rank = 0
+    num_ranks = 1
+
+
+class Snapshot:
+    """System snapshot (particles, bonds, box) on the host."""
+
+    def __init__(self):
+        self.particles = _Particles()
+        self.bonds = _Bonds()
+        self.configuration = _Configuration()
+        self.communicator = _Communicator()
+
+
+# --------------------------------------------------------------------- devices etc.
+class _GPU:
+    def __init__(self, gpu_ids=None):
+        self.gpu_ids = gpu_ids or [0]
+
+
+class _CPU:
+    def __init__(self, *a, **k):
+        raise RuntimeError("this framework runs the force path on the GPU only (no CPU fallback)")
+
+
+device = _types.SimpleNamespace(GPU=_GPU, CPU=_CPU)
+
+
+class _All:
+    pass
+
+
+filter = _types.SimpleNamespace(All=_All)
+
+
+class _Cell:
+    """Cell neighbour list: radius max(r_cut) + buffer, bond exclusions."""
+
+    def __init__(self, buffer=0.4, exclusions=("bond",)):
+        self.buffer = float(buffer)
+        self.exclusions = tuple(exclusions)
+        if "bond" not in self.exclusions:
+            raise ValueError("oxDNA forces require exclusions=('bond',)")
+
+
+class _Langevin:
+    def __init__(self, filter=None, kT=1.0, default_gamma=1.0, default_gamma_r=(1.0, 1.0, 1.0)):
+        self.filter = filter
+        self.kT = float(kT)
+        self.default_gamma = float(default_gamma)
+        g = tuple(default_gamma_r) if hasattr(default_gamma_r, "__len__") else (default_gamma_r,) * 3
+        if len(set(g)) != 1:
+            raise ValueError("anisotropic gamma_r is not supported")
+        self.default_gamma_r = g
+
+
+class _Integrator:
+    def __init__(self, dt, integrate_rotational_dof=False, forces=(), methods=()):
+        self.dt = float(dt)
+        self.integrate_rotational_dof = bool(integrate_rotational_dof)
+        self.forces = list(forces)
+        self.methods = list(methods)
+
+
+md = _types.SimpleNamespace(
+    Integrator=_Integrator,
+    methods=_types.SimpleNamespace(Langevin=_Langevin),
+    nlist=_types.SimpleNamespace(Cell=_Cell),
+)
+
+
+class _Operations:
+    def __init__(self, sim):
+        self._sim = sim
+        self._integrator = None
+
+    @property
+    def integrator(self):
+        return self._integrator
+
+    @integrator.setter
+    def integrator(self, integ):
+        self._integrator = integ
+        self._sim._detach()
+
+
+class _State:
+    def __init__(self, sim):
+        self._sim = sim
+
+    @property
+    def N_particles(self):
+        return self._sim._snap.particles.N
+
+    def get_snapshot(self):
+        return self._sim._pull_snapshot()
+
+
+# --------------------------------------------------------------------- simulation
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Simulation:
+    """Owns one native system (state resident on the GPU) and its forces."""
+
+    def __init__(self, device=None, seed=0):
+        self.device = device or _GPU()
+        self.seed = int(seed)
+        self.operations = _Operations(self)
+        self.state = None
+        self.timestep = 0
+        self._snap = None
+        self._ctx = None
+        self._sys = None
+        self._attached = False
+        self._cache = {}
+        self._stream = None
+
+    def set_stream(self, handle):
+        """Run every later engine call on this CUDA stream (a cudaStream_t handle,
+        e.g. ``torch.cuda.Stream().cuda_stream``)."""
+        self._stream = handle
+        if self._sys:
+            _abi.check(_abi.lib().oxg_system_set_stream(self._sys, C.c_void_p(handle)),
+                       "oxg_system_set_stream")
+
+    # -- state ---------------------------------------------------------------
+    def create_state_from_snapshot(self, snap):
+        if self._snap is not None:
+            raise RuntimeError("state already created")
+        self._snap = snap
+        self.state = _State(self)
+
+    def _types(self):
+        return list(self._snap.particles.types)
+
+    def _detach(self):
+        self._free()
+        self._attached = False
+        self._cache = {}
+
+    def _free(self):
+        L = _abi.lib()
+        if self._sys:
+            L.oxg_system_destroy(self._sys)
+            self._sys = None
+        if self._ctx:
+            L.oxg_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self._free()
+        except Exception:
+            pass
+
+    # -- attach: parameters -> context, snapshot -> device state ----------------
+    def _attach(self):
+        if self._attached:
+            return
+        integ = self.operations.integrator
+        if integ is None:
+            raise RuntimeError("no integrator set")
+        L = _abi.lib()
+        snap = self._snap
+        types = self._types()
+        nt = len(types)
+        bond_types = list(snap.bonds.types) or ["backbone"]
+        ctx = C.c_void_p()
+        _abi.check(L.oxg_create(C.byref(ctx), nt, len(bond_types)), "oxg_create")
+        self._ctx = ctx
+        self._pair_forces = {}
+        self._bonded = None
+        self._nlist = None
+        setters = {
+            _abi.EXCVOL: L.oxg_set_excvol_params, _abi.HBOND: L.oxg_set_hbond_params,
+            _abi.CROSS: L.oxg_set_cross_params, _abi.HBONDCROSS: L.oxg_set_hbondcross_params,
+            _abi.COAX: L.oxg_set_coax_params, _abi.DEBYE: L.oxg_set_debye_params,
+        }
+        for f in integ.forces:
+            f._simulation = self
+            if isinstance(f, OxDNABonded):
+                if self._bonded is not None:
+                    raise RuntimeError("only one OxDNABonded force can be attached")
+                self._bonded = f
+                for bt, name in enumerate(bond_types):
+                    if name not in f.params:
+                        raise KeyError(f"OxDNABonded has no parameters for bond type {name!r}")
+                    p = _abi.bonded_from_dict(f.params[name])
+                    _abi.check(L.oxg_set_bonded_params(ctx, bt, C.byref(p)), "oxg_set_bonded_params")
+            elif isinstance(f, _PairForce):
+                t = f._term
+                if t in self._pair_forces:
+                    raise RuntimeError(f"two forces of kind {_abi.TERM_NAMES[t]} attached")
+                if self._nlist is None:
+                    self._nlist = f.nlist
+                self._pair_forces[t] = f
+                conv = _abi.FROM_DICT[t]
+                for a in range(nt):
+                    for b in range(a, nt):
+                        key = (types[a], types[b])
+                        if key not in f.params:
+                            raise KeyError(f"{type(f).__name__} has no parameters for {key}")
+                        p = conv(f.params[key])
+                        _abi.check(setters[t](ctx, a, b, C.byref(p), f.rcut_for(*key)),
+                                   "set params")
+            else:
+                raise TypeError(f"unsupported force {type(f).__name__}")
+        n = snap.particles.N
+        box = (C.c_float * 3)(*[float(x) for x in snap.configuration.box[:3]])
+        bonds = np.zeros((max(1, snap.bonds.N), 3), dtype=np.int32)
+        if snap.bonds.N:
+            bonds[:snap.bonds.N, 0:2] = np.asarray(snap.bonds.group, dtype=np.int32)
+            bonds[:snap.bonds.N, 2] = np.asarray(snap.bonds.typeid, dtype=np.int32)
+        sys_ = C.c_void_p()
+        _abi.check(L.oxg_system_create(C.byref(sys_), ctx, n, box, int(snap.bonds.N),
+                                       bonds.ctypes.data_as(C.POINTER(C.c_int32))),
+                   "oxg_system_create")
+        self._sys = sys_
+        if self._stream is not None:
+            _abi.check(L.oxg_system_set_stream(sys_, C.c_void_p(self._stream)), "set stream")
+        if self._nlist is not None:
+            _abi.check(L.oxg_system_set_nlist_buffer(sys_, self._nlist.buffer), "set buffer")
+        self._push_state()
+        self._mask = 0
+        for t in self._pair_forces:
+            self._mask |= 1 << t
+        lang = [m for m in integ.methods if isinstance(m, _Langevin)]
+        if len(integ.methods) != len(lang) or len(lang) > 1:
+            raise RuntimeError("only a single Langevin method is supported")
+        self._langevin = lang[0] if lang else None
+        if self._langevin is not None:
+            if not integ.integrate_rotational_dof:
+                raise RuntimeError("oxDNA dynamics need integrate_rotational_dof=True")
+            _abi.check(L.oxg_system_set_integrator(
+                sys_, integ.dt, self._langevin.kT, self._langevin.default_gamma,
+                self._langevin.default_gamma_r[0], self.seed, self._mask,
+                1 if self._bonded else 0), "oxg_system_set_integrator")
+        self._attached = True
+
+    def push_state_arrays(self, pos_type, quat, vel, angmom):
+        """Copy host float32 (N, 4) arrays (pinned or not) into the device state."""
+        L = _abi.lib()
+        ptr = lambda a: C.c_void_p(a.ctypes.data) if a is not None else None  # noqa: E731
+        _abi.check(L.oxg_system_set_state(self._sys, ptr(pos_type), ptr(quat), ptr(vel),
+                                          ptr(angmom), None), "oxg_system_set_state")
+
+    def pull_state_arrays(self, pos_type, quat, vel, angmom):
+        """Copy the device state into host float32 (N, 4) arrays."""
+        L = _abi.lib()
+        ptr = lambda a: C.c_void_p(a.ctypes.data) if a is not None else None  # noqa: E731
+        _abi.check(L.oxg_system_get_state(self._sys, ptr(pos_type), ptr(quat), ptr(vel),
+                                          ptr(angmom)), "oxg_system_get_state")
+
+    def _push_state(self):
+        L = _abi.lib()
+        p = self._snap.particles
+        n = p.N
+        pos = np.zeros((n, 4), np.float32)
+        pos[:, :3] = p.position
+        pos[:, 3] = np.asarray(p.typeid, np.int32).view(np.float32)
+        vel = np.zeros((n, 4), np.float32)
+        vel[:, :3] = p.velocity
+        vel[:, 3] = p.mass
+        q = _f32(p.orientation)
+        am = _f32(p.angmom)
+        ch = _f32(p.charge)
+        vp = C.c_void_p
+        _abi.check(L.oxg_system_set_state(self._sys, vp(pos.ctypes.data), vp(q.ctypes.data),
+                                          vp(vel.ctypes.data), vp(am.ctypes.data),
+                                          vp(ch.ctypes.data)), "oxg_system_set_state")
+
+    def _pull_snapshot(self):
+        import copy
+        snap = copy.deepcopy(self._snap)
+        if not self._attached:
+            return snap
+        L = _abi.lib()
+        n = snap.particles.N
+        pos = np.zeros((n, 4), np.float32)
+        q = np.zeros((n, 4), np.float32)
+        vel = np.zeros((n, 4), np.float32)
+        am = np.zeros((n, 4), np.float32)
+        vp = C.c_void_p
+        _abi.check(L.oxg_system_get_state(self._sys, vp(pos.ctypes.data), vp(q.ctypes.data),
+                                          vp(vel.ctypes.data), vp(am.ctypes.data)), "get_state")
+        snap.particles.position[:] = pos[:, :3]
+        snap.particles.orientation[:] = q
+        snap.particles.velocity[:] = vel[:, :3]
+        snap.particles.angmom[:] = am
+        return snap
+
+    # -- running -------------------------------------------------------------
+    def run(self, steps):
+        self._attach()
+        self._cache = {}
+        L = _abi.lib()
+        steps = int(steps)
+        if steps > 0 and self._langevin is not None:
+            _abi.check(L.oxg_system_run(self._sys, steps), "oxg_system_run")
+        self.timestep += steps
+
+    # -- read-outs -----------------------------------------------------------
+    def _energies(self):
+        if "energies" not in self._cache:
+            L = _abi.lib()
+            pe = (C.c_double * 6)()
+            be = (C.c_double * 3)()
+            _abi.check(L.oxg_system_compute(self._sys, self._mask, 1 if self._bonded else 0,
+                                            None, None, pe, be), "oxg_system_compute")
+            self._cache["energies"] = (list(pe), list(be))
+        return self._cache["energies"]
+
+    def _force_energy(self, f):
+        pe, be = self._energies()
+        if f is self._bonded:
+            return float(sum(be))
+        return float(pe[f._term])
+
+    def _bonded_energy(self, k):
+        return float(self._energies()[1][k])
+
+    def _force_arrays(self, f):
+        key = ("arrays", id(f))
+        if key not in self._cache:
+            L = _abi.lib()
+            n = self._snap.particles.N
+            force = np.zeros((n, 4), np.float32)
+            torque = np.zeros((n, 4), np.float32)
+            mask = 0 if f is self._bonded else (1 << f._term)
+            _abi.check(L.oxg_system_compute(self._sys, mask, 1 if f is self._bonded else 0,
+                                            C.c_void_p(force.ctypes.data),
+                                            C.c_void_p(torque.ctypes.data), None, None),
+                       "oxg_system_compute")
+            self._cache[key] = (force[:, :3].astype(np.float64), torque[:, :3].astype(np.float64),
+                                force[:, 3].astype(np.float64))
+        return self._cache[key]
+
+    def native_stats(self):
+        L = _abi.lib()
+        out = (C.c_int64 * 5)()
+        _abi.check(L.oxg_system_stats(self._sys, out, 5), "oxg_system_stats")
+        return dict(steps=out[0], nlist_builds=out[1], pairs_short=out[2], pairs_long=out[3])

@@ -1,0 +1,277 @@
+/*
+ * oxdna_gb300.h - C ABI of the GB300 (sm_103a) oxDNA / oxRNA force engine.
+ *
+ * Plain C: every entry point takes plain pointers, sizes and an opaque CUDA stream
+ * (void*, a cudaStream_t; NULL = the legacy default stream). No C++ or torch types
+ * cross this boundary. Every function returns an int status (OXG_OK = 0).
+ *
+ * Two levels are exported.
+ *
+ *  1. Evaluator level: the drop-in for the reference plugin's GPU force drivers.
+ *     A HOOMD-side wrapper owns all particle buffers and hands device pointers in:
+ *       oxg_pair_forces    replaces gpu_compute_pair_aniso_forces<EvaluatorPairOxDNA*>
+ *                          (src/AnisoPotentialPairOxDNA*GPUKernel.cu:14-18), one call
+ *                          for any subset of the six nonbonded evaluators;
+ *       oxg_bonded_forces  replaces kernel::gpu_compute_oxdna_bonded_forces
+ *                          (src/OxDNABondedGPU.cu:125-159) together with
+ *                          OxDNABondedForceComputeGPU::computeForces/reduceSplit
+ *                          (src/OxDNABondedForceComputeGPU.cc:51-101).
+ *     Parameter setters replace the pybind dict -> param_type constructors
+ *     (e.g. src/EvaluatorPairOxDNAHBondCross.h:69-101, src/OxDNABondedParams.h:97-127).
+ *
+ *  2. System level: a self-contained engine (state + cell neighbour list + fused
+ *     force kernels + Langevin / NO_SQUISH integrator, CUDA-graph captured) that
+ *     stands in for the HOOMD runtime the reference plugin runs inside.
+ *
+ * Data layout (device, structure of arrays, 16-byte aligned):
+ *   pos_type[4*N]  x, y, z, type   The evaluator-level calls take HOOMD's Scalar4
+ *                                   (double) arrays with the type in .w as the int
+ *                                   bit pattern of the low word (HOOMD's
+ *                                   __scalar_as_int, src/OxDNABondedGPU.cu:51-53);
+ *                                   the system engine keeps float4 with the type as
+ *                                   the int bit pattern of the float.
+ *   quat[4*N]      w, x, y, z      (HOOMD Scalar4 quaternion order: s in .x)
+ *   charge[N]      per-particle charge (Debye-Hueckel only)
+ *   force[4*N]     fx, fy, fz, per-particle energy (0.5 * pair energy to each end)
+ *   torque[4*N]    tx, ty, tz, 0   (lab frame)
+ *   virial[6*N]    xx, xy, xz, yy, yz, zz, component-major with pitch N (optional)
+ * Per-term energies are FP64 sums reduced on the device.
+ *
+ * Sign conventions follow the reference evaluators: dr = r_i - r_j (minimum image),
+ * the evaluator force is the force on i, torques are lab-frame
+ * (src/OxDNAAnisoPair.h:91-105, src/OxDNABaseBase.h:233-235).
+ */
+#ifndef OXDNA_GB300_H
+#define OXDNA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define OXG_OK 0
+#define OXG_ERR_INVALID_ARG 1    /* bad pointer, size, type index or term id        */
+#define OXG_ERR_CUDA 2           /* a CUDA runtime call failed                       */
+#define OXG_ERR_NLIST_OVERFLOW 3 /* neighbour / pair / cell capacity exceeded        */
+#define OXG_ERR_BAD_INDEX 4      /* a bond or neighbour index outside [0, N)         */
+#define OXG_ERR_TIMEOUT 5        /* a bounded device-side wait gave up               */
+#define OXG_ERR_NO_PARAMS 6      /* a requested term has no parameters set           */
+#define OXG_ERR_CAPACITY 7       /* a fixed-size resource is too small               */
+#define OXG_ERR_NONFINITE 8      /* the state holds NaN/Inf (integrator blew up)     */
+
+/* ---- nonbonded term ids (one per reference evaluator, getName() in brackets) - */
+#define OXG_EXCVOL 0      /* EvaluatorPairOxDNAExcVol      [oxdna_excvol]        */
+#define OXG_HBOND 1       /* EvaluatorPairOxDNAHBond       [oxdna_hbond]         */
+#define OXG_CROSS 2       /* EvaluatorPairOxDNACrossStacking [oxdna_crossstacking] */
+#define OXG_HBONDCROSS 3  /* EvaluatorPairOxDNAHBondCross  [oxdna_hbondcross]    */
+#define OXG_COAX 4        /* EvaluatorPairOxDNACoaxStacking [oxdna_coaxstacking] */
+#define OXG_DEBYE 5       /* EvaluatorPairOxDNADebye       [oxdna_debye]         */
+#define OXG_N_PAIR_TERMS 6
+#define OXG_TERM_BIT(t) (1u << (t))
+
+/* bonded split energies (OxDNABondedForceCompute getFene/getBondedExcVol/getStacking) */
+#define OXG_E_FENE 0
+#define OXG_E_BEXC 1
+#define OXG_E_STACK 2
+
+/* ---- parameter PODs ---------------------------------------------------------
+ * One struct per reference param_type, fields in the reference's order and units.
+ * f4 sets are (A, B, T0, TS, TC); f5 sets are (A, B, XC, XS); f1 is
+ * (a, r0, rlow, rhigh, rclow, rchigh, blow, bhigh); f2 is
+ * (k, r0, rc, rlow, rhigh, rclow, rchigh, blow, bhigh).                         */
+
+/* src/EvaluatorPairOxDNAExcVol.h:30-39. Site pair k: 0 back-back, 1 base-base,
+ * 2 base(i)-back(j), 3 back(i)-base(j). */
+typedef struct oxg_excvol_params {
+    double eps;
+    double base_site[3];
+    double back_site[3];
+    double sigma[4];
+    double rstar[4];
+    double b[4];
+    double rc[4];
+} oxg_excvol_params;
+
+/* src/EvaluatorPairOxDNAHBond.h:30-36. eps == 0 disables the pair (non-complementary). */
+typedef struct oxg_hbond_params {
+    double eps;
+    double shift_factor;
+    double base_site[3];
+    double f1[8];
+    double t1[5], t23[5], t4[5], t78[5];
+} oxg_hbond_params;
+
+/* src/EvaluatorPairOxDNACrossStacking.h:30-37. t4_enabled = 0 drops f4(theta4) (oxRNA). */
+typedef struct oxg_cross_params {
+    double base_site[3];
+    double f2[9];
+    double t1[5], t23[5], t4[5], t78[5];
+    int32_t t4_enabled;
+    int32_t pad_;
+} oxg_cross_params;
+
+/* src/EvaluatorPairOxDNAHBondCross.h:37-47 (fused HB + cross-stacking). */
+typedef struct oxg_hbondcross_params {
+    double base_site[3];
+    double eps;
+    double shift_factor;
+    double f1[8];
+    double hb_t1[5], hb_t23[5], hb_t4[5], hb_t78[5];
+    double f2[9];
+    double cs_t1[5], cs_t23[5], cs_t4[5], cs_t78[5];
+} oxg_hbondcross_params;
+
+/* src/EvaluatorPairOxDNACoaxStacking.h:32-47. t1_mode 0 = oxDNA1 reflection,
+ * 1 = oxDNA2 harmonic SA*(t-SB)^2; rna_coax selects the oxRNA two-dihedral form. */
+typedef struct oxg_coax_params {
+    double stack_site[3];
+    double stack_back_ref[3];
+    double gamma;
+    double f2[9];
+    double t1[5], t4[5], t56[5];
+    double phi3[4];
+    double phi4[4];
+    int32_t t1_mode;
+    int32_t pad0_;
+    double t1_sa, t1_sb;
+    int32_t phi3_enabled;
+    int32_t rna_coax;
+} oxg_coax_params;
+
+/* src/EvaluatorPairOxDNADebye.h:28-31 (needs per-particle charge). */
+typedef struct oxg_debye_params {
+    double back_site[3];
+    double minus_kappa, prefactor, b_smooth, rc, rhigh;
+} oxg_debye_params;
+
+/* src/OxDNABondedParams.h:35-73 (FENE + bonded excluded volume + DNA/RNA stacking).
+ * Bonded exc-vol site pair k: 0 base-base, 1 base(A)-back(B), 2 back(A)-base(B).
+ * st_eps[typeA][typeB] with A the 3' end of the bond, B = A's 5' neighbour. */
+typedef struct oxg_bonded_params {
+    double eps_backbone, r0_backbone, delta_backbone, delta2;
+    double back_site[3];
+    double base_site[3];
+    double excl_eps;
+    double bx_sigma[3], bx_rstar[3], bx_b[3], bx_rc[3];
+    int32_t stacking_enabled;
+    int32_t rna_stacking;
+    double stack_site[3];
+    double stack_back_ref[3];
+    double st_gamma;
+    double st_f1[9]; /* a, r0, rlow, rhigh, rclow, rchigh, blow, bhigh, shift_factor */
+    double st_eps[4][4];
+    double t4[5];    /* f4 theta4 */
+    double t5[5];    /* f4 theta5 (== theta6) */
+    double p1[4];    /* f5 phi1 (== phi2) */
+    double stack_3_site[3], stack_5_site[3];
+    double bbvector_3[3], bbvector_5[3];
+    double tB1[5], tB2[5];
+} oxg_bonded_params;
+
+/* ---- level 1: evaluator-level drop-in ----------------------------------------- */
+typedef struct oxg_context oxg_context;
+
+/* Create a parameter context for n_types particle types on the current device.
+ * Replaces the per-evaluator param GPUArray set-up done by HOOMD's AnisoPotentialPair
+ * and OxDNABondedForceComputeGPU (src/OxDNABondedForceComputeGPU.cc:18-38). */
+int oxg_create(oxg_context** out, int n_types, int n_bond_types);
+int oxg_destroy(oxg_context* ctx);
+
+/* Set one unordered type pair (both (ti,tj) and (tj,ti) are written) and the COM
+ * cutoff r_cut of that term. Mirrors params[(t1,t2)] = dict(...) with
+ * default_r_cut (oxdna/forces.py:129-311, oxdna/model/dna2.py:100-204). */
+int oxg_set_excvol_params(oxg_context* ctx, int ti, int tj, const oxg_excvol_params* p, double r_cut);
+int oxg_set_hbond_params(oxg_context* ctx, int ti, int tj, const oxg_hbond_params* p, double r_cut);
+int oxg_set_cross_params(oxg_context* ctx, int ti, int tj, const oxg_cross_params* p, double r_cut);
+int oxg_set_hbondcross_params(oxg_context* ctx, int ti, int tj, const oxg_hbondcross_params* p, double r_cut);
+int oxg_set_coax_params(oxg_context* ctx, int ti, int tj, const oxg_coax_params* p, double r_cut);
+int oxg_set_debye_params(oxg_context* ctx, int ti, int tj, const oxg_debye_params* p, double r_cut);
+/* OxDNABondedForceCompute::setParams (src/OxDNABondedForceCompute.cc:39-45). */
+int oxg_set_bonded_params(oxg_context* ctx, int bond_type, const oxg_bonded_params* p);
+
+/* Nonbonded forces over a HOOMD-layout FULL neighbour list (each pair listed from both
+ * ends): neighbours of i are nlist[head_list[i] + k], k < n_neigh[i]. Evaluates the
+ * terms in term_mask (OXG_TERM_BIT(...)) and ADDS into force/torque/virial (the caller
+ * zeroes them, as HOOMD's net-force sum would). One warp per particle, lanes over
+ * neighbours, warp-shuffle reductions, no atomics on force/torque.
+ * term_energy (device, OXG_N_PAIR_TERMS doubles, may be NULL) receives the per-term
+ * FP64 totals (ADDED). virial may be NULL. box = orthorhombic edge lengths.
+ * The call is asynchronous on `stream`. A neighbour index outside [0, N) is skipped
+ * and recorded; oxg_context_status() reports it (OXG_ERR_BAD_INDEX). */
+int oxg_pair_forces(oxg_context* ctx, uint32_t term_mask, int N,
+                    const double* pos_type, const double* quat, const double* charge,
+                    const float box[3],
+                    const uint32_t* n_neigh, const uint32_t* nlist, const uint64_t* head_list,
+                    float* force, float* torque, float* virial, double* term_energy,
+                    void* stream);
+
+/* Bonded forces. bonds[3*b] = (A, B, bond_type) with B the 5' neighbour of A
+ * (oxdna/io.py:219-220), device array. One thread per bond; ADDS into
+ * force/torque/virial; split energies (device, 3 doubles: fene, bexc, stack, may be
+ * NULL) are ADDED. virial may be NULL. Asynchronous; a bond with an index outside
+ * [0, N) or an unknown bond type is skipped and recorded for oxg_context_status(). */
+int oxg_bonded_forces(oxg_context* ctx, int N,
+                      const double* pos_type, const double* quat, const float box[3],
+                      int n_bonds, const int32_t* bonds,
+                      float* force, float* torque, float* virial, double* split_energy,
+                      void* stream);
+
+/* Synchronise the context's last stream and return (and, if clear != 0, reset) the
+ * first error recorded by the asynchronous device calls (OXG_OK when none). */
+int oxg_context_status(oxg_context* ctx, int clear);
+
+/* ---- level 2: system engine -------------------------------------------------- */
+typedef struct oxg_system oxg_system;
+
+/* Create a system of N particles (host arrays, copied to the device). bonds as in
+ * oxg_bonded_forces (may be NULL when n_bonds == 0). The context's parameters are
+ * read at every force evaluation, so they may be changed later. */
+int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box[3],
+                      int n_bonds, const int32_t* bonds_host);
+int oxg_system_destroy(oxg_system* sys);
+/* Work stream for every later call on this system (NULL = legacy default stream). */
+int oxg_system_set_stream(oxg_system* sys, void* stream);
+/* Host <-> device state transfer. Any pointer may be NULL to skip that array.
+ * vel[4*N] = vx, vy, vz, mass; angmom[4*N] = quaternion conjugate momentum. */
+int oxg_system_set_state(oxg_system* sys, const float* pos_type, const float* quat,
+                         const float* vel, const float* angmom, const float* charge);
+int oxg_system_get_state(oxg_system* sys, float* pos_type, float* quat, float* vel,
+                         float* angmom);
+/* Device pointers of the resident state (4*N floats each; charge N floats). */
+int oxg_system_device_state(oxg_system* sys, float** pos_type, float** quat, float** vel,
+                            float** angmom, float** charge);
+/* Neighbour-list skin (HOOMD Cell nlist buffer, default 0.4). */
+int oxg_system_set_nlist_buffer(oxg_system* sys, double buffer);
+/* Evaluate forces at the current state: pair terms in term_mask plus (if bonded != 0)
+ * the bonded force. Outputs are host arrays (any may be NULL): force/torque 4*N floats,
+ * pair_energy OXG_N_PAIR_TERMS doubles, bonded_energy 3 doubles. */
+int oxg_system_compute(oxg_system* sys, uint32_t term_mask, int bonded,
+                       float* force, float* torque, double* pair_energy,
+                       double* bonded_energy);
+/* Langevin dynamics (velocity Verlet + NO_SQUISH rotation, gamma / gamma_r damping,
+ * kT bath, counter-based RNG keyed by seed, step and particle).
+ * Forces: pair terms in term_mask and the bonded force if bonded != 0. */
+int oxg_system_set_integrator(oxg_system* sys, double dt, double kT, double gamma,
+                              double gamma_r, uint64_t seed, uint32_t term_mask,
+                              int bonded);
+/* Advance nsteps steps. Steps are replayed from a captured CUDA graph. */
+int oxg_system_run(oxg_system* sys, long nsteps);
+/* Per-term energies at the current state (device reduction, FP64) into host arrays. */
+int oxg_system_energies(oxg_system* sys, double* pair_energy, double* bonded_energy);
+/* Counters: index 0 steps run, 1 neighbour-list builds, 2 pair-list entries (short),
+ * 3 pair-list entries (long), 4 kernels launched per step. */
+int oxg_system_stats(oxg_system* sys, int64_t* out, int n);
+
+/* Text of the last error raised on the calling thread (CUDA error string etc.). */
+const char* oxg_last_error(void);
+/* Version / build string of the loaded library. */
+const char* oxg_version(void);
+/* Human-readable text for a status code. */
+const char* oxg_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OXDNA_GB300_H */

@@ -1,0 +1,327 @@
+/*
+ * ref_wrap.cpp - C wrapper around the reference plugin's OWN evaluator and bonded
+ * headers, compiled unchanged from the reference tree by oracle/build_ref.sh into
+ * oracle/_ref/ (never committed). TEST INFRASTRUCTURE ONLY: it pins the C oracle
+ * (oracle/oxdna_oracle.c) and generates the golden fixtures in tests/golden/.
+ *
+ * Built twice: FP64 (HOOMD_HAS_FORCEREAL undefined, ForceReal == Scalar == double:
+ * the reference's upstream-HOOMD arithmetic) and FP32 (HOOMD_HAS_FORCEREAL defined,
+ * ForceReal == float: the reference's mixed-precision GPU arithmetic emulated on the
+ * host, src/MixedPrecisionCompat.h:20-35).
+ *
+ * Each ref_* function converts this project's POD parameter structs into the
+ * reference param_type (same fields) and calls evaluate() / oxdna_bonded_pair().
+ */
+#include <pybind11/pybind11.h>
+
+#include "EvaluatorPairOxDNACoaxStacking.h"
+#include "EvaluatorPairOxDNACrossStacking.h"
+#include "EvaluatorPairOxDNADebye.h"
+#include "EvaluatorPairOxDNAExcVol.h"
+#include "EvaluatorPairOxDNAHBond.h"
+#include "EvaluatorPairOxDNAHBondCross.h"
+#include "OxDNABondedKernel.h"
+
+#include "../include/oxdna_gb300.h"
+
+using namespace hoomd;
+using namespace hoomd::md;
+
+namespace
+{
+vec3<Scalar> v3(const double* a) { return vec3<Scalar>(a[0], a[1], a[2]); }
+void cp(Scalar* dst, const double* src, int n)
+{
+    for (int k = 0; k < n; ++k)
+        dst[k] = src[k];
+}
+
+OxDNAExcVolParams cvt(const oxg_excvol_params* s)
+{
+    OxDNAExcVolParams p;
+    p.eps = s->eps;
+    p.base_site = v3(s->base_site);
+    p.back_site = v3(s->back_site);
+    cp(p.sigma, s->sigma, 4);
+    cp(p.rstar, s->rstar, 4);
+    cp(p.b, s->b, 4);
+    cp(p.rc, s->rc, 4);
+    return p;
+}
+OxDNAHBondParams cvt(const oxg_hbond_params* s)
+{
+    OxDNAHBondParams p;
+    p.eps = s->eps;
+    p.shift_factor = s->shift_factor;
+    p.base_site = v3(s->base_site);
+    p.f1_a = s->f1[0];
+    p.f1_r0 = s->f1[1];
+    p.f1_rlow = s->f1[2];
+    p.f1_rhigh = s->f1[3];
+    p.f1_rclow = s->f1[4];
+    p.f1_rchigh = s->f1[5];
+    p.f1_blow = s->f1[6];
+    p.f1_bhigh = s->f1[7];
+    cp(p.t1, s->t1, 5);
+    cp(p.t23, s->t23, 5);
+    cp(p.t4, s->t4, 5);
+    cp(p.t78, s->t78, 5);
+    return p;
+}
+OxDNACrossStackingParams cvt(const oxg_cross_params* s)
+{
+    OxDNACrossStackingParams p;
+    p.base_site = v3(s->base_site);
+    p.f2_k = s->f2[0];
+    p.f2_r0 = s->f2[1];
+    p.f2_rc = s->f2[2];
+    p.f2_rlow = s->f2[3];
+    p.f2_rhigh = s->f2[4];
+    p.f2_rclow = s->f2[5];
+    p.f2_rchigh = s->f2[6];
+    p.f2_blow = s->f2[7];
+    p.f2_bhigh = s->f2[8];
+    cp(p.t1, s->t1, 5);
+    cp(p.t23, s->t23, 5);
+    cp(p.t4, s->t4, 5);
+    cp(p.t78, s->t78, 5);
+    p.t4_enabled = s->t4_enabled != 0;
+    return p;
+}
+OxDNAHBondCrossParams cvt(const oxg_hbondcross_params* s)
+{
+    OxDNAHBondCrossParams p;
+    p.base_site = v3(s->base_site);
+    p.eps = s->eps;
+    p.shift_factor = s->shift_factor;
+    p.f1_a = s->f1[0];
+    p.f1_r0 = s->f1[1];
+    p.f1_rlow = s->f1[2];
+    p.f1_rhigh = s->f1[3];
+    p.f1_rclow = s->f1[4];
+    p.f1_rchigh = s->f1[5];
+    p.f1_blow = s->f1[6];
+    p.f1_bhigh = s->f1[7];
+    cp(p.hb_t1, s->hb_t1, 5);
+    cp(p.hb_t23, s->hb_t23, 5);
+    cp(p.hb_t4, s->hb_t4, 5);
+    cp(p.hb_t78, s->hb_t78, 5);
+    p.f2_k = s->f2[0];
+    p.f2_r0 = s->f2[1];
+    p.f2_rc = s->f2[2];
+    p.f2_rlow = s->f2[3];
+    p.f2_rhigh = s->f2[4];
+    p.f2_rclow = s->f2[5];
+    p.f2_rchigh = s->f2[6];
+    p.f2_blow = s->f2[7];
+    p.f2_bhigh = s->f2[8];
+    cp(p.cs_t1, s->cs_t1, 5);
+    cp(p.cs_t23, s->cs_t23, 5);
+    cp(p.cs_t4, s->cs_t4, 5);
+    cp(p.cs_t78, s->cs_t78, 5);
+    return p;
+}
+OxDNACoaxStackingParams cvt(const oxg_coax_params* s)
+{
+    OxDNACoaxStackingParams p;
+    p.stack_site = v3(s->stack_site);
+    p.stack_back_ref = v3(s->stack_back_ref);
+    p.gamma = s->gamma;
+    p.f2_k = s->f2[0];
+    p.f2_r0 = s->f2[1];
+    p.f2_rc = s->f2[2];
+    p.f2_rlow = s->f2[3];
+    p.f2_rhigh = s->f2[4];
+    p.f2_rclow = s->f2[5];
+    p.f2_rchigh = s->f2[6];
+    p.f2_blow = s->f2[7];
+    p.f2_bhigh = s->f2[8];
+    cp(p.t1, s->t1, 5);
+    cp(p.t4, s->t4, 5);
+    cp(p.t56, s->t56, 5);
+    cp(p.phi3, s->phi3, 4);
+    cp(p.phi4, s->phi4, 4);
+    p.t1_mode = s->t1_mode;
+    p.t1_sa = s->t1_sa;
+    p.t1_sb = s->t1_sb;
+    p.phi3_enabled = s->phi3_enabled != 0;
+    p.rna_coax = s->rna_coax != 0;
+    return p;
+}
+OxDNADebyeParams cvt(const oxg_debye_params* s)
+{
+    OxDNADebyeParams p;
+    p.back_site = v3(s->back_site);
+    p.minus_kappa = s->minus_kappa;
+    p.prefactor = s->prefactor;
+    p.b_smooth = s->b_smooth;
+    p.rc = s->rc;
+    p.rhigh = s->rhigh;
+    return p;
+}
+oxdna_bonded_params cvt(const oxg_bonded_params* s)
+{
+    oxdna_bonded_params p;
+    p.eps_backbone = s->eps_backbone;
+    p.r0_backbone = s->r0_backbone;
+    p.delta_backbone = s->delta_backbone;
+    p.delta2 = s->delta2;
+    p.back_site = v3(s->back_site);
+    p.base_site = v3(s->base_site);
+    p.excl_eps = s->excl_eps;
+    cp(p.bx_sigma, s->bx_sigma, 3);
+    cp(p.bx_rstar, s->bx_rstar, 3);
+    cp(p.bx_b, s->bx_b, 3);
+    cp(p.bx_rc, s->bx_rc, 3);
+    p.stacking_enabled = s->stacking_enabled != 0;
+    p.stack_site = v3(s->stack_site);
+    p.stack_back_ref = v3(s->stack_back_ref);
+    p.st_gamma = s->st_gamma;
+    p.st_a = s->st_f1[0];
+    p.st_r0 = s->st_f1[1];
+    p.st_rlow = s->st_f1[2];
+    p.st_rhigh = s->st_f1[3];
+    p.st_rclow = s->st_f1[4];
+    p.st_rchigh = s->st_f1[5];
+    p.st_blow = s->st_f1[6];
+    p.st_bhigh = s->st_f1[7];
+    p.st_shift_factor = s->st_f1[8];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            p.st_eps[i][j] = s->st_eps[i][j];
+    p.t4_a = s->t4[0];
+    p.t4_b = s->t4[1];
+    p.t4_t0 = s->t4[2];
+    p.t4_ts = s->t4[3];
+    p.t4_tc = s->t4[4];
+    p.t5_a = s->t5[0];
+    p.t5_b = s->t5[1];
+    p.t5_t0 = s->t5[2];
+    p.t5_ts = s->t5[3];
+    p.t5_tc = s->t5[4];
+    p.p1_a = s->p1[0];
+    p.p1_b = s->p1[1];
+    p.p1_xc = s->p1[2];
+    p.p1_xs = s->p1[3];
+    p.rna_stacking = s->rna_stacking != 0;
+    p.stack_3_site = v3(s->stack_3_site);
+    p.stack_5_site = v3(s->stack_5_site);
+    p.bbvector_3 = v3(s->bbvector_3);
+    p.bbvector_5 = v3(s->bbvector_5);
+    p.tB1_a = s->tB1[0];
+    p.tB1_b = s->tB1[1];
+    p.tB1_t0 = s->tB1[2];
+    p.tB1_ts = s->tB1[3];
+    p.tB1_tc = s->tB1[4];
+    p.tB2_a = s->tB2[0];
+    p.tB2_b = s->tB2[1];
+    p.tB2_t0 = s->tB2[2];
+    p.tB2_ts = s->tB2[3];
+    p.tB2_tc = s->tB2[4];
+    return p;
+}
+
+template<class Eval, class P>
+int run_eval(const P& p, const double dr[3], const double qi[4], const double qj[4],
+             double rcutsq, double ci, double cj, double f[3], double* e, double ti[3],
+             double tj[3])
+{
+    ForceReal3 d;
+    d.x = ForceReal(dr[0]);
+    d.y = ForceReal(dr[1]);
+    d.z = ForceReal(dr[2]);
+    Scalar4 a = make_scalar4(qi[0], qi[1], qi[2], qi[3]);
+    Scalar4 b = make_scalar4(qj[0], qj[1], qj[2], qj[3]);
+    Eval ev(d, a, b, ForceReal(rcutsq), p);
+    ev.setCharge(ci, cj);
+    ForceReal3 F, Ti, Tj;
+    ForceReal E = 0;
+    bool r = ev.evaluate(F, E, false, Ti, Tj);
+    if (!r) {
+        f[0] = f[1] = f[2] = ti[0] = ti[1] = ti[2] = tj[0] = tj[1] = tj[2] = 0.0;
+        *e = 0.0;
+        return 0;
+    }
+    f[0] = F.x;
+    f[1] = F.y;
+    f[2] = F.z;
+    ti[0] = Ti.x;
+    ti[1] = Ti.y;
+    ti[2] = Ti.z;
+    tj[0] = Tj.x;
+    tj[1] = Tj.y;
+    tj[2] = Tj.z;
+    *e = E;
+    return 1;
+}
+} // namespace
+
+extern "C" {
+
+int ref_is_fp32(void) { return sizeof(ForceReal) == 4; }
+
+int ref_excvol(const oxg_excvol_params* p, const double dr[3], const double qi[4],
+               const double qj[4], double rcutsq, double f[3], double* e, double ti[3],
+               double tj[3])
+{
+    return run_eval<EvaluatorPairOxDNAExcVol>(cvt(p), dr, qi, qj, rcutsq, 1, 1, f, e, ti, tj);
+}
+int ref_hbond(const oxg_hbond_params* p, const double dr[3], const double qi[4],
+              const double qj[4], double rcutsq, double f[3], double* e, double ti[3],
+              double tj[3])
+{
+    return run_eval<EvaluatorPairOxDNAHBond>(cvt(p), dr, qi, qj, rcutsq, 1, 1, f, e, ti, tj);
+}
+int ref_cross(const oxg_cross_params* p, const double dr[3], const double qi[4],
+              const double qj[4], double rcutsq, double f[3], double* e, double ti[3],
+              double tj[3])
+{
+    return run_eval<EvaluatorPairOxDNACrossStacking>(cvt(p), dr, qi, qj, rcutsq, 1, 1, f, e,
+                                                     ti, tj);
+}
+int ref_hbondcross(const oxg_hbondcross_params* p, const double dr[3], const double qi[4],
+                   const double qj[4], double rcutsq, double f[3], double* e, double ti[3],
+                   double tj[3])
+{
+    return run_eval<EvaluatorPairOxDNAHBondCross>(cvt(p), dr, qi, qj, rcutsq, 1, 1, f, e, ti,
+                                                  tj);
+}
+int ref_coax(const oxg_coax_params* p, const double dr[3], const double qi[4],
+             const double qj[4], double rcutsq, double f[3], double* e, double ti[3],
+             double tj[3])
+{
+    return run_eval<EvaluatorPairOxDNACoaxStacking>(cvt(p), dr, qi, qj, rcutsq, 1, 1, f, e,
+                                                    ti, tj);
+}
+int ref_debye(const oxg_debye_params* p, const double dr[3], const double qi[4],
+              const double qj[4], double rcutsq, double ci, double cj, double f[3],
+              double* e, double ti[3], double tj[3])
+{
+    return run_eval<EvaluatorPairOxDNADebye>(cvt(p), dr, qi, qj, rcutsq, ci, cj, f, e, ti, tj);
+}
+void ref_bonded(const oxg_bonded_params* pp, const double Rc[3], const double qA[4],
+                const double qB[4], int typeA, int typeB, double FB[3], double tauA[3],
+                double tauB[3], double e[3], double vir[6])
+{
+    oxdna_bonded_params p = cvt(pp);
+    quat<Scalar> a(make_scalar4(qA[0], qA[1], qA[2], qA[3]));
+    quat<Scalar> b(make_scalar4(qB[0], qB[1], qB[2], qB[3]));
+    oxdna::BondedResult r;
+    oxdna::oxdna_bonded_pair(p, vec3<Scalar>(Rc[0], Rc[1], Rc[2]), a, b, (unsigned)typeA,
+                             (unsigned)typeB, r);
+    FB[0] = r.FB.x;
+    FB[1] = r.FB.y;
+    FB[2] = r.FB.z;
+    tauA[0] = r.tauA.x;
+    tauA[1] = r.tauA.y;
+    tauA[2] = r.tauA.z;
+    tauB[0] = r.tauB.x;
+    tauB[1] = r.tauB.y;
+    tauB[2] = r.tauB.z;
+    e[0] = r.e_fene;
+    e[1] = r.e_bexc;
+    e[2] = r.e_stack;
+    for (int k = 0; k < 6; ++k)
+        vir[k] = r.vir[k];
+}
+} // extern "C"

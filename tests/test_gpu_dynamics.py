@@ -1,0 +1,95 @@
+"""GPU engine at the benchmark sizes: energies against the FP64 oracle on the 8000-nt
+system, size-independent properties (Newton's third law, fused == separate), and the
+Langevin / NO_SQUISH integrator (oracle trajectory, duplex stability, equipartition)."""
+
+import numpy as np
+import pytest
+
+from _util import TOL_GPU
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim(snap, forces, dt=0.0, kT=None, seed=1):
+    from oxdna import runtime
+    sim = runtime.Simulation(device=runtime.device.GPU(), seed=seed)
+    sim.create_state_from_snapshot(snap)
+    methods = [] if kT is None else [runtime.md.methods.Langevin(filter=runtime.filter.All(), kT=kT)]
+    sim.operations.integrator = runtime.md.Integrator(dt=dt, integrate_rotational_dof=True,
+                                                      forces=list(forces), methods=methods)
+    sim.run(0)
+    return sim
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_8000nt_energies_match_oracle(native, oracle, fused):
+    """200 x 20-bp duplexes, box 100 (the headline system): every per-term energy."""
+    from oxdna import io
+    from oxdna.model import dna2
+    s = io.duplex_system(200, 20, 100.0, seed=2)
+    forces, _ = dna2.forces(fused=fused)
+    sim = _sim(io.system_snapshot(s), forces)
+    model = oracle.Model(forces, io.DNA_BASES)
+    r = oracle.forces(model, oracle.System(s["pos"], s["quat"], s["typeid"], s["box"], s["bonds"]))
+    for f in forces[1:]:
+        ref = r["pair_energy"][f._term]
+        assert abs(f.energy - ref) <= TOL_GPU * max(abs(ref), 1e-6), type(f).__name__
+    b = forces[0]
+    for k, v in enumerate((b.fene_energy, b.bonded_excvol_energy, b.stacking_energy)):
+        ref = r["bonded_energy"][k]
+        assert abs(v - ref) <= TOL_GPU * max(abs(ref), 1e-6)
+    # Newton's third law on the summed GPU forces
+    F = sum(sim._force_arrays(f)[0] for f in forces)
+    assert np.linalg.norm(F.sum(axis=0)) < 1e-4 * np.abs(F).max() * np.sqrt(len(F))
+
+
+def test_short_trajectory_tracks_oracle(native, oracle):
+    """Same counter-based RNG on both sides: 20 Langevin steps agree closely."""
+    from oxdna import io
+    from oxdna.model import dna1, dna2
+    s = io.duplex_system(8, 20, 40.0, seed=1)
+    kT = dna1.kT_from_temperature(296.15)
+    forces, _ = dna2.forces()
+    sim = _sim(io.system_snapshot(s), forces, dt=0.003, kT=kT, seed=7)
+    sim.run(20)
+    snap = sim.state.get_snapshot()
+    model = oracle.Model(forces, io.DNA_BASES)
+    o = oracle.System(s["pos"], s["quat"], s["typeid"], s["box"], s["bonds"])
+    n = len(s["pos"])
+    _, vel, am = oracle.langevin(model, o, np.zeros((n, 3)), np.zeros((n, 4)), steps=20, dt=0.003,
+                                 kT=kT, seed=7)
+    d = snap.particles.position - o.pos
+    d -= 40.0 * np.round(d / 40.0)
+    assert np.abs(d).max() < 2e-3
+    assert np.abs(snap.particles.velocity - vel).max() < 2e-2
+    q = snap.particles.orientation
+    assert np.abs(np.abs(np.einsum("ij,ij->i", q, o.quat)) - 1.0).max() < 1e-3
+
+
+def test_duplexes_stay_bound_and_thermalise(native):
+    """pytest/test_oxdna2.py:72-80: HB per nucleotide < -0.15 after 2000 steps; the
+    kinetic temperatures approach kT (equipartition, 3 + 3 degrees of freedom)."""
+    from oxdna import io
+    from oxdna.model import dna1, dna2
+    s = io.duplex_system(8, 20, 40.0, seed=1)
+    kT = dna1.kT_from_temperature(296.15)
+    forces, _ = dna2.forces()
+    sim = _sim(io.system_snapshot(s), forces, dt=0.003, kT=kT, seed=5)
+    sim.run(2000)
+    n = len(s["pos"])
+    snap = sim.state.get_snapshot()
+    assert np.isfinite(snap.particles.position).all()
+    assert forces[2].energy / n < -0.15
+    ke_t, ke_r = [], []
+    for _ in range(20):
+        sim.run(50)
+        p = sim.state.get_snapshot().particles
+        ke_t.append(0.5 * (p.velocity ** 2).sum() / n)
+        q, pm = p.orientation, p.angmom
+        # body angular momentum s = (1/2 conj(q) p).v, unit inertia
+        sv = 0.5 * (q[:, :1] * pm[:, 1:] - pm[:, :1] * q[:, 1:] - np.cross(q[:, 1:], pm[:, 1:]))
+        ke_r.append(0.5 * (sv ** 2).sum() / n)
+    assert abs(np.mean(ke_t) / (1.5 * kT) - 1.0) < 0.1
+    assert abs(np.mean(ke_r) / (1.5 * kT) - 1.0) < 0.1
+    st = sim.native_stats()
+    assert st["nlist_builds"] >= 1 and st["steps"] == 3000

@@ -1,0 +1,115 @@
+"""Host-side logic: parameter dicts, ABI structs, models, builders, library exports."""
+
+import ctypes as C
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+from _util import model_forces
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_hb_complementarity():
+    """pytest/test_hbond.py:27-30."""
+    from oxdna.model import dna1
+    assert dna1.hb_epsilon("A", "T") > 0 and dna1.hb_epsilon("G", "C") > 0
+    for a, b in [("A", "A"), ("A", "G"), ("A", "C"), ("G", "G"), ("G", "T"), ("C", "T")]:
+        assert dna1.hb_epsilon(a, b) == 0.0
+
+
+def test_param_dict_validation():
+    from oxdna.model import dna2
+    nl = dna2.make_neighbor_list()
+    f = dna2.debye_huckel(nl)
+    assert f.params[("T", "A")] == f.params[("A", "T")]  # unordered pair keys
+    with pytest.raises(KeyError):
+        f.params[("A", "A")] = dict(back_site=(0, 0, 0))  # missing 'debye'
+    with pytest.raises(ValueError):
+        f.params[("A", "A")] = dict(back_site=(0, 0), debye=(1, 2, 3, 4, 5))
+    with pytest.raises(KeyError):
+        f.params[("A", "A")] = dict(back_site=(0, 0, 0), debye=(1, 2, 3, 4, 5), bogus=1)
+    c = dna2.coaxial_stacking(nl)
+    assert c.params[("A", "C")]["f5_phi4"] == (0.0,) * 4 and c.params[("A", "C")]["rna_coax"] is False
+    with pytest.raises(ValueError):
+        dna2.ExcludedVolume if False else None
+        from oxdna.forces import ExcludedVolume
+        ExcludedVolume(nl, 2.0, mode="shift")
+
+
+def test_abi_struct_conversion():
+    from oxdna import _abi
+    pair, bonded = model_forces("rna2")
+    p = _abi.cross_from_dict(pair[2].params[("A", "A")])
+    assert p.t4_enabled == 0 and abs(p.f2[0] - 59.9626) < 1e-12
+    b = _abi.bonded_from_dict(bonded.params["backbone"])
+    assert b.stacking_enabled == 1 and b.rna_stacking == 1
+    assert abs(b.delta2 - 0.0625) < 1e-15
+    assert abs(b.stack_5_site[0] - 0.124906078525) < 1e-15
+    # sizes match the C layout (double-aligned, no hidden padding differences)
+    assert C.sizeof(_abi.CoaxParams) == 8 * (3 + 3 + 1 + 9 + 15 + 8) + 4 * 2 + 8 * 2 + 4 * 2
+    assert C.sizeof(_abi.CrossParams) % 8 == 0
+
+
+def test_debye_parameters():
+    """dna2.debye_params at 296.15 K, 0.5 M: lambda 0.50815, rc 2.2867 (SURVEY config 1)."""
+    from oxdna.model import dna2
+    mk, pref, b, rc, rhigh = dna2.debye_params(296.15, 0.5)
+    assert abs(-1.0 / mk - 0.50815) < 1e-4 and abs(rc - 2.2867) < 1e-3
+    assert abs(rhigh - 3 * (-1.0 / mk)) < 1e-12
+
+
+def test_duplex_builder_geometry():
+    """Ideal B-form duplexes: every FENE bond within delta, a1/a3 conventions."""
+    from oxdna import io
+    from oxdna.model import dna2
+    s = io.duplex_system(8, 20, 40.0, seed=1)
+    R = io.quat_to_matrix(s["quat"])
+    back = s["pos"] + np.einsum("nij,j->ni", R, dna2.BACK_SITE)
+    for a, b in s["bonds"]:
+        d = back[b] - back[a]
+        d -= 40.0 * np.round(d / 40.0)
+        assert abs(np.linalg.norm(d) - dna2.FENE_R0) < 0.25
+    assert len(s["pos"]) == 320 and len(s["bonds"]) == 8 * 38
+    # complementary strands: paired bases sum to 3
+    t = s["typeid"][:40]
+    assert all(t[k] + t[39 - k] == 3 for k in range(20))
+
+
+def test_quaternion_roundtrip():
+    from oxdna import io
+    rng = np.random.default_rng(3)
+    q = rng.normal(size=(50, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    R = io.quat_to_matrix(q)
+    q2 = io.orientations_to_quaternions(R[:, :, 0], R[:, :, 2])
+    assert np.allclose(np.abs(np.einsum("ij,ij->i", q, q2)), 1.0, atol=1e-12)
+
+
+def test_replica_sharding():
+    from oxdna import replicas
+    shards = [replicas.shard(103, r, 4) for r in range(4)]
+    assert sorted(np.concatenate(shards).tolist()) == list(range(103))
+    assert max(len(x) for x in shards) - min(len(x) for x in shards) <= 1
+
+
+def _header_functions():
+    src = open(os.path.join(ROOT, "include", "oxdna_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(oxg_\w+)\(", src, re.M)))
+
+
+def test_library_exports_every_header_symbol():
+    """The C-ABI library builds for sm_103a, loads without a GPU and exports every
+    entry point include/oxdna_gb300.h declares (no compute call is made)."""
+    from oxdna import _abi, _build
+    _build.build()
+    L = C.CDLL(_abi.LIB_PATH)
+    names = _header_functions()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(_abi.EXPORTS)
+    assert b"sm_103a" in _abi.lib().oxg_version()
