@@ -232,6 +232,14 @@ def run_ours(args):
     ms = replicas.max_over_ranks(ms, dist)
     steps_per_s = world * args.steps / (ms * 1e-3)
     stats = sim.native_stats()
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": steps_per_s, "unit": "steps/s",
+                              "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                              "quick": True, "clocks": clk.summary()}), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
 
     # --- roofline of the dominant kernel (force evaluation launch set) ---------
     kernel_ms = time_force_kernel(sim, 200, stream)
@@ -253,20 +261,20 @@ def run_ours(args):
 
     # --- end to end through the public API with host buffers ----------------------
     pin = lambda: torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()  # noqa: E731
-    hp, hq, hv, ha = pin(), pin(), pin(), pin()
-    sim.pull_state_arrays(hp, hq, hv, ha)
+    hp, hl, hq, hv, ha = pin(), pin(), pin(), pin(), pin()
+    sim.pull_state_arrays(hp, hl, hq, hv, ha)
     e2e_steps = max(20, min(200, args.steps // 50))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        sim.push_state_arrays(hp, hq, hv, ha)   # H2D: this step's inputs
+        sim.push_state_arrays(hp, hl, hq, hv, ha)   # H2D: this step's inputs
         sim.run(1)
-        sim.pull_state_arrays(hp, hq, hv, ha)   # D2H: this step's result
+        sim.pull_state_arrays(hp, hl, hq, hv, ha)   # D2H: this step's result
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = replicas.max_over_ranks(e2e_s, dist)
     e2e = {"value": world * e2e_steps / e2e_s, "unit": "steps/s",
-           "h2d_bytes_per_step": 4 * 16 * n, "d2h_bytes_per_step": 4 * 16 * n,
+           "h2d_bytes_per_step": 5 * 16 * n, "d2h_bytes_per_step": 5 * 16 * n,
            "path": "Simulation.push_state_arrays -> run(1) -> pull_state_arrays "
                    "(oxg_system_set_state / oxg_system_run / oxg_system_get_state)"}
 
@@ -311,6 +319,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=500)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--quick", action="store_true",
+                    help="resident timing only (no fused / e2e / CPU legs); for profiling runs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

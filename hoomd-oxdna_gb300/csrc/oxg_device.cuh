@@ -14,21 +14,25 @@
 
 #include "oxg_params.h"
 
+// Physics functions are host+device so that the exact FP32 arithmetic of the kernels
+// can also be exercised by the host-side numerics tests (tests/native/).
+#define OXG_HD __host__ __device__ __forceinline__
+
 namespace oxg {
 
 constexpr float kPi = 3.14159265358979323846f;
 
 // ------------------------------------------------------------------ float3 algebra
-__device__ __forceinline__ float3 mk3(float x, float y, float z) { return make_float3(x, y, z); }
-__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 operator-(float3 a) { return mk3(-a.x, -a.y, -a.z); }
-__device__ __forceinline__ float3 operator*(float3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float3 operator*(float s, float3 a) { return mk3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ void operator+=(float3& a, float3 b) { a.x += b.x; a.y += b.y; a.z += b.z; }
-__device__ __forceinline__ void operator-=(float3& a, float3 b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; }
-__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ float3 cross(float3 a, float3 b)
+OXG_HD float3 mk3(float x, float y, float z) { return make_float3(x, y, z); }
+OXG_HD float3 operator+(float3 a, float3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+OXG_HD float3 operator-(float3 a, float3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+OXG_HD float3 operator-(float3 a) { return mk3(-a.x, -a.y, -a.z); }
+OXG_HD float3 operator*(float3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+OXG_HD float3 operator*(float s, float3 a) { return mk3(a.x * s, a.y * s, a.z * s); }
+OXG_HD void operator+=(float3& a, float3 b) { a.x += b.x; a.y += b.y; a.z += b.z; }
+OXG_HD void operator-=(float3& a, float3 b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; }
+OXG_HD float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+OXG_HD float3 cross(float3 a, float3 b)
 {
     return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
@@ -39,7 +43,7 @@ __device__ __forceinline__ float3 cross(float3 a, float3 b)
 struct Frame {
     float3 a1, a2, a3;
 };
-__device__ __forceinline__ Frame quat_frame(float4 q)
+OXG_HD Frame quat_frame(float4 q)
 {
     const float s = q.x, x = q.y, y = q.z, z = q.w;
     const float ss = s * s, xx = x * x, yy = y * y, zz = z * z;
@@ -50,25 +54,29 @@ __device__ __forceinline__ Frame quat_frame(float4 q)
     f.a3 = mk3(2.f * (xz + sy), 2.f * (yz - sx), ss - xx - yy + zz);
     return f;
 }
-__device__ __forceinline__ float3 body_to_lab(const Frame& f, const float* s)
+OXG_HD float3 body_to_lab(const Frame& f, const float* s)
 {
     return f.a1 * s[0] + f.a2 * s[1] + f.a3 * s[2];
 }
 
 // ---------------------------------------------------------------- numerics (L1)
 // src/OxDNANumerics.h:194-198
-__device__ __forceinline__ float clamp_cos(float c) { return c > 1.f ? 1.f : (c < -1.f ? -1.f : c); }
+OXG_HD float clamp_cos(float c) { return c > 1.f ? 1.f : (c < -1.f ? -1.f : c); }
 
 // src/OxDNANumerics.h:201-215
-__device__ __forceinline__ float f4_angle(float t, const F4& p)
+OXG_HD float f4_angle(float t, const F4& p)
 {
     const float d = fabsf(t - p.t0);
     if (!(d < p.tc)) return 0.f;
     if (d > p.ts) return p.b * (p.tc - d) * (p.tc - d);
     return 1.f - p.a * d * d;
 }
-// (d f4 / d theta) / sin(theta); src/OxDNANumerics.h:218-244
-__device__ __forceinline__ float f4_dsin(float t, const F4& p)
+// (d f4 / d theta) / sin(theta); src/OxDNANumerics.h:218-244, with sin(theta) passed in.
+// Callers compute sin(theta) once per angle and pass sin(pi - theta) = sin(theta) and
+// sin(2 pi - theta) = -sin(theta) for the reflected branches: the same quantities as
+// the reference, without the FP32 rounding of pi and 2 pi that otherwise dominates
+// near theta = 0 or pi, where the two reflected 1/sin terms cancel.
+OXG_HD float f4_dsin(float t, float st, const F4& p)
 {
     float d = t - p.t0;
     float m = 1.f;
@@ -77,28 +85,27 @@ __device__ __forceinline__ float f4_dsin(float t, const F4& p)
         m = -1.f;
     }
     if (!(d < p.tc)) return 0.f;
-    const float st = sinf(t);
     if (d > p.ts) return m * 2.f * p.b * (d - p.tc) / st;
     if (st * st > 1e-8f) return -m * 2.f * p.a * d / st;
     return -m * 2.f * p.a;
 }
 // cos(theta) in the open support interval of f4 (or, symmetrised, of f4(pi - theta))
 template <bool SYM>
-__device__ __forceinline__ bool f4_support(float c, const F4& p)
+OXG_HD bool f4_support(float c, const F4& p)
 {
     bool in = (c > p.cmin) & (c < p.cmax);
     if (SYM) in |= (-c > p.cmin) & (-c < p.cmax);
     return in;
 }
 // src/OxDNANumerics.h:261-290 (f = (A, B, XC, XS))
-__device__ __forceinline__ float f5_val(float f, const float* p)
+OXG_HD float f5_val(float f, const float* p)
 {
     if (!(f > p[2])) return 0.f;
     if (f < p[3]) return p[1] * (p[2] - f) * (p[2] - f);
     if (f < 0.f) return 1.f - p[0] * f * f;
     return 1.f;
 }
-__device__ __forceinline__ float f5_deriv(float f, const float* p)
+OXG_HD float f5_deriv(float f, const float* p)
 {
     if (!(f > p[2])) return 0.f;
     if (f < p[3]) return 2.f * p[1] * (f - p[2]);
@@ -106,7 +113,7 @@ __device__ __forceinline__ float f5_deriv(float f, const float* p)
     return 0.f;
 }
 // f1 Morse radial value and derivative, one exp (src/OxDNANumerics.h:114-155)
-__device__ __forceinline__ void f1_eval(float r, const float* f1, float eps, float shift,
+OXG_HD void f1_eval(float r, const float* f1, float eps, float shift,
                                         float& val, float& der)
 {
     const float a = f1[0], r0 = f1[1], rlow = f1[2], rhigh = f1[3], rclow = f1[4],
@@ -129,7 +136,7 @@ __device__ __forceinline__ void f1_eval(float r, const float* f1, float eps, flo
     }
 }
 // f2 harmonic radial value and derivative (src/OxDNANumerics.h:158-192)
-__device__ __forceinline__ void f2_eval(float r, const float* f2, float& val, float& der)
+OXG_HD void f2_eval(float r, const float* f2, float& val, float& der)
 {
     const float k = f2[0], r0 = f2[1], rc = f2[2], rlow = f2[3], rhigh = f2[4], rclow = f2[5],
                 rchigh = f2[6], blow = f2[7], bhigh = f2[8];
@@ -150,7 +157,7 @@ __device__ __forceinline__ void f2_eval(float r, const float* f2, float& val, fl
 }
 // Smoothed LJ core; returns E and the force on the second site (r = site_q - site_p).
 // src/OxDNANumerics.h:76-107 (sigma2 = sigma^2, rstar2 = r*^2, rc2 = rc^2).
-__device__ __forceinline__ float repulsive_lj(float3 r, float eps, float sigma2, float rstar2,
+OXG_HD float repulsive_lj(float3 r, float eps, float sigma2, float rstar2,
                                               float b, float rc, float rc2, float3& fq)
 {
     const float rsq = dot(r, r);
@@ -177,7 +184,7 @@ struct PairAcc {
 
 // ------------------------------------------------------------- excluded volume
 // src/EvaluatorPairOxDNAExcVol.h:107-149. rc = r_j - r_i (= -dr).
-__device__ __forceinline__ float excvol_term(const DExcVol& p, float3 rc, const Frame& fi,
+OXG_HD float excvol_term(const DExcVol& p, float3 rc, const Frame& fi,
                                              const Frame& fj, PairAcc& acc)
 {
     const float3 back_i = body_to_lab(fi, p.back), base_i = body_to_lab(fi, p.base);
@@ -203,17 +210,35 @@ struct Ang {
     float val, dsin;
 };
 // one acos per angle; the reflected branch reuses pi - theta (src/OxDNABaseBase.h:52-67)
-template <bool SYM>
-__device__ __forceinline__ Ang angular(float cost, const F4& t, float sign)
+// theta and sin(theta) of the angle whose cosine is c = u . v (u, v unit vectors).
+// acos(c) as in the reference; for parameter sets flagged `precise` and |c| > 0.9 the
+// same angle from atan2(|u x v|, c), which keeps full FP32 accuracy near 0 and pi.
+OXG_HD void angle_of(float c, float3 u, float3 v, const F4& t, float& th, float& st)
 {
-    const float th = acosf(clamp_cos(cost));
+    if (t.precise != 0.f && fabsf(c) > 0.9f) {
+        const float3 w = cross(u, v);
+        st = sqrtf(dot(w, w));
+        th = atan2f(st, c);
+    } else {
+        th = acosf(clamp_cos(c));
+        st = sinf(th);
+    }
+}
+
+// f4 value and torque coefficient of one angle; the reflected branch (SYM) reuses
+// pi - theta and sin(pi - theta) = sin(theta) (src/OxDNABaseBase.h:52-67).
+template <bool SYM>
+OXG_HD Ang angular(float cost, float3 u, float3 v, const F4& t, float sign)
+{
+    float th, st;
+    angle_of(cost, u, v, t, th, st);
     Ang a;
     a.val = f4_angle(th, t);
-    float d = f4_dsin(th, t);
+    float d = f4_dsin(th, st, t);
     if (SYM) {
         const float thn = kPi - th;
         a.val += f4_angle(thn, t);
-        d -= f4_dsin(thn, t);
+        d -= f4_dsin(thn, st, t);
     }
     a.dsin = sign * d;
     return a;
@@ -224,7 +249,7 @@ struct BBGeom {
     float3 rdir, base_i, base_j;
     float rmod, c1, c2, c3, c4, c7, c8;
 };
-__device__ __forceinline__ bool bb_geometry(float3 rc, const Frame& fi, const Frame& fj,
+OXG_HD bool bb_geometry(float3 rc, const Frame& fi, const Frame& fj,
                                             const float* base, BBGeom& g)
 {
     g.base_i = body_to_lab(fi, base);
@@ -247,18 +272,18 @@ __device__ __forceinline__ bool bb_geometry(float3 rc, const Frame& fi, const Fr
 struct RadialF1 {  // hydrogen bonding: Morse with per-pair eps
     const float* f1;
     float eps, shift;
-    __device__ __forceinline__ bool support(float r) const { return eps != 0.f && r > f1[4] && r < f1[5]; }
-    __device__ __forceinline__ void eval(float r, float& v, float& d) const { f1_eval(r, f1, eps, shift, v, d); }
+    OXG_HD bool support(float r) const { return eps != 0.f && r > f1[4] && r < f1[5]; }
+    OXG_HD void eval(float r, float& v, float& d) const { f1_eval(r, f1, eps, shift, v, d); }
 };
 struct RadialF2 {  // cross-stacking: harmonic
     const float* f2;
-    __device__ __forceinline__ bool support(float r) const { return f2[0] != 0.f && r > f2[5] && r < f2[6]; }
-    __device__ __forceinline__ void eval(float r, float& v, float& d) const { f2_eval(r, f2, v, d); }
+    OXG_HD bool support(float r) const { return f2[0] != 0.f && r > f2[5] && r < f2[6]; }
+    OXG_HD void eval(float r, float& v, float& d) const { f2_eval(r, f2, v, d); }
 };
 
 // One BASE-BASE term; adds force on i and both torques. src/OxDNABaseBase.h:128-219.
 template <bool SYM, class Radial>
-__device__ __forceinline__ float bb_term(const BBGeom& g, const Frame& fi, const Frame& fj,
+OXG_HD float bb_term(const BBGeom& g, const Frame& fi, const Frame& fj,
                                          const F4& t1, const F4& t23, const F4& t4,
                                          const F4& t78, bool inc_t4, const Radial& R,
                                          PairAcc& acc)
@@ -268,14 +293,15 @@ __device__ __forceinline__ float bb_term(const BBGeom& g, const Frame& fi, const
           f4_support<false>(g.c3, t23) && (!inc_t4 || f4_support<SYM>(g.c4, t4)) &&
           f4_support<SYM>(g.c7, t78) && f4_support<SYM>(g.c8, t78)))
         return 0.f;
-    const Ang A1 = angular<false>(g.c1, t1, -1.f);
-    const Ang A2 = angular<false>(g.c2, t23, -1.f);
-    const Ang A3 = angular<false>(g.c3, t23, 1.f);
+    // cosines with the vector pairs they are dot products of (src/OxDNABaseBase.h:113-118)
+    const Ang A1 = angular<false>(g.c1, -fi.a1, fj.a1, t1, -1.f);
+    const Ang A2 = angular<false>(g.c2, -fj.a1, g.rdir, t23, -1.f);
+    const Ang A3 = angular<false>(g.c3, fi.a1, g.rdir, t23, 1.f);
     Ang A4;
-    if (inc_t4) A4 = angular<SYM>(g.c4, t4, 1.f);
+    if (inc_t4) A4 = angular<SYM>(g.c4, fi.a3, fj.a3, t4, 1.f);
     else { A4.val = 1.f; A4.dsin = 0.f; }
-    const Ang A7 = angular<SYM>(g.c7, t78, -1.f);
-    const Ang A8 = angular<SYM>(g.c8, t78, 1.f);
+    const Ang A7 = angular<SYM>(g.c7, -fj.a3, g.rdir, t78, -1.f);
+    const Ang A8 = angular<SYM>(g.c8, fi.a3, g.rdir, t78, 1.f);
     float rv, rd;
     R.eval(g.rmod, rv, rd);
     const float prod = A1.val * A2.val * A3.val * A4.val * A7.val * A8.val;
@@ -318,7 +344,7 @@ __device__ __forceinline__ float bb_term(const BBGeom& g, const Frame& fi, const
 
 // ------------------------------------------------------------ coaxial stacking
 // src/EvaluatorPairOxDNACoaxStacking.h:134-372. rc = r_j - r_i.
-__device__ __forceinline__ float coax_term(const DCoax& p, float3 rc, const Frame& fi,
+OXG_HD float coax_term(const DCoax& p, float3 rc, const Frame& fi,
                                            const Frame& fj, PairAcc& acc)
 {
     const float3 stack_i = body_to_lab(fi, p.stack), stack_j = body_to_lab(fj, p.stack);
@@ -341,9 +367,11 @@ __device__ __forceinline__ float coax_term(const DCoax& p, float3 rc, const Fram
 
     float f2v, f2D;
     f2_eval(rsm, p.f2, f2v, f2D);
-    const float th1 = acosf(clamp_cos(c1));
-    const float th4 = acosf(clamp_cos(c4));
-    const float th5 = acosf(clamp_cos(c5)), th6 = acosf(clamp_cos(c6));
+    float th1, th4, th5, th6, s1, s4, s5, s6;
+    angle_of(c1, -a1, b1, p.t1, th1, s1);
+    angle_of(c4, a3, b3, p.t4, th4, s4);
+    angle_of(c5, a3, rsd, p.t56, th5, s5);
+    angle_of(c6, -b3, rsd, p.t56, th6, s6);
     const float th5n = kPi - th5, th6n = kPi - th6;
     float f4t1 = f4_angle(th1, p.t1);
     if (p.t1_mode == 0) f4t1 += f4_angle(2.f * kPi - th1, p.t1);
@@ -364,16 +392,15 @@ __device__ __forceinline__ float coax_term(const DCoax& p, float3 rc, const Fram
     const float energy = f2v * f4t1 * f4t4 * f4t5 * f4t6 * phif;
     if (energy == 0.f) return 0.f;
 
-    float f4t1D = -f4_dsin(th1, p.t1);
-    if (p.t1_mode == 0) f4t1D += -f4_dsin(2.f * kPi - th1, p.t1);
+    float f4t1D = -f4_dsin(th1, s1, p.t1);
+    if (p.t1_mode == 0) f4t1D += -f4_dsin(2.f * kPi - th1, -s1, p.t1);  // sin(2pi - t) = -sin t
     else if (th1 > p.t1_sb) {
-        const float s1 = sinf(th1);
         const float hd = (s1 * s1 > 1e-8f) ? 2.f * p.t1_sa * (th1 - p.t1_sb) / s1 : 2.f * p.t1_sa;
         f4t1D += -hd;
     }
-    const float f4t4D = f4_dsin(th4, p.t4);
-    const float f4t5D = f4_dsin(th5, p.t56) - f4_dsin(th5n, p.t56);
-    const float f4t6D = -f4_dsin(th6, p.t56) + f4_dsin(th6n, p.t56);
+    const float f4t4D = f4_dsin(th4, s4, p.t4);
+    const float f4t5D = f4_dsin(th5, s5, p.t56) - f4_dsin(th5n, s5, p.t56);
+    const float f4t6D = -f4_dsin(th6, s6, p.t56) + f4_dsin(th6n, s6, p.t56);
 
     float3 fq = rsd * (-(f2D * f4t1 * f4t4 * f4t5 * f4t6 * phif));
     float3 tp = mk3(0.f, 0.f, 0.f), tq = mk3(0.f, 0.f, 0.f);
@@ -454,7 +481,7 @@ __device__ __forceinline__ float coax_term(const DCoax& p, float3 rc, const Fram
 
 // ------------------------------------------------------------------ Debye-Hueckel
 // src/EvaluatorPairOxDNADebye.h:244-303. rc = r_j - r_i.
-__device__ __forceinline__ float debye_term(const DDebye& p, float3 rc, const Frame& fi,
+OXG_HD float debye_term(const DDebye& p, float3 rc, const Frame& fi,
                                             const Frame& fj, float ci, float cj, PairAcc& acc)
 {
     const float3 back_i = body_to_lab(fi, p.back), back_j = body_to_lab(fj, p.back);
@@ -489,7 +516,7 @@ struct BondAcc {
     double e[3];  // fene, bexc, stack
     float vir[6];
 };
-__device__ __forceinline__ void vir_acc(float* v, float3 r, float3 f)
+OXG_HD void vir_acc(float* v, float3 r, float3 f)
 {
     // src/OxDNABondedKernel.h:48-58
     v[0] += 0.5f * r.x * f.x;
@@ -501,7 +528,7 @@ __device__ __forceinline__ void vir_acc(float* v, float3 r, float3 f)
 }
 
 // DNA stacking, oxDNA p = B, q = A (src/OxDNABondedKernel.h:69-231). Rc = r_B - r_A.
-__device__ __forceinline__ float stacking_dna(const DBonded& p, float3 Rc, const Frame& fA,
+OXG_HD float stacking_dna(const DBonded& p, float3 Rc, const Frame& fA,
                                               const Frame& fB, int tA, int tB, BondAcc& acc)
 {
     const float3 a1 = fB.a1, a2 = fB.a2, a3 = fB.a3;
@@ -531,7 +558,8 @@ __device__ __forceinline__ float stacking_dna(const DBonded& p, float3 Rc, const
     const float f5p1 = f5_val(cp1, p.p1), f5p2 = f5_val(cp2, p.p1);
     const float es = f1 * f4t4 * f4t5 * f4t6 * f5p1 * f5p2;
     if (es == 0.f) return 0.f;
-    const float f4t4D = f4_dsin(th4, p.t4), f4t5D = f4_dsin(th5, p.t5), f4t6D = f4_dsin(th6, p.t5);
+    const float f4t4D = f4_dsin(th4, sinf(th4), p.t4), f4t5D = f4_dsin(th5, sinf(th5), p.t5),
+                f4t6D = f4_dsin(th6, sinf(th6), p.t5);
     const float f5p1D = f5_deriv(cp1, p.p1), f5p2D = f5_deriv(cp2, p.p1);
 
     float3 force = rsd * (-(f1D * f4t4 * f4t5 * f4t6 * f5p1 * f5p2));
@@ -595,7 +623,7 @@ __device__ __forceinline__ float stacking_dna(const DBonded& p, float3 Rc, const
 }
 
 // RNA stacking, p = B, q = A (src/OxDNABondedKernel.h:238-353).
-__device__ __forceinline__ float stacking_rna(const DBonded& p, float3 Rc, const Frame& fA,
+OXG_HD float stacking_rna(const DBonded& p, float3 Rc, const Frame& fA,
                                               const Frame& fB, int tA, int tB, BondAcc& acc)
 {
     const float3 a2 = fB.a2, a3 = fB.a3, b2 = fA.a2, b3 = fA.a3;
@@ -628,8 +656,8 @@ __device__ __forceinline__ float stacking_rna(const DBonded& p, float3 Rc, const
     const float f5p1 = f5_val(cp1, p.p1), f5p2 = f5_val(cp2, p.p1);
     const float es = f1 * f4t5 * f4t6 * f4B1 * f4B2 * f5p1 * f5p2;
     if (es == 0.f) return 0.f;
-    const float f4t5D = f4_dsin(th5, p.t5), f4t6D = f4_dsin(th6, p.t5);
-    const float f4B1D = f4_dsin(thB1, p.tB1), f4B2D = f4_dsin(thB2, p.tB2);
+    const float f4t5D = f4_dsin(th5, sinf(th5), p.t5), f4t6D = f4_dsin(th6, sinf(th6), p.t5);
+    const float f4B1D = f4_dsin(thB1, sinf(thB1), p.tB1), f4B2D = f4_dsin(thB2, sinf(thB2), p.tB2);
     const float f5p1D = f5_deriv(cp1, p.p1), f5p2D = f5_deriv(cp2, p.p1);
 
     float3 force = rsd * (-(f1D * f4t5 * f4t6 * f4B1 * f4B2 * f5p1 * f5p2));
@@ -663,7 +691,7 @@ __device__ __forceinline__ float stacking_rna(const DBonded& p, float3 Rc, const
 // One bond (A, B = A's 5' neighbour): FENE in FP64, bonded excluded volume and
 // stacking in FP32. src/OxDNABondedKernel.h:357-431. Rc = r_B - r_A in double;
 // qA, qB the quaternions (promoted to double for FENE).
-__device__ __forceinline__ void bonded_pair(const DBonded& p, double3 Rc, double4_32a qA,
+OXG_HD void bonded_pair(const DBonded& p, double3 Rc, double4_32a qA,
                                             double4_32a qB, int tA, int tB, BondAcc& acc)
 {
     acc.fB = mk3(0.f, 0.f, 0.f);

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/oxdna_gb300.h"
+#include "oxg_convert.h"
 #include "oxg_kernels.cuh"
 
 using namespace oxg;
@@ -53,163 +54,6 @@ void dfree(T*& p)
 {
     if (p) cudaFree(p);
     p = nullptr;
-}
-
-// f4 set (A, B, T0, TS, TC) -> device form with the cosine support interval, widened
-// by 1e-5 so the zero-factor test stays conservative under FP32 rounding.
-F4 mk_f4(const double* t)
-{
-    F4 f;
-    f.a = (float)t[0];
-    f.b = (float)t[1];
-    f.t0 = (float)t[2];
-    f.ts = (float)t[3];
-    f.tc = (float)t[4];
-    const double lo = t[2] - t[4], hi = t[2] + t[4];
-    f.cmax = lo > 0.0 ? (float)(std::cos(lo) + 1e-5) : 2.f;
-    f.cmin = hi < M_PI ? (float)(std::cos(hi) - 1e-5) : -2.f;
-    f.pad = 0.f;
-    return f;
-}
-void cp3(float* d, const double* s) { d[0] = (float)s[0]; d[1] = (float)s[1]; d[2] = (float)s[2]; }
-void cpn(float* d, const double* s, int n) { for (int k = 0; k < n; ++k) d[k] = (float)s[k]; }
-float sq(double r) { return (float)(r * r); }
-
-DExcVol to_dev(const oxg_excvol_params& s, double rcut)
-{
-    DExcVol d;
-    std::memset(&d, 0, sizeof(d));
-    d.eps = (float)s.eps;
-    cp3(d.base, s.base_site);
-    cp3(d.back, s.back_site);
-    for (int k = 0; k < 4; ++k) {
-        d.sigma2[k] = sq(s.sigma[k]);
-        d.rstar2[k] = sq(s.rstar[k]);
-        d.b[k] = (float)s.b[k];
-        d.rc[k] = (float)s.rc[k];
-        d.rc2[k] = sq(s.rc[k]);
-    }
-    d.rcutsq = sq(rcut);
-    return d;
-}
-DHBond to_dev(const oxg_hbond_params& s, double rcut)
-{
-    DHBond d;
-    std::memset(&d, 0, sizeof(d));
-    d.shift_factor = (float)s.shift_factor;
-    cp3(d.base, s.base_site);
-    cpn(d.f1, s.f1, 8);
-    d.t1 = mk_f4(s.t1);
-    d.t23 = mk_f4(s.t23);
-    d.t4 = mk_f4(s.t4);
-    d.t78 = mk_f4(s.t78);
-    d.rcutsq = sq(rcut);
-    return d;
-}
-DCross to_dev(const oxg_cross_params& s, double rcut)
-{
-    DCross d;
-    std::memset(&d, 0, sizeof(d));
-    cp3(d.base, s.base_site);
-    cpn(d.f2, s.f2, 9);
-    d.t1 = mk_f4(s.t1);
-    d.t23 = mk_f4(s.t23);
-    d.t4 = mk_f4(s.t4);
-    d.t78 = mk_f4(s.t78);
-    d.rcutsq = sq(rcut);
-    d.t4_enabled = s.t4_enabled;
-    return d;
-}
-DHBCross to_dev(const oxg_hbondcross_params& s, double rcut)
-{
-    DHBCross d;
-    std::memset(&d, 0, sizeof(d));
-    cp3(d.base, s.base_site);
-    d.shift_factor = (float)s.shift_factor;
-    cpn(d.f1, s.f1, 8);
-    d.hb_t1 = mk_f4(s.hb_t1);
-    d.hb_t23 = mk_f4(s.hb_t23);
-    d.hb_t4 = mk_f4(s.hb_t4);
-    d.hb_t78 = mk_f4(s.hb_t78);
-    cpn(d.f2, s.f2, 9);
-    d.cs_t1 = mk_f4(s.cs_t1);
-    d.cs_t23 = mk_f4(s.cs_t23);
-    d.cs_t4 = mk_f4(s.cs_t4);
-    d.cs_t78 = mk_f4(s.cs_t78);
-    d.rcutsq = sq(rcut);
-    return d;
-}
-DCoax to_dev(const oxg_coax_params& s, double rcut)
-{
-    DCoax d;
-    std::memset(&d, 0, sizeof(d));
-    cp3(d.stack, s.stack_site);
-    cp3(d.bref, s.stack_back_ref);
-    d.gamma = (float)s.gamma;
-    cpn(d.f2, s.f2, 9);
-    d.t1 = mk_f4(s.t1);
-    d.t4 = mk_f4(s.t4);
-    d.t56 = mk_f4(s.t56);
-    cpn(d.phi3, s.phi3, 4);
-    cpn(d.phi4, s.phi4, 4);
-    d.t1_mode = s.t1_mode;
-    d.phi3_enabled = s.phi3_enabled;
-    d.rna_coax = s.rna_coax;
-    d.t1_sa = (float)s.t1_sa;
-    d.t1_sb = (float)s.t1_sb;
-    d.rcutsq = sq(rcut);
-    return d;
-}
-DDebye to_dev(const oxg_debye_params& s, double rcut)
-{
-    DDebye d;
-    std::memset(&d, 0, sizeof(d));
-    cp3(d.back, s.back_site);
-    d.minus_kappa = (float)s.minus_kappa;
-    d.prefactor = (float)s.prefactor;
-    d.b_smooth = (float)s.b_smooth;
-    d.rc = (float)s.rc;
-    d.rhigh = (float)s.rhigh;
-    d.rcutsq = sq(rcut);
-    return d;
-}
-DBonded to_dev(const oxg_bonded_params& s)
-{
-    DBonded d;
-    std::memset(&d, 0, sizeof(d));
-    d.eps_backbone = s.eps_backbone;
-    d.r0_backbone = s.r0_backbone;
-    d.delta_backbone = s.delta_backbone;
-    d.delta2 = s.delta2;
-    for (int k = 0; k < 3; ++k) d.back_site[k] = s.back_site[k];
-    cp3(d.back, s.back_site);
-    cp3(d.base, s.base_site);
-    d.excl_eps = (float)s.excl_eps;
-    for (int k = 0; k < 3; ++k) {
-        d.bx_sigma2[k] = sq(s.bx_sigma[k]);
-        d.bx_rstar2[k] = sq(s.bx_rstar[k]);
-        d.bx_b[k] = (float)s.bx_b[k];
-        d.bx_rc[k] = (float)s.bx_rc[k];
-    }
-    d.stacking_enabled = s.stacking_enabled;
-    d.rna_stacking = s.rna_stacking;
-    cp3(d.stack, s.stack_site);
-    cp3(d.bref, s.stack_back_ref);
-    d.gamma = (float)s.st_gamma;
-    cpn(d.f1, s.st_f1, 8);
-    d.shift_factor = (float)s.st_f1[8];
-    for (int i = 0; i < kMaxTypes; ++i)
-        for (int j = 0; j < kMaxTypes; ++j) d.st_eps[i][j] = (float)s.st_eps[i][j];
-    d.t4 = mk_f4(s.t4);
-    d.t5 = mk_f4(s.t5);
-    d.tB1 = mk_f4(s.tB1);
-    d.tB2 = mk_f4(s.tB2);
-    cpn(d.p1, s.p1, 4);
-    cp3(d.stack3, s.stack_3_site);
-    cp3(d.stack5, s.stack_5_site);
-    cp3(d.bbv3, s.bbvector_3);
-    cp3(d.bbv5, s.bbvector_5);
-    return d;
 }
 
 size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -365,7 +209,7 @@ int build_block(oxg_context* c)
     return OXG_OK;
 }
 
-const ParamHeader& header(const oxg_context* c) { return *reinterpret_cast<const ParamHeader*>(c->block.data()); }
+
 
 template <class POD>
 int set_pair(oxg_context* c, TermTable<POD>& tt, int ti, int tj, const POD* p, double rcut)
@@ -573,7 +417,7 @@ struct oxg_system {
     float3 L, invL;
     cudaStream_t stream = nullptr;
     // resident state
-    float4 *pos = nullptr, *quat = nullptr, *vel = nullptr, *angmom = nullptr;
+    float4 *pos = nullptr, *pos_lo = nullptr, *quat = nullptr, *vel = nullptr, *angmom = nullptr;
     float4 *accel = nullptr, *tnet = nullptr, *pos_ref = nullptr;
     float4 *force = nullptr, *torque = nullptr;
     float* charge = nullptr;
@@ -603,7 +447,8 @@ struct oxg_system {
     bool integ_set = false;
     unsigned long long timestep = 0;
     // checkpoint of the state at the start of a graph chunk
-    float4 *ck_pos = nullptr, *ck_quat = nullptr, *ck_vel = nullptr, *ck_angmom = nullptr;
+    float4 *ck_pos = nullptr, *ck_pos_lo = nullptr, *ck_quat = nullptr, *ck_vel = nullptr,
+           *ck_angmom = nullptr;
     // graph
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
@@ -714,6 +559,7 @@ ForceArgs force_args(oxg_system* s, uint32_t mask, int bonded)
     a.N = s->N;
     a.n_bonds = s->n_bonds;
     a.pos = s->pos;
+    a.pos_lo = s->pos_lo;
     a.quat = s->quat;
     a.charge = s->charge;
     a.bonds = s->bonds;
@@ -721,6 +567,8 @@ ForceArgs force_args(oxg_system* s, uint32_t mask, int bonded)
     a.pairs_long = s->pairs_long;
     a.st = s->st;
     a.st_rw = s->st;
+    a.cap_short = (int)std::min<long long>(s->cap_short, 0x7fffffff);
+    a.cap_long = (int)std::min<long long>(s->cap_long, 0x7fffffff);
     a.L = s->L;
     a.invL = s->invL;
     a.force = s->force;
@@ -735,6 +583,7 @@ IntegArgs integ_args(oxg_system* s)
     IntegArgs a;
     a.N = s->N;
     a.pos = s->pos;
+    a.pos_lo = s->pos_lo;
     a.quat = s->quat;
     a.vel = s->vel;
     a.angmom = s->angmom;
@@ -866,7 +715,8 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
         oxg_system_destroy(s);
         return code;
     };
-    if ((rc = dalloc(&s->pos, N)) || (rc = dalloc(&s->quat, N)) || (rc = dalloc(&s->vel, N)) ||
+    if ((rc = dalloc(&s->pos, N)) || (rc = dalloc(&s->pos_lo, N)) || (rc = dalloc(&s->ck_pos_lo, N)) ||
+        (rc = dalloc(&s->quat, N)) || (rc = dalloc(&s->vel, N)) ||
         (rc = dalloc(&s->angmom, N)) || (rc = dalloc(&s->accel, N)) || (rc = dalloc(&s->tnet, N)) ||
         (rc = dalloc(&s->pos_ref, N)) || (rc = dalloc(&s->force, N)) || (rc = dalloc(&s->torque, N)) ||
         (rc = dalloc(&s->charge, N)) || (rc = dalloc(&s->bonds, std::max(1, n_bonds))) ||
@@ -888,6 +738,7 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
     cudaMemcpy(s->vel, v.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
     cudaMemcpy(s->quat, q.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
     cudaMemcpy(s->pos, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->pos_lo, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
     cudaMemcpy(s->angmom, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
     cudaMemcpy(s->accel, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
     cudaMemcpy(s->tnet, z.data(), sizeof(float4) * N, cudaMemcpyHostToDevice);
@@ -902,7 +753,7 @@ int oxg_system_destroy(oxg_system* s)
 {
     if (!s) return OXG_OK;
     if (s->graph) cudaGraphExecDestroy(s->graph);
-    dfree(s->pos); dfree(s->quat); dfree(s->vel); dfree(s->angmom); dfree(s->accel);
+    dfree(s->pos); dfree(s->pos_lo); dfree(s->ck_pos_lo); dfree(s->quat); dfree(s->vel); dfree(s->angmom); dfree(s->accel);
     dfree(s->tnet); dfree(s->pos_ref); dfree(s->force); dfree(s->torque); dfree(s->charge);
     dfree(s->bonds); dfree(s->excl); dfree(s->st); dfree(s->energy);
     dfree(s->cell_count); dfree(s->cell_list); dfree(s->pairs_short); dfree(s->pairs_long);
@@ -920,12 +771,24 @@ int oxg_system_set_stream(oxg_system* s, void* stream)
     return OXG_OK;
 }
 
-int oxg_system_set_state(oxg_system* s, const float* pos_type, const float* quat, const float* vel,
-                         const float* angmom, const float* charge)
+int oxg_system_set_state(oxg_system* s, const float* pos_type, const float* pos_lo,
+                         const float* quat, const float* vel, const float* angmom,
+                         const float* charge)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
     const size_t b4 = sizeof(float4) * s->N;
-    if (pos_type) OXG_CUDA(cudaMemcpyAsync(s->pos, pos_type, b4, cudaMemcpyHostToDevice, s->stream));
+    if (pos_type) {
+        for (int i = 0; i < s->N; ++i) {
+            int t;
+            std::memcpy(&t, pos_type + 4 * (size_t)i + 3, sizeof(int));
+            if (t < 0 || t >= s->ctx->n_types)
+                return set_err(OXG_ERR_BAD_INDEX, "particle " + std::to_string(i) + " has type " +
+                                                      std::to_string(t) + " outside the context's types");
+        }
+        OXG_CUDA(cudaMemcpyAsync(s->pos, pos_type, b4, cudaMemcpyHostToDevice, s->stream));
+        if (!pos_lo) OXG_CUDA(cudaMemsetAsync(s->pos_lo, 0, b4, s->stream));
+    }
+    if (pos_lo) OXG_CUDA(cudaMemcpyAsync(s->pos_lo, pos_lo, b4, cudaMemcpyHostToDevice, s->stream));
     if (quat) OXG_CUDA(cudaMemcpyAsync(s->quat, quat, b4, cudaMemcpyHostToDevice, s->stream));
     if (vel) OXG_CUDA(cudaMemcpyAsync(s->vel, vel, b4, cudaMemcpyHostToDevice, s->stream));
     if (angmom) OXG_CUDA(cudaMemcpyAsync(s->angmom, angmom, b4, cudaMemcpyHostToDevice, s->stream));
@@ -934,11 +797,13 @@ int oxg_system_set_state(oxg_system* s, const float* pos_type, const float* quat
     return OXG_OK;
 }
 
-int oxg_system_get_state(oxg_system* s, float* pos_type, float* quat, float* vel, float* angmom)
+int oxg_system_get_state(oxg_system* s, float* pos_type, float* pos_lo, float* quat, float* vel,
+                         float* angmom)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
     const size_t b4 = sizeof(float4) * s->N;
     if (pos_type) OXG_CUDA(cudaMemcpyAsync(pos_type, s->pos, b4, cudaMemcpyDeviceToHost, s->stream));
+    if (pos_lo) OXG_CUDA(cudaMemcpyAsync(pos_lo, s->pos_lo, b4, cudaMemcpyDeviceToHost, s->stream));
     if (quat) OXG_CUDA(cudaMemcpyAsync(quat, s->quat, b4, cudaMemcpyDeviceToHost, s->stream));
     if (vel) OXG_CUDA(cudaMemcpyAsync(vel, s->vel, b4, cudaMemcpyDeviceToHost, s->stream));
     if (angmom) OXG_CUDA(cudaMemcpyAsync(angmom, s->angmom, b4, cudaMemcpyDeviceToHost, s->stream));
@@ -946,11 +811,12 @@ int oxg_system_get_state(oxg_system* s, float* pos_type, float* quat, float* vel
     return OXG_OK;
 }
 
-int oxg_system_device_state(oxg_system* s, float** pos_type, float** quat, float** vel,
-                            float** angmom, float** charge)
+int oxg_system_device_state(oxg_system* s, float** pos_type, float** pos_lo, float** quat,
+                            float** vel, float** angmom, float** charge)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
     if (pos_type) *pos_type = reinterpret_cast<float*>(s->pos);
+    if (pos_lo) *pos_lo = reinterpret_cast<float*>(s->pos_lo);
     if (quat) *quat = reinterpret_cast<float*>(s->quat);
     if (vel) *vel = reinterpret_cast<float*>(s->vel);
     if (angmom) *angmom = reinterpret_cast<float*>(s->angmom);
@@ -1077,9 +943,9 @@ static int build_graph(oxg_system* s, int steps)
 static int checkpoint(oxg_system* s, bool restore)
 {
     const size_t b4 = sizeof(float4) * s->N;
-    float4* src[4] = {s->pos, s->quat, s->vel, s->angmom};
-    float4* dst[4] = {s->ck_pos, s->ck_quat, s->ck_vel, s->ck_angmom};
-    for (int k = 0; k < 4; ++k) {
+    float4* src[5] = {s->pos, s->pos_lo, s->quat, s->vel, s->angmom};
+    float4* dst[5] = {s->ck_pos, s->ck_pos_lo, s->ck_quat, s->ck_vel, s->ck_angmom};
+    for (int k = 0; k < 5; ++k) {
         if (restore) OXG_CUDA(cudaMemcpyAsync(src[k], dst[k], b4, cudaMemcpyDeviceToDevice, s->stream));
         else OXG_CUDA(cudaMemcpyAsync(dst[k], src[k], b4, cudaMemcpyDeviceToDevice, s->stream));
     }

@@ -169,6 +169,14 @@ __device__ __forceinline__ float3 min_image(float3 d, float3 L, float3 invL)
 
 __device__ __forceinline__ int type_of(float4 p) { return __float_as_int(p.w); }
 
+// r_i - r_j from double-float positions (hi + lo): the high parts of nearby particles
+// subtract almost exactly, so dr keeps ~1e-7 absolute precision in a 230-sigma box.
+__device__ __forceinline__ float3 pair_delta(float4 hi_i, float4 lo_i, float4 hi_j, float4 lo_j)
+{
+    return mk3((hi_i.x - hi_j.x) + (lo_i.x - lo_j.x), (hi_i.y - hi_j.y) + (lo_i.y - lo_j.y),
+               (hi_i.z - hi_j.z) + (lo_i.z - lo_j.z));
+}
+
 // ----------------------------------------------------------- engine force kernel
 struct ForceArgs {
     const unsigned char* params;
@@ -177,7 +185,8 @@ struct ForceArgs {
     int bonded;           // evaluate bonds
     int N;
     int n_bonds;
-    const float4* pos;    // x, y, z, type bits
+    const float4* pos;    // x, y, z (high parts), type bits
+    const float4* pos_lo; // low parts of x, y, z (double-float positions)
     const float4* quat;
     const float* charge;
     const int4* bonds;    // A, B, type, unused
@@ -185,6 +194,7 @@ struct ForceArgs {
     const int2* pairs_long;
     const DevStatus* st;  // n_short / n_long
     DevStatus* st_rw;     // rebuild flag cleared here
+    int cap_short, cap_long;  // list capacities (counts past them were not stored)
     float3 L, invL;
     float4* force;        // accumulated (pre-zeroed)
     float4* torque;
@@ -200,8 +210,11 @@ __global__ void __launch_bounds__(256) k_forces(ForceArgs a)
         a.st_rw->rebuild = 0u;
         a.st_rw->gen += 1u;
     }
-    const int n_short = (int)a.st->n_short;
-    const int n_long = (int)a.st->n_long;
+    // after an overflow the counters exceed the capacities; only stored pairs are read
+    const int n_short = (int)min(a.st->n_short, (uint32_t)a.cap_short);
+    const int n_long = (int)min(a.st->n_long, (uint32_t)a.cap_long);
+    const int n_types = P.h().n_types;
+    bool bad_type = false;
     const int n_bonds = a.bonded ? a.n_bonds : 0;
     const int total = n_short + n_bonds + n_long;
     double eacc[kNTerms + 3];
@@ -215,9 +228,14 @@ __global__ void __launch_bounds__(256) k_forces(ForceArgs a)
             const int2 pr = is_short ? a.pairs_short[w] : a.pairs_long[w - n_short - n_bonds];
             const int i = pr.x, j = pr.y;
             const float4 pi = a.pos[i], pj = a.pos[j];
-            const float3 dr = min_image(mk3(pi.x - pj.x, pi.y - pj.y, pi.z - pj.z), a.L, a.invL);
+            const float3 dr = min_image(pair_delta(pi, a.pos_lo[i], pj, a.pos_lo[j]), a.L, a.invL);
             const float rsq = dot(dr, dr);
-            const int pidx = type_of(pi) * kMaxTypes + type_of(pj);
+            const int ti = type_of(pi), tj = type_of(pj);
+            if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
+                bad_type = true;
+                continue;
+            }
+            const int pidx = ti * kMaxTypes + tj;
             PairAcc acc;
             acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
             float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -243,8 +261,12 @@ __global__ void __launch_bounds__(256) k_forces(ForceArgs a)
             const int4 bd = a.bonds[w - n_short];
             const int A = bd.x, B = bd.y;
             const float4 pA = a.pos[A], pB = a.pos[B];
-            const float3 Rcf = min_image(mk3(pB.x - pA.x, pB.y - pA.y, pB.z - pA.z), a.L, a.invL);
+            const float3 Rcf = min_image(pair_delta(pB, a.pos_lo[B], pA, a.pos_lo[A]), a.L, a.invL);
             const float4 qA = a.quat[A], qB = a.quat[B];
+            if ((unsigned)type_of(pA) >= (unsigned)n_types || (unsigned)type_of(pB) >= (unsigned)n_types) {
+                bad_type = true;
+                continue;
+            }
             BondAcc acc;
             bonded_pair(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
                         make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
@@ -270,6 +292,7 @@ __global__ void __launch_bounds__(256) k_forces(ForceArgs a)
             if (lane == 0 && s != 0.0) atomicAdd(a.energy + t, s);
         }
     }
+    if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
 }
 
 // --------------------------------------------------- drop-in: HOOMD full nlist
@@ -303,6 +326,7 @@ __global__ void __launch_bounds__(256) k_pairs_hoomd(HoomdPairArgs a)
     const double4_32a qid = a.quat[i];
     const float4 qi = make_float4((float)qid.x, (float)qid.y, (float)qid.z, (float)qid.w);
     const int ti = (int)(__double_as_longlong(pi.w) & 0xffffffffLL);
+    const int n_types = P.h().n_types;
     const float ci = a.charge ? (float)a.charge[i] : 1.f;
     const int nn = (int)a.n_neigh[i];
     const unsigned long long head = a.head_list[i];
@@ -327,6 +351,10 @@ __global__ void __launch_bounds__(256) k_pairs_hoomd(HoomdPairArgs a)
         const double4_32a qjd = a.quat[j];
         const float4 qj = make_float4((float)qjd.x, (float)qjd.y, (float)qjd.z, (float)qjd.w);
         const int tj = (int)(__double_as_longlong(pj.w) & 0xffffffffLL);
+        if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
+            bad = true;
+            continue;
+        }
         const float cj = a.charge ? (float)a.charge[j] : 1.f;
         PairAcc acc;
         acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
@@ -409,17 +437,21 @@ __global__ void __launch_bounds__(256) k_bonds_dropin(BondDropinArgs a)
     bool bad = false;
     if (b < a.n_bonds) {
         const int A = a.bonds[3 * b], B = a.bonds[3 * b + 1], bt = a.bonds[3 * b + 2];
-        const int nbt = P.h().n_bond_types;
-        if (A < 0 || B < 0 || A >= a.N || B >= a.N || bt < 0 || bt >= nbt) {
-            bad = true;
-        } else {
-            const double4_32a pA = a.pos[A], pB = a.pos[B];
+        bad = A < 0 || B < 0 || A >= a.N || B >= a.N || bt < 0 || bt >= P.h().n_bond_types;
+        double4_32a pA, pB;
+        int tA = 0, tB = 0;
+        if (!bad) {
+            pA = a.pos[A];
+            pB = a.pos[B];
+            tA = (int)(__double_as_longlong(pA.w) & 0xffffffffLL);
+            tB = (int)(__double_as_longlong(pB.w) & 0xffffffffLL);
+            bad = (unsigned)tA >= (unsigned)P.h().n_types || (unsigned)tB >= (unsigned)P.h().n_types;
+        }
+        if (!bad) {
             double dx = pB.x - pA.x, dy = pB.y - pA.y, dz = pB.z - pA.z;
             dx -= a.L.x * rint(dx / a.L.x);
             dy -= a.L.y * rint(dy / a.L.y);
             dz -= a.L.z * rint(dz / a.L.z);
-            const int tA = (int)(__double_as_longlong(pA.w) & 0xffffffffLL);
-            const int tB = (int)(__double_as_longlong(pB.w) & 0xffffffffLL);
             BondAcc acc;
             bonded_pair(P.bonded(bt), make_double3(dx, dy, dz), a.quat[A], a.quat[B], tA, tB, acc);
             const float eh = (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2]));
@@ -618,7 +650,8 @@ __device__ __forceinline__ void philox4x32(uint32_t c[4], uint32_t k0, uint32_t 
 
 struct IntegArgs {
     int N;
-    float4* pos;       // x, y, z, type
+    float4* pos;       // x, y, z (high parts), type
+    float4* pos_lo;    // low parts
     float4* quat;
     float4* vel;       // vx, vy, vz, mass
     float4* angmom;
@@ -677,15 +710,22 @@ __global__ void k_step_one(IntegArgs a)
         float4 v = a.vel[i];
         const float4 ac = a.accel[i];
         float4 x = a.pos[i];
+        const float4 xl = a.pos_lo[i];
         v.x += 0.5f * a.dt * ac.x;
         v.y += 0.5f * a.dt * ac.y;
         v.z += 0.5f * a.dt * ac.z;
-        x.x += a.dt * v.x;
-        x.y += a.dt * v.y;
-        x.z += a.dt * v.z;
-        x.x -= a.L.x * rintf(x.x * a.invL.x);
-        x.y -= a.L.y * rintf(x.y * a.invL.y);
-        x.z -= a.L.z * rintf(x.z * a.invL.z);
+        // position update in double (hi + lo), then split back into two floats
+        double X = (double)x.x + (double)xl.x + (double)a.dt * v.x;
+        double Y = (double)x.y + (double)xl.y + (double)a.dt * v.y;
+        double Z = (double)x.z + (double)xl.z + (double)a.dt * v.z;
+        X -= (double)a.L.x * rint(X / (double)a.L.x);
+        Y -= (double)a.L.y * rint(Y / (double)a.L.y);
+        Z -= (double)a.L.z * rint(Z / (double)a.L.z);
+        x.x = (float)X;
+        x.y = (float)Y;
+        x.z = (float)Z;
+        a.pos_lo[i] = make_float4((float)(X - (double)x.x), (float)(Y - (double)x.y),
+                                  (float)(Z - (double)x.z), 0.f);
         float4 q = a.quat[i], p = a.angmom[i];
         const float4 tn = a.tnet[i];
         const float3 tb = rot_conj(q, mk3(tn.x, tn.y, tn.z));

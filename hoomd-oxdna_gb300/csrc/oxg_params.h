@@ -18,8 +18,11 @@ constexpr int kMaxBondTypes = 4;
 // f4 angular modulation (A, B, T0, TS, TC) plus the open interval (cmin, cmax) of
 // cos(theta) on which f4(theta) != 0, i.e. |theta - T0| < TC
 // (src/OxDNANumerics.h:201-215). Used to skip acos for pairs whose energy is 0.
+// `precise` is 1 when the support reaches theta = 0 or pi while T0 is away from them:
+// there f4 has a non-zero slope where acos of an FP32 cosine cannot resolve the angle,
+// so the kernels take the angle from atan2(|u x v|, u . v) instead.
 struct F4 {
-    float a, b, t0, ts, tc, cmin, cmax, pad;
+    float a, b, t0, ts, tc, cmin, cmax, precise;
 };
 
 struct DExcVol {  // src/EvaluatorPairOxDNAExcVol.h:30-39

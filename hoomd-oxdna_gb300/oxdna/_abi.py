@@ -281,10 +281,10 @@ def lib():
         "oxg_system_create": ([C.POINTER(vp), vp, i32, fp, i32, C.POINTER(C.c_int32)], i32),
         "oxg_system_destroy": ([vp], i32),
         "oxg_system_set_stream": ([vp, vp], i32),
-        "oxg_system_set_state": ([vp, vp, vp, vp, vp, vp], i32),
-        "oxg_system_get_state": ([vp, vp, vp, vp, vp], i32),
+        "oxg_system_set_state": ([vp, vp, vp, vp, vp, vp, vp], i32),
+        "oxg_system_get_state": ([vp, vp, vp, vp, vp, vp], i32),
         "oxg_system_device_state": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
-                                     C.POINTER(vp), C.POINTER(vp)], i32),
+                                     C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)], i32),
         "oxg_system_set_nlist_buffer": ([vp, f64], i32),
         "oxg_system_compute": ([vp, u32, i32, vp, vp, vp, vp], i32),
         "oxg_system_set_integrator": ([vp, f64, f64, f64, f64, C.c_uint64, u32, i32], i32),

@@ -311,27 +311,30 @@ class Simulation:
                 1 if self._bonded else 0), "oxg_system_set_integrator")
         self._attached = True
 
-    def push_state_arrays(self, pos_type, quat, vel, angmom):
+    def push_state_arrays(self, pos_type, pos_lo, quat, vel, angmom):
         """Copy host float32 (N, 4) arrays (pinned or not) into the device state."""
         L = _abi.lib()
         ptr = lambda a: C.c_void_p(a.ctypes.data) if a is not None else None  # noqa: E731
-        _abi.check(L.oxg_system_set_state(self._sys, ptr(pos_type), ptr(quat), ptr(vel),
-                                          ptr(angmom), None), "oxg_system_set_state")
+        _abi.check(L.oxg_system_set_state(self._sys, ptr(pos_type), ptr(pos_lo), ptr(quat),
+                                          ptr(vel), ptr(angmom), None), "oxg_system_set_state")
 
-    def pull_state_arrays(self, pos_type, quat, vel, angmom):
+    def pull_state_arrays(self, pos_type, pos_lo, quat, vel, angmom):
         """Copy the device state into host float32 (N, 4) arrays."""
         L = _abi.lib()
         ptr = lambda a: C.c_void_p(a.ctypes.data) if a is not None else None  # noqa: E731
-        _abi.check(L.oxg_system_get_state(self._sys, ptr(pos_type), ptr(quat), ptr(vel),
-                                          ptr(angmom)), "oxg_system_get_state")
+        _abi.check(L.oxg_system_get_state(self._sys, ptr(pos_type), ptr(pos_lo), ptr(quat),
+                                          ptr(vel), ptr(angmom)), "oxg_system_get_state")
 
     def _push_state(self):
         L = _abi.lib()
         p = self._snap.particles
         n = p.N
         pos = np.zeros((n, 4), np.float32)
-        pos[:, :3] = p.position
+        x = np.asarray(p.position, np.float64)
+        pos[:, :3] = x
         pos[:, 3] = np.asarray(p.typeid, np.int32).view(np.float32)
+        lo = np.zeros((n, 4), np.float32)
+        lo[:, :3] = x - pos[:, :3].astype(np.float64)
         vel = np.zeros((n, 4), np.float32)
         vel[:, :3] = p.velocity
         vel[:, 3] = p.mass
@@ -339,9 +342,10 @@ class Simulation:
         am = _f32(p.angmom)
         ch = _f32(p.charge)
         vp = C.c_void_p
-        _abi.check(L.oxg_system_set_state(self._sys, vp(pos.ctypes.data), vp(q.ctypes.data),
-                                          vp(vel.ctypes.data), vp(am.ctypes.data),
-                                          vp(ch.ctypes.data)), "oxg_system_set_state")
+        _abi.check(L.oxg_system_set_state(self._sys, vp(pos.ctypes.data), vp(lo.ctypes.data),
+                                          vp(q.ctypes.data), vp(vel.ctypes.data),
+                                          vp(am.ctypes.data), vp(ch.ctypes.data)),
+                   "oxg_system_set_state")
 
     def _pull_snapshot(self):
         import copy
@@ -351,13 +355,15 @@ class Simulation:
         L = _abi.lib()
         n = snap.particles.N
         pos = np.zeros((n, 4), np.float32)
+        lo = np.zeros((n, 4), np.float32)
         q = np.zeros((n, 4), np.float32)
         vel = np.zeros((n, 4), np.float32)
         am = np.zeros((n, 4), np.float32)
         vp = C.c_void_p
-        _abi.check(L.oxg_system_get_state(self._sys, vp(pos.ctypes.data), vp(q.ctypes.data),
-                                          vp(vel.ctypes.data), vp(am.ctypes.data)), "get_state")
-        snap.particles.position[:] = pos[:, :3]
+        _abi.check(L.oxg_system_get_state(self._sys, vp(pos.ctypes.data), vp(lo.ctypes.data),
+                                          vp(q.ctypes.data), vp(vel.ctypes.data),
+                                          vp(am.ctypes.data)), "get_state")
+        snap.particles.position[:] = pos[:, :3].astype(np.float64) + lo[:, :3]
         snap.particles.orientation[:] = q
         snap.particles.velocity[:] = vel[:, :3]
         snap.particles.angmom[:] = am

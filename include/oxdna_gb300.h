@@ -234,14 +234,17 @@ int oxg_system_destroy(oxg_system* sys);
 /* Work stream for every later call on this system (NULL = legacy default stream). */
 int oxg_system_set_stream(oxg_system* sys, void* stream);
 /* Host <-> device state transfer. Any pointer may be NULL to skip that array.
+ * Positions are double-float: x = pos_type.xyz + pos_lo.xyz (pos_lo[4*N], .w unused;
+ * NULL when setting = zero), which keeps ~1e-7 absolute precision in large boxes.
  * vel[4*N] = vx, vy, vz, mass; angmom[4*N] = quaternion conjugate momentum. */
-int oxg_system_set_state(oxg_system* sys, const float* pos_type, const float* quat,
-                         const float* vel, const float* angmom, const float* charge);
-int oxg_system_get_state(oxg_system* sys, float* pos_type, float* quat, float* vel,
-                         float* angmom);
+int oxg_system_set_state(oxg_system* sys, const float* pos_type, const float* pos_lo,
+                         const float* quat, const float* vel, const float* angmom,
+                         const float* charge);
+int oxg_system_get_state(oxg_system* sys, float* pos_type, float* pos_lo, float* quat,
+                         float* vel, float* angmom);
 /* Device pointers of the resident state (4*N floats each; charge N floats). */
-int oxg_system_device_state(oxg_system* sys, float** pos_type, float** quat, float** vel,
-                            float** angmom, float** charge);
+int oxg_system_device_state(oxg_system* sys, float** pos_type, float** pos_lo, float** quat,
+                            float** vel, float** angmom, float** charge);
 /* Neighbour-list skin (HOOMD Cell nlist buffer, default 0.4). */
 int oxg_system_set_nlist_buffer(oxg_system* sys, double buffer);
 /* Evaluate forces at the current state: pair terms in term_mask plus (if bonded != 0)
