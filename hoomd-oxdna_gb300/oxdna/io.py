@@ -246,12 +246,24 @@ def pack_molecules(molecules, box_len, rng, min_dist=1.5, max_tries=2000):
     orientation in a periodic cube without any inter-molecule COM pair closer than
     min_dist. Returns the concatenated system arrays."""
     L = float(box_len)
-    cell = max(min_dist, 1e-3)
-    ncell = max(1, int(L // cell))
-    grid = {}
+    ncell = max(1, int(L // max(min_dist, 1e-3)))
+    cap = 64
+    # occupancy grid: per cell up to `cap` placed positions (NaN = empty)
+    grid = np.full((ncell, ncell, ncell, cap, 3), np.nan)
+    count = np.zeros((ncell, ncell, ncell), dtype=np.int64)
+    offs = np.array([(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)])
 
-    def cell_of(p):
-        return tuple(((np.floor((p + L / 2) / L * ncell)).astype(int)) % ncell)
+    def cells(p):
+        return (np.floor((p + L / 2) / L * ncell).astype(np.int64)) % ncell
+
+    def overlaps(p):
+        ci = cells(p)
+        nb = (ci[:, None, :] + offs[None, :, :]) % ncell          # (n, 27, 3)
+        cand = grid[nb[..., 0], nb[..., 1], nb[..., 2]]           # (n, 27, cap, 3)
+        d = p[:, None, None, :] - cand
+        d -= L * np.round(d / L)
+        r2 = np.einsum("...k,...k->...", d, d)
+        return bool(np.any(r2 < min_dist * min_dist))            # NaN compares False
 
     out_pos, out_a1, out_a3, out_t, out_b, out_ends, out_mol = [], [], [], [], [], [], []
     offset = 0
@@ -263,34 +275,17 @@ def pack_molecules(molecules, box_len, rng, min_dist=1.5, max_tries=2000):
             c = (rng.random(3) - 0.5) * L
             p = centred @ R.T + c
             p = p - L * np.round(p / L)
-            ok = True
-            for x in p:
-                ci = cell_of(x)
-                for dx in (-1, 0, 1):
-                    for dy in (-1, 0, 1):
-                        for dz in (-1, 0, 1):
-                            key = ((ci[0] + dx) % ncell, (ci[1] + dy) % ncell, (ci[2] + dz) % ncell)
-                            for y in grid.get(key, ()):
-                                d = x - y
-                                d -= L * np.round(d / L)
-                                if d @ d < min_dist * min_dist:
-                                    ok = False
-                                    break
-                            if not ok:
-                                break
-                        if not ok:
-                            break
-                    if not ok:
-                        break
-                if not ok:
-                    break
-            if ok:
+            if not overlaps(p):
                 placed = True
                 break
         if not placed:
             raise RuntimeError(f"could not place molecule {mid} without overlap")
-        for x in p:
-            grid.setdefault(cell_of(x), []).append(x)
+        for x, ci in zip(p, cells(p)):
+            k = count[ci[0], ci[1], ci[2]]
+            if k >= cap:
+                raise RuntimeError("placement grid cell overflow")
+            grid[ci[0], ci[1], ci[2], k] = x
+            count[ci[0], ci[1], ci[2]] = k + 1
         out_pos.append(p)
         out_a1.append(a1 @ R.T)
         out_a3.append(a3 @ R.T)
