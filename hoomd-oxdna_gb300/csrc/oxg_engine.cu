@@ -148,14 +148,14 @@ bool add_term(const oxg_context* c, const TermTable<POD>& tt, int tid, ParamHead
     return true;
 }
 
-int build_block(oxg_context* c)
+// Host image of a context's FP32 parameter block (header, term structs, bonded).
+int assemble_block(const oxg_context* c, std::vector<unsigned char>& blk)
 {
-    if (!c->dirty) return OXG_OK;
     ParamHeader H;
     std::memset(&H, 0, sizeof(H));
     H.n_types = c->n_types;
     H.n_bond_types = c->n_bond_types;
-    std::vector<unsigned char> blk(align16(sizeof(ParamHeader)), 0);
+    blk.assign(align16(sizeof(ParamHeader)), 0);
     float rmax2 = 0.f, rshort2 = 0.f;
     bool ok = add_term<oxg_excvol_params, DExcVol>(c, c->excvol, kExcVol, H, blk, rmax2, rshort2, true) &&
               add_term<oxg_hbond_params, DHBond>(c, c->hbond, kHBond, H, blk, rmax2, rshort2, true) &&
@@ -196,6 +196,15 @@ int build_block(oxg_context* c)
     std::memcpy(blk.data(), &H, sizeof(H));
     if (blk.size() > (size_t)kParamBlockMax)
         return set_err(OXG_ERR_CAPACITY, "parameter block larger than the shared-memory budget");
+    return OXG_OK;
+}
+
+int build_block(oxg_context* c)
+{
+    if (!c->dirty) return OXG_OK;
+    std::vector<unsigned char> blk;
+    const int arc = assemble_block(c, blk);
+    if (arc) return arc;
     if ((int)blk.size() > c->block_bytes) {
         dfree(c->d_block);
         int rc = dalloc(&c->d_block, kParamBlockMax);
@@ -1055,3 +1064,249 @@ int oxg_system_stats(oxg_system* s, int64_t* out, int n)
 }
 
 }  // extern "C"
+
+// =================================================================== allocation-free
+// oxg_pair_forces_noalloc: the system engine's nonbonded evaluation (cell list, split
+// pair lists, fused force kernel) for callers that cannot allocate GPU memory. All of
+// its scratch (parameter block, status, zero low-order positions, exclusions, cells,
+// pair lists) lives in one file-scope device array of fixed size; every GPU that loads
+// this library holds it until the process exits. The entry point calls no cudaMalloc,
+// cudaFree or other allocating routine: it only copies into and launches on that array.
+#include <mutex>
+
+namespace {
+
+constexpr int kNaMaxParticles = OXG_NOALLOC_MAX_PARTICLES;
+constexpr int kNaMaxCellsDim = 20;  // larger boxes get larger (still >= r_list) cells
+constexpr int kNaMaxCells = kNaMaxCellsDim * kNaMaxCellsDim * kNaMaxCellsDim;
+constexpr int kNaCellCap = 64;
+constexpr long long kNaShortCap = 32LL * kNaMaxParticles;
+constexpr long long kNaLongCap = 48LL * kNaMaxParticles;
+constexpr uint32_t kStExclOverflow = 16u;  // a particle with more than 4 bonds
+
+constexpr size_t na_align(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kNaOffParams = 0;
+constexpr size_t kNaOffStatus = na_align(kNaOffParams + kParamBlockMax);
+constexpr size_t kNaOffEnergy = na_align(kNaOffStatus + sizeof(DevStatus));
+constexpr size_t kNaOffPosLo = na_align(kNaOffEnergy + 16 * sizeof(double));
+constexpr size_t kNaOffPosRef = na_align(kNaOffPosLo + sizeof(float4) * kNaMaxParticles);
+constexpr size_t kNaOffExcl = na_align(kNaOffPosRef + sizeof(float4) * kNaMaxParticles);
+constexpr size_t kNaOffCellCount = na_align(kNaOffExcl + sizeof(int4) * kNaMaxParticles);
+constexpr size_t kNaOffCellList = na_align(kNaOffCellCount + sizeof(uint32_t) * 2 * kNaMaxCells);
+constexpr size_t kNaOffShort = na_align(kNaOffCellList + sizeof(int) * (size_t)kNaMaxCells * kNaCellCap);
+constexpr size_t kNaOffLong = na_align(kNaOffShort + sizeof(int2) * kNaShortCap);
+constexpr size_t kNaBytes = na_align(kNaOffLong + sizeof(int2) * kNaLongCap);  // ~7.8 MB
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+namespace {
+
+std::mutex g_na_mutex;
+void* g_na_ptr[256];  // device address of g_noalloc_scratch, per device ordinal
+
+// Set-up, once per device with that device current: the symbol's device address.
+int noalloc_scratch(unsigned char** out)
+{
+    int dev = 0;
+    OXG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return set_err(OXG_ERR_INVALID_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return set_err(OXG_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_na_ptr[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_na_ptr[dev]);
+    return OXG_OK;
+}
+
+// Clear everything the evaluation expects to start at zero (or empty) for this call.
+__global__ void k_noalloc_prepare(int N, float4* pos_lo, int4* excl, float4* force,
+                                  float4* torque, uint32_t* cell_count, int n_count,
+                                  DevStatus* st, double* energy)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int c = i; c < n_count; c += gridDim.x * blockDim.x) cell_count[c] = 0u;
+    if (i < N) {
+        pos_lo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        excl[i] = make_int4(-1, -1, -1, -1);
+        force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (i == 0) {
+        st->flags = 0u;
+        st->rebuild = 1u;
+        st->gen = 0u;
+        st->n_short = 0u;
+        st->n_long = 0u;
+        st->builds = 0u;
+        st->max_cell = 0u;
+        st->step = 0ull;
+        for (int t = 0; t < 16; ++t) energy[t] = 0.0;
+    }
+}
+
+// Bond exclusions from (A, B, type) triples: up to 4 partners per particle.
+__global__ void k_noalloc_excl(int N, int n_bonds, const int* bonds, int4* excl, DevStatus* st)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_bonds) return;
+    const int A = bonds[3 * b], B = bonds[3 * b + 1];
+    if (A < 0 || B < 0 || A >= N || B >= N || A == B) {
+        atomicOr(&st->flags, kStBadIndex);
+        return;
+    }
+    for (int pass = 0; pass < 2; ++pass) {
+        int* e = reinterpret_cast<int*>(excl + (pass ? B : A));
+        const int other = pass ? A : B;
+        bool stored = false;
+        for (int k = 0; k < 4 && !stored; ++k) stored = atomicCAS(e + k, -1, other) == -1;
+        if (!stored) atomicOr(&st->flags, kStExclOverflow);
+    }
+}
+
+}  // namespace
+
+extern "C" int oxg_pair_forces_noalloc(oxg_context* c, uint32_t mask, int N,
+                                       const float* pos_type, const float* quat,
+                                       const float* charge, const float box[3], int n_bonds,
+                                       const int32_t* bonds, float* force, float* torque,
+                                       double* term_energy, void* stream)
+{
+    if (!c || !box || N < 0 || n_bonds < 0) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (N > kNaMaxParticles)
+        return set_err(OXG_ERR_CAPACITY, "oxg_pair_forces_noalloc: N = " + std::to_string(N) +
+                                             " exceeds the fixed maximum of " +
+                                             std::to_string(kNaMaxParticles) + " particles");
+    if (n_bonds > 2 * kNaMaxParticles)
+        return set_err(OXG_ERR_CAPACITY, "oxg_pair_forces_noalloc: more than " +
+                                             std::to_string(2 * kNaMaxParticles) + " bonds");
+    if (mask & ~present_mask(c)) return set_err(OXG_ERR_NO_PARAMS, "a requested term has no parameters");
+    if (N == 0 || mask == 0) return OXG_OK;
+    if (!pos_type || !quat || !force || !torque || (n_bonds > 0 && !bonds))
+        return set_err(OXG_ERR_INVALID_ARG, "null device array");
+    if (!(box[0] > 0.f && box[1] > 0.f && box[2] > 0.f)) return set_err(OXG_ERR_INVALID_ARG, "bad box");
+
+    unsigned char* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    std::vector<unsigned char> blk;
+    if ((rc = assemble_block(c, blk))) return rc;
+    const ParamHeader& H = *reinterpret_cast<const ParamHeader*>(blk.data());
+    cudaStream_t s = (cudaStream_t)stream;
+
+    // neighbour-list geometry for a one-shot evaluation (no buffer)
+    double rmax = 0.0, rshort = 0.0;
+    auto upd = [&](bool any, const double* r, bool is_short, int t) {
+        if (!any || !((mask >> t) & 1u)) return;
+        for (int k = 0; k < kMaxPairs; ++k) {
+            rmax = std::max(rmax, r[k]);
+            if (is_short) rshort = std::max(rshort, r[k]);
+        }
+    };
+    upd(c->excvol.any, c->excvol.rcut, true, kExcVol);
+    upd(c->hbond.any, c->hbond.rcut, true, kHBond);
+    upd(c->cross.any, c->cross.rcut, true, kCross);
+    upd(c->hbx.any, c->hbx.rcut, true, kHBCross);
+    upd(c->coax.any, c->coax.rcut, true, kCoax);
+    upd(c->debye.any, c->debye.rcut, false, kDebye);
+    const double rlist = rmax * (1.0 + 1e-6);
+    int n[3];
+    int use_cells = 1;
+    for (int d = 0; d < 3; ++d) {
+        n[d] = std::min(kNaMaxCellsDim, (int)std::floor(box[d] / rlist));
+        if (n[d] < 3) use_cells = 0;
+    }
+    if (!use_cells) n[0] = n[1] = n[2] = 1;
+
+    DevStatus* st = reinterpret_cast<DevStatus*>(scratch + kNaOffStatus);
+    double* energy_scratch = reinterpret_cast<double*>(scratch + kNaOffEnergy);
+    float4* pos_lo = reinterpret_cast<float4*>(scratch + kNaOffPosLo);
+    uint32_t* cell_count = reinterpret_cast<uint32_t*>(scratch + kNaOffCellCount);
+    const int n_cells = n[0] * n[1] * n[2];
+
+    OXG_CUDA(cudaMemcpyAsync(scratch + kNaOffParams, blk.data(), blk.size(), cudaMemcpyHostToDevice, s));
+    const int threads = 256;
+    const int nb = std::max(1, (std::max(N, 2 * n_cells) + threads - 1) / threads);
+    k_noalloc_prepare<<<nb, threads, 0, s>>>(N, pos_lo, reinterpret_cast<int4*>(scratch + kNaOffExcl),
+                                             reinterpret_cast<float4*>(force),
+                                             reinterpret_cast<float4*>(torque), cell_count,
+                                             2 * n_cells, st, energy_scratch);
+    if (n_bonds > 0)
+        k_noalloc_excl<<<(n_bonds + threads - 1) / threads, threads, 0, s>>>(
+            N, n_bonds, bonds, reinterpret_cast<int4*>(scratch + kNaOffExcl), st);
+    if (term_energy) OXG_CUDA(cudaMemsetAsync(term_energy, 0, sizeof(double) * kNTerms, s));
+
+    NlistArgs na;
+    na.N = N;
+    na.pos = reinterpret_cast<const float4*>(pos_type);
+    na.pos_ref = reinterpret_cast<float4*>(scratch + kNaOffPosRef);
+    na.excl = reinterpret_cast<const int4*>(scratch + kNaOffExcl);
+    na.nc = make_int3(n[0], n[1], n[2]);
+    na.use_cells = use_cells;
+    na.cell_cap = kNaCellCap;
+    na.n_cells = n_cells;
+    na.cell_count = cell_count;
+    na.cell_list = reinterpret_cast<int*>(scratch + kNaOffCellList);
+    na.L = make_float3(box[0], box[1], box[2]);
+    na.invL = make_float3(1.f / box[0], 1.f / box[1], 1.f / box[2]);
+    na.rlist2 = (float)(rlist * rlist);
+    na.rshort2 = (float)(rshort * rshort);
+    na.pairs_short = reinterpret_cast<int2*>(scratch + kNaOffShort);
+    na.pairs_long = reinterpret_cast<int2*>(scratch + kNaOffLong);
+    na.cap_short = (int)kNaShortCap;
+    na.cap_long = (int)kNaLongCap;
+    na.st = st;
+    k_nlist_bin<<<std::max(1, (std::max(N, n_cells) + threads - 1) / threads), threads, 0, s>>>(na);
+    k_nlist_pairs<<<(N + threads - 1) / threads, threads, 0, s>>>(na);
+
+    ForceArgs fa;
+    fa.params = scratch + kNaOffParams;
+    fa.param_bytes = (int)blk.size();
+    fa.mask = mask;
+    fa.bonded = 0;
+    fa.N = N;
+    fa.n_bonds = 0;
+    fa.pos = reinterpret_cast<const float4*>(pos_type);
+    fa.pos_lo = pos_lo;
+    fa.quat = reinterpret_cast<const float4*>(quat);
+    fa.charge = charge;
+    fa.bonds = nullptr;
+    fa.pairs_short = na.pairs_short;
+    fa.pairs_long = na.pairs_long;
+    fa.st = st;
+    fa.st_rw = st;
+    fa.cap_short = na.cap_short;
+    fa.cap_long = na.cap_long;
+    fa.L = na.L;
+    fa.invL = na.invL;
+    fa.force = reinterpret_cast<float4*>(force);
+    fa.torque = reinterpret_cast<float4*>(torque);
+    fa.energy = term_energy ? term_energy : energy_scratch;
+    fa.virial = nullptr;
+    int per_sm = 0;
+    OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces<true>, 256, (int)blk.size()));
+    const int grid = num_sms() * std::max(1, per_sm);
+    if (term_energy) k_forces<true><<<grid, 256, blk.size(), s>>>(fa);
+    else k_forces<false><<<grid, 256, blk.size(), s>>>(fa);
+    OXG_CUDA(cudaGetLastError());
+
+    DevStatus d;
+    OXG_CUDA(cudaMemcpyAsync(&d, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    OXG_CUDA(cudaStreamSynchronize(s));
+    (void)H;
+    if (d.flags & kStBadIndex) return set_err(OXG_ERR_BAD_INDEX, "a bond or particle type index is out of range");
+    if (d.flags & kStExclOverflow) return set_err(OXG_ERR_CAPACITY, "a particle has more than 4 bonds");
+    if (d.flags & kStCellOverflow)
+        return set_err(OXG_ERR_CAPACITY, "a cell holds more than " + std::to_string(kNaCellCap) +
+                                             " particles (fixed scratch limit)");
+    if (d.flags & kStPairOverflow)
+        return set_err(OXG_ERR_CAPACITY, "more neighbour pairs than the fixed scratch holds (" +
+                                             std::to_string(kNaShortCap) + " short, " +
+                                             std::to_string(kNaLongCap) + " long)");
+    return OXG_OK;
+}

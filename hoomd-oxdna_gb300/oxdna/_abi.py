@@ -236,7 +236,7 @@ EXPORTS = [
     "oxg_system_set_state", "oxg_system_get_state", "oxg_system_device_state",
     "oxg_system_set_nlist_buffer", "oxg_system_compute", "oxg_system_set_integrator",
     "oxg_system_run", "oxg_system_energies", "oxg_system_stats", "oxg_last_error",
-    "oxg_version", "oxg_status_string",
+    "oxg_version", "oxg_status_string", "oxg_pair_forces_noalloc",
 ]
 
 _lib = None
@@ -291,6 +291,7 @@ def lib():
         "oxg_system_run": ([vp, C.c_long], i32),
         "oxg_system_energies": ([vp, vp, vp], i32),
         "oxg_system_stats": ([vp, C.POINTER(C.c_int64), i32], i32),
+        "oxg_pair_forces_noalloc": ([vp, u32, i32, vp, vp, vp, fp, i32, vp, vp, vp, vp, vp], i32),
         "oxg_last_error": ([], C.c_char_p),
         "oxg_version": ([], C.c_char_p),
         "oxg_status_string": ([i32], C.c_char_p),

@@ -267,6 +267,42 @@ int oxg_system_energies(oxg_system* sys, double* pair_energy, double* bonded_ene
  * 3 pair-list entries (long), 4 kernels launched per step. */
 int oxg_system_stats(oxg_system* sys, int64_t* out, int n);
 
+/* ---- allocation-free nonbonded evaluation -------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot allocate GPU
+ * memory at all, e.g. code running inside a framework that has reserved the whole
+ * device memory pool for its own allocator, or a host that forbids allocation (and
+ * the implicit device synchronisation of cudaMalloc) once its simulation loop runs.
+ *
+ * Same evaluation as the system engine's nonbonded forces (cell list with bond
+ * exclusions, split pair lists, the fused force kernel), but every scratch buffer it
+ * needs lives in one fixed-size static device array inside this library (about
+ * 7.8 MB, held by every GPU that loads the library until the process exits). The
+ * call allocates nothing: no cudaMalloc, cudaFree or allocating library routine.
+ *
+ * Inputs (device): pos_type[4*N] (x, y, z, type as the float's int bits), quat[4*N],
+ * charge[N] (NULL = unit charge), bonds[3*n_bonds] = (A, B, type) used for the
+ * exclusions only. Outputs (device, overwritten): force[4*N] (F on each particle,
+ * per-particle energy in .w when term_energy != NULL), torque[4*N], and term_energy
+ * (OXG_N_PAIR_TERMS doubles, per-term totals; may be NULL). Parameters come from ctx
+ * (its own device memory is not used).
+ *
+ * Limits: N <= OXG_NOALLOC_MAX_PARTICLES and n_bonds <= 2 * that, rejected with
+ * OXG_ERR_CAPACITY before any GPU work; at most 64 particles per cell, 32 short-range
+ * and 48 long-range neighbour pairs per allowed particle on average, at most 4 bonds
+ * per particle: exceeding these is reported as OXG_ERR_CAPACITY after the run (the
+ * call waits for its work on `stream` to finish before returning).
+ *
+ * The first call on a device looks up the array's device address (once per device,
+ * with that device current); make that first call before any stream capture. Every
+ * call uses the same array and leaves its contents behind; the call clears what must
+ * start empty. Calls whose GPU work overlaps (several streams or threads) race on the
+ * shared array. */
+#define OXG_NOALLOC_MAX_PARTICLES 8192
+int oxg_pair_forces_noalloc(oxg_context* ctx, uint32_t term_mask, int N,
+                            const float* pos_type, const float* quat, const float* charge,
+                            const float box[3], int n_bonds, const int32_t* bonds,
+                            float* force, float* torque, double* term_energy, void* stream);
+
 /* Text of the last error raised on the calling thread (CUDA error string etc.). */
 const char* oxg_last_error(void);
 /* Version / build string of the loaded library. */
