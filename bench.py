@@ -258,6 +258,17 @@ def run_ours(args):
     sim_f.run(0)
     ms_f = time_resident(sim_f, min(args.steps, 5000), args.warmup, stream)
     fused_sps = min(args.steps, 5000) / (ms_f * 1e-3)
+    del sim_f
+
+    # --- 100k nt (2500 x 20-bp duplexes, box 230): the plain path at the large size --
+    big = build_system(n_dup=2500, n_bp=20, box=230.0, seed=5 + rank)
+    sim_b, _ = make_sim(big, fused=False, seed=1 + rank, stream=stream.cuda_stream)
+    sim_b.run(0)
+    nb_steps = min(args.steps, 2000)
+    ms_b = time_resident(sim_b, nb_steps, args.warmup, stream)
+    big_sps = nb_steps / (ms_b * 1e-3)
+    big_stats = sim_b.native_stats()
+    del sim_b
 
     # --- end to end through the public API with host buffers ----------------------
     pin = lambda: torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()  # noqa: E731
@@ -285,7 +296,7 @@ def run_ours(args):
     if rank != 0:
         dist.destroy_process_group()
         return
-    launches_per_step = 5
+    launches_per_step = 4  # nlist bin, nlist pairs (both exit unless rebuilding), forces, step
     line = {
         "metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -295,6 +306,9 @@ def run_ours(args):
                    "pairs_short": st["pairs_short"], "pairs_long": st["pairs_long"],
                    "l2": "flushed (256 MB write) before every timed block of 100 steps",
                    "fused_true_steps_per_s": fused_sps,
+                   "nt100k_steps_per_s": big_sps,
+                   "nt100k_nt_steps_per_s": big_sps * len(big["pos"]),
+                   "nt100k_pairs": [big_stats["pairs_short"], big_stats["pairs_long"]],
                    "reference_published": "~4600 steps/s unfused, ~5000 fused (RTX 4090, "
                                           "8192-nt tiled duplex, box 64; README.md:97-98)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -302,7 +316,7 @@ def run_ours(args):
                      "kernel": "nlist check + k_forces (energies off)",
                      "kernel_ms": kernel_ms, "alg_bytes": alg_bytes},
         "cpu_baseline": cb, "e2e": e2e,
-        "gpu_launches": (args.steps + args.warmup) * launches_per_step + 4 * (
+        "gpu_launches": (args.steps + args.warmup) * launches_per_step + 5 * (
             (args.steps + 99) // 100 + 1),
         "clocks": clk.summary(),
         "nlist_builds": stats["nlist_builds"],

@@ -282,6 +282,17 @@ struct RadialF2 {  // cross-stacking: harmonic
 };
 
 // One BASE-BASE term; adds force on i and both torques. src/OxDNABaseBase.h:128-219.
+// True when no factor of the BASE-BASE term is exactly zero: the tests bb_term starts
+// with, used to decide which pairs go on to the full (acos-heavy) evaluation.
+template <bool SYM, class Radial>
+OXG_HD bool bb_support(const BBGeom& g, const F4& t1, const F4& t23, const F4& t4, const F4& t78,
+                       bool inc_t4, const Radial& R)
+{
+    return R.support(g.rmod) && f4_support<false>(g.c1, t1) && f4_support<false>(g.c2, t23) &&
+           f4_support<false>(g.c3, t23) && (!inc_t4 || f4_support<SYM>(g.c4, t4)) &&
+           f4_support<SYM>(g.c7, t78) && f4_support<SYM>(g.c8, t78);
+}
+
 template <bool SYM, class Radial>
 OXG_HD float bb_term(const BBGeom& g, const Frame& fi, const Frame& fj,
                                          const F4& t1, const F4& t23, const F4& t4,
@@ -344,6 +355,17 @@ OXG_HD float bb_term(const BBGeom& g, const Frame& fi, const Frame& fj,
 
 // ------------------------------------------------------------ coaxial stacking
 // src/EvaluatorPairOxDNACoaxStacking.h:134-372. rc = r_j - r_i.
+// The zero-factor tests coax_term starts with (radial f2 and the theta4/5/6 supports).
+OXG_HD bool coax_support(const DCoax& p, float3 rc, const Frame& fi, const Frame& fj)
+{
+    const float3 rstack = rc + body_to_lab(fj, p.stack) - body_to_lab(fi, p.stack);
+    const float rsm = sqrtf(dot(rstack, rstack));
+    if (!(rsm > 0.f && p.f2[0] != 0.f && rsm > p.f2[5] && rsm < p.f2[6])) return false;
+    const float3 rsd = rstack * (1.f / rsm);
+    return f4_support<false>(dot(fi.a3, fj.a3), p.t4) && f4_support<true>(dot(fi.a3, rsd), p.t56) &&
+           f4_support<true>(-dot(fj.a3, rsd), p.t56);
+}
+
 OXG_HD float coax_term(const DCoax& p, float3 rc, const Frame& fi,
                                            const Frame& fj, PairAcc& acc)
 {

@@ -578,6 +578,7 @@ ForceArgs force_args(oxg_system* s, uint32_t mask, int bonded)
     a.st_rw = s->st;
     a.cap_short = (int)std::min<long long>(s->cap_short, 0x7fffffff);
     a.cap_long = (int)std::min<long long>(s->cap_long, 0x7fffffff);
+    a.advance_step = 0;
     a.L = s->L;
     a.invL = s->invL;
     a.force = s->force;
@@ -627,14 +628,15 @@ int forces_grid(oxg_system* s)
 }
 
 // Launch nlist (if flagged) + forces on s->stream.
-int launch_nlist_forces(oxg_system* s, uint32_t mask, int bonded, bool energy)
+int launch_nlist_forces(oxg_system* s, uint32_t mask, int bonded, bool energy, bool md_step = false)
 {
     const NlistArgs na = nlist_args(s);
     const int threads = 256;
     const int nb = std::max(1, (std::max(s->N, s->n_cells) + threads - 1) / threads);
     k_nlist_bin<<<nb, threads, 0, s->stream>>>(na);
     k_nlist_pairs<<<std::max(1, (s->N + threads - 1) / threads), threads, 0, s->stream>>>(na);
-    const ForceArgs fa = force_args(s, mask, bonded);
+    ForceArgs fa = force_args(s, mask, bonded);
+    fa.advance_step = md_step ? 1 : 0;
     const int grid = forces_grid(s);
     if (energy) k_forces<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
     else k_forces<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
@@ -899,16 +901,25 @@ int oxg_system_set_integrator(oxg_system* s, double dt, double kT, double gamma,
     return OXG_OK;
 }
 
-// One MD step as kernel launches on s->stream.
-static int enqueue_step(oxg_system* s)
+// Step sequence of a run of n steps (velocity Verlet split as HOOMD does):
+//   prepRun, step_one, n - 1 x [nlist, forces, step_two_one], nlist, forces, step_two
+// where step_two_one is step two of one step fused with step one of the next.
+static int enqueue_step_one(oxg_system* s)
 {
     const IntegArgs ia = integ_args(s);
-    const int threads = 256;
-    const int nb = (s->N + threads - 1) / threads;
-    k_step_one<<<nb, threads, 0, s->stream>>>(ia);
-    int rc = launch_nlist_forces(s, s->run_mask, s->run_bonded, false);
+    k_step_one<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
+    OXG_CUDA(cudaGetLastError());
+    return OXG_OK;
+}
+
+// One step body: forces of the current positions, then step two (+ next step one).
+static int enqueue_step(oxg_system* s, bool last)
+{
+    int rc = launch_nlist_forces(s, s->run_mask, s->run_bonded, false, true);
     if (rc) return rc;
-    k_step_two<<<nb, threads, 0, s->stream>>>(ia);
+    const IntegArgs ia = integ_args(s);
+    if (last) k_step_two<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
+    else k_step_two_one<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
     OXG_CUDA(cudaGetLastError());
     return OXG_OK;
 }
@@ -936,7 +947,7 @@ static int build_graph(oxg_system* s, int steps)
         return set_err(OXG_ERR_CUDA, std::string("begin capture: ") + cudaGetErrorString(e));
     }
     int rc = OXG_OK;
-    for (int k = 0; k < steps && rc == OXG_OK; ++k) rc = enqueue_step(s);
+    for (int k = 0; k < steps && rc == OXG_OK; ++k) rc = enqueue_step(s, false);
     e = cudaStreamEndCapture(cap, &g);
     s->stream = saved;
     if (own) cudaStreamDestroy(cap);
@@ -952,6 +963,10 @@ static int build_graph(oxg_system* s, int steps)
 static int checkpoint(oxg_system* s, bool restore)
 {
     const size_t b4 = sizeof(float4) * s->N;
+    if (restore) {  // the aborted chunk left partial sums in the accumulators
+        OXG_CUDA(cudaMemsetAsync(s->force, 0, b4, s->stream));
+        OXG_CUDA(cudaMemsetAsync(s->torque, 0, b4, s->stream));
+    }
     float4* src[5] = {s->pos, s->pos_lo, s->quat, s->vel, s->angmom};
     float4* dst[5] = {s->ck_pos, s->ck_pos_lo, s->ck_quat, s->ck_vel, s->ck_angmom};
     for (int k = 0; k < 5; ++k) {
@@ -1000,13 +1015,19 @@ int oxg_system_run(oxg_system* s, long nsteps)
         OXG_CUDA(cudaStreamSynchronize(s->stream));
         return OXG_OK;
     }
-    const int chunk = (int)std::min<long>(nsteps, 100);
+    if ((rc = enqueue_step_one(s))) return rc;
+    // nsteps - 1 fused bodies in graph chunks, then the closing body with step two.
+    // Chunk boundaries sit after a step one; on a list overflow the chunk is replayed
+    // from its checkpoint with a forced neighbour-list rebuild.
+    const long bodies = nsteps - 1;
+    const int chunk = 100;
     long done = 0;
     int retries = 0;
-    while (done < nsteps) {
-        const int todo = (int)std::min<long>(chunk, nsteps - done);
-        const uint64_t key = ((uint64_t)todo << 32) ^ s->ctx->version ^ ((uint64_t)(uintptr_t)s->stream << 8);
+    while (done < bodies) {
+        const int todo = (int)std::min<long>(chunk, bodies - done);
         if (todo == chunk) {
+            const uint64_t key = ((uint64_t)todo << 32) ^ s->ctx->version ^
+                                 ((uint64_t)(uintptr_t)s->stream << 8);
             if (s->graph_key != key || !s->graph) {
                 if ((rc = build_graph(s, todo))) return rc;
                 s->graph_key = key;
@@ -1018,7 +1039,7 @@ int oxg_system_run(oxg_system* s, long nsteps)
         if (todo == chunk) {
             OXG_CUDA(cudaGraphLaunch(s->graph, s->stream));
         } else {
-            for (int k = 0; k < todo && rc == OXG_OK; ++k) rc = enqueue_step(s);
+            for (int k = 0; k < todo && rc == OXG_OK; ++k) rc = enqueue_step(s, false);
             if (rc) return rc;
         }
         DevStatus d;
@@ -1029,16 +1050,36 @@ int oxg_system_run(oxg_system* s, long nsteps)
             bool grew = false;
             if ((rc = grow_for(s, d, &grew))) return rc;
             if ((rc = checkpoint(s, true))) return rc;
-            // restore the RNG counter and redo this chunk with a fresh prepRun
             OXG_CUDA(cudaMemcpyAsync(&s->st->step, &before.step, sizeof(unsigned long long),
                                      cudaMemcpyHostToDevice, s->stream));
-            if ((rc = prep_run(s))) return rc;
+            if ((rc = clear_flags(s)) || (rc = set_rebuild(s))) return rc;
             s->graph_key = ~0ull;
             continue;
         }
         done += todo;
-        s->timestep = d.step;
         s->steps_run += todo;
+    }
+    // closing body: forces at the last positions and step two
+    for (int attempt = 0;; ++attempt) {
+        if ((rc = checkpoint(s, false))) return rc;
+        DevStatus before;
+        if ((rc = read_status(s, &before))) return rc;
+        if ((rc = enqueue_step(s, true))) return rc;
+        DevStatus d;
+        if ((rc = read_status(s, &d))) return rc;
+        if (d.flags & kStNonFinite) return set_err(OXG_ERR_NONFINITE, "non-finite positions or orientations");
+        if (!(d.flags & (kStCellOverflow | kStPairOverflow))) {
+            s->timestep = d.step;
+            s->steps_run += 1;
+            break;
+        }
+        if (attempt >= 8) return set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
+        bool grew = false;
+        if ((rc = grow_for(s, d, &grew))) return rc;
+        if ((rc = checkpoint(s, true))) return rc;
+        OXG_CUDA(cudaMemcpyAsync(&s->st->step, &before.step, sizeof(unsigned long long),
+                                 cudaMemcpyHostToDevice, s->stream));
+        if ((rc = clear_flags(s)) || (rc = set_rebuild(s))) return rc;
     }
     OXG_CUDA(cudaStreamSynchronize(s->stream));
     return OXG_OK;

@@ -195,6 +195,7 @@ struct ForceArgs {
     const DevStatus* st;  // n_short / n_long
     DevStatus* st_rw;     // rebuild flag cleared here
     int cap_short, cap_long;  // list capacities (counts past them were not stored)
+    int advance_step;     // MD step: advance the RNG step counter read by step two
     float3 L, invL;
     float4* force;        // accumulated (pre-zeroed)
     float4* torque;
@@ -202,94 +203,274 @@ struct ForceArgs {
     float* virial;        // unused by the engine
 };
 
+// Deferred (acos-heavy) terms of the short-range pairs. Each warp takes 32 pairs at a
+// time, evaluates the cheap terms (excluded volume, Debye) inline and runs only the
+// zero-factor tests of the heavy ones; pairs that pass go into a per-warp queue in
+// shared memory, and a queue is evaluated whenever it holds 32 pairs, so the heavy
+// code runs with every lane busy instead of with the few lanes whose pair passed.
+enum { kQHB = 0, kQCS = 1, kQHBX = 2, kQCX = 3, kNQ = 4 };
+constexpr int kQCap = 64;  // < 32 waiting + 32 pushed per batch
+constexpr int kForceWarps = 8;
+
+struct PairIn {
+    int i, j, pidx;
+    float3 rc;  // r_j - r_i
+    float rsq;
+    float ci, cj;
+};
+
+__device__ __forceinline__ bool load_short_pair(const ForceArgs& a, int w, int n_types, PairIn& p,
+                                                bool& bad_type)
+{
+    const int2 pr = a.pairs_short[w];
+    p.i = pr.x;
+    p.j = pr.y;
+    const float4 pi = a.pos[p.i], pj = a.pos[p.j];
+    const float3 dr = min_image(pair_delta(pi, a.pos_lo[p.i], pj, a.pos_lo[p.j]), a.L, a.invL);
+    p.rc = -dr;
+    p.rsq = dot(dr, dr);
+    const int ti = type_of(pi), tj = type_of(pj);
+    if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
+        bad_type = true;
+        return false;
+    }
+    p.pidx = ti * kMaxTypes + tj;
+    p.ci = a.charge ? a.charge[p.i] : 1.f;
+    p.cj = a.charge ? a.charge[p.j] : 1.f;
+    return true;
+}
+
+template <bool ENERGY>
+__device__ __forceinline__ void scatter(const ForceArgs& a, int i, int j, const PairAcc& acc, float e)
+{
+    const float eh = ENERGY ? 0.5f * e : 0.f;
+    atomicAdd(a.force + i, make_float4(acc.fi.x, acc.fi.y, acc.fi.z, eh));
+    atomicAdd(a.force + j, make_float4(-acc.fi.x, -acc.fi.y, -acc.fi.z, eh));
+    atomicAdd(a.torque + i, make_float4(acc.ti.x, acc.ti.y, acc.ti.z, 0.f));
+    atomicAdd(a.torque + j, make_float4(acc.tj.x, acc.tj.y, acc.tj.z, 0.f));
+}
+
+// Full evaluation of one deferred term for short pair w (warp-uniform q).
+template <bool ENERGY>
+__device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamView& P, int q, int w,
+                                              double* eacc)
+{
+    const ParamHeader& H = P.h();
+    PairIn p;
+    bool dummy = false;
+    if (!load_short_pair(a, w, H.n_types, p, dummy)) return;
+    const Frame fi = quat_frame(a.quat[p.i]), fj = quat_frame(a.quat[p.j]);
+    PairAcc acc;
+    acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+    float e = 0.f;
+    int term = kHBond;
+    BBGeom g;
+    if (q == kQHB) {
+        const DHBond& ph = P.term<DHBond>(kHBond, p.pidx);
+        if (bb_geometry(p.rc, fi, fj, ph.base, g)) {
+            RadialF1 R{ph.f1, H.hb_eps[p.pidx], H.hb_shift[p.pidx]};
+            e = bb_term<false>(g, fi, fj, ph.t1, ph.t23, ph.t4, ph.t78, true, R, acc);
+        }
+    } else if (q == kQCS) {
+        term = kCross;
+        const DCross& pc = P.term<DCross>(kCross, p.pidx);
+        if (bb_geometry(p.rc, fi, fj, pc.base, g)) {
+            RadialF2 R{pc.f2};
+            e = bb_term<true>(g, fi, fj, pc.t1, pc.t23, pc.t4, pc.t78, pc.t4_enabled != 0, R, acc);
+        }
+    } else if (q == kQHBX) {
+        term = kHBCross;
+        const DHBCross& px = P.term<DHBCross>(kHBCross, p.pidx);
+        if (bb_geometry(p.rc, fi, fj, px.base, g)) {
+            RadialF1 R1{px.f1, H.hbx_eps[p.pidx], H.hbx_shift[p.pidx]};
+            e = bb_term<false>(g, fi, fj, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1, acc);
+            RadialF2 R2{px.f2};
+            e += bb_term<true>(g, fi, fj, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2, acc);
+        }
+    } else {
+        term = kCoax;
+        e = coax_term(P.term<DCoax>(kCoax, p.pidx), p.rc, fi, fj, acc);
+    }
+    scatter<ENERGY>(a, p.i, p.j, acc, e);
+    if (ENERGY) eacc[term] += (double)e;
+}
+
 template <bool ENERGY>
 __global__ void __launch_bounds__(256) k_forces(ForceArgs a)
 {
     const ParamView P = stage_params(a.params, a.param_bytes);
-    if (blockIdx.x == 0 && threadIdx.x == 0 && a.st_rw->rebuild) {
-        a.st_rw->rebuild = 0u;
-        a.st_rw->gen += 1u;
+    __shared__ int queue[kForceWarps][kNQ][kQCap];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.st_rw->rebuild) {
+            a.st_rw->rebuild = 0u;
+            a.st_rw->gen += 1u;
+        }
+        if (a.advance_step) a.st_rw->step += 1ull;
     }
+    const ParamHeader& H = P.h();
     // after an overflow the counters exceed the capacities; only stored pairs are read
     const int n_short = (int)min(a.st->n_short, (uint32_t)a.cap_short);
     const int n_long = (int)min(a.st->n_long, (uint32_t)a.cap_long);
-    const int n_types = P.h().n_types;
+    const int n_types = H.n_types;
     bool bad_type = false;
-    const int n_bonds = a.bonded ? a.n_bonds : 0;
-    const int total = n_short + n_bonds + n_long;
     double eacc[kNTerms + 3];
 #pragma unroll
     for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
-    const uint32_t long_mask = a.mask & (1u << kDebye);
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t mask = a.mask;
+    int qn[kNQ] = {0, 0, 0, 0};  // warp-uniform queue lengths
 
-    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < total; w += gridDim.x * blockDim.x) {
-        if (w < n_short || w >= n_short + n_bonds) {
-            const bool is_short = w < n_short;
-            const int2 pr = is_short ? a.pairs_short[w] : a.pairs_long[w - n_short - n_bonds];
-            const int i = pr.x, j = pr.y;
-            const float4 pi = a.pos[i], pj = a.pos[j];
-            const float3 dr = min_image(pair_delta(pi, a.pos_lo[i], pj, a.pos_lo[j]), a.L, a.invL);
-            const float rsq = dot(dr, dr);
-            const int ti = type_of(pi), tj = type_of(pj);
-            if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
-                bad_type = true;
-                continue;
-            }
-            const int pidx = ti * kMaxTypes + tj;
+    auto drain = [&](int q, int n) {
+        const int w = lane < n ? queue[wib][q][lane] : -1;
+        __syncwarp();
+        const int rest = qn[q] - n;
+        const int moved = lane < rest ? queue[wib][q][n + lane] : 0;
+        __syncwarp();
+        if (lane < rest) queue[wib][q][lane] = moved;
+        qn[q] = rest;
+        __syncwarp();
+        if (w >= 0) eval_deferred<ENERGY>(a, P, q, w, eacc);
+    };
+
+    // ---- short-range pairs: cheap terms inline, heavy terms through the queues ----
+    for (int base = gwarp * 32; base < n_short; base += nwarps * 32) {
+        const int w = base + lane;
+        bool want[kNQ] = {false, false, false, false};
+        PairIn p;
+        if (w < n_short && load_short_pair(a, w, n_types, p, bad_type) && p.rsq < H.rcutsq_max) {
+            const Frame fi = quat_frame(a.quat[p.i]), fj = quat_frame(a.quat[p.j]);
             PairAcc acc;
             acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
-            float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
-            const bool any = eval_pair(P, is_short ? a.mask : long_mask, pidx, dr, rsq, a.quat[i],
-                                       a.quat[j], ci, cj, acc, E);
-            if (any) {
-                float eh = 0.f;
-                if (ENERGY) {
-#pragma unroll
-                    for (int t = 0; t < kNTerms; ++t) {
-                        eacc[t] += (double)E[t];
-                        eh += E[t];
-                    }
-                    eh *= 0.5f;
+            float e_inline = 0.f;
+            bool inl = false;
+            if (mask & (1u << kExcVol)) {
+                const DExcVol& pe = P.term<DExcVol>(kExcVol, p.pidx);
+                if (p.rsq < pe.rcutsq) {
+                    const float e = excvol_term(pe, p.rc, fi, fj, acc);
+                    e_inline += e;
+                    if (ENERGY) eacc[kExcVol] += (double)e;
+                    inl = true;
                 }
-                atomicAdd(a.force + i, make_float4(acc.fi.x, acc.fi.y, acc.fi.z, eh));
-                atomicAdd(a.force + j, make_float4(-acc.fi.x, -acc.fi.y, -acc.fi.z, eh));
-                atomicAdd(a.torque + i, make_float4(acc.ti.x, acc.ti.y, acc.ti.z, 0.f));
-                atomicAdd(a.torque + j, make_float4(acc.tj.x, acc.tj.y, acc.tj.z, 0.f));
             }
-        } else {
-            const int4 bd = a.bonds[w - n_short];
-            const int A = bd.x, B = bd.y;
-            const float4 pA = a.pos[A], pB = a.pos[B];
-            const float3 Rcf = min_image(pair_delta(pB, a.pos_lo[B], pA, a.pos_lo[A]), a.L, a.invL);
-            const float4 qA = a.quat[A], qB = a.quat[B];
-            if ((unsigned)type_of(pA) >= (unsigned)n_types || (unsigned)type_of(pB) >= (unsigned)n_types) {
-                bad_type = true;
-                continue;
+            if (mask & (1u << kDebye)) {
+                const DDebye& pd = P.term<DDebye>(kDebye, p.pidx);
+                if (p.rsq < pd.rcutsq) {
+                    const float e = debye_term(pd, p.rc, fi, fj, p.ci, p.cj, acc);
+                    e_inline += e;
+                    if (ENERGY) eacc[kDebye] += (double)e;
+                    inl = true;
+                }
             }
-            BondAcc acc;
-            bonded_pair(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
-                        make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
-                        type_of(pA), type_of(pB), acc);
-            float eh = 0.f;
-            if (ENERGY) {
-                eacc[kNTerms + 0] += acc.e[0];
-                eacc[kNTerms + 1] += acc.e[1];
-                eacc[kNTerms + 2] += acc.e[2];
-                eh = (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2]));
+            if (inl) scatter<ENERGY>(a, p.i, p.j, acc, e_inline);
+            BBGeom g;
+            bool gv = false;
+            if (mask & (1u << kHBond)) {
+                const DHBond& ph = P.term<DHBond>(kHBond, p.pidx);
+                if (p.rsq < ph.rcutsq && H.hb_eps[p.pidx] != 0.f) {
+                    gv = bb_geometry(p.rc, fi, fj, ph.base, g);
+                    RadialF1 R{ph.f1, H.hb_eps[p.pidx], H.hb_shift[p.pidx]};
+                    want[kQHB] = gv && bb_support<false>(g, ph.t1, ph.t23, ph.t4, ph.t78, true, R);
+                }
             }
-            atomicAdd(a.force + A, make_float4(-acc.fB.x, -acc.fB.y, -acc.fB.z, eh));
-            atomicAdd(a.force + B, make_float4(acc.fB.x, acc.fB.y, acc.fB.z, eh));
-            atomicAdd(a.torque + A, make_float4(acc.tA.x, acc.tA.y, acc.tA.z, 0.f));
-            atomicAdd(a.torque + B, make_float4(acc.tB.x, acc.tB.y, acc.tB.z, 0.f));
+            if (mask & (1u << kCross)) {
+                const DCross& pc = P.term<DCross>(kCross, p.pidx);
+                if (p.rsq < pc.rcutsq) {
+                    if (!gv || !H.hb_cs_same_site) gv = bb_geometry(p.rc, fi, fj, pc.base, g);
+                    RadialF2 R{pc.f2};
+                    want[kQCS] = gv && bb_support<true>(g, pc.t1, pc.t23, pc.t4, pc.t78,
+                                                        pc.t4_enabled != 0, R);
+                }
+            }
+            if (mask & (1u << kHBCross)) {
+                const DHBCross& px = P.term<DHBCross>(kHBCross, p.pidx);
+                if (p.rsq < px.rcutsq && bb_geometry(p.rc, fi, fj, px.base, g)) {
+                    RadialF1 R1{px.f1, H.hbx_eps[p.pidx], H.hbx_shift[p.pidx]};
+                    RadialF2 R2{px.f2};
+                    want[kQHBX] = bb_support<false>(g, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1) ||
+                                  bb_support<true>(g, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2);
+                }
+            }
+            if (mask & (1u << kCoax)) {
+                const DCoax& pc = P.term<DCoax>(kCoax, p.pidx);
+                want[kQCX] = p.rsq < pc.rcutsq && coax_support(pc, p.rc, fi, fj);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kNQ; ++q) {
+            const unsigned m = __ballot_sync(0xffffffffu, want[q]);
+            if (want[q]) queue[wib][q][qn[q] + __popc(m & lt_mask)] = w;
+            qn[q] += __popc(m);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < kNQ; ++q)
+            if (qn[q] >= 32) drain(q, 32);
+    }
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q)
+        if (qn[q] > 0) drain(q, qn[q]);
+
+    // ---- bonds (FENE FP64, bonded excluded volume, stacking) ----
+    const int n_bonds = a.bonded ? a.n_bonds : 0;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    for (int b = tid; b < n_bonds; b += nthreads) {
+        const int4 bd = a.bonds[b];
+        const int A = bd.x, B = bd.y;
+        const float4 pA = a.pos[A], pB = a.pos[B];
+        if ((unsigned)type_of(pA) >= (unsigned)n_types || (unsigned)type_of(pB) >= (unsigned)n_types) {
+            bad_type = true;
+            continue;
+        }
+        const float3 Rcf = min_image(pair_delta(pB, a.pos_lo[B], pA, a.pos_lo[A]), a.L, a.invL);
+        const float4 qA = a.quat[A], qB = a.quat[B];
+        BondAcc acc;
+        bonded_pair(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
+                    make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
+                    type_of(pA), type_of(pB), acc);
+        float eh = 0.f;
+        if (ENERGY) {
+            eacc[kNTerms + 0] += acc.e[0];
+            eacc[kNTerms + 1] += acc.e[1];
+            eacc[kNTerms + 2] += acc.e[2];
+            eh = (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2]));
+        }
+        atomicAdd(a.force + A, make_float4(-acc.fB.x, -acc.fB.y, -acc.fB.z, eh));
+        atomicAdd(a.force + B, make_float4(acc.fB.x, acc.fB.y, acc.fB.z, eh));
+        atomicAdd(a.torque + A, make_float4(acc.tA.x, acc.tA.y, acc.tA.z, 0.f));
+        atomicAdd(a.torque + B, make_float4(acc.tB.x, acc.tB.y, acc.tB.z, 0.f));
+    }
+
+    // ---- long-range pairs: Debye only ----
+    const uint32_t long_mask = mask & (1u << kDebye);
+    for (int w = tid; w < n_long && long_mask; w += nthreads) {
+        const int2 pr = a.pairs_long[w];
+        const int i = pr.x, j = pr.y;
+        const float4 pi = a.pos[i], pj = a.pos[j];
+        const int ti = type_of(pi), tj = type_of(pj);
+        if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
+            bad_type = true;
+            continue;
+        }
+        const float3 dr = min_image(pair_delta(pi, a.pos_lo[i], pj, a.pos_lo[j]), a.L, a.invL);
+        PairAcc acc;
+        acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+        float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
+        if (eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), a.quat[i], a.quat[j], ci,
+                      cj, acc, E)) {
+            if (ENERGY) eacc[kDebye] += (double)E[kDebye];
+            scatter<ENERGY>(a, i, j, acc, E[kDebye]);
         }
     }
+
     if (ENERGY) {
-        const int lane = threadIdx.x & 31;
 #pragma unroll
         for (int t = 0; t < kNTerms + 3; ++t) {
-            const double s = warp_sum(eacc[t]);
-            if (lane == 0 && s != 0.0) atomicAdd(a.energy + t, s);
+            const double sum = warp_sum(eacc[t]);
+            if (lane == 0 && sum != 0.0) atomicAdd(a.energy + t, sum);
         }
     }
     if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
@@ -697,91 +878,83 @@ __device__ __forceinline__ void free_rotor(int k, float h, float I, float4& p, f
     q = make_float4(c * q.x + s * pq.x, c * q.y + s * pq.y, c * q.z + s * pq.z, c * q.w + s * pq.w);
 }
 
-// Step one: v += dt/2 a; x += dt v (wrapped); p += dt q*(0, t_body); NO_SQUISH free
-// rotor (axes 3, 2 at dt/2, 1 at dt, 2, 3 at dt/2); renormalise q. Zeroes the force
-// accumulators and flags a neighbour-list rebuild when a particle moved more than
-// half the buffer since the last build.
-__global__ void k_step_one(IntegArgs a)
+// x_hi + x_lo += d for a double-float coordinate (Knuth's TwoSum, FP32 only), then
+// wrap the high part into [-L/2, L/2); subtracting L there is exact (Sterbenz).
+__device__ __forceinline__ void dd_advance(float& hi, float& lo, float d, float L)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) a.st->step += 1ull;
-    bool far = false, bad = false;
-    if (i < a.N) {
-        float4 v = a.vel[i];
-        const float4 ac = a.accel[i];
-        float4 x = a.pos[i];
-        const float4 xl = a.pos_lo[i];
-        v.x += 0.5f * a.dt * ac.x;
-        v.y += 0.5f * a.dt * ac.y;
-        v.z += 0.5f * a.dt * ac.z;
-        // position update in double (hi + lo), then split back into two floats
-        double X = (double)x.x + (double)xl.x + (double)a.dt * v.x;
-        double Y = (double)x.y + (double)xl.y + (double)a.dt * v.y;
-        double Z = (double)x.z + (double)xl.z + (double)a.dt * v.z;
-        X -= (double)a.L.x * rint(X / (double)a.L.x);
-        Y -= (double)a.L.y * rint(Y / (double)a.L.y);
-        Z -= (double)a.L.z * rint(Z / (double)a.L.z);
-        x.x = (float)X;
-        x.y = (float)Y;
-        x.z = (float)Z;
-        a.pos_lo[i] = make_float4((float)(X - (double)x.x), (float)(Y - (double)x.y),
-                                  (float)(Z - (double)x.z), 0.f);
-        float4 q = a.quat[i], p = a.angmom[i];
-        const float4 tn = a.tnet[i];
-        const float3 tb = rot_conj(q, mk3(tn.x, tn.y, tn.z));
-        const float4 dq = qmul_vec(q, tb);
-        p.x += a.dt * dq.x;
-        p.y += a.dt * dq.y;
-        p.z += a.dt * dq.z;
-        p.w += a.dt * dq.w;
-        free_rotor(3, 0.5f * a.dt, a.inertia.z, p, q);
-        free_rotor(2, 0.5f * a.dt, a.inertia.y, p, q);
-        free_rotor(1, a.dt, a.inertia.x, p, q);
-        free_rotor(2, 0.5f * a.dt, a.inertia.y, p, q);
-        free_rotor(3, 0.5f * a.dt, a.inertia.z, p, q);
-        const float nq = rsqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
-        q = make_float4(q.x * nq, q.y * nq, q.z * nq, q.w * nq);
-        bad = !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(q.x));
-        a.pos[i] = x;
-        a.vel[i] = v;
-        a.quat[i] = q;
-        a.angmom[i] = p;
-        a.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        a.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 r = a.pos_ref[i];
-        const float3 d = min_image(mk3(x.x - r.x, x.y - r.y, x.z - r.z), a.L, a.invL);
-        far = dot(d, d) > a.half_buf2;
-    }
-    if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&a.st->rebuild, 1u);
-    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&a.st->flags, kStNonFinite);
+    const float s = lo + d;
+    const float t = hi + s;
+    const float bp = t - hi;
+    lo = (hi - (t - bp)) + (s - bp);
+    hi = t;
+    if (hi >= 0.5f * L) hi -= L;
+    else if (hi < -0.5f * L) hi += L;
 }
 
-// Step two (HOOMD TwoStepLangevin semantics): bath force u*sqrt(6 gamma kT/dt) -
-// gamma v with u uniform in [-1, 1); bath torque (body frame) n*sqrt(2 gamma_r kT/dt)
-// - gamma_r L/I with n standard normal; a = (F + F_bath)/m; v += dt/2 a;
-// tnet = T + R(q) T_bath; p += dt q*(0, t_body). RNG counter (tag, step, stream).
-__global__ void k_step_two(IntegArgs a)
+// Step one for particle i with acceleration ac and net lab torque tn:
+// v += dt/2 a; x += dt v (double-float, wrapped); p += dt q*(0, t_body); NO_SQUISH
+// free rotor (axes 3, 2 at dt/2, 1 at dt, 2, 3 at dt/2); renormalise q. Zeroes the
+// force accumulators; reports whether the particle moved more than half the buffer.
+__device__ __forceinline__ void particle_step_one(const IntegArgs& a, int i, float4 v, float4 ac,
+                                                  float4 tn, float4 q, float4 p, bool& far,
+                                                  bool& bad)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.N) return;
-    const unsigned long long step = a.st->step;
+    v.x += 0.5f * a.dt * ac.x;
+    v.y += 0.5f * a.dt * ac.y;
+    v.z += 0.5f * a.dt * ac.z;
+    float4 x = a.pos[i];
+    float4 xl = a.pos_lo[i];
+    dd_advance(x.x, xl.x, a.dt * v.x, a.L.x);
+    dd_advance(x.y, xl.y, a.dt * v.y, a.L.y);
+    dd_advance(x.z, xl.z, a.dt * v.z, a.L.z);
+    const float3 tb = rot_conj(q, mk3(tn.x, tn.y, tn.z));
+    const float4 dq = qmul_vec(q, tb);
+    p.x += a.dt * dq.x;
+    p.y += a.dt * dq.y;
+    p.z += a.dt * dq.z;
+    p.w += a.dt * dq.w;
+    free_rotor(3, 0.5f * a.dt, a.inertia.z, p, q);
+    free_rotor(2, 0.5f * a.dt, a.inertia.y, p, q);
+    free_rotor(1, a.dt, a.inertia.x, p, q);
+    free_rotor(2, 0.5f * a.dt, a.inertia.y, p, q);
+    free_rotor(3, 0.5f * a.dt, a.inertia.z, p, q);
+    const float nq = rsqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+    q = make_float4(q.x * nq, q.y * nq, q.z * nq, q.w * nq);
+    bad = !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(q.x));
+    a.pos[i] = x;
+    a.pos_lo[i] = xl;
+    a.vel[i] = v;
+    a.quat[i] = q;
+    a.angmom[i] = p;
+    a.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    a.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 r = a.pos_ref[i];
+    const float3 d = min_image(mk3(x.x - r.x, x.y - r.y, x.z - r.z), a.L, a.invL);
+    far = dot(d, d) > a.half_buf2;
+}
+
+// Step two for particle i (HOOMD TwoStepLangevin semantics): bath force
+// u*sqrt(6 gamma kT/dt) - gamma v with u uniform in [-1, 1); bath torque (body frame)
+// n*sqrt(2 gamma_r kT/dt) - gamma_r L/I with n standard normal; a = (F + F_bath)/m;
+// v += dt/2 a; tnet = T + R(q) T_bath; p += dt q*(0, t_body). RNG counter is
+// (tag, step, stream) with the step number of this step.
+__device__ __forceinline__ void particle_step_two(const IntegArgs& a, int i,
+                                                  unsigned long long step, float4& v,
+                                                  float4& ac, float4& tn, float4 q, float4& p)
+{
     uint32_t r0[4] = {(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 0u};
     uint32_t r1[4] = {(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 1u};
     philox4x32(r0, a.seed_lo, a.seed_hi);
     philox4x32(r1, a.seed_lo, a.seed_hi);
     const float ct = sqrtf(6.f * a.gamma * a.kT / a.dt);
     const float cr = sqrtf(2.f * a.gamma_r * a.kT / a.dt);
-    float4 v = a.vel[i];
     const float minv = 1.f / v.w;
     const float4 F = a.force[i];
     const float inv31 = 1.f / 2147483648.f;
-    float4 ac;
     ac.x = (F.x + (float)(int32_t)r0[0] * inv31 * ct - a.gamma * v.x) * minv;
     ac.y = (F.y + (float)(int32_t)r0[1] * inv31 * ct - a.gamma * v.y) * minv;
     ac.z = (F.z + (float)(int32_t)r0[2] * inv31 * ct - a.gamma * v.z) * minv;
     ac.w = 0.f;
-    const float4 q = a.quat[i];
-    float4 p = a.angmom[i];
     // s = (1/2 conj(q) p).v : body-frame angular momentum
     const float sx = 0.5f * (q.x * p.y - p.x * q.y - (q.z * p.w - q.w * p.z));
     const float sy = 0.5f * (q.x * p.z - p.x * q.z - (q.w * p.y - q.y * p.w));
@@ -801,7 +974,7 @@ __global__ void k_step_two(IntegArgs a)
     const Frame fq = quat_frame(q);
     const float3 btl = fq.a1 * bt.x + fq.a2 * bt.y + fq.a3 * bt.z;
     const float4 T = a.torque[i];
-    const float4 tn = make_float4(T.x + btl.x, T.y + btl.y, T.z + btl.z, 0.f);
+    tn = make_float4(T.x + btl.x, T.y + btl.y, T.z + btl.z, 0.f);
     v.x += 0.5f * a.dt * ac.x;
     v.y += 0.5f * a.dt * ac.y;
     v.z += 0.5f * a.dt * ac.z;
@@ -811,10 +984,46 @@ __global__ void k_step_two(IntegArgs a)
     p.y += a.dt * dq.y;
     p.z += a.dt * dq.z;
     p.w += a.dt * dq.w;
+}
+
+// First step one of a run (accelerations and torques from prepRun / the last step).
+__global__ void k_step_one(IntegArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool far = false, bad = false;
+    if (i < a.N)
+        particle_step_one(a, i, a.vel[i], a.accel[i], a.tnet[i], a.quat[i], a.angmom[i], far, bad);
+    if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&a.st->rebuild, 1u);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&a.st->flags, kStNonFinite);
+}
+
+// Last step two of a run: also stores a and tnet so a later run can continue.
+__global__ void k_step_two(IntegArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    float4 v = a.vel[i], p = a.angmom[i], ac, tn;
+    particle_step_two(a, i, a.st->step, v, ac, tn, a.quat[i], p);
     a.vel[i] = v;
     a.angmom[i] = p;
     a.accel[i] = ac;
     a.tnet[i] = tn;
+}
+
+// Step two of step n fused with step one of step n + 1 (per particle, no grid-wide
+// dependency between them): the bath forces, kicks and drift in one pass.
+__global__ void k_step_two_one(IntegArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool far = false, bad = false;
+    if (i < a.N) {
+        float4 v = a.vel[i], p = a.angmom[i], ac, tn;
+        const float4 q = a.quat[i];
+        particle_step_two(a, i, a.st->step, v, ac, tn, q, p);
+        particle_step_one(a, i, v, ac, tn, q, p, far, bad);
+    }
+    if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&a.st->rebuild, 1u);
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&a.st->flags, kStNonFinite);
 }
 
 // prepRun: accelerations from the forces alone (no bath), as HOOMD does at run start.
