@@ -441,6 +441,7 @@ struct oxg_system {
     uint32_t* cell_count = nullptr;
     int* cell_list = nullptr;
     int2 *pairs_short = nullptr, *pairs_long = nullptr;
+    int* queue = nullptr;  // 4 deferred-term queues of cap_short entries
     long long cap_short = 0, cap_long = 0;
     float rlist2 = 0.f, rshort2 = 0.f;
     uint32_t nlist_mask = 0xffffffffu;  // term mask the current sizing was made for
@@ -475,12 +476,14 @@ int sys_alloc_nlist(oxg_system* s)
     dfree(s->cell_list);
     dfree(s->pairs_short);
     dfree(s->pairs_long);
+    dfree(s->queue);
     int rc;
     if ((rc = dalloc(&s->cell_count, (size_t)2 * s->n_cells))) return rc;
     OXG_CUDA(cudaMemset(s->cell_count, 0, sizeof(uint32_t) * 2 * s->n_cells));
     if ((rc = dalloc(&s->cell_list, (size_t)s->n_cells * s->cell_cap))) return rc;
     if ((rc = dalloc(&s->pairs_short, (size_t)s->cap_short))) return rc;
     if ((rc = dalloc(&s->pairs_long, (size_t)s->cap_long))) return rc;
+    if ((rc = dalloc(&s->queue, (size_t)4 * s->cap_short))) return rc;
     return OXG_OK;
 }
 
@@ -579,6 +582,7 @@ ForceArgs force_args(oxg_system* s, uint32_t mask, int bonded)
     a.cap_short = (int)std::min<long long>(s->cap_short, 0x7fffffff);
     a.cap_long = (int)std::min<long long>(s->cap_long, 0x7fffffff);
     a.advance_step = 0;
+    a.queue = s->queue;
     a.L = s->L;
     a.invL = s->invL;
     a.force = s->force;
@@ -620,7 +624,7 @@ int forces_grid(oxg_system* s)
 {
     if (s->grid_forces == 0) {
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces<false>, 256, s->ctx->block_bytes);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces_a<false>, 256, s->ctx->block_bytes);
         if (per_sm < 1) per_sm = 1;
         s->grid_forces = num_sms() * per_sm;
     }
@@ -638,8 +642,15 @@ int launch_nlist_forces(oxg_system* s, uint32_t mask, int bonded, bool energy, b
     ForceArgs fa = force_args(s, mask, bonded);
     fa.advance_step = md_step ? 1 : 0;
     const int grid = forces_grid(s);
-    if (energy) k_forces<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-    else k_forces<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    if (!md_step)  // MD steps: the integrator kernels reset the queue lengths
+        OXG_CUDA(cudaMemsetAsync(s->st->qcount, 0, sizeof(s->st->qcount), s->stream));
+    if (energy) {
+        k_forces_a<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+        k_forces_b<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    } else {
+        k_forces_a<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+        k_forces_b<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    }
     OXG_CUDA(cudaGetLastError());
     return OXG_OK;
 }
@@ -768,6 +779,7 @@ int oxg_system_destroy(oxg_system* s)
     dfree(s->tnet); dfree(s->pos_ref); dfree(s->force); dfree(s->torque); dfree(s->charge);
     dfree(s->bonds); dfree(s->excl); dfree(s->st); dfree(s->energy);
     dfree(s->cell_count); dfree(s->cell_list); dfree(s->pairs_short); dfree(s->pairs_long);
+    dfree(s->queue);
     dfree(s->ck_pos); dfree(s->ck_quat); dfree(s->ck_vel); dfree(s->ck_angmom);
     if (s->st_host) cudaFreeHost(s->st_host);
     delete s;
@@ -1136,7 +1148,8 @@ constexpr size_t kNaOffCellCount = na_align(kNaOffExcl + sizeof(int4) * kNaMaxPa
 constexpr size_t kNaOffCellList = na_align(kNaOffCellCount + sizeof(uint32_t) * 2 * kNaMaxCells);
 constexpr size_t kNaOffShort = na_align(kNaOffCellList + sizeof(int) * (size_t)kNaMaxCells * kNaCellCap);
 constexpr size_t kNaOffLong = na_align(kNaOffShort + sizeof(int2) * kNaShortCap);
-constexpr size_t kNaBytes = na_align(kNaOffLong + sizeof(int2) * kNaLongCap);  // ~7.8 MB
+constexpr size_t kNaOffQueue = na_align(kNaOffLong + sizeof(int2) * kNaLongCap);
+constexpr size_t kNaBytes = na_align(kNaOffQueue + sizeof(int) * 4 * kNaShortCap);  // ~11.9 MB
 
 }  // namespace
 
@@ -1187,6 +1200,7 @@ __global__ void k_noalloc_prepare(int N, float4* pos_lo, int4* excl, float4* for
         st->builds = 0u;
         st->max_cell = 0u;
         st->step = 0ull;
+        for (int q = 0; q < 4; ++q) st->qcount[q] = 0u;
         for (int t = 0; t < 16; ++t) energy[t] = 0.0;
     }
 }
@@ -1323,6 +1337,8 @@ extern "C" int oxg_pair_forces_noalloc(oxg_context* c, uint32_t mask, int N,
     fa.st_rw = st;
     fa.cap_short = na.cap_short;
     fa.cap_long = na.cap_long;
+    fa.advance_step = 0;
+    fa.queue = reinterpret_cast<int*>(scratch + kNaOffQueue);
     fa.L = na.L;
     fa.invL = na.invL;
     fa.force = reinterpret_cast<float4*>(force);
@@ -1330,10 +1346,15 @@ extern "C" int oxg_pair_forces_noalloc(oxg_context* c, uint32_t mask, int N,
     fa.energy = term_energy ? term_energy : energy_scratch;
     fa.virial = nullptr;
     int per_sm = 0;
-    OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces<true>, 256, (int)blk.size()));
+    OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces_a<true>, 256, (int)blk.size()));
     const int grid = num_sms() * std::max(1, per_sm);
-    if (term_energy) k_forces<true><<<grid, 256, blk.size(), s>>>(fa);
-    else k_forces<false><<<grid, 256, blk.size(), s>>>(fa);
+    if (term_energy) {
+        k_forces_a<true><<<grid, 256, blk.size(), s>>>(fa);
+        k_forces_b<true><<<grid, 256, blk.size(), s>>>(fa);
+    } else {
+        k_forces_a<false><<<grid, 256, blk.size(), s>>>(fa);
+        k_forces_b<false><<<grid, 256, blk.size(), s>>>(fa);
+    }
     OXG_CUDA(cudaGetLastError());
 
     DevStatus d;

@@ -39,6 +39,7 @@ struct DevStatus {
     uint32_t max_cell;     // largest cell occupancy seen
     uint32_t pad;
     unsigned long long step;  // current timestep (RNG counter)
+    uint32_t qcount[4];    // deferred-term queue lengths (k_forces_a -> k_forces_b)
 };
 
 // ------------------------------------------------------------ parameter view
@@ -196,6 +197,7 @@ struct ForceArgs {
     DevStatus* st_rw;     // rebuild flag cleared here
     int cap_short, cap_long;  // list capacities (counts past them were not stored)
     int advance_step;     // MD step: advance the RNG step counter read by step two
+    int* queue;           // 4 deferred-term queues of cap_short short-pair indices
     float3 L, invL;
     float4* force;        // accumulated (pre-zeroed)
     float4* torque;
@@ -203,14 +205,17 @@ struct ForceArgs {
     float* virial;        // unused by the engine
 };
 
-// Deferred (acos-heavy) terms of the short-range pairs. Each warp takes 32 pairs at a
-// time, evaluates the cheap terms (excluded volume, Debye) inline and runs only the
-// zero-factor tests of the heavy ones; pairs that pass go into a per-warp queue in
-// shared memory, and a queue is evaluated whenever it holds 32 pairs, so the heavy
-// code runs with every lane busy instead of with the few lanes whose pair passed.
+// The force evaluation is split in two launches so that the acos-heavy terms run with
+// every lane busy (whatever the system size):
+//  k_forces_a  one thread per short-range pair evaluates the cheap terms (excluded
+//              volume, Debye) and the zero-factor tests of the heavy ones (HB,
+//              cross-stacking, fused HB+CS, coaxial stacking), appending each pair that
+//              passes to that term's queue (warp-aggregated atomics); then the
+//              long-range (Debye-only) pairs;
+//  k_forces_b  term-uniform warps over [HB | CS | HB+CS | coax | bonds]: each warp
+//              evaluates 32 queued pairs (or bonds) of one term.
+// The integrator kernels reset the queue lengths for the next step.
 enum { kQHB = 0, kQCS = 1, kQHBX = 2, kQCX = 3, kNQ = 4 };
-constexpr int kQCap = 64;  // < 32 waiting + 32 pushed per batch
-constexpr int kForceWarps = 8;
 
 struct PairIn {
     int i, j, pidx;
@@ -296,10 +301,21 @@ __device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamVie
 }
 
 template <bool ENERGY>
-__global__ void __launch_bounds__(256) k_forces(ForceArgs a)
+__device__ __forceinline__ void reduce_energies(const ForceArgs& a, double* eacc)
+{
+    if (!ENERGY) return;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int t = 0; t < kNTerms + 3; ++t) {
+        const double sum = warp_sum(eacc[t]);
+        if (lane == 0 && sum != 0.0) atomicAdd(a.energy + t, sum);
+    }
+}
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(256) k_forces_a(ForceArgs a)
 {
     const ParamView P = stage_params(a.params, a.param_bytes);
-    __shared__ int queue[kForceWarps][kNQ][kQCap];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (a.st_rw->rebuild) {
             a.st_rw->rebuild = 0u;
@@ -316,26 +332,12 @@ __global__ void __launch_bounds__(256) k_forces(ForceArgs a)
     double eacc[kNTerms + 3];
 #pragma unroll
     for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t mask = a.mask;
-    int qn[kNQ] = {0, 0, 0, 0};  // warp-uniform queue lengths
 
-    auto drain = [&](int q, int n) {
-        const int w = lane < n ? queue[wib][q][lane] : -1;
-        __syncwarp();
-        const int rest = qn[q] - n;
-        const int moved = lane < rest ? queue[wib][q][n + lane] : 0;
-        __syncwarp();
-        if (lane < rest) queue[wib][q][lane] = moved;
-        qn[q] = rest;
-        __syncwarp();
-        if (w >= 0) eval_deferred<ENERGY>(a, P, q, w, eacc);
-    };
-
-    // ---- short-range pairs: cheap terms inline, heavy terms through the queues ----
     for (int base = gwarp * 32; base < n_short; base += nwarps * 32) {
         const int w = base + lane;
         bool want[kNQ] = {false, false, false, false};
@@ -401,23 +403,73 @@ __global__ void __launch_bounds__(256) k_forces(ForceArgs a)
 #pragma unroll
         for (int q = 0; q < kNQ; ++q) {
             const unsigned m = __ballot_sync(0xffffffffu, want[q]);
-            if (want[q]) queue[wib][q][qn[q] + __popc(m & lt_mask)] = w;
-            qn[q] += __popc(m);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                uint32_t base_q = 0;
+                if (lane == leader) base_q = atomicAdd(&a.st_rw->qcount[q], (uint32_t)__popc(m));
+                base_q = __shfl_sync(0xffffffffu, base_q, leader);
+                if (want[q]) a.queue[(size_t)q * a.cap_short + base_q + __popc(m & lt_mask)] = w;
+            }
         }
-        __syncwarp();
-#pragma unroll
-        for (int q = 0; q < kNQ; ++q)
-            if (qn[q] >= 32) drain(q, 32);
     }
-#pragma unroll
-    for (int q = 0; q < kNQ; ++q)
-        if (qn[q] > 0) drain(q, qn[q]);
 
-    // ---- bonds (FENE FP64, bonded excluded volume, stacking) ----
-    const int n_bonds = a.bonded ? a.n_bonds : 0;
+    // long-range pairs: Debye only (uniform, cheap)
+    const uint32_t long_mask = mask & (1u << kDebye);
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
-    for (int b = tid; b < n_bonds; b += nthreads) {
-        const int4 bd = a.bonds[b];
+    for (int w = tid; w < n_long && long_mask; w += nthreads) {
+        const int2 pr = a.pairs_long[w];
+        const int i = pr.x, j = pr.y;
+        const float4 pi = a.pos[i], pj = a.pos[j];
+        const int ti = type_of(pi), tj = type_of(pj);
+        if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
+            bad_type = true;
+            continue;
+        }
+        const float3 dr = min_image(pair_delta(pi, a.pos_lo[i], pj, a.pos_lo[j]), a.L, a.invL);
+        PairAcc acc;
+        acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+        float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
+        if (eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), a.quat[i], a.quat[j], ci,
+                      cj, acc, E)) {
+            if (ENERGY) eacc[kDebye] += (double)E[kDebye];
+            scatter<ENERGY>(a, i, j, acc, E[kDebye]);
+        }
+    }
+    reduce_energies<ENERGY>(a, eacc);
+    if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
+}
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(256) k_forces_b(ForceArgs a)
+{
+    const ParamView P = stage_params(a.params, a.param_bytes);
+    const int n_types = P.h().n_types;
+    // segments [HB | CS | HB+CS | coax | bonds], each padded to whole warps
+    int cnt[kNQ + 1], seg[kNQ + 2];
+    seg[0] = 0;
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) cnt[q] = (int)min(a.st->qcount[q], (uint32_t)a.cap_short);
+    cnt[kNQ] = a.bonded ? a.n_bonds : 0;
+#pragma unroll
+    for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
+    double eacc[kNTerms + 3];
+#pragma unroll
+    for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
+    bool bad_type = false;
+    const int lane = threadIdx.x & 31;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int wbase = gwarp * 32; wbase < seg[kNQ + 1]; wbase += nwarps * 32) {
+        int q = 0;
+        while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
+        const int k = wbase - seg[q] + lane;
+        if (k >= cnt[q]) continue;
+        if (q < kNQ) {
+            eval_deferred<ENERGY>(a, P, q, a.queue[(size_t)q * a.cap_short + k], eacc);
+            continue;
+        }
+        const int4 bd = a.bonds[k];
         const int A = bd.x, B = bd.y;
         const float4 pA = a.pos[A], pB = a.pos[B];
         if ((unsigned)type_of(pA) >= (unsigned)n_types || (unsigned)type_of(pB) >= (unsigned)n_types) {
@@ -442,37 +494,7 @@ __global__ void __launch_bounds__(256) k_forces(ForceArgs a)
         atomicAdd(a.torque + A, make_float4(acc.tA.x, acc.tA.y, acc.tA.z, 0.f));
         atomicAdd(a.torque + B, make_float4(acc.tB.x, acc.tB.y, acc.tB.z, 0.f));
     }
-
-    // ---- long-range pairs: Debye only ----
-    const uint32_t long_mask = mask & (1u << kDebye);
-    for (int w = tid; w < n_long && long_mask; w += nthreads) {
-        const int2 pr = a.pairs_long[w];
-        const int i = pr.x, j = pr.y;
-        const float4 pi = a.pos[i], pj = a.pos[j];
-        const int ti = type_of(pi), tj = type_of(pj);
-        if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
-            bad_type = true;
-            continue;
-        }
-        const float3 dr = min_image(pair_delta(pi, a.pos_lo[i], pj, a.pos_lo[j]), a.L, a.invL);
-        PairAcc acc;
-        acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
-        float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
-        if (eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), a.quat[i], a.quat[j], ci,
-                      cj, acc, E)) {
-            if (ENERGY) eacc[kDebye] += (double)E[kDebye];
-            scatter<ENERGY>(a, i, j, acc, E[kDebye]);
-        }
-    }
-
-    if (ENERGY) {
-#pragma unroll
-        for (int t = 0; t < kNTerms + 3; ++t) {
-            const double sum = warp_sum(eacc[t]);
-            if (lane == 0 && sum != 0.0) atomicAdd(a.energy + t, sum);
-        }
-    }
+    reduce_energies<ENERGY>(a, eacc);
     if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
 }
 
@@ -987,9 +1009,15 @@ __device__ __forceinline__ void particle_step_two(const IntegArgs& a, int i,
 }
 
 // First step one of a run (accelerations and torques from prepRun / the last step).
+__device__ __forceinline__ void reset_queues(DevStatus* st)
+{
+    if (blockIdx.x == 0 && threadIdx.x < 4) st->qcount[threadIdx.x] = 0u;
+}
+
 __global__ void k_step_one(IntegArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    reset_queues(a.st);
     bool far = false, bad = false;
     if (i < a.N)
         particle_step_one(a, i, a.vel[i], a.accel[i], a.tnet[i], a.quat[i], a.angmom[i], far, bad);
@@ -1001,6 +1029,7 @@ __global__ void k_step_one(IntegArgs a)
 __global__ void k_step_two(IntegArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    reset_queues(a.st);
     if (i >= a.N) return;
     float4 v = a.vel[i], p = a.angmom[i], ac, tn;
     particle_step_two(a, i, a.st->step, v, ac, tn, a.quat[i], p);
@@ -1015,6 +1044,7 @@ __global__ void k_step_two(IntegArgs a)
 __global__ void k_step_two_one(IntegArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    reset_queues(a.st);
     bool far = false, bad = false;
     if (i < a.N) {
         float4 v = a.vel[i], p = a.angmom[i], ac, tn;
@@ -1030,6 +1060,7 @@ __global__ void k_step_two_one(IntegArgs a)
 __global__ void k_prep_accel(IntegArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    reset_queues(a.st);
     if (i >= a.N) return;
     const float4 F = a.force[i], T = a.torque[i], v = a.vel[i];
     const float minv = 1.f / v.w;

@@ -276,7 +276,7 @@ int oxg_system_stats(oxg_system* sys, int64_t* out, int n);
  * Same evaluation as the system engine's nonbonded forces (cell list with bond
  * exclusions, split pair lists, the fused force kernel), but every scratch buffer it
  * needs lives in one fixed-size static device array inside this library (about
- * 7.8 MB, held by every GPU that loads the library until the process exits). The
+ * 11.9 MB, held by every GPU that loads the library until the process exits). The
  * call allocates nothing: no cudaMalloc, cudaFree or allocating library routine.
  *
  * Inputs (device): pos_type[4*N] (x, y, z, type as the float's int bits), quat[4*N],
