@@ -1372,3 +1372,40 @@ extern "C" int oxg_pair_forces_noalloc(oxg_context* c, uint32_t mask, int N,
                                              std::to_string(kNaLongCap) + " long)");
     return OXG_OK;
 }
+
+// =================================================================== internal helpers
+#include "oxg_internal.h"
+
+namespace oxg {
+
+int internal_set_error(int code, const std::string& msg) { return set_err(code, msg); }
+int internal_assemble_block(const oxg_context* c, std::vector<unsigned char>& out)
+{
+    return assemble_block(c, out);
+}
+uint32_t internal_present_mask(const oxg_context* c) { return present_mask(c); }
+double internal_max_rcut(const oxg_context* c, uint32_t mask, bool short_only)
+{
+    double r = 0.0;
+    auto upd = [&](bool any, const double* rc, bool is_short, int t) {
+        if (!any || !((mask >> t) & 1u) || (short_only && !is_short)) return;
+        for (int k = 0; k < kMaxPairs; ++k) r = std::max(r, rc[k]);
+    };
+    upd(c->excvol.any, c->excvol.rcut, true, kExcVol);
+    upd(c->hbond.any, c->hbond.rcut, true, kHBond);
+    upd(c->cross.any, c->cross.rcut, true, kCross);
+    upd(c->hbx.any, c->hbx.rcut, true, kHBCross);
+    upd(c->coax.any, c->coax.rcut, true, kCoax);
+    upd(c->debye.any, c->debye.rcut, false, kDebye);
+    return r;
+}
+int internal_n_types(const oxg_context* c) { return c->n_types; }
+bool internal_bonded_complete(const oxg_context* c)
+{
+    for (int t = 0; t < c->n_bond_types; ++t)
+        if (!c->bonded_set[t]) return false;
+    return true;
+}
+int internal_num_sms() { return num_sms(); }
+
+}  // namespace oxg

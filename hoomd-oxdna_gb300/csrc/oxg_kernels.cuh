@@ -632,6 +632,7 @@ struct BondDropinArgs {
     uint32_t* status;
 };
 
+#ifndef OXG_DEVICE_FUNCTIONS_ONLY  // the engine's translation unit defines the kernels
 __global__ void __launch_bounds__(256) k_bonds_dropin(BondDropinArgs a)
 {
     const ParamView P = stage_params(a.params, a.param_bytes);
@@ -685,6 +686,7 @@ __global__ void __launch_bounds__(256) k_bonds_dropin(BondDropinArgs a)
     }
     if (bad) atomicOr(a.status, kStBadIndex);
 }
+#endif
 
 // ------------------------------------------------------------ neighbour list
 struct NlistArgs {
@@ -714,6 +716,7 @@ __device__ __forceinline__ int cell_coord(float x, float invL, int n)
     return c >= n ? n - 1 : (c < 0 ? 0 : c);
 }
 
+#ifndef OXG_DEVICE_FUNCTIONS_ONLY
 __global__ void k_nlist_bin(NlistArgs a)
 {
     if (!a.st->rebuild) return;
@@ -738,6 +741,7 @@ __global__ void k_nlist_bin(NlistArgs a)
     else atomicOr(&a.st->flags, kStCellOverflow);
     atomicMax(&a.st->max_cell, slot + 1u);
 }
+#endif
 
 __device__ __forceinline__ bool is_excluded(int4 e, int j) { return e.x == j || e.y == j || e.z == j || e.w == j; }
 
@@ -798,6 +802,7 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t n)
     return base + incl - n;
 }
 
+#ifndef OXG_DEVICE_FUNCTIONS_ONLY
 __global__ void k_nlist_pairs(NlistArgs a)
 {
     if (!a.st->rebuild) return;
@@ -832,6 +837,7 @@ __global__ void k_nlist_pairs(NlistArgs a)
     if (over) atomicOr(&a.st->flags, kStPairOverflow);
     if (i == 0) atomicAdd(&a.st->builds, 1u);
 }
+#endif
 
 // ------------------------------------------------------------------ integrator
 __device__ __forceinline__ void philox4x32(uint32_t c[4], uint32_t k0, uint32_t k1)
@@ -913,70 +919,66 @@ __device__ __forceinline__ void dd_advance(float& hi, float& lo, float d, float 
     else if (hi < -0.5f * L) hi += L;
 }
 
-// Step one for particle i with acceleration ac and net lab torque tn:
-// v += dt/2 a; x += dt v (double-float, wrapped); p += dt q*(0, t_body); NO_SQUISH
-// free rotor (axes 3, 2 at dt/2, 1 at dt, 2, 3 at dt/2); renormalise q. Zeroes the
-// force accumulators; reports whether the particle moved more than half the buffer.
-__device__ __forceinline__ void particle_step_one(const IntegArgs& a, int i, float4 v, float4 ac,
-                                                  float4 tn, float4 q, float4 p, bool& far,
-                                                  bool& bad)
+// Per-particle integrator state (positions double-float).
+struct PState {
+    float4 x, xl, v, q, p;  // x.w = type bits, v.w = mass
+};
+
+// Step one with acceleration ac and net lab torque tn: v += dt/2 a; x += dt v
+// (double-float, wrapped into [-L/2, L/2)); p += dt q*(0, t_body); NO_SQUISH free rotor
+// (axes 3, 2 at dt/2, 1 at dt, 2, 3 at dt/2); renormalise q. Returns false on a
+// non-finite result.
+__device__ __forceinline__ bool step_one_pure(PState& s, float4 ac, float4 tn, float dt, float3 L,
+                                              float3 inertia)
 {
-    v.x += 0.5f * a.dt * ac.x;
-    v.y += 0.5f * a.dt * ac.y;
-    v.z += 0.5f * a.dt * ac.z;
-    float4 x = a.pos[i];
-    float4 xl = a.pos_lo[i];
-    dd_advance(x.x, xl.x, a.dt * v.x, a.L.x);
-    dd_advance(x.y, xl.y, a.dt * v.y, a.L.y);
-    dd_advance(x.z, xl.z, a.dt * v.z, a.L.z);
+    s.v.x += 0.5f * dt * ac.x;
+    s.v.y += 0.5f * dt * ac.y;
+    s.v.z += 0.5f * dt * ac.z;
+    dd_advance(s.x.x, s.xl.x, dt * s.v.x, L.x);
+    dd_advance(s.x.y, s.xl.y, dt * s.v.y, L.y);
+    dd_advance(s.x.z, s.xl.z, dt * s.v.z, L.z);
+    float4 q = s.q, p = s.p;
     const float3 tb = rot_conj(q, mk3(tn.x, tn.y, tn.z));
     const float4 dq = qmul_vec(q, tb);
-    p.x += a.dt * dq.x;
-    p.y += a.dt * dq.y;
-    p.z += a.dt * dq.z;
-    p.w += a.dt * dq.w;
-    free_rotor(3, 0.5f * a.dt, a.inertia.z, p, q);
-    free_rotor(2, 0.5f * a.dt, a.inertia.y, p, q);
-    free_rotor(1, a.dt, a.inertia.x, p, q);
-    free_rotor(2, 0.5f * a.dt, a.inertia.y, p, q);
-    free_rotor(3, 0.5f * a.dt, a.inertia.z, p, q);
+    p.x += dt * dq.x;
+    p.y += dt * dq.y;
+    p.z += dt * dq.z;
+    p.w += dt * dq.w;
+    free_rotor(3, 0.5f * dt, inertia.z, p, q);
+    free_rotor(2, 0.5f * dt, inertia.y, p, q);
+    free_rotor(1, dt, inertia.x, p, q);
+    free_rotor(2, 0.5f * dt, inertia.y, p, q);
+    free_rotor(3, 0.5f * dt, inertia.z, p, q);
     const float nq = rsqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
-    q = make_float4(q.x * nq, q.y * nq, q.z * nq, q.w * nq);
-    bad = !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(q.x));
-    a.pos[i] = x;
-    a.pos_lo[i] = xl;
-    a.vel[i] = v;
-    a.quat[i] = q;
-    a.angmom[i] = p;
-    a.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    a.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 r = a.pos_ref[i];
-    const float3 d = min_image(mk3(x.x - r.x, x.y - r.y, x.z - r.z), a.L, a.invL);
-    far = dot(d, d) > a.half_buf2;
+    s.q = make_float4(q.x * nq, q.y * nq, q.z * nq, q.w * nq);
+    s.p = p;
+    return isfinite(s.x.x) && isfinite(s.x.y) && isfinite(s.x.z) && isfinite(s.q.x);
 }
 
-// Step two for particle i (HOOMD TwoStepLangevin semantics): bath force
-// u*sqrt(6 gamma kT/dt) - gamma v with u uniform in [-1, 1); bath torque (body frame)
-// n*sqrt(2 gamma_r kT/dt) - gamma_r L/I with n standard normal; a = (F + F_bath)/m;
-// v += dt/2 a; tnet = T + R(q) T_bath; p += dt q*(0, t_body). RNG counter is
-// (tag, step, stream) with the step number of this step.
-__device__ __forceinline__ void particle_step_two(const IntegArgs& a, int i,
-                                                  unsigned long long step, float4& v,
-                                                  float4& ac, float4& tn, float4 q, float4& p)
+// Step two (HOOMD TwoStepLangevin semantics) with force F and torque T: bath force
+// u*sqrt(6 gamma kT/dt) - gamma v, u uniform in [-1, 1); bath torque (body frame)
+// n*sqrt(2 gamma_r kT/dt) - gamma_r L/I, n standard normal; a = (F + F_bath)/m;
+// v += dt/2 a; tnet = T + R(q) T_bath; p += dt q*(0, t_body). The Philox counter is
+// (tag, step, stream) under the key (seed_lo, seed_hi).
+__device__ __forceinline__ void step_two_pure(PState& s, float4 F, float4 T, uint32_t tag,
+                                              unsigned long long step, uint32_t seed_lo,
+                                              uint32_t seed_hi, float dt, float kT, float gamma,
+                                              float gamma_r, float3 inertia, float4& ac, float4& tn)
 {
-    uint32_t r0[4] = {(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 0u};
-    uint32_t r1[4] = {(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 1u};
-    philox4x32(r0, a.seed_lo, a.seed_hi);
-    philox4x32(r1, a.seed_lo, a.seed_hi);
-    const float ct = sqrtf(6.f * a.gamma * a.kT / a.dt);
-    const float cr = sqrtf(2.f * a.gamma_r * a.kT / a.dt);
-    const float minv = 1.f / v.w;
-    const float4 F = a.force[i];
+    uint32_t r0[4] = {tag, (uint32_t)step, (uint32_t)(step >> 32), 0u};
+    uint32_t r1[4] = {tag, (uint32_t)step, (uint32_t)(step >> 32), 1u};
+    philox4x32(r0, seed_lo, seed_hi);
+    philox4x32(r1, seed_lo, seed_hi);
+    const float ct = sqrtf(6.f * gamma * kT / dt);
+    const float cr = sqrtf(2.f * gamma_r * kT / dt);
+    const float minv = 1.f / s.v.w;
     const float inv31 = 1.f / 2147483648.f;
-    ac.x = (F.x + (float)(int32_t)r0[0] * inv31 * ct - a.gamma * v.x) * minv;
-    ac.y = (F.y + (float)(int32_t)r0[1] * inv31 * ct - a.gamma * v.y) * minv;
-    ac.z = (F.z + (float)(int32_t)r0[2] * inv31 * ct - a.gamma * v.z) * minv;
+    ac.x = (F.x + (float)(int32_t)r0[0] * inv31 * ct - gamma * s.v.x) * minv;
+    ac.y = (F.y + (float)(int32_t)r0[1] * inv31 * ct - gamma * s.v.y) * minv;
+    ac.z = (F.z + (float)(int32_t)r0[2] * inv31 * ct - gamma * s.v.z) * minv;
     ac.w = 0.f;
+    const float4 q = s.q;
+    float4 p = s.p;
     // s = (1/2 conj(q) p).v : body-frame angular momentum
     const float sx = 0.5f * (q.x * p.y - p.x * q.y - (q.z * p.w - q.w * p.z));
     const float sy = 0.5f * (q.x * p.z - p.x * q.z - (q.w * p.y - q.y * p.w));
@@ -990,22 +992,59 @@ __device__ __forceinline__ void particle_step_two(const IntegArgs& a, int i,
     float s2a, c2a, s2b, c2b;
     sincosf(2.f * kPi * u2, &s2a, &c2a);
     sincosf(2.f * kPi * u4, &s2b, &c2b);
-    const float3 bt = mk3(ra * c2a * cr - a.gamma_r * sx / a.inertia.x,
-                          ra * s2a * cr - a.gamma_r * sy / a.inertia.y,
-                          rb * c2b * cr - a.gamma_r * sz / a.inertia.z);
+    const float3 bt = mk3(ra * c2a * cr - gamma_r * sx / inertia.x,
+                          ra * s2a * cr - gamma_r * sy / inertia.y,
+                          rb * c2b * cr - gamma_r * sz / inertia.z);
     const Frame fq = quat_frame(q);
     const float3 btl = fq.a1 * bt.x + fq.a2 * bt.y + fq.a3 * bt.z;
-    const float4 T = a.torque[i];
     tn = make_float4(T.x + btl.x, T.y + btl.y, T.z + btl.z, 0.f);
-    v.x += 0.5f * a.dt * ac.x;
-    v.y += 0.5f * a.dt * ac.y;
-    v.z += 0.5f * a.dt * ac.z;
+    s.v.x += 0.5f * dt * ac.x;
+    s.v.y += 0.5f * dt * ac.y;
+    s.v.z += 0.5f * dt * ac.z;
     const float3 tb = rot_conj(q, mk3(tn.x, tn.y, tn.z));
     const float4 dq = qmul_vec(q, tb);
-    p.x += a.dt * dq.x;
-    p.y += a.dt * dq.y;
-    p.z += a.dt * dq.z;
-    p.w += a.dt * dq.w;
+    p.x += dt * dq.x;
+    p.y += dt * dq.y;
+    p.z += dt * dq.z;
+    p.w += dt * dq.w;
+    s.p = p;
+}
+
+__device__ __forceinline__ PState load_pstate(const IntegArgs& a, int i)
+{
+    PState s;
+    s.x = a.pos[i];
+    s.xl = a.pos_lo[i];
+    s.v = a.vel[i];
+    s.q = a.quat[i];
+    s.p = a.angmom[i];
+    return s;
+}
+
+// Step one of particle i in the resident arrays; zeroes its force accumulators and
+// reports whether it moved more than half the buffer since the last list build.
+__device__ __forceinline__ void particle_step_one(const IntegArgs& a, int i, PState s, float4 ac,
+                                                  float4 tn, bool& far, bool& bad)
+{
+    bad = !step_one_pure(s, ac, tn, a.dt, a.L, a.inertia);
+    a.pos[i] = s.x;
+    a.pos_lo[i] = s.xl;
+    a.vel[i] = s.v;
+    a.quat[i] = s.q;
+    a.angmom[i] = s.p;
+    a.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    a.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 r = a.pos_ref[i];
+    const float3 d = min_image(mk3(s.x.x - r.x, s.x.y - r.y, s.x.z - r.z), a.L, a.invL);
+    far = dot(d, d) > a.half_buf2;
+}
+
+__device__ __forceinline__ void particle_step_two(const IntegArgs& a, int i,
+                                                  unsigned long long step, PState& s, float4& ac,
+                                                  float4& tn)
+{
+    step_two_pure(s, a.force[i], a.torque[i], (uint32_t)i, step, a.seed_lo, a.seed_hi, a.dt, a.kT,
+                  a.gamma, a.gamma_r, a.inertia, ac, tn);
 }
 
 // First step one of a run (accelerations and torques from prepRun / the last step).
@@ -1014,13 +1053,13 @@ __device__ __forceinline__ void reset_queues(DevStatus* st)
     if (blockIdx.x == 0 && threadIdx.x < 4) st->qcount[threadIdx.x] = 0u;
 }
 
+#ifndef OXG_DEVICE_FUNCTIONS_ONLY
 __global__ void k_step_one(IntegArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     reset_queues(a.st);
     bool far = false, bad = false;
-    if (i < a.N)
-        particle_step_one(a, i, a.vel[i], a.accel[i], a.tnet[i], a.quat[i], a.angmom[i], far, bad);
+    if (i < a.N) particle_step_one(a, i, load_pstate(a, i), a.accel[i], a.tnet[i], far, bad);
     if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&a.st->rebuild, 1u);
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&a.st->flags, kStNonFinite);
 }
@@ -1031,10 +1070,11 @@ __global__ void k_step_two(IntegArgs a)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     reset_queues(a.st);
     if (i >= a.N) return;
-    float4 v = a.vel[i], p = a.angmom[i], ac, tn;
-    particle_step_two(a, i, a.st->step, v, ac, tn, a.quat[i], p);
-    a.vel[i] = v;
-    a.angmom[i] = p;
+    PState s = load_pstate(a, i);
+    float4 ac, tn;
+    particle_step_two(a, i, a.st->step, s, ac, tn);
+    a.vel[i] = s.v;
+    a.angmom[i] = s.p;
     a.accel[i] = ac;
     a.tnet[i] = tn;
 }
@@ -1047,10 +1087,10 @@ __global__ void k_step_two_one(IntegArgs a)
     reset_queues(a.st);
     bool far = false, bad = false;
     if (i < a.N) {
-        float4 v = a.vel[i], p = a.angmom[i], ac, tn;
-        const float4 q = a.quat[i];
-        particle_step_two(a, i, a.st->step, v, ac, tn, q, p);
-        particle_step_one(a, i, v, ac, tn, q, p, far, bad);
+        PState s = load_pstate(a, i);
+        float4 ac, tn;
+        particle_step_two(a, i, a.st->step, s, ac, tn);
+        particle_step_one(a, i, s, ac, tn, far, bad);
     }
     if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&a.st->rebuild, 1u);
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&a.st->flags, kStNonFinite);
@@ -1067,5 +1107,6 @@ __global__ void k_prep_accel(IntegArgs a)
     a.accel[i] = make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f);
     a.tnet[i] = make_float4(T.x, T.y, T.z, 0.f);
 }
+#endif
 
 }  // namespace oxg

@@ -237,6 +237,9 @@ EXPORTS = [
     "oxg_system_set_nlist_buffer", "oxg_system_compute", "oxg_system_set_integrator",
     "oxg_system_run", "oxg_system_energies", "oxg_system_stats", "oxg_last_error",
     "oxg_version", "oxg_status_string", "oxg_pair_forces_noalloc",
+    "oxg_batch_create", "oxg_batch_destroy", "oxg_batch_set_stream", "oxg_batch_set_state",
+    "oxg_batch_get_state", "oxg_batch_set_integrator", "oxg_batch_set_tiling", "oxg_batch_tune",
+    "oxg_batch_run", "oxg_batch_compute",
 ]
 
 _lib = None
@@ -292,6 +295,17 @@ def lib():
         "oxg_system_energies": ([vp, vp, vp], i32),
         "oxg_system_stats": ([vp, C.POINTER(C.c_int64), i32], i32),
         "oxg_pair_forces_noalloc": ([vp, u32, i32, vp, vp, vp, fp, i32, vp, vp, vp, vp, vp], i32),
+        "oxg_batch_create": ([C.POINTER(vp), i32, C.POINTER(vp), C.POINTER(C.c_int32), fp,
+                              C.POINTER(C.c_int32), C.POINTER(C.c_int32)], i32),
+        "oxg_batch_destroy": ([vp], i32),
+        "oxg_batch_set_stream": ([vp, vp], i32),
+        "oxg_batch_set_state": ([vp, vp, vp, vp, vp, vp, vp], i32),
+        "oxg_batch_get_state": ([vp, vp, vp, vp, vp, vp], i32),
+        "oxg_batch_set_integrator": ([vp, f64, dp, f64, f64, C.c_uint64, u32, i32], i32),
+        "oxg_batch_set_tiling": ([vp, i32, i32], i32),
+        "oxg_batch_tune": ([vp, i32, C.POINTER(C.c_int), C.POINTER(C.c_int), dp], i32),
+        "oxg_batch_run": ([vp, C.c_long], i32),
+        "oxg_batch_compute": ([vp, u32, i32, vp, vp, vp], i32),
         "oxg_last_error": ([], C.c_char_p),
         "oxg_version": ([], C.c_char_p),
         "oxg_status_string": ([i32], C.c_char_p),

@@ -231,10 +231,19 @@ class Simulation:
     def _attach(self):
         if self._attached:
             return
+        self._make_context()
+        self._make_system()
+
+    def _make_context(self):
+        """Native parameter context from the attached forces (sets _ctx, _mask,
+        _bonded, _nlist, _langevin)."""
         integ = self.operations.integrator
         if integ is None:
             raise RuntimeError("no integrator set")
         L = _abi.lib()
+        if self._ctx:
+            L.oxg_destroy(self._ctx)
+            self._ctx = None
         snap = self._snap
         types = self._types()
         nt = len(types)
@@ -279,6 +288,21 @@ class Simulation:
                                    "set params")
             else:
                 raise TypeError(f"unsupported force {type(f).__name__}")
+        self._mask = 0
+        for t in self._pair_forces:
+            self._mask |= 1 << t
+        lang = [m for m in integ.methods if isinstance(m, _Langevin)]
+        if len(integ.methods) != len(lang) or len(lang) > 1:
+            raise RuntimeError("only a single Langevin method is supported")
+        self._langevin = lang[0] if lang else None
+        if self._langevin is not None and not integ.integrate_rotational_dof:
+            raise RuntimeError("oxDNA dynamics need integrate_rotational_dof=True")
+
+    def _make_system(self):
+        L = _abi.lib()
+        snap = self._snap
+        integ = self.operations.integrator
+        ctx = self._ctx
         n = snap.particles.N
         box = (C.c_float * 3)(*[float(x) for x in snap.configuration.box[:3]])
         bonds = np.zeros((max(1, snap.bonds.N), 3), dtype=np.int32)
@@ -295,16 +319,7 @@ class Simulation:
         if self._nlist is not None:
             _abi.check(L.oxg_system_set_nlist_buffer(sys_, self._nlist.buffer), "set buffer")
         self._push_state()
-        self._mask = 0
-        for t in self._pair_forces:
-            self._mask |= 1 << t
-        lang = [m for m in integ.methods if isinstance(m, _Langevin)]
-        if len(integ.methods) != len(lang) or len(lang) > 1:
-            raise RuntimeError("only a single Langevin method is supported")
-        self._langevin = lang[0] if lang else None
         if self._langevin is not None:
-            if not integ.integrate_rotational_dof:
-                raise RuntimeError("oxDNA dynamics need integrate_rotational_dof=True")
             _abi.check(L.oxg_system_set_integrator(
                 sys_, integ.dt, self._langevin.kT, self._langevin.default_gamma,
                 self._langevin.default_gamma_r[0], self.seed, self._mask,
@@ -327,6 +342,16 @@ class Simulation:
 
     def _push_state(self):
         L = _abi.lib()
+        pos, lo, q, vel, am, ch = self._state_arrays()
+        vp = C.c_void_p
+        _abi.check(L.oxg_system_set_state(self._sys, vp(pos.ctypes.data), vp(lo.ctypes.data),
+                                          vp(q.ctypes.data), vp(vel.ctypes.data),
+                                          vp(am.ctypes.data), vp(ch.ctypes.data)),
+                   "oxg_system_set_state")
+
+    def _state_arrays(self):
+        """The snapshot as engine arrays: pos_type, pos_lo, quat, vel (mass in w),
+        angmom (float32, N x 4) and charge (N)."""
         p = self._snap.particles
         n = p.N
         pos = np.zeros((n, 4), np.float32)
@@ -341,11 +366,7 @@ class Simulation:
         q = _f32(p.orientation)
         am = _f32(p.angmom)
         ch = _f32(p.charge)
-        vp = C.c_void_p
-        _abi.check(L.oxg_system_set_state(self._sys, vp(pos.ctypes.data), vp(lo.ctypes.data),
-                                          vp(q.ctypes.data), vp(vel.ctypes.data),
-                                          vp(am.ctypes.data), vp(ch.ctypes.data)),
-                   "oxg_system_set_state")
+        return pos, lo, q, vel, am, ch
 
     def _pull_snapshot(self):
         import copy

@@ -267,6 +267,44 @@ int oxg_system_energies(oxg_system* sys, double* pair_energy, double* bonded_ene
  * 3 pair-list entries (long), 4 kernels launched per step. */
 int oxg_system_stats(oxg_system* sys, int64_t* out, int n);
 
+/* ---- batched independent replicas ---------------------------------------------
+ * No counterpart in the reference (which runs one HOOMD simulation per process):
+ * R small systems stepped together in one persistent launch. Replica r has its own
+ * context ctxs[r] (parameters, e.g. temperature-dependent stacking and Debye terms),
+ * n_particles[r] particles, periodic box boxes[3r..3r+2], and n_bonds[r] bonds
+ * (A, B, type) in replica-local indices, stored back to back in `bonds`. The state
+ * arrays of oxg_batch_set_state / get_state hold the replicas back to back (replica
+ * r starts at particle sum(n_particles[0..r-1])), in the oxg_system_set_state layout.
+ * Replica r integrates with Langevin at kT[r] and Philox seed `seed + r`, so it
+ * reproduces an oxg_system run of the same replica with that seed. Every pair of a
+ * replica is tested (no neighbour list): meant for replicas of up to 512 particles.
+ */
+typedef struct oxg_batch oxg_batch;
+int oxg_batch_create(oxg_batch** out, int n_replicas, oxg_context* const* ctxs,
+                     const int32_t* n_particles, const float* boxes, const int32_t* n_bonds,
+                     const int32_t* bonds);
+int oxg_batch_destroy(oxg_batch* b);
+int oxg_batch_set_stream(oxg_batch* b, void* stream);
+/* host arrays, back to back over the replicas; NULL leaves a field unchanged */
+int oxg_batch_set_state(oxg_batch* b, const float* pos_type, const float* pos_lo, const float* quat,
+                        const float* vel, const float* angmom, const float* charge);
+int oxg_batch_get_state(oxg_batch* b, float* pos_type, float* pos_lo, float* quat, float* vel,
+                        float* angmom);
+/* kT: n_replicas temperatures; mask/bonded select the terms as in oxg_system_set_integrator */
+int oxg_batch_set_integrator(oxg_batch* b, double dt, const double* kT, double gamma,
+                             double gamma_r, uint64_t seed, uint32_t term_mask, int bonded);
+/* tile shape: at most tile_particles particles per CTA (1..512), threads 64/128/256 */
+int oxg_batch_set_tiling(oxg_batch* b, int tile_particles, int threads);
+/* time trial_steps for each admissible tile shape, keep the fastest (state unchanged) */
+int oxg_batch_tune(oxg_batch* b, int trial_steps, int* tile_particles, int* threads,
+                   double* best_ms);
+int oxg_batch_run(oxg_batch* b, long nsteps);
+/* host outputs: force[4N], torque[4N] (may be NULL), energies[9 * n_replicas] = per
+ * replica the OXG_N_PAIR_TERMS pair-term totals then FENE, bonded excluded volume and
+ * stacking */
+int oxg_batch_compute(oxg_batch* b, uint32_t term_mask, int bonded, float* force,
+                      float* torque, double* energies);
+
 /* ---- allocation-free nonbonded evaluation -------------------------------------
  * No counterpart in the reference: an addition for callers that cannot allocate GPU
  * memory at all, e.g. code running inside a framework that has reserved the whole
