@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -464,6 +465,10 @@ struct oxg_system {
     int graph_steps = 0;
     uint64_t graph_key = ~0ull;
     int grid_forces = 0;
+    // persistent run kernel
+    GridBarrier* bar = nullptr;
+    int grid_run = 0;
+    bool persistent = true;
     // stats
     long long steps_run = 0;
 };
@@ -744,8 +749,9 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
         (rc = dalloc(&s->charge, N)) || (rc = dalloc(&s->bonds, std::max(1, n_bonds))) ||
         (rc = dalloc(&s->excl, N)) || (rc = dalloc(&s->st, 1)) || (rc = dalloc(&s->energy, 9)) ||
         (rc = dalloc(&s->ck_pos, N)) || (rc = dalloc(&s->ck_quat, N)) || (rc = dalloc(&s->ck_vel, N)) ||
-        (rc = dalloc(&s->ck_angmom, N)))
+        (rc = dalloc(&s->ck_angmom, N)) || (rc = dalloc(&s->bar, 1)))
         return fail(rc);
+    if (const char* m = std::getenv("OXG_RUN_MODE")) s->persistent = std::string(m) != "graph";
     if (cudaMallocHost((void**)&s->st_host, sizeof(DevStatus)) != cudaSuccess)
         return fail(set_err(OXG_ERR_CUDA, "cudaMallocHost failed"));
     cudaMemcpy(s->bonds, bnd.data(), sizeof(int4) * bnd.size(), cudaMemcpyHostToDevice);
@@ -781,6 +787,7 @@ int oxg_system_destroy(oxg_system* s)
     dfree(s->cell_count); dfree(s->cell_list); dfree(s->pairs_short); dfree(s->pairs_long);
     dfree(s->queue);
     dfree(s->ck_pos); dfree(s->ck_quat); dfree(s->ck_vel); dfree(s->ck_angmom);
+    dfree(s->bar);
     if (s->st_host) cudaFreeHost(s->st_host);
     delete s;
     return OXG_OK;
@@ -988,6 +995,67 @@ static int checkpoint(oxg_system* s, bool restore)
     return OXG_OK;
 }
 
+// The persistent run kernel: one cooperative launch of `bodies` step bodies.
+static int launch_run(oxg_system* s, int bodies, bool closing)
+{
+    const int block_bytes = s->ctx->block_bytes;
+    if (s->grid_run == 0) {
+        int per_sm = 0;
+        OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run, 256, block_bytes));
+        if (per_sm < 1) return set_err(OXG_ERR_CUDA, "the run kernel does not fit on an SM");
+        s->grid_run = num_sms() * std::min(per_sm, 2);
+    }
+    RunArgs ra;
+    ra.f = force_args(s, s->run_mask, s->run_bonded);
+    ra.n = nlist_args(s);
+    ra.g = integ_args(s);
+    ra.bar = s->bar;
+    ra.bodies = bodies;
+    ra.closing = closing ? 1 : 0;
+    OXG_CUDA(cudaMemsetAsync(s->bar, 0, sizeof(GridBarrier), s->stream));
+    void* kargs[] = {&ra};
+    OXG_CUDA(cudaLaunchCooperativeKernel((const void*)k_run, dim3(s->grid_run), dim3(256), kargs,
+                                         (size_t)block_bytes, s->stream));
+    return OXG_OK;
+}
+
+// Bodies of a run on the persistent kernel, in launches of up to `chunk` bodies, each
+// from a checkpoint it is replayed from (with a forced rebuild into grown lists) when
+// a neighbour-list capacity overflowed.
+static int run_persistent(oxg_system* s, long bodies)
+{
+    const int chunk = 2000;
+    long done = 0;
+    int retries = 0, rc;
+    DevStatus d;
+    while (done < bodies) {
+        const int todo = (int)std::min<long>(chunk, bodies - done);
+        const bool closing = done + todo == bodies;
+        if ((rc = checkpoint(s, false))) return rc;
+        DevStatus before;
+        if ((rc = read_status(s, &before))) return rc;
+        if ((rc = launch_run(s, todo, closing))) return rc;
+        if ((rc = read_status(s, &d))) return rc;
+        if (d.flags & kStBarrierTimeout) return set_err(OXG_ERR_TIMEOUT, "a grid barrier wait of the run kernel gave up");
+        if (d.flags & kStNonFinite) return set_err(OXG_ERR_NONFINITE, "non-finite positions or orientations");
+        if (d.flags & (kStCellOverflow | kStPairOverflow)) {
+            if (++retries > 8) return set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
+            bool grew = false;
+            if ((rc = grow_for(s, d, &grew))) return rc;
+            if ((rc = checkpoint(s, true))) return rc;
+            OXG_CUDA(cudaMemcpyAsync(&s->st->step, &before.step, sizeof(unsigned long long),
+                                     cudaMemcpyHostToDevice, s->stream));
+            OXG_CUDA(cudaMemsetAsync(s->st->qcount, 0, sizeof(s->st->qcount), s->stream));
+            if ((rc = clear_flags(s)) || (rc = set_rebuild(s))) return rc;
+            continue;
+        }
+        done += todo;
+        s->steps_run += todo;
+    }
+    s->timestep = d.step;
+    return OXG_OK;
+}
+
 // prepRun: fresh neighbour list, forces, a = F/m (HOOMD computes the net force at
 // the start of every run() call).
 static int prep_run(oxg_system* s)
@@ -1028,6 +1096,11 @@ int oxg_system_run(oxg_system* s, long nsteps)
         return OXG_OK;
     }
     if ((rc = enqueue_step_one(s))) return rc;
+    if (s->persistent) {
+        if ((rc = run_persistent(s, nsteps))) return rc;
+        OXG_CUDA(cudaStreamSynchronize(s->stream));
+        return OXG_OK;
+    }
     // nsteps - 1 fused bodies in graph chunks, then the closing body with step two.
     // Chunk boundaries sit after a step one; on a list overflow the chunk is replayed
     // from its checkpoint with a forced neighbour-list rebuild.

@@ -26,6 +26,7 @@ enum : uint32_t {
     kStPairOverflow = 2u,
     kStBadIndex = 4u,
     kStNonFinite = 8u,
+    kStBarrierTimeout = 32u,  // a grid-barrier wait of the persistent run kernel gave up
 };
 
 // device-resident bookkeeping of one system
@@ -227,11 +228,11 @@ struct PairIn {
 __device__ __forceinline__ bool load_short_pair(const ForceArgs& a, int w, int n_types, PairIn& p,
                                                 bool& bad_type)
 {
-    const int2 pr = a.pairs_short[w];
+    const int2 pr = __ldcg(a.pairs_short + w);
     p.i = pr.x;
     p.j = pr.y;
-    const float4 pi = a.pos[p.i], pj = a.pos[p.j];
-    const float3 dr = min_image(pair_delta(pi, a.pos_lo[p.i], pj, a.pos_lo[p.j]), a.L, a.invL);
+    const float4 pi = __ldcg(a.pos + p.i), pj = __ldcg(a.pos + p.j);
+    const float3 dr = min_image(pair_delta(pi, __ldcg(a.pos_lo + p.i), pj, __ldcg(a.pos_lo + p.j)), a.L, a.invL);
     p.rc = -dr;
     p.rsq = dot(dr, dr);
     const int ti = type_of(pi), tj = type_of(pj);
@@ -264,7 +265,7 @@ __device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamVie
     PairIn p;
     bool dummy = false;
     if (!load_short_pair(a, w, H.n_types, p, dummy)) return;
-    const Frame fi = quat_frame(a.quat[p.i]), fj = quat_frame(a.quat[p.j]);
+    const Frame fi = quat_frame(__ldcg(a.quat + p.i)), fj = quat_frame(__ldcg(a.quat + p.j));
     PairAcc acc;
     acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
     float e = 0.f;
@@ -312,30 +313,22 @@ __device__ __forceinline__ void reduce_energies(const ForceArgs& a, double* eacc
     }
 }
 
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(const volatile uint32_t*)p; }
+
+// Warp `gwarp` of `nwarps`: short-range pairs in units of 32 (cheap terms inline, heavy
+// ones queued), then the long-range pairs. Counters are read with volatile loads: the
+// persistent run kernel calls this after a neighbour-list rebuild in the same launch.
 template <bool ENERGY>
-__global__ void __launch_bounds__(256) k_forces_a(ForceArgs a)
+__device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamView& P, int gwarp,
+                                              int nwarps, double* eacc, bool& bad_type)
 {
-    const ParamView P = stage_params(a.params, a.param_bytes);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (a.st_rw->rebuild) {
-            a.st_rw->rebuild = 0u;
-            a.st_rw->gen += 1u;
-        }
-        if (a.advance_step) a.st_rw->step += 1ull;
-    }
     const ParamHeader& H = P.h();
     // after an overflow the counters exceed the capacities; only stored pairs are read
-    const int n_short = (int)min(a.st->n_short, (uint32_t)a.cap_short);
-    const int n_long = (int)min(a.st->n_long, (uint32_t)a.cap_long);
+    const int n_short = (int)min(ld_volatile(&a.st_rw->n_short), (uint32_t)a.cap_short);
+    const int n_long = (int)min(ld_volatile(&a.st_rw->n_long), (uint32_t)a.cap_long);
     const int n_types = H.n_types;
-    bool bad_type = false;
-    double eacc[kNTerms + 3];
-#pragma unroll
-    for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t mask = a.mask;
 
     for (int base = gwarp * 32; base < n_short; base += nwarps * 32) {
@@ -343,7 +336,7 @@ __global__ void __launch_bounds__(256) k_forces_a(ForceArgs a)
         bool want[kNQ] = {false, false, false, false};
         PairIn p;
         if (w < n_short && load_short_pair(a, w, n_types, p, bad_type) && p.rsq < H.rcutsq_max) {
-            const Frame fi = quat_frame(a.quat[p.i]), fj = quat_frame(a.quat[p.j]);
+            const Frame fi = quat_frame(__ldcg(a.quat + p.i)), fj = quat_frame(__ldcg(a.quat + p.j));
             PairAcc acc;
             acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
             float e_inline = 0.f;
@@ -415,69 +408,86 @@ __global__ void __launch_bounds__(256) k_forces_a(ForceArgs a)
 
     // long-range pairs: Debye only (uniform, cheap)
     const uint32_t long_mask = mask & (1u << kDebye);
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    const int tid = gwarp * 32 + lane, nthreads = nwarps * 32;
     for (int w = tid; w < n_long && long_mask; w += nthreads) {
-        const int2 pr = a.pairs_long[w];
+        const int2 pr = __ldcg(a.pairs_long + w);
         const int i = pr.x, j = pr.y;
-        const float4 pi = a.pos[i], pj = a.pos[j];
+        const float4 pi = __ldcg(a.pos + i), pj = __ldcg(a.pos + j);
         const int ti = type_of(pi), tj = type_of(pj);
         if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
             bad_type = true;
             continue;
         }
-        const float3 dr = min_image(pair_delta(pi, a.pos_lo[i], pj, a.pos_lo[j]), a.L, a.invL);
+        const float3 dr = min_image(pair_delta(pi, __ldcg(a.pos_lo + i), pj, __ldcg(a.pos_lo + j)), a.L, a.invL);
         PairAcc acc;
         acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
         float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
-        if (eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), a.quat[i], a.quat[j], ci,
+        if (eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), __ldcg(a.quat + i), __ldcg(a.quat + j), ci,
                       cj, acc, E)) {
             if (ENERGY) eacc[kDebye] += (double)E[kDebye];
             scatter<ENERGY>(a, i, j, acc, E[kDebye]);
         }
     }
-    reduce_energies<ENERGY>(a, eacc);
-    if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
 }
 
+// Warps interleaved across the blocks (warp w of block b is unit w * gridDim + b), so
+// that a short list of work units is spread over every SM rather than the first blocks.
+__device__ __forceinline__ int spread_warp() { return (threadIdx.x >> 5) * gridDim.x + blockIdx.x; }
+
 template <bool ENERGY>
-__global__ void __launch_bounds__(256) k_forces_b(ForceArgs a)
+__global__ void __launch_bounds__(256) k_forces_a(ForceArgs a)
 {
     const ParamView P = stage_params(a.params, a.param_bytes);
-    const int n_types = P.h().n_types;
-    // segments [HB | CS | HB+CS | coax | bonds], each padded to whole warps
-    int cnt[kNQ + 1], seg[kNQ + 2];
-    seg[0] = 0;
-#pragma unroll
-    for (int q = 0; q < kNQ; ++q) cnt[q] = (int)min(a.st->qcount[q], (uint32_t)a.cap_short);
-    cnt[kNQ] = a.bonded ? a.n_bonds : 0;
-#pragma unroll
-    for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (a.st_rw->rebuild) {
+            a.st_rw->rebuild = 0u;
+            a.st_rw->gen += 1u;
+        }
+        if (a.advance_step) a.st_rw->step += 1ull;
+    }
     double eacc[kNTerms + 3];
 #pragma unroll
     for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
     bool bad_type = false;
+    forces_a_body<ENERGY>(a, P, spread_warp(), (gridDim.x * blockDim.x) >> 5, eacc, bad_type);
+    reduce_energies<ENERGY>(a, eacc);
+    if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
+}
+
+// Warp `gwarp` of `nwarps` over the segments [HB | CS | HB+CS | coax | bonds], each
+// padded to whole warps: every warp evaluates 32 items of one term.
+template <bool ENERGY>
+__device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamView& P, int gwarp,
+                                              int nwarps, double* eacc, bool& bad_type)
+{
+    const int n_types = P.h().n_types;
+    int cnt[kNQ + 1], seg[kNQ + 2];
+    seg[0] = 0;
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) cnt[q] = (int)min(ld_volatile(&a.st_rw->qcount[q]), (uint32_t)a.cap_short);
+    cnt[kNQ] = a.bonded ? a.n_bonds : 0;
+#pragma unroll
+    for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
     const int lane = threadIdx.x & 31;
-    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int wbase = gwarp * 32; wbase < seg[kNQ + 1]; wbase += nwarps * 32) {
         int q = 0;
         while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
         if (q < kNQ) {
-            eval_deferred<ENERGY>(a, P, q, a.queue[(size_t)q * a.cap_short + k], eacc);
+            eval_deferred<ENERGY>(a, P, q, __ldcg(a.queue + (size_t)q * a.cap_short + k), eacc);
             continue;
         }
         const int4 bd = a.bonds[k];
         const int A = bd.x, B = bd.y;
-        const float4 pA = a.pos[A], pB = a.pos[B];
+        const float4 pA = __ldcg(a.pos + A), pB = __ldcg(a.pos + B);
         if ((unsigned)type_of(pA) >= (unsigned)n_types || (unsigned)type_of(pB) >= (unsigned)n_types) {
             bad_type = true;
             continue;
         }
-        const float3 Rcf = min_image(pair_delta(pB, a.pos_lo[B], pA, a.pos_lo[A]), a.L, a.invL);
-        const float4 qA = a.quat[A], qB = a.quat[B];
+        const float3 Rcf = min_image(pair_delta(pB, __ldcg(a.pos_lo + B), pA, __ldcg(a.pos_lo + A)), a.L, a.invL);
+        const float4 qA = __ldcg(a.quat + A), qB = __ldcg(a.quat + B);
         BondAcc acc;
         bonded_pair(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
                     make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
@@ -494,6 +504,17 @@ __global__ void __launch_bounds__(256) k_forces_b(ForceArgs a)
         atomicAdd(a.torque + A, make_float4(acc.tA.x, acc.tA.y, acc.tA.z, 0.f));
         atomicAdd(a.torque + B, make_float4(acc.tB.x, acc.tB.y, acc.tB.z, 0.f));
     }
+}
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(256) k_forces_b(ForceArgs a)
+{
+    const ParamView P = stage_params(a.params, a.param_bytes);
+    double eacc[kNTerms + 3];
+#pragma unroll
+    for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
+    bool bad_type = false;
+    forces_b_body<ENERGY>(a, P, spread_warp(), (gridDim.x * blockDim.x) >> 5, eacc, bad_type);
     reduce_energies<ENERGY>(a, eacc);
     if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
 }
@@ -716,21 +737,23 @@ __device__ __forceinline__ int cell_coord(float x, float invL, int n)
     return c >= n ? n - 1 : (c < 0 ? 0 : c);
 }
 
-#ifndef OXG_DEVICE_FUNCTIONS_ONLY
-__global__ void k_nlist_bin(NlistArgs a)
+// Thread `t` of `nthreads`: zero the other parity's cell counts (for the next rebuild)
+// and the pair counters.
+__device__ __forceinline__ void nlist_zero_other(const NlistArgs& a, int t, int nthreads, uint32_t par)
 {
-    if (!a.st->rebuild) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t par = a.st->gen & 1u;
-    // zero the other generation's counts for the next rebuild
     uint32_t* other = a.cell_count + (size_t)(par ^ 1u) * a.n_cells;
-    for (int c = i; c < a.n_cells; c += gridDim.x * blockDim.x) other[c] = 0u;
-    if (i == 0) {
+    for (int c = t; c < a.n_cells; c += nthreads) other[c] = 0u;
+    if (t == 0) {
         a.st->n_short = 0u;
         a.st->n_long = 0u;
     }
-    if (i >= a.N) return;
-    const float4 p = a.pos[i];
+}
+
+// Bin particle i < N into the counts of generation parity `par`; record its position
+// as the list's reference.
+__device__ __forceinline__ void nlist_bin_particle(const NlistArgs& a, int i, uint32_t par)
+{
+    const float4 p = __ldcg(a.pos + i);
     a.pos_ref[i] = p;
     if (!a.use_cells) return;
     const int cx = cell_coord(p.x, a.invL.x, a.nc.x), cy = cell_coord(p.y, a.invL.y, a.nc.y),
@@ -740,6 +763,16 @@ __global__ void k_nlist_bin(NlistArgs a)
     if (slot < (uint32_t)a.cell_cap) a.cell_list[(size_t)c * a.cell_cap + slot] = i;
     else atomicOr(&a.st->flags, kStCellOverflow);
     atomicMax(&a.st->max_cell, slot + 1u);
+}
+
+#ifndef OXG_DEVICE_FUNCTIONS_ONLY
+__global__ void k_nlist_bin(NlistArgs a)
+{
+    if (!a.st->rebuild) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t par = a.st->gen & 1u;
+    nlist_zero_other(a, i, gridDim.x * blockDim.x, par);
+    if (i < a.N) nlist_bin_particle(a, i, par);
 }
 #endif
 
@@ -761,12 +794,12 @@ __device__ __forceinline__ void for_each_candidate(const NlistArgs& a, int i, fl
                 for (int dx = -1; dx <= 1; ++dx) {
                     const int x = (cx + dx + a.nc.x) % a.nc.x;
                     const int c = (z * a.nc.y + y) * a.nc.x + x;
-                    const int n = min((int)counts[c], a.cell_cap);
+                    const int n = min((int)__ldcg(counts + c), a.cell_cap);
                     const int* lst = a.cell_list + (size_t)c * a.cell_cap;
                     for (int q = 0; q < n; ++q) {
-                        const int j = lst[q];
+                        const int j = __ldcg(lst + q);
                         if (j <= i || is_excluded(ex, j)) continue;
-                        const float4 pj = a.pos[j];
+                        const float4 pj = __ldcg(a.pos + j);
                         const float3 d = min_image(mk3(p.x - pj.x, p.y - pj.y, p.z - pj.z), a.L, a.invL);
                         const float r2 = dot(d, d);
                         if (r2 < a.rlist2) fn(j, r2);
@@ -777,7 +810,7 @@ __device__ __forceinline__ void for_each_candidate(const NlistArgs& a, int i, fl
     } else {
         for (int j = i + 1; j < a.N; ++j) {
             if (is_excluded(ex, j)) continue;
-            const float4 pj = a.pos[j];
+            const float4 pj = __ldcg(a.pos + j);
             const float3 d = min_image(mk3(p.x - pj.x, p.y - pj.y, p.z - pj.z), a.L, a.invL);
             const float r2 = dot(d, d);
             if (r2 < a.rlist2) fn(j, r2);
@@ -802,17 +835,16 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t n)
     return base + incl - n;
 }
 
-#ifndef OXG_DEVICE_FUNCTIONS_ONLY
-__global__ void k_nlist_pairs(NlistArgs a)
+// Particle i's pairs j > i from the cells of parity `par` (whole warps: the slots are
+// reserved with warp-aggregated atomics).
+__device__ __forceinline__ void nlist_pairs_body(const NlistArgs& a, int i, uint32_t par)
 {
-    if (!a.st->rebuild) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < a.N;
-    const uint32_t* counts = a.cell_count + (size_t)(a.st->gen & 1u) * a.n_cells;
+    const uint32_t* counts = a.cell_count + (size_t)par * a.n_cells;
     float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
     uint32_t ns = 0, nl = 0;
     if (active) {
-        p = a.pos[i];
+        p = __ldcg(a.pos + i);
         for_each_candidate(a, i, p, counts, [&](int, float r2) {
             if (r2 < a.rshort2) ++ns;
             else ++nl;
@@ -836,6 +868,13 @@ __global__ void k_nlist_pairs(NlistArgs a)
     });
     if (over) atomicOr(&a.st->flags, kStPairOverflow);
     if (i == 0) atomicAdd(&a.st->builds, 1u);
+}
+
+#ifndef OXG_DEVICE_FUNCTIONS_ONLY
+__global__ void k_nlist_pairs(NlistArgs a)
+{
+    if (!a.st->rebuild) return;
+    nlist_pairs_body(a, blockIdx.x * blockDim.x + threadIdx.x, a.st->gen & 1u);
 }
 #endif
 
@@ -1043,7 +1082,7 @@ __device__ __forceinline__ void particle_step_two(const IntegArgs& a, int i,
                                                   unsigned long long step, PState& s, float4& ac,
                                                   float4& tn)
 {
-    step_two_pure(s, a.force[i], a.torque[i], (uint32_t)i, step, a.seed_lo, a.seed_hi, a.dt, a.kT,
+    step_two_pure(s, __ldcg(a.force + i), __ldcg(a.torque + i), (uint32_t)i, step, a.seed_lo, a.seed_hi, a.dt, a.kT,
                   a.gamma, a.gamma_r, a.inertia, ac, tn);
 }
 
@@ -1106,6 +1145,127 @@ __global__ void k_prep_accel(IntegArgs a)
     const float minv = 1.f / v.w;
     a.accel[i] = make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f);
     a.tnet[i] = make_float4(T.x, T.y, T.z, 0.f);
+}
+#endif
+
+// ------------------------------------------------------- persistent run kernel
+// One cooperative launch runs many MD step bodies; its blocks (all co-resident, which
+// the cooperative launch guarantees) meet at grid barriers between the phases, so the
+// code stays in the instruction caches and the parameters in shared memory for the
+// whole launch instead of being fetched again by five launches per step.
+struct GridBarrier {
+    uint32_t arrive;  // bit 31 flips each time every block has arrived
+    uint32_t abort;   // set by a block whose wait gave up: the others leave too
+    uint32_t pad[30]; // a line of its own
+};
+
+constexpr long long kBarrierSpinLimit = 1LL << 22;  // polls of >= 0.1 us: about a second
+
+// Arrive-and-wait over all blocks of the launch. Block 0 adds 2^31 - (blocks - 1),
+// every other block 1, so bit 31 of the counter flips exactly when the last block
+// arrives (and the counter needs no reset). The fences on both sides make every write
+// before the barrier visible to every read after it. Returns false if the wait gave up
+// (after kBarrierSpinLimit polls) or another block did; the caller must then return.
+__device__ __forceinline__ bool grid_barrier(GridBarrier* gb)
+{
+    __shared__ int bar_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const uint32_t add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+        __threadfence();
+        const uint32_t old = atomicAdd(&gb->arrive, add);
+        long long polls = 0;
+        while (((old ^ ld_volatile(&gb->arrive)) & 0x80000000u) == 0u) {
+            if (ld_volatile(&gb->abort)) {
+                ok = 0;
+                break;
+            }
+            if (++polls > kBarrierSpinLimit) {
+                atomicExch(&gb->abort, 1u);
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+        bar_ok = ok;
+    }
+    __syncthreads();
+    return bar_ok != 0;
+}
+
+struct RunArgs {
+    ForceArgs f;
+    NlistArgs n;
+    IntegArgs g;
+    GridBarrier* bar;
+    int bodies;   // step bodies in this launch
+    int closing;  // the last body is the run's last step (step two only)
+};
+
+#ifndef OXG_DEVICE_FUNCTIONS_ONLY
+// Each body: [neighbour-list rebuild if flagged: bin | pairs] | forces part one |
+// forces part two | step two + step one of the next step. The rebuild flag is read by
+// every block right after a barrier and cleared one barrier later; a list overflow
+// ends the launch (the host grows the lists and replays from its checkpoint).
+__global__ void __launch_bounds__(256, 2) k_run(RunArgs a)
+{
+    const ParamView P = stage_params(a.f.params, a.f.param_bytes);
+    DevStatus* st = a.f.st_rw;
+    const int lane = threadIdx.x & 31;
+    const int gwarp = spread_warp();
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int gthread = gwarp * 32 + lane, nthreads = nwarps * 32;
+    double eacc[kNTerms + 3];  // unused: MD steps evaluate no energies
+    bool bad_type = false;
+    for (int body = 0; body < a.bodies; ++body) {
+        const bool rebuild = ld_volatile(&st->rebuild) != 0u;
+        if (rebuild) {
+            const uint32_t par = ld_volatile(&st->gen) & 1u;
+            nlist_zero_other(a.n, gthread, nthreads, par);
+            for (int i = gthread; i < a.n.N; i += nthreads) nlist_bin_particle(a.n, i, par);
+            if (!grid_barrier(a.bar)) break;
+            for (int base = gwarp * 32; base < a.n.N; base += nthreads) nlist_pairs_body(a.n, base + lane, par);
+            if (!grid_barrier(a.bar)) break;
+            if (ld_volatile(&st->flags) & (kStCellOverflow | kStPairOverflow)) break;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            if (rebuild) st->gen += 1u;
+            st->step += 1ull;
+        }
+        forces_a_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+        if (!grid_barrier(a.bar)) break;
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->rebuild = 0u;
+        forces_b_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+        if (!grid_barrier(a.bar)) break;
+        // step two of this step (+ step one of the next)
+        const bool last = a.closing && body == a.bodies - 1;
+        const unsigned long long step = *(const volatile unsigned long long*)&st->step;
+        if (blockIdx.x == 0 && threadIdx.x < 4) st->qcount[threadIdx.x] = 0u;
+        bool far = false, bad = false;
+        for (int i = gthread; i < a.g.N; i += nthreads) {
+            PState s = load_pstate(a.g, i);
+            float4 ac, tn;
+            particle_step_two(a.g, i, step, s, ac, tn);
+            if (last) {
+                a.g.vel[i] = s.v;
+                a.g.angmom[i] = s.p;
+                a.g.accel[i] = ac;
+                a.g.tnet[i] = tn;
+            } else {
+                bool f1 = false, b1 = false;
+                particle_step_one(a.g, i, s, ac, tn, f1, b1);
+                far |= f1;
+                bad |= b1;
+            }
+        }
+        if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->rebuild, 1u);
+        if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
+        if (!grid_barrier(a.bar)) break;
+    }
+    if (__syncthreads_or(bad_type) && threadIdx.x == 0) atomicOr(&st->flags, kStBadIndex);
+    if (threadIdx.x == 0 && ld_volatile(&a.bar->abort)) atomicOr(&st->flags, kStBarrierTimeout);
 }
 #endif
 

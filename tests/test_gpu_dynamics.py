@@ -43,10 +43,13 @@ def test_8000nt_energies_match_oracle(native, oracle, fused):
     assert np.linalg.norm(F.sum(axis=0)) < 1e-4 * np.abs(F).max() * np.sqrt(len(F))
 
 
-def test_short_trajectory_tracks_oracle(native, oracle):
-    """Same counter-based RNG on both sides: 20 Langevin steps agree closely."""
+@pytest.mark.parametrize("mode", ["persistent", "graph"])
+def test_short_trajectory_tracks_oracle(native, oracle, monkeypatch, mode):
+    """Same counter-based RNG on both sides: 20 Langevin steps agree closely, on the
+    persistent run kernel and on the per-step kernels replayed from a CUDA graph."""
     from oxdna import io
     from oxdna.model import dna1, dna2
+    monkeypatch.setenv("OXG_RUN_MODE", mode)
     s = io.duplex_system(8, 20, 40.0, seed=1)
     kT = dna1.kT_from_temperature(296.15)
     forces, _ = dna2.forces()
@@ -64,6 +67,32 @@ def test_short_trajectory_tracks_oracle(native, oracle):
     assert np.abs(snap.particles.velocity - vel).max() < 2e-2
     q = snap.particles.orientation
     assert np.abs(np.abs(np.einsum("ij,ij->i", q, o.quat)) - 1.0).max() < 1e-3
+
+
+def test_large_system_frequent_rebuilds_track_oracle(native, oracle):
+    """84,000 nt (more particles than the persistent run kernel has threads) with a
+    0.002-sigma list buffer, so the kernel rebuilds its neighbour list every step or two:
+    20 steps follow the FP64 oracle's Langevin trajectory (same Philox stream)."""
+    import os
+    from oxdna import io
+    from oxdna.model import dna1, dna2
+    s = io.duplex_system(2100, 20, 220.0, seed=3)
+    kT = dna1.kT_from_temperature(296.15)
+    forces, _ = dna2.forces(nlist=dna2.make_neighbor_list(buffer=0.002))
+    sim = _sim(io.system_snapshot(s), forces, dt=0.003, kT=kT, seed=7)
+    sim.run(20)
+    st = sim.native_stats()
+    assert st["nlist_builds"] >= 5
+    snap = sim.state.get_snapshot()
+    model = oracle.Model(forces, io.DNA_BASES)
+    o = oracle.System(s["pos"], s["quat"], s["typeid"], s["box"], s["bonds"])
+    n = len(s["pos"])
+    _, vel, _ = oracle.langevin(model, o, np.zeros((n, 3)), np.zeros((n, 4)), steps=20,
+                                dt=0.003, kT=kT, seed=7, threads=os.cpu_count())
+    d = snap.particles.position - o.pos
+    d -= 220.0 * np.round(d / 220.0)
+    assert np.abs(d).max() < 2e-3
+    assert np.abs(snap.particles.velocity - vel).max() < 2e-2
 
 
 def test_duplexes_stay_bound_and_thermalise(native):
