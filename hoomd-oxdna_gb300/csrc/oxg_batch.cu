@@ -104,7 +104,7 @@ __host__ __device__ inline size_t smem_bytes(int max_reps, int tile_cap, int qca
     b += 2 * sizeof(int4) * (size_t)tile_cap;
     b += a16(sizeof(int) * tile_cap);
     b += a16(sizeof(int) * (size_t)kNQ * qcap);
-    b += 16;
+    b += 32;  // queue counters (8 ints, kNQ used)
     if (energy) b += a16(sizeof(double) * 9 * max_reps);
     return b;
 }
@@ -138,7 +138,7 @@ __device__ inline Smem carve(unsigned char* base, const BatchArgs& a, bool energ
     s.queue = reinterpret_cast<int*>(base + o);
     o += a16(sizeof(int) * (size_t)kNQ * a.qcap);
     s.qcnt = reinterpret_cast<int*>(base + o);
-    o += 16;
+    o += 32;
     s.eacc = energy ? reinterpret_cast<double*>(base + o) : nullptr;
     return s;
 }
@@ -207,7 +207,7 @@ __device__ __noinline__ void batch_heavy(const Smem& s, const BatchArgs& a, int 
             RadialF2 Rr{pc.f2};
             e = bb_term<true>(g, fi, fj, pc.t1, pc.t23, pc.t4, pc.t78, pc.t4_enabled != 0, Rr, acc);
         }
-    } else if (q == kQHBX) {
+    } else if (q == kQHBX || q == kQHBX0) {
         term = kHBCross;
         const DHBCross& px = P.term<DHBCross>(kHBCross, pidx);
         if (bb_geometry(rc, fi, fj, px.base, g)) {
@@ -291,7 +291,7 @@ __device__ void tile_forces(const Smem& s, const BatchArgs& a, int nrep, int np,
                 atomicAdd(&s.eacc[r * 9 + kDebye], (double)ed);
             }
         }
-        bool want[kNQ] = {false, false, false, false};
+        bool want[kNQ] = {};
         BBGeom g;
         bool gv = false;
         if (mask & (1u << kHBond)) {

@@ -21,6 +21,7 @@
 
 #include "../../include/oxdna_gb300.h"
 #include "oxg_convert.h"
+#include "oxg_internal.h"
 #include "oxg_kernels.cuh"
 
 using namespace oxg;
@@ -442,7 +443,7 @@ struct oxg_system {
     uint32_t* cell_count = nullptr;
     int* cell_list = nullptr;
     int2 *pairs_short = nullptr, *pairs_long = nullptr;
-    int* queue = nullptr;  // 4 deferred-term queues of cap_short entries
+    int* queue = nullptr;  // kNQ deferred-term queues of cap_short entries
     long long cap_short = 0, cap_long = 0;
     float rlist2 = 0.f, rshort2 = 0.f;
     uint32_t nlist_mask = 0xffffffffu;  // term mask the current sizing was made for
@@ -467,8 +468,14 @@ struct oxg_system {
     int grid_forces = 0;
     // persistent run kernel
     GridBarrier* bar = nullptr;
-    int grid_run = 0;
+    int grid_run = 0, grid_run_surr = 0;
     bool persistent = true;
+    // learned surrogate of the fused HB + cross-stacking term
+    const MlpDev* mlp = nullptr;
+    SurrogateAudit* audit = nullptr;
+    int surr_flags = 0;
+    uint32_t audit_every = 0, audit_mod = 100;
+    float audit_tol = 0.f;
     // stats
     long long steps_run = 0;
 };
@@ -488,7 +495,7 @@ int sys_alloc_nlist(oxg_system* s)
     if ((rc = dalloc(&s->cell_list, (size_t)s->n_cells * s->cell_cap))) return rc;
     if ((rc = dalloc(&s->pairs_short, (size_t)s->cap_short))) return rc;
     if ((rc = dalloc(&s->pairs_long, (size_t)s->cap_long))) return rc;
-    if ((rc = dalloc(&s->queue, (size_t)4 * s->cap_short))) return rc;
+    if ((rc = dalloc(&s->queue, (size_t)kNQ * s->cap_short))) return rc;
     return OXG_OK;
 }
 
@@ -597,6 +604,18 @@ ForceArgs force_args(oxg_system* s, uint32_t mask, int bonded)
     return a;
 }
 
+// The surrogate, if set for this use (OXG_SURROGATE_RUN / _COMPUTE), into force args.
+void surrogate_args(oxg_system* s, ForceArgs& a, bool md)
+{
+    const int want = md ? OXG_SURROGATE_RUN : OXG_SURROGATE_COMPUTE;
+    if (!s->mlp || !(s->surr_flags & want) || !((a.mask >> kHBCross) & 1u)) return;
+    a.mlp = s->mlp;
+    a.audit = s->audit;
+    a.audit_every = md ? s->audit_every : 0u;
+    a.audit_mod = s->audit_mod;
+    a.audit_tol = s->audit_tol;
+}
+
 IntegArgs integ_args(oxg_system* s)
 {
     IntegArgs a;
@@ -646,15 +665,19 @@ int launch_nlist_forces(oxg_system* s, uint32_t mask, int bonded, bool energy, b
     k_nlist_pairs<<<std::max(1, (s->N + threads - 1) / threads), threads, 0, s->stream>>>(na);
     ForceArgs fa = force_args(s, mask, bonded);
     fa.advance_step = md_step ? 1 : 0;
+    surrogate_args(s, fa, md_step);
     const int grid = forces_grid(s);
     if (!md_step)  // MD steps: the integrator kernels reset the queue lengths
         OXG_CUDA(cudaMemsetAsync(s->st->qcount, 0, sizeof(s->st->qcount), s->stream));
+    const bool surr = fa.mlp != nullptr;
     if (energy) {
         k_forces_a<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-        k_forces_b<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+        if (surr) k_forces_b<true, true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+        else k_forces_b<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
     } else {
         k_forces_a<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-        k_forces_b<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+        if (surr) k_forces_b<false, true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+        else k_forces_b<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
     }
     OXG_CUDA(cudaGetLastError());
     return OXG_OK;
@@ -749,8 +772,9 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
         (rc = dalloc(&s->charge, N)) || (rc = dalloc(&s->bonds, std::max(1, n_bonds))) ||
         (rc = dalloc(&s->excl, N)) || (rc = dalloc(&s->st, 1)) || (rc = dalloc(&s->energy, 9)) ||
         (rc = dalloc(&s->ck_pos, N)) || (rc = dalloc(&s->ck_quat, N)) || (rc = dalloc(&s->ck_vel, N)) ||
-        (rc = dalloc(&s->ck_angmom, N)) || (rc = dalloc(&s->bar, 1)))
+        (rc = dalloc(&s->ck_angmom, N)) || (rc = dalloc(&s->bar, 1)) || (rc = dalloc(&s->audit, 1)))
         return fail(rc);
+    cudaMemset(s->audit, 0, sizeof(SurrogateAudit));
     if (const char* m = std::getenv("OXG_RUN_MODE")) s->persistent = std::string(m) != "graph";
     if (cudaMallocHost((void**)&s->st_host, sizeof(DevStatus)) != cudaSuccess)
         return fail(set_err(OXG_ERR_CUDA, "cudaMallocHost failed"));
@@ -788,6 +812,7 @@ int oxg_system_destroy(oxg_system* s)
     dfree(s->queue);
     dfree(s->ck_pos); dfree(s->ck_quat); dfree(s->ck_vel); dfree(s->ck_angmom);
     dfree(s->bar);
+    dfree(s->audit);
     if (s->st_host) cudaFreeHost(s->st_host);
     delete s;
     return OXG_OK;
@@ -999,14 +1024,18 @@ static int checkpoint(oxg_system* s, bool restore)
 static int launch_run(oxg_system* s, int bodies, bool closing)
 {
     const int block_bytes = s->ctx->block_bytes;
-    if (s->grid_run == 0) {
-        int per_sm = 0;
-        OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_run, 256, block_bytes));
-        if (per_sm < 1) return set_err(OXG_ERR_CUDA, "the run kernel does not fit on an SM");
-        s->grid_run = num_sms() * std::min(per_sm, 2);
-    }
     RunArgs ra;
     ra.f = force_args(s, s->run_mask, s->run_bonded);
+    surrogate_args(s, ra.f, true);
+    const bool surr = ra.f.mlp != nullptr;
+    const void* fn = surr ? (const void*)k_run<true> : (const void*)k_run<false>;
+    int& grid = surr ? s->grid_run_surr : s->grid_run;
+    if (grid == 0) {
+        int per_sm = 0;
+        OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, block_bytes));
+        if (per_sm < 1) return set_err(OXG_ERR_CUDA, "the run kernel does not fit on an SM");
+        grid = num_sms() * std::min(per_sm, 2);
+    }
     ra.n = nlist_args(s);
     ra.g = integ_args(s);
     ra.bar = s->bar;
@@ -1014,8 +1043,7 @@ static int launch_run(oxg_system* s, int bodies, bool closing)
     ra.closing = closing ? 1 : 0;
     OXG_CUDA(cudaMemsetAsync(s->bar, 0, sizeof(GridBarrier), s->stream));
     void* kargs[] = {&ra};
-    OXG_CUDA(cudaLaunchCooperativeKernel((const void*)k_run, dim3(s->grid_run), dim3(256), kargs,
-                                         (size_t)block_bytes, s->stream));
+    OXG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), kargs, (size_t)block_bytes, s->stream));
     return OXG_OK;
 }
 
@@ -1178,6 +1206,129 @@ int oxg_system_energies(oxg_system* s, double* pair_energy, double* bonded_energ
     return oxg_system_compute(s, mask, bonded, nullptr, nullptr, pair_energy, bonded_energy);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Training samples of the surrogate: every queued fused HB + CS pair (both classes)
+// gives its 7 base-base features, its class and the plain evaluator's pair energy.
+__global__ void k_hbx_samples(ForceArgs a, int max_n, float* feats, float* energy, uint32_t* counter)
+{
+    const ParamView P = stage_params(a.params, a.param_bytes);
+    const ParamHeader& H = P.h();
+    const int n1 = (int)min(ld_volatile(&a.st_rw->qcount[kQHBX]), (uint32_t)a.cap_short);
+    const int n0 = (int)min(ld_volatile(&a.st_rw->qcount[kQHBX0]), (uint32_t)a.cap_short);
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n1 + n0; it += gridDim.x * blockDim.x) {
+        const int q = it < n1 ? kQHBX : kQHBX0, k = it < n1 ? it : it - n1;
+        PairIn p;
+        bool bad = false;
+        if (!load_short_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad)) continue;
+        const Frame fi = quat_frame(__ldcg(a.quat + p.i)), fj = quat_frame(__ldcg(a.quat + p.j));
+        const DHBCross& px = P.term<DHBCross>(kHBCross, p.pidx);
+        BBGeom g;
+        if (!bb_geometry(p.rc, fi, fj, px.base, g)) continue;
+        PairAcc acc;
+        acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+        RadialF1 R1{px.f1, H.hbx_eps[p.pidx], H.hbx_shift[p.pidx]};
+        float e = bb_term<false>(g, fi, fj, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1, acc);
+        RadialF2 R2{px.f2};
+        e += bb_term<true>(g, fi, fj, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2, acc);
+        const uint32_t slot = atomicAdd(counter, 1u);
+        if (slot >= (uint32_t)max_n) continue;
+        float x[kMlpIn];
+        mlp_features(g, x);
+        for (int f = 0; f < kMlpIn; ++f) feats[(size_t)slot * 8 + f] = x[f];
+        feats[(size_t)slot * 8 + 7] = q == kQHBX ? 1.f : 0.f;
+        energy[slot] = e;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int oxg_system_hbx_samples(oxg_system* s, int max_n, float* feats, float* energy, int* n_out)
+{
+    if (!s || max_n < 0 || (max_n > 0 && (!feats || !energy)) || !n_out)
+        return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (!s->ctx->hbx.any) return set_err(OXG_ERR_NO_PARAMS, "no fused HB + cross-stacking parameters");
+    const uint32_t mask = 1u << kHBCross;
+    int rc = sys_setup_nlist(s, mask | s->run_mask, false);
+    if (rc) return rc;
+    uint32_t* counter = nullptr;
+    if ((rc = dalloc(&counter, 1))) return rc;
+    for (int attempt = 0;; ++attempt) {
+        OXG_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), s->stream));
+        if ((rc = clear_flags(s)) || (rc = set_rebuild(s))) break;
+        if ((rc = launch_nlist_forces(s, mask, 0, false))) break;
+        DevStatus d;
+        if ((rc = read_status(s, &d))) break;
+        bool grew = false;
+        if ((rc = grow_for(s, d, &grew))) break;
+        if (grew) {
+            if (attempt == 7) {
+                rc = set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
+                break;
+            }
+            continue;
+        }
+        const ForceArgs fa = force_args(s, mask, 0);
+        k_hbx_samples<<<2 * num_sms(), 256, s->ctx->block_bytes, s->stream>>>(fa, max_n, feats, energy, counter);
+        if (cudaGetLastError() != cudaSuccess) {
+            rc = set_err(OXG_ERR_CUDA, "sample kernel launch failed");
+            break;
+        }
+        uint32_t n = 0;
+        if (cudaMemcpyAsync(&n, counter, sizeof(n), cudaMemcpyDeviceToHost, s->stream) != cudaSuccess ||
+            cudaStreamSynchronize(s->stream) != cudaSuccess) {
+            rc = set_err(OXG_ERR_CUDA, "sample read-back failed");
+            break;
+        }
+        *n_out = (int)std::min<uint32_t>(n, (uint32_t)max_n);
+        break;
+    }
+    // the evaluation zeroes nothing the MD state needs, but leaves queue lengths behind
+    cudaMemsetAsync(s->st->qcount, 0, sizeof(s->st->qcount), s->stream);
+    cudaMemsetAsync(s->force, 0, sizeof(float4) * s->N, s->stream);
+    cudaMemsetAsync(s->torque, 0, sizeof(float4) * s->N, s->stream);
+    cudaStreamSynchronize(s->stream);
+    dfree(counter);
+    return rc;
+}
+
+int oxg_system_set_surrogate(oxg_system* s, const oxg_mlp* mlp, int flags, int audit_every,
+                             int audit_mod, double audit_tol)
+{
+    if (!s || flags < 0 || flags > (OXG_SURROGATE_RUN | OXG_SURROGATE_COMPUTE) || audit_every < 0 ||
+        audit_mod < 1 || !(audit_tol >= 0.0))
+        return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (mlp && flags && !s->ctx->hbx.any)
+        return set_err(OXG_ERR_NO_PARAMS, "the surrogate replaces the fused HB + cross-stacking term, which has no parameters");
+    s->mlp = static_cast<const MlpDev*>(internal_mlp_device(mlp));
+    s->surr_flags = mlp ? flags : 0;
+    s->audit_every = (uint32_t)audit_every;
+    s->audit_mod = (uint32_t)audit_mod;
+    s->audit_tol = (float)audit_tol;
+    OXG_CUDA(cudaMemsetAsync(s->audit, 0, sizeof(SurrogateAudit), s->stream));
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    return OXG_OK;
+}
+
+int oxg_system_surrogate_stats(oxg_system* s, double* out, int n)
+{
+    if (!s || !out) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    SurrogateAudit h;
+    OXG_CUDA(cudaMemcpyAsync(&h, s->audit, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    const double na = h.n_audited ? (double)h.n_audited : 1.0;
+    const double v[9] = {(double)h.disabled, (double)h.n_audited, (double)h.n_over,
+                         std::sqrt(h.sum_sq_de / na), std::sqrt(h.sum_sq_e / na),
+                         std::sqrt(h.sum_sq_df / na), std::sqrt(h.sum_sq_f / na),
+                         (double)h.max_abs_de, (double)h.max_abs_df};
+    for (int k = 0; k < n && k < 9; ++k) out[k] = v[k];
+    return OXG_OK;
+}
+
 int oxg_system_stats(oxg_system* s, int64_t* out, int n)
 {
     if (!s || !out) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
@@ -1222,7 +1373,7 @@ constexpr size_t kNaOffCellList = na_align(kNaOffCellCount + sizeof(uint32_t) * 
 constexpr size_t kNaOffShort = na_align(kNaOffCellList + sizeof(int) * (size_t)kNaMaxCells * kNaCellCap);
 constexpr size_t kNaOffLong = na_align(kNaOffShort + sizeof(int2) * kNaShortCap);
 constexpr size_t kNaOffQueue = na_align(kNaOffLong + sizeof(int2) * kNaLongCap);
-constexpr size_t kNaBytes = na_align(kNaOffQueue + sizeof(int) * 4 * kNaShortCap);  // ~11.9 MB
+constexpr size_t kNaBytes = na_align(kNaOffQueue + sizeof(int) * kNQ * kNaShortCap);  // ~12.9 MB
 
 }  // namespace
 
@@ -1273,7 +1424,7 @@ __global__ void k_noalloc_prepare(int N, float4* pos_lo, int4* excl, float4* for
         st->builds = 0u;
         st->max_cell = 0u;
         st->step = 0ull;
-        for (int q = 0; q < 4; ++q) st->qcount[q] = 0u;
+        for (int q = 0; q < kNQ; ++q) st->qcount[q] = 0u;
         for (int t = 0; t < 16; ++t) energy[t] = 0.0;
     }
 }

@@ -22,5 +22,7 @@ double internal_max_rcut(const oxg_context* c, uint32_t mask, bool short_only);
 int internal_n_types(const oxg_context* c);
 bool internal_bonded_complete(const oxg_context* c);
 int internal_num_sms();
+// Device image (an MlpDev) of a surrogate network, or null.
+const void* internal_mlp_device(const oxg_mlp* m);
 
 }  // namespace oxg

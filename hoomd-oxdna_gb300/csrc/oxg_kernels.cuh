@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include "oxg_device.cuh"
+#include "oxg_mlp.cuh"
 #include "oxg_params.h"
 
 namespace oxg {
@@ -40,7 +41,7 @@ struct DevStatus {
     uint32_t max_cell;     // largest cell occupancy seen
     uint32_t pad;
     unsigned long long step;  // current timestep (RNG counter)
-    uint32_t qcount[4];    // deferred-term queue lengths (k_forces_a -> k_forces_b)
+    uint32_t qcount[8];    // deferred-term queue lengths, kNQ used (k_forces_a -> k_forces_b)
 };
 
 // ------------------------------------------------------------ parameter view
@@ -198,12 +199,31 @@ struct ForceArgs {
     DevStatus* st_rw;     // rebuild flag cleared here
     int cap_short, cap_long;  // list capacities (counts past them were not stored)
     int advance_step;     // MD step: advance the RNG step counter read by step two
-    int* queue;           // 4 deferred-term queues of cap_short short-pair indices
+    int* queue;           // kNQ deferred-term queues of cap_short short-pair indices
     float3 L, invL;
     float4* force;        // accumulated (pre-zeroed)
     float4* torque;
     double* energy;       // [6 pair terms][3 bonded] (ENERGY only)
     float* virial;        // unused by the engine
+    // learned surrogate of the fused HB + cross-stacking term (null: plain evaluator)
+    const MlpDev* mlp = nullptr;
+    struct SurrogateAudit* audit = nullptr;
+    uint32_t audit_every = 0;  // steps between audits (0: never)
+    uint32_t audit_mod = 100;  // one queued pair in audit_mod is audited
+    float audit_tol = 0.f;     // largest accepted |E_surrogate - E_plain| of one pair
+};
+
+// Statistics of the audits of the surrogate by the plain evaluator; `disabled` is the
+// kill switch the force kernels read (set by the first pair over the tolerance).
+struct SurrogateAudit {
+    uint32_t disabled;
+    uint32_t n_audited;
+    uint32_t n_over;
+    uint32_t pad;
+    double sum_sq_de, sum_sq_e;  // pair energy error and reference
+    double sum_sq_df, sum_sq_f;  // force (on i) error and reference
+    float max_abs_de, max_abs_df;
+    float pad2[2];
 };
 
 // The force evaluation is split in two launches so that the acos-heavy terms run with
@@ -216,7 +236,9 @@ struct ForceArgs {
 //  k_forces_b  term-uniform warps over [HB | CS | HB+CS | coax | bonds]: each warp
 //              evaluates 32 queued pairs (or bonds) of one term.
 // The integrator kernels reset the queue lengths for the next step.
-enum { kQHB = 0, kQCS = 1, kQHBX = 2, kQCX = 3, kNQ = 4 };
+// The fused HB + cross-stacking pairs are queued by class (complementary bases in kQHBX,
+// the rest in kQHBX0) so that a warp of the surrogate evaluates one network.
+enum { kQHB = 0, kQCS = 1, kQHBX = 2, kQCX = 3, kQHBX0 = 4, kNQ = 5 };
 
 struct PairIn {
     int i, j, pidx;
@@ -284,7 +306,7 @@ __device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamVie
             RadialF2 R{pc.f2};
             e = bb_term<true>(g, fi, fj, pc.t1, pc.t23, pc.t4, pc.t78, pc.t4_enabled != 0, R, acc);
         }
-    } else if (q == kQHBX) {
+    } else if (q == kQHBX || q == kQHBX0) {
         term = kHBCross;
         const DHBCross& px = P.term<DHBCross>(kHBCross, p.pidx);
         if (bb_geometry(p.rc, fi, fj, px.base, g)) {
@@ -333,7 +355,7 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
 
     for (int base = gwarp * 32; base < n_short; base += nwarps * 32) {
         const int w = base + lane;
-        bool want[kNQ] = {false, false, false, false};
+        bool want[kNQ] = {};
         PairIn p;
         if (w < n_short && load_short_pair(a, w, n_types, p, bad_type) && p.rsq < H.rcutsq_max) {
             const Frame fi = quat_frame(__ldcg(a.quat + p.i)), fj = quat_frame(__ldcg(a.quat + p.j));
@@ -384,8 +406,9 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
                 if (p.rsq < px.rcutsq && bb_geometry(p.rc, fi, fj, px.base, g)) {
                     RadialF1 R1{px.f1, H.hbx_eps[p.pidx], H.hbx_shift[p.pidx]};
                     RadialF2 R2{px.f2};
-                    want[kQHBX] = bb_support<false>(g, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1) ||
-                                  bb_support<true>(g, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2);
+                    want[H.hbx_eps[p.pidx] != 0.f ? kQHBX : kQHBX0] =
+                        bb_support<false>(g, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1) ||
+                        bb_support<true>(g, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2);
                 }
             }
             if (mask & (1u << kCoax)) {
@@ -455,9 +478,105 @@ __global__ void __launch_bounds__(256) k_forces_a(ForceArgs a)
     if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
 }
 
+// ------------------------------------------------------------ surrogate path
+// Plain evaluation of an audited pair next to the surrogate's: energy and force errors
+// into the statistics, and the kill switch when the energy error exceeds the tolerance.
+static __device__ __noinline__ void surrogate_audit(const ForceArgs& a, const ParamView& P, int pidx,
+                                             const BBGeom& g, const Frame& fi, const Frame& fj,
+                                             float e_sur, const PairAcc& acc_sur)
+{
+    const ParamHeader& H = P.h();
+    const DHBCross& px = P.term<DHBCross>(kHBCross, pidx);
+    PairAcc pa;
+    pa.fi = pa.ti = pa.tj = mk3(0.f, 0.f, 0.f);
+    RadialF1 R1{px.f1, H.hbx_eps[pidx], H.hbx_shift[pidx]};
+    float e = bb_term<false>(g, fi, fj, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1, pa);
+    RadialF2 R2{px.f2};
+    e += bb_term<true>(g, fi, fj, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2, pa);
+    const float de = e_sur - e;
+    const float3 df = acc_sur.fi - pa.fi;
+    const float df2 = dot(df, df);
+    SurrogateAudit* au = a.audit;
+    atomicAdd(&au->n_audited, 1u);
+    atomicAdd(&au->sum_sq_de, (double)de * de);
+    atomicAdd(&au->sum_sq_e, (double)e * e);
+    atomicAdd(&au->sum_sq_df, (double)df2);
+    atomicAdd(&au->sum_sq_f, (double)dot(pa.fi, pa.fi));
+    // non-negative floats order like their bit patterns
+    atomicMax(reinterpret_cast<int*>(&au->max_abs_de), __float_as_int(fabsf(de)));
+    atomicMax(reinterpret_cast<int*>(&au->max_abs_df), __float_as_int(sqrtf(df2)));
+    if (!(fabsf(de) <= a.audit_tol)) {
+        atomicAdd(&au->n_over, 1u);
+        atomicExch(&au->disabled, 1u);
+    }
+}
+
+__device__ __forceinline__ bool audit_pick(int k, unsigned long long step, uint32_t mod)
+{
+    const uint32_t h = ((uint32_t)k * 2654435761u) ^ ((uint32_t)step * 40503u + 0x9e3779b9u);
+    return (h % mod) == 0u;
+}
+
+// A warp over up to 32 queued fused HB + CS pairs of one class (q = kQHBX complementary,
+// kQHBX0 not), in two rows-of-16 passes through the network: features from the plain
+// evaluator's base-base geometry, energy and input gradient from the MLP, forces and
+// torques from the gradient. On audit steps a hashed 1 / audit_mod of the pairs is also
+// evaluated by the plain evaluator.
+template <bool ENERGY>
+__device__ __noinline__ void surrogate_segment(const ForceArgs& a, const ParamView& P, int q, int kbase,
+                                               int cnt, double* eacc)
+{
+    const int lane = threadIdx.x & 31;
+    const ParamHeader& H = P.h();
+    const int cls = q == kQHBX ? 1 : 0;
+    const MlpVec& V = a.mlp->vec[cls];
+    const unsigned long long step = *(const volatile unsigned long long*)&a.st_rw->step;
+    const bool audit_step = a.audit_every != 0u && (step % a.audit_every) == 0ull;
+    for (int h = 0; h < 2; ++h) {
+        const int k0 = kbase + 16 * h;
+        if (k0 >= cnt) break;
+        const int k = k0 + (lane & 15);
+        bool valid = lane < 16 && k < cnt;
+        PairIn p;
+        BBGeom g;
+        Frame fi, fj;
+        float x[kMlpIn];
+#pragma unroll
+        for (int f = 0; f < kMlpIn; ++f) x[f] = 0.f;
+        if (valid) {
+            bool bad = false;
+            valid = load_short_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad);
+            if (valid) {
+                fi = quat_frame(__ldcg(a.quat + p.i));
+                fj = quat_frame(__ldcg(a.quat + p.j));
+                valid = bb_geometry(p.rc, fi, fj, P.term<DHBCross>(kHBCross, p.pidx).base, g);
+            }
+            if (valid) {
+                mlp_features(g, x);
+#pragma unroll
+                for (int f = 0; f < kMlpIn; ++f) x[f] = (x[f] - V.mu[f]) * V.inv_sd[f];
+            }
+        }
+        float y, dydx[kMlpIn];
+        mlp_rows16(*a.mlp, cls, x, y, dydx);
+        if (valid) {
+            const float e = V.e_scale * y + V.e_shift;
+            float dE[kMlpIn];
+#pragma unroll
+            for (int f = 0; f < kMlpIn; ++f) dE[f] = V.e_scale * dydx[f] * V.inv_sd[f];
+            PairAcc acc;
+            acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+            mlp_grad_to_forces(g, fi, fj, dE, acc);
+            scatter<ENERGY>(a, p.i, p.j, acc, e);
+            if (ENERGY) eacc[kHBCross] += (double)e;
+            if (audit_step && audit_pick(k, step, a.audit_mod)) surrogate_audit(a, P, p.pidx, g, fi, fj, e, acc);
+        }
+    }
+}
+
 // Warp `gwarp` of `nwarps` over the segments [HB | CS | HB+CS | coax | bonds], each
 // padded to whole warps: every warp evaluates 32 items of one term.
-template <bool ENERGY>
+template <bool ENERGY, bool SURR = false>
 __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamView& P, int gwarp,
                                               int nwarps, double* eacc, bool& bad_type)
 {
@@ -470,9 +589,19 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
 #pragma unroll
     for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
     const int lane = threadIdx.x & 31;
+    // the surrogate path is a separate instantiation: its registers would otherwise
+    // lower the occupancy of the plain kernels
+    bool surrogate = false;
+    if constexpr (SURR) surrogate = a.mlp != nullptr && __shfl_sync(0xffffffffu, ld_volatile(&a.audit->disabled), 0) == 0u;
     for (int wbase = gwarp * 32; wbase < seg[kNQ + 1]; wbase += nwarps * 32) {
         int q = 0;
         while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
+        if constexpr (SURR) {
+            if (surrogate && (q == kQHBX || q == kQHBX0)) {
+                surrogate_segment<ENERGY>(a, P, q, wbase - seg[q], cnt[q], eacc);
+                continue;
+            }
+        }
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
         if (q < kNQ) {
@@ -506,7 +635,7 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
     }
 }
 
-template <bool ENERGY>
+template <bool ENERGY, bool SURR = false>
 __global__ void __launch_bounds__(256) k_forces_b(ForceArgs a)
 {
     const ParamView P = stage_params(a.params, a.param_bytes);
@@ -514,7 +643,7 @@ __global__ void __launch_bounds__(256) k_forces_b(ForceArgs a)
 #pragma unroll
     for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
     bool bad_type = false;
-    forces_b_body<ENERGY>(a, P, spread_warp(), (gridDim.x * blockDim.x) >> 5, eacc, bad_type);
+    forces_b_body<ENERGY, SURR>(a, P, spread_warp(), (gridDim.x * blockDim.x) >> 5, eacc, bad_type);
     reduce_energies<ENERGY>(a, eacc);
     if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
 }
@@ -1089,7 +1218,7 @@ __device__ __forceinline__ void particle_step_two(const IntegArgs& a, int i,
 // First step one of a run (accelerations and torques from prepRun / the last step).
 __device__ __forceinline__ void reset_queues(DevStatus* st)
 {
-    if (blockIdx.x == 0 && threadIdx.x < 4) st->qcount[threadIdx.x] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
 }
 
 #ifndef OXG_DEVICE_FUNCTIONS_ONLY
@@ -1209,6 +1338,7 @@ struct RunArgs {
 // forces part two | step two + step one of the next step. The rebuild flag is read by
 // every block right after a barrier and cleared one barrier later; a list overflow
 // ends the launch (the host grows the lists and replays from its checkpoint).
+template <bool SURR>
 __global__ void __launch_bounds__(256, 2) k_run(RunArgs a)
 {
     const ParamView P = stage_params(a.f.params, a.f.param_bytes);
@@ -1237,12 +1367,12 @@ __global__ void __launch_bounds__(256, 2) k_run(RunArgs a)
         forces_a_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
         if (!grid_barrier(a.bar)) break;
         if (blockIdx.x == 0 && threadIdx.x == 0) st->rebuild = 0u;
-        forces_b_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+        forces_b_body<false, SURR>(a.f, P, gwarp, nwarps, eacc, bad_type);
         if (!grid_barrier(a.bar)) break;
         // step two of this step (+ step one of the next)
         const bool last = a.closing && body == a.bodies - 1;
         const unsigned long long step = *(const volatile unsigned long long*)&st->step;
-        if (blockIdx.x == 0 && threadIdx.x < 4) st->qcount[threadIdx.x] = 0u;
+        if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
         bool far = false, bad = false;
         for (int i = gthread; i < a.g.N; i += nthreads) {
             PState s = load_pstate(a.g, i);

@@ -240,7 +240,14 @@ EXPORTS = [
     "oxg_batch_create", "oxg_batch_destroy", "oxg_batch_set_stream", "oxg_batch_set_state",
     "oxg_batch_get_state", "oxg_batch_set_integrator", "oxg_batch_set_tiling", "oxg_batch_tune",
     "oxg_batch_run", "oxg_batch_compute",
+    "oxg_mlp_create", "oxg_mlp_destroy", "oxg_mlp_set_params", "oxg_mlp_get_params",
+    "oxg_mlp_set_normalization", "oxg_mlp_gradient", "oxg_mlp_train_step", "oxg_mlp_predict",
+    "oxg_system_set_surrogate", "oxg_system_surrogate_stats", "oxg_system_hbx_samples",
 ]
+
+MLP_PARAMS = 9480  # OXG_MLP_PARAMS
+SURROGATE_RUN = 1
+SURROGATE_COMPUTE = 2
 
 _lib = None
 
@@ -306,6 +313,17 @@ def lib():
         "oxg_batch_tune": ([vp, i32, C.POINTER(C.c_int), C.POINTER(C.c_int), dp], i32),
         "oxg_batch_run": ([vp, C.c_long], i32),
         "oxg_batch_compute": ([vp, u32, i32, vp, vp, vp], i32),
+        "oxg_mlp_create": ([C.POINTER(vp)], i32),
+        "oxg_mlp_destroy": ([vp], i32),
+        "oxg_mlp_set_params": ([vp, vp], i32),
+        "oxg_mlp_get_params": ([vp, vp], i32),
+        "oxg_mlp_set_normalization": ([vp, i32, vp, vp, C.c_float, C.c_float], i32),
+        "oxg_mlp_gradient": ([vp, i32, vp, vp, vp, i32, vp, vp, vp], i32),
+        "oxg_mlp_train_step": ([vp, i32, vp, vp, vp, i32, C.c_float, vp, vp], i32),
+        "oxg_mlp_predict": ([vp, i32, vp, i32, vp, vp, vp], i32),
+        "oxg_system_set_surrogate": ([vp, vp, i32, i32, i32, f64], i32),
+        "oxg_system_surrogate_stats": ([vp, dp, i32], i32),
+        "oxg_system_hbx_samples": ([vp, i32, vp, vp, C.POINTER(C.c_int)], i32),
         "oxg_last_error": ([], C.c_char_p),
         "oxg_version": ([], C.c_char_p),
         "oxg_status_string": ([i32], C.c_char_p),

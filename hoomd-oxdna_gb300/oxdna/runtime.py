@@ -436,6 +436,34 @@ class Simulation:
                                 force[:, 3].astype(np.float64))
         return self._cache[key]
 
+    # -- learned surrogate (extension; see oxdna.surrogate) ----------------------
+    def set_surrogate(self, network, run=True, compute=False, audit_every=100,
+                      audit_fraction=0.01, tol=0.05):
+        """Evaluate the fused HB + cross-stacking term (forces(fused=True)) with a
+        trained surrogate network in MD steps (run) and / or in energy and force
+        read-outs (compute). Every audit_every steps about audit_fraction of the pairs is
+        also evaluated by the plain evaluator; a pair energy error above tol switches
+        the surrogate off for the rest of the simulation. network=None restores the
+        plain evaluator."""
+        self._attach()
+        flags = (_abi.SURROGATE_RUN if run else 0) | (_abi.SURROGATE_COMPUTE if compute else 0)
+        mod = max(1, int(round(1.0 / audit_fraction))) if audit_fraction > 0 else 1
+        every = int(audit_every) if audit_fraction > 0 else 0
+        _abi.check(_abi.lib().oxg_system_set_surrogate(
+            self._sys, network.handle if network is not None else None,
+            flags if network is not None else 0, every, mod, float(tol)), "oxg_system_set_surrogate")
+        self._surrogate = network
+        self._cache = {}
+
+    def surrogate_stats(self):
+        """Audit statistics: disabled (the kill switch tripped), audited pairs, pairs
+        over tolerance, rms / max energy and force errors against the plain evaluator."""
+        out = (C.c_double * 9)()
+        _abi.check(_abi.lib().oxg_system_surrogate_stats(self._sys, out, 9), "oxg_system_surrogate_stats")
+        keys = ("disabled", "n_audited", "n_over", "rms_de", "rms_e", "rms_df", "rms_f",
+                "max_abs_de", "max_abs_df")
+        return dict(zip(keys, list(out)))
+
     def native_stats(self):
         L = _abi.lib()
         out = (C.c_int64 * 5)()

@@ -267,6 +267,57 @@ int oxg_system_energies(oxg_system* sys, double* pair_energy, double* bonded_ene
  * 3 pair-list entries (long), 4 kernels launched per step. */
 int oxg_system_stats(oxg_system* sys, int64_t* out, int n);
 
+/* ---- learned surrogate of the fused HB + cross-stacking term -------------------
+ * No counterpart in the reference: an extension. A 7 -> 64 -> 64 -> 64 -> 1 SiLU MLP per
+ * pair class (complementary bases / the rest) maps the base-base geometry the plain
+ * evaluator computes (BASE-BASE distance and the cosines c1, c2, c3, c4, c7, c8, in
+ * that order) to the pair energy; forces and torques come from its analytic input
+ * gradient. Weights are BF16 on the tensor cores with FP32 accumulation; FP32 master
+ * parameters (OXG_MLP_PARAMS floats per class: W1[64][16] whose input columns 7..15
+ * stay zero, b1[64], W2[64][64], b2[64], W3[64][64], b3[64], w4[64], b4, padding) are
+ * trained by the library's own kernels. Inputs are normalised as (x - mu) * inv_sd and
+ * the output is E = e_scale * y + e_shift.
+ * Device-pointer arguments: feats[8*n] (7 raw features, class as 0/1), target[n],
+ * idx[nb] (minibatch sample indices), y[n], dydx[7*n] (normalised units).            */
+#define OXG_MLP_PARAMS 9480
+typedef struct oxg_mlp oxg_mlp;
+int oxg_mlp_create(oxg_mlp** out);
+int oxg_mlp_destroy(oxg_mlp* m);
+/* host arrays: 2 * OXG_MLP_PARAMS floats (class 0 then class 1) */
+int oxg_mlp_set_params(oxg_mlp* m, const float* params);
+int oxg_mlp_get_params(oxg_mlp* m, float* params);
+int oxg_mlp_set_normalization(oxg_mlp* m, int cls, const float* mu, const float* inv_sd,
+                              float e_scale, float e_shift);
+/* gradient of L = sum_s (y_s - (target_s - e_shift) / e_scale)^2 / nb with respect to the
+ * class's masters (host, OXG_MLP_PARAMS floats; NULL keeps it accumulated on the device)
+ * and the sum of squared errors (host, may be NULL) */
+int oxg_mlp_gradient(oxg_mlp* m, int cls, const float* feats, const float* target, const int* idx,
+                     int nb, float* grad_host, double* sse_host, void* stream);
+/* one Adam step (beta 0.9 / 0.999) of one class on a minibatch */
+int oxg_mlp_train_step(oxg_mlp* m, int cls, const float* feats, const float* target,
+                       const int* idx, int nb, float lr, double* sse_host, void* stream);
+int oxg_mlp_predict(oxg_mlp* m, int cls, const float* feats, int n, float* y, float* dydx,
+                    void* stream);
+
+/* Surrogate use by a system. flags: OXG_SURROGATE_RUN replaces the fused HB + cross-
+ * stacking pairs of MD steps (oxg_system_run), OXG_SURROGATE_COMPUTE those of
+ * oxg_system_compute. Every audit_every MD steps (0 = never) a hashed 1 / audit_mod of
+ * the pairs is also evaluated by the plain evaluator; the first pair whose energy error
+ * exceeds audit_tol switches the surrogate off (the plain evaluator takes over) until
+ * the next set_surrogate. mlp = NULL or flags = 0 restores the plain evaluator. */
+#define OXG_SURROGATE_RUN 1
+#define OXG_SURROGATE_COMPUTE 2
+int oxg_system_set_surrogate(oxg_system* sys, const oxg_mlp* mlp, int flags, int audit_every,
+                             int audit_mod, double audit_tol);
+/* out[0..8]: disabled, audited pairs, pairs over tolerance, rms energy error, rms
+ * reference energy, rms force error, rms reference force, max |energy error|, max
+ * |force error| */
+int oxg_system_surrogate_stats(oxg_system* sys, double* out, int n);
+/* Training samples from the system's current state: every fused HB + CS pair that
+ * passes the zero-factor tests gives feats[8*k..] (7 features, class) and the plain
+ * evaluator's pair energy (device arrays of max_n samples); *n_out samples written. */
+int oxg_system_hbx_samples(oxg_system* sys, int max_n, float* feats, float* energy, int* n_out);
+
 /* ---- batched independent replicas ---------------------------------------------
  * No counterpart in the reference (which runs one HOOMD simulation per process):
  * R small systems stepped together in one persistent launch. Replica r has its own
@@ -314,7 +365,7 @@ int oxg_batch_compute(oxg_batch* b, uint32_t term_mask, int bonded, float* force
  * Same evaluation as the system engine's nonbonded forces (cell list with bond
  * exclusions, split pair lists, the fused force kernel), but every scratch buffer it
  * needs lives in one fixed-size static device array inside this library (about
- * 11.9 MB, held by every GPU that loads the library until the process exits). The
+ * 12.9 MB, held by every GPU that loads the library until the process exits). The
  * call allocates nothing: no cudaMalloc, cudaFree or allocating library routine.
  *
  * Inputs (device): pos_type[4*N] (x, y, z, type as the float's int bits), quat[4*N],

@@ -84,3 +84,36 @@ extern "C" void devmath_bonded(const oxg_bonded_params* p, const double* Rc, con
     for (int k = 0; k < 3; ++k) e[k] = acc.e[k];
     for (int k = 0; k < 6; ++k) vir[k] = acc.vir[k];
 }
+
+// The surrogate's map from an energy's feature gradient to forces and torques
+// (mlp_grad_to_forces), on a smooth test energy of the base-base features,
+// E = sum_k a_k x_k + b_k x_k^2 with x = (r, c1, c2, c3, c4, c7, c8); the caller checks
+// it against finite differences of E over positions and rotations.
+#include "../../hoomd-oxdna_gb300/csrc/oxg_mlp.cuh"
+
+extern "C" int devmath_mlp_map(const double* base_site, const double* dr, const double* qi,
+                               const double* qj, const double* coef, double* e, double* f,
+                               double* ti, double* tj)
+{
+    const float base[3] = {(float)base_site[0], (float)base_site[1], (float)base_site[2]};
+    const Frame fi = quat_frame(make_float4((float)qi[0], (float)qi[1], (float)qi[2], (float)qi[3]));
+    const Frame fj = quat_frame(make_float4((float)qj[0], (float)qj[1], (float)qj[2], (float)qj[3]));
+    const float3 rc = make_float3((float)-dr[0], (float)-dr[1], (float)-dr[2]);
+    BBGeom g;
+    if (!bb_geometry(rc, fi, fj, base, g)) return 0;
+    float x[kMlpIn], dE[kMlpIn];
+    mlp_features(g, x);
+    double E = 0.0;
+    for (int k = 0; k < kMlpIn; ++k) {
+        E += coef[k] * x[k] + coef[kMlpIn + k] * x[k] * x[k];
+        dE[k] = (float)(coef[k] + 2.0 * coef[kMlpIn + k] * x[k]);
+    }
+    PairAcc acc;
+    acc.fi = acc.ti = acc.tj = make_float3(0.f, 0.f, 0.f);
+    mlp_grad_to_forces(g, fi, fj, dE, acc);
+    *e = E;
+    f[0] = acc.fi.x; f[1] = acc.fi.y; f[2] = acc.fi.z;
+    ti[0] = acc.ti.x; ti[1] = acc.ti.y; ti[2] = acc.ti.z;
+    tj[0] = acc.tj.x; tj[1] = acc.tj.y; tj[2] = acc.tj.z;
+    return 1;
+}

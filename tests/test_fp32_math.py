@@ -35,6 +35,8 @@ def devmath():
                                C.c_double, dp, dp, dp, dp]
     L.devmath_pair.restype = C.c_int
     L.devmath_bonded.argtypes = [C.c_void_p, dp, dp, dp, C.c_int, C.c_int, dp, dp, dp, dp, dp]
+    L.devmath_mlp_map.argtypes = [dp] * 9
+    L.devmath_mlp_map.restype = C.c_int
     return L
 
 
@@ -93,3 +95,58 @@ def test_fp32_bonded_math(devmath, model, avg):
         assert maxrel(got, ref) < TOL_GPU, f"{model} {avg} {key}: {maxrel(got, ref):.2e}"
     e = np.array(out["energy"])
     assert np.array_equal(e[:, 0] >= 1e12, ~ok)
+
+
+def _qmul(a, b):
+    w1, x1, y1, z1 = a
+    w2, x2, y2, z2 = b
+    return np.array([w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2, w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
+                     w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2])
+
+
+def test_surrogate_force_map_matches_finite_differences(devmath):
+    """mlp_grad_to_forces (the surrogate's map from dE/d(features) to forces and lab
+    torques, base-site offsets included) against central differences of a smooth test
+    energy of the base-base features over positions and small lab-frame rotations."""
+    rng = np.random.Generator(np.random.PCG64(3))
+    base = np.array([0.4, 0.0, 0.0])
+    coef = rng.normal(0.0, 1.0, 14)
+    out = [np.zeros(3) for _ in range(4)]
+
+    def run(dr, qi, qj):
+        e = np.zeros(1)
+        ok = devmath.devmath_mlp_map(_p(base), _p(dr), _p(qi), _p(qj), _p(coef), _p(e), _p(out[1]),
+                                     _p(out[2]), _p(out[3]))
+        assert ok
+        return e[0], out[1].copy(), out[2].copy(), out[3].copy()
+
+    for trial in range(20):
+        qi = rng.normal(size=4)
+        qi /= np.linalg.norm(qi)
+        qj = rng.normal(size=4)
+        qj /= np.linalg.norm(qj)
+        dr = rng.normal(size=3)
+        dr *= rng.uniform(0.6, 1.2) / np.linalg.norm(dr)
+        _, F, Ti, Tj = run(dr, qi, qj)
+
+        def central(fn, h):
+            # Richardson-extrapolated central difference, O(h^4)
+            d1 = (fn(h) - fn(-h)) / (2 * h)
+            d2 = (fn(h / 2) - fn(-h / 2)) / h
+            return (4 * d2 - d1) / 3
+
+        def rot(k, a):
+            return np.concatenate([[np.cos(a / 2)], np.sin(a / 2) * np.eye(3)[k]])
+
+        h = 1e-2
+        fd_f = np.zeros(3)
+        fd_ti = np.zeros(3)
+        fd_tj = np.zeros(3)
+        for k in range(3):
+            fd_f[k] = -central(lambda a: run(dr + a * np.eye(3)[k], qi, qj)[0], h)
+            fd_ti[k] = -central(lambda a: run(dr, _qmul(rot(k, a), qi), qj)[0], h)
+            fd_tj[k] = -central(lambda a: run(dr, qi, _qmul(rot(k, a), qj))[0], h)
+        scale = max(np.abs(np.concatenate([fd_f, fd_ti, fd_tj])).max(), 1e-3)
+        assert np.abs(F - fd_f).max() < 2e-3 * scale, (trial, F, fd_f)
+        assert np.abs(Ti - fd_ti).max() < 2e-3 * scale, (trial, Ti, fd_ti)
+        assert np.abs(Tj - fd_tj).max() < 2e-3 * scale, (trial, Tj, fd_tj)

@@ -1,0 +1,144 @@
+"""Learned surrogate of the fused HB + cross-stacking term: the GPU training kernels'
+loss gradients and the inference pass against the CPU oracle (oracle/mlp_oracle.py),
+training on the plain evaluator's own samples (and what the trained network gains over
+the untrained one), and its use inside the engine with audits and the kill switch."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BLOCKS = {"W1": (0, 1024), "b1": (1024, 1088), "W2": (1088, 5184), "b2": (5184, 5248),
+          "W3": (5248, 9344), "b3": (9344, 9408), "w4": (9408, 9472), "b4": (9472, 9473)}
+
+
+def _synthetic(n, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    f = np.zeros((n, 8), np.float32)
+    f[:, 0] = rng.uniform(0.3, 1.6, n)
+    f[:, 1:7] = rng.uniform(-1.0, 1.0, (n, 6))
+    f[:, 7] = rng.integers(0, 2, n)
+    return f, rng.normal(-0.3, 0.4, n).astype(np.float32)
+
+
+def _net(seed):
+    from oxdna import surrogate
+    p = surrogate.init_params(seed)
+    rng = np.random.Generator(np.random.PCG64(seed + 7))
+    for c in (0, 1):
+        for name in ("b1", "b2", "b3"):
+            a, b = BLOCKS[name]
+            p[c, a:b] = rng.normal(0.0, 0.2, b - a)
+        p[c, 9472] = 0.1
+    net = surrogate.Network(params=p)
+    for c in (0, 1):
+        net.set_normalization(c, mu=[0.9, 0, 0, 0, 0, 0, 0], sd=[0.4, 0.6, 0.6, 0.6, 0.6, 0.6, 0.6],
+                              e_scale=0.4, e_shift=-0.3)
+    return net, p
+
+
+def test_training_gradient_matches_oracle(native):
+    """k_mlp_train's loss gradient (every parameter block, both classes) against the
+    BF16-emulating numpy oracle on the same minibatch."""
+    import torch
+    from oracle import mlp_oracle as M
+    net, p = _net(3)
+    f, t = _synthetic(1000, 4)
+    ft = torch.from_numpy(f).cuda()
+    tt = torch.from_numpy(t).cuda()
+    for c in (0, 1):
+        idx = np.nonzero(f[:, 7] == c)[0].astype(np.int32)
+        g, sse = net.gradient(c, ft, tt, torch.from_numpy(idx).cuda())
+        mu, inv, es, sh = net.norm[c]
+        xn = M.normalise(f[idx], mu, inv)
+        yt = ((t[idx] - np.float32(sh)) / np.float32(es)).astype(np.float32)
+        g_ref, sse_ref = M.loss_gradient(p[c], xn, yt.astype(np.float64))
+        assert abs(sse - sse_ref) <= 1e-4 * sse_ref
+        for name, (a, b) in BLOCKS.items():
+            ref = g_ref[a:b]
+            scale = np.abs(ref).max()
+            assert np.abs(g[a:b] - ref).max() <= 5e-3 * scale, (c, name)
+
+
+def test_inference_matches_oracle(native):
+    """mlp_rows16 (energy and input gradient, the pass the force kernels run) against the
+    oracle's emulation of the same BF16 rounding points."""
+    import torch
+    from oracle import mlp_oracle as M
+    net, p = _net(5)
+    f, _ = _synthetic(777, 6)
+    for c in (0, 1):
+        fc = f[f[:, 7] == c]
+        y, d = net.predict(c, torch.from_numpy(fc).cuda())
+        mu, inv, _, _ = net.norm[c]
+        y_ref, d_ref = M.input_gradient(p[c], M.normalise(fc, mu, inv))
+        assert np.abs(y.cpu().numpy() - y_ref).max() <= 2e-3 * np.abs(y_ref).max()
+        assert np.abs(d.cpu().numpy() - d_ref).max() <= 5e-3 * np.abs(d_ref).max()
+
+
+@pytest.fixture(scope="module")
+def trained():
+    """A network trained on pair geometries of a 1600-nt duplex system at 300 and 340 K
+    (the plain evaluator's samples), with a held-out tenth."""
+    import torch
+    from oxdna import surrogate
+    f, e = surrogate.training_set(n_target=240_000, temperatures=(300, 340), n_dup=40, box=60.0,
+                                  equil=400, every=50, seed=21)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    perm = torch.randperm(f.shape[0], generator=g, device="cuda")
+    n_hold = f.shape[0] // 10
+    hold, train = perm[:n_hold], perm[n_hold:]
+    net = surrogate.Network(seed=0)
+    net.fit_normalization(f[train], e[train])
+    rms0 = float(torch.sqrt(((net.energies(f[hold]) - e[hold]) ** 2).mean()))
+    hist = net.train(f[train].contiguous(), e[train].contiguous(), epochs=12, batch=2048, lr=3e-3)
+    rms1 = float(torch.sqrt(((net.energies(f[hold]) - e[hold]) ** 2).mean()))
+    return dict(net=net, hist=hist, rms0=rms0, rms1=rms1, e_sd=float(e.std()))
+
+
+def test_training_gains_over_untrained(native, trained):
+    """What the trained network gains: held-out rms pair-energy error far below the
+    untrained network's and a small fraction of the energy spread."""
+    assert trained["hist"][-1] < trained["hist"][0]
+    assert trained["rms1"] < 0.1 * trained["rms0"], trained
+    assert trained["rms1"] < 0.1 * trained["e_sd"], trained
+
+
+def _fused_sim(seed=3, T=300.0):
+    from oxdna import io, runtime
+    from oxdna.model import dna1, dna2
+    s = io.duplex_system(40, 20, 60.0, seed=seed)
+    forces, _ = dna2.forces(temperature=T, fused=True)
+    sim = runtime.Simulation(device=runtime.device.GPU(), seed=seed)
+    sim.create_state_from_snapshot(io.system_snapshot(s))
+    lang = runtime.md.methods.Langevin(filter=runtime.filter.All(), kT=dna1.kT_from_temperature(T))
+    sim.operations.integrator = runtime.md.Integrator(dt=0.003, integrate_rotational_dof=True,
+                                                      forces=forces, methods=[lang])
+    sim.run(0)
+    return sim, forces
+
+
+def test_engine_surrogate_energy_audits_and_kill_switch(native, trained):
+    """Inside the engine: the surrogate's fused-term energy close to the plain one,
+    audits counted during MD, and a zero tolerance tripping the kill switch, after which
+    the plain evaluator's result is back."""
+    sim, forces = _fused_sim()
+    hbx = forces[2]
+    e_plain = hbx.energy
+    net = trained["net"]
+    sim.set_surrogate(net, run=True, compute=True, audit_every=10, audit_fraction=0.2, tol=1e9)
+    e_sur = hbx.energy
+    assert abs(e_sur - e_plain) < 0.05 * abs(e_plain), (e_sur, e_plain)
+    sim.run(50)
+    st = sim.surrogate_stats()
+    assert st["n_audited"] > 0 and st["disabled"] == 0 and st["n_over"] == 0
+    assert st["rms_de"] < 0.1 * st["rms_e"], st
+    # kill switch
+    sim.set_surrogate(net, run=True, compute=True, audit_every=1, audit_fraction=1.0, tol=0.0)
+    sim.run(2)
+    st = sim.surrogate_stats()
+    assert st["disabled"] == 1 and st["n_over"] > 0
+    e_after = hbx.energy
+    sim.set_surrogate(None)
+    assert abs(e_after - hbx.energy) <= 1e-6 * abs(hbx.energy)
