@@ -469,6 +469,9 @@ struct oxg_system {
     // persistent run kernel
     GridBarrier* bar = nullptr;
     int grid_run = 0, grid_run_surr = 0;
+    cudaEvent_t ev_run[2] = {nullptr, nullptr};  // around each run-kernel launch
+    double run_kernel_ms = 0.0;
+    long long run_kernel_launches = 0, run_kernel_bodies = 0;
     bool persistent = true;
     // learned surrogate of the fused HB + cross-stacking term
     const MlpDev* mlp = nullptr;
@@ -813,6 +816,8 @@ int oxg_system_destroy(oxg_system* s)
     dfree(s->ck_pos); dfree(s->ck_quat); dfree(s->ck_vel); dfree(s->ck_angmom);
     dfree(s->bar);
     dfree(s->audit);
+    for (int k = 0; k < 2; ++k)
+        if (s->ev_run[k]) cudaEventDestroy(s->ev_run[k]);
     if (s->st_host) cudaFreeHost(s->st_host);
     delete s;
     return OXG_OK;
@@ -1062,8 +1067,20 @@ static int run_persistent(oxg_system* s, long bodies)
         if ((rc = checkpoint(s, false))) return rc;
         DevStatus before;
         if ((rc = read_status(s, &before))) return rc;
+        if (!s->ev_run[0]) {
+            OXG_CUDA(cudaEventCreate(&s->ev_run[0]));
+            OXG_CUDA(cudaEventCreate(&s->ev_run[1]));
+        }
+        OXG_CUDA(cudaEventRecord(s->ev_run[0], s->stream));
         if ((rc = launch_run(s, todo, closing))) return rc;
+        OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
         if ((rc = read_status(s, &d))) return rc;
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, s->ev_run[0], s->ev_run[1]) == cudaSuccess) {
+            s->run_kernel_ms += ms;
+            s->run_kernel_launches += 1;
+            s->run_kernel_bodies += todo;
+        }
         if (d.flags & kStBarrierTimeout) return set_err(OXG_ERR_TIMEOUT, "a grid barrier wait of the run kernel gave up");
         if (d.flags & kStNonFinite) return set_err(OXG_ERR_NONFINITE, "non-finite positions or orientations");
         if (d.flags & (kStCellOverflow | kStPairOverflow)) {
@@ -1294,6 +1311,18 @@ int oxg_system_hbx_samples(oxg_system* s, int max_n, float* feats, float* energy
     cudaStreamSynchronize(s->stream);
     dfree(counter);
     return rc;
+}
+
+int oxg_system_run_timing(oxg_system* s, double* out, int n, int reset)
+{
+    if (!s || !out) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    const double v[3] = {s->run_kernel_ms, (double)s->run_kernel_launches, (double)s->run_kernel_bodies};
+    for (int k = 0; k < n && k < 3; ++k) out[k] = v[k];
+    if (reset) {
+        s->run_kernel_ms = 0.0;
+        s->run_kernel_launches = s->run_kernel_bodies = 0;
+    }
+    return OXG_OK;
 }
 
 int oxg_system_set_surrogate(oxg_system* s, const oxg_mlp* mlp, int flags, int audit_every,

@@ -464,6 +464,14 @@ class Simulation:
                 "max_abs_de", "max_abs_df")
         return dict(zip(keys, list(out)))
 
+    def run_kernel_timing(self, reset=False):
+        """(ms, launches, steps) of the persistent run kernel since the last reset, timed
+        with CUDA events around each launch."""
+        out = (C.c_double * 3)()
+        _abi.check(_abi.lib().oxg_system_run_timing(self._sys, out, 3, 1 if reset else 0),
+                   "oxg_system_run_timing")
+        return out[0], int(out[1]), int(out[2])
+
     def native_stats(self):
         L = _abi.lib()
         out = (C.c_int64 * 5)()

@@ -266,6 +266,10 @@ int oxg_system_energies(oxg_system* sys, double* pair_energy, double* bonded_ene
 /* Counters: index 0 steps run, 1 neighbour-list builds, 2 pair-list entries (short),
  * 3 pair-list entries (long), 4 kernels launched per step. */
 int oxg_system_stats(oxg_system* sys, int64_t* out, int n);
+/* Device time of the persistent run kernel measured with CUDA events around each of its
+ * launches on the system's stream: out[0] milliseconds, out[1] launches, out[2] step
+ * bodies, accumulated since the last reset (reset != 0 clears after reading). */
+int oxg_system_run_timing(oxg_system* sys, double* out, int n, int reset);
 
 /* ---- learned surrogate of the fused HB + cross-stacking term -------------------
  * No counterpart in the reference: an extension. A 7 -> 64 -> 64 -> 64 -> 1 SiLU MLP per

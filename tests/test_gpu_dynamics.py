@@ -43,6 +43,31 @@ def test_8000nt_energies_match_oracle(native, oracle, fused):
     assert np.linalg.norm(F.sum(axis=0)) < 1e-4 * np.abs(F).max() * np.sqrt(len(F))
 
 
+def test_rna_hairpins_energies_match_oracle_and_run(native, oracle):
+    """oxRNA2 on 64 hairpins x 48 nt (16-bp stem, 16-nt loop, extended-helix start), box
+    80, 310.15 K, 1 M salt: every per-term energy against the FP64 oracle, then 500
+    Langevin steps (dt 0.002) that stay finite and keep the stems paired."""
+    from oxdna import io
+    from oxdna.model import dna1, rna2
+    s = io.hairpin_system(64, stem=16, loop=16, box_len=80.0, seed=3)
+    forces, _ = rna2.forces(temperature=310.15, salt=1.0)
+    kT = dna1.kT_from_temperature(310.15)
+    sim = _sim(io.system_snapshot(s), forces, dt=0.002, kT=kT, seed=9)
+    model = oracle.Model(forces, io.DNA_BASES)
+    r = oracle.forces(model, oracle.System(s["pos"], s["quat"], s["typeid"], s["box"], s["bonds"]))
+    for f in forces[1:]:
+        ref = r["pair_energy"][f._term]
+        assert abs(f.energy - ref) <= TOL_GPU * max(abs(ref), 1e-6), type(f).__name__
+    b = forces[0]
+    for k, v in enumerate((b.fene_energy, b.bonded_excvol_energy, b.stacking_energy)):
+        ref = r["bonded_energy"][k]
+        assert abs(v - ref) <= TOL_GPU * max(abs(ref), 1e-6)
+    sim.run(500)
+    assert np.isfinite(sim.state.get_snapshot().particles.position).all()
+    hb = [f for f in forces if type(f).__name__ == "HydrogenBonding"][0]
+    assert hb.energy < 0.0
+
+
 @pytest.mark.parametrize("mode", ["persistent", "graph"])
 def test_short_trajectory_tracks_oracle(native, oracle, monkeypatch, mode):
     """Same counter-based RNG on both sides: 20 Langevin steps agree closely, on the
