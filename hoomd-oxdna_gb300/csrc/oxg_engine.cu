@@ -665,7 +665,7 @@ int launch_nlist_forces(oxg_system* s, uint32_t mask, int bonded, bool energy, b
     const int threads = 256;
     const int nb = std::max(1, (std::max(s->N, s->n_cells) + threads - 1) / threads);
     k_nlist_bin<<<nb, threads, 0, s->stream>>>(na);
-    k_nlist_pairs<<<std::max(1, (s->N + threads - 1) / threads), threads, 0, s->stream>>>(na);
+    k_nlist_pairs<<<std::max(1, (s->N + 7) / 8), threads, 0, s->stream>>>(na);  // a warp per particle
     ForceArgs fa = force_args(s, mask, bonded);
     fa.advance_step = md_step ? 1 : 0;
     surrogate_args(s, fa, md_step);
@@ -1570,7 +1570,7 @@ extern "C" int oxg_pair_forces_noalloc(oxg_context* c, uint32_t mask, int N,
     na.cap_long = (int)kNaLongCap;
     na.st = st;
     k_nlist_bin<<<std::max(1, (std::max(N, n_cells) + threads - 1) / threads), threads, 0, s>>>(na);
-    k_nlist_pairs<<<(N + threads - 1) / threads, threads, 0, s>>>(na);
+    k_nlist_pairs<<<std::max(1, (N + 7) / 8), threads, 0, s>>>(na);  // a warp per particle
 
     ForceArgs fa;
     fa.params = scratch + kNaOffParams;

@@ -907,103 +907,100 @@ __global__ void k_nlist_bin(NlistArgs a)
 
 __device__ __forceinline__ bool is_excluded(int4 e, int j) { return e.x == j || e.y == j || e.z == j || e.w == j; }
 
-// Visit every candidate j > i (bond-excluded, within rlist) of particle i.
-template <class F>
-__device__ __forceinline__ void for_each_candidate(const NlistArgs& a, int i, float4 p,
-                                                   const uint32_t* counts, F&& fn)
+// Particle i's pairs j > i (bond-excluded, within r_list) from the cells of parity
+// `par`, found by a whole warp (i warp-uniform): lanes 0..26 take the member counts of
+// the 27 neighbour cells, a prefix sum flattens the candidates, and each round the 32
+// lanes test 32 candidates at once (cell of a candidate by binary search over the
+// prefix sums); found pairs are appended with one atomic per warp and list per round.
+__device__ __forceinline__ void nlist_pairs_warp(const NlistArgs& a, int i, uint32_t par)
 {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const uint32_t* counts = a.cell_count + (size_t)par * a.n_cells;
+    const float4 p = __ldcg(a.pos + i);
     const int4 ex = a.excl[i];
+    int n_l = 0, cbase = 0;
     if (a.use_cells) {
-        const int cx = cell_coord(p.x, a.invL.x, a.nc.x), cy = cell_coord(p.y, a.invL.y, a.nc.y),
-                  cz = cell_coord(p.z, a.invL.z, a.nc.z);
-        for (int dz = -1; dz <= 1; ++dz) {
-            const int z = (cz + dz + a.nc.z) % a.nc.z;
-            for (int dy = -1; dy <= 1; ++dy) {
-                const int y = (cy + dy + a.nc.y) % a.nc.y;
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const int x = (cx + dx + a.nc.x) % a.nc.x;
-                    const int c = (z * a.nc.y + y) * a.nc.x + x;
-                    const int n = min((int)__ldcg(counts + c), a.cell_cap);
-                    const int* lst = a.cell_list + (size_t)c * a.cell_cap;
-                    for (int q = 0; q < n; ++q) {
-                        const int j = __ldcg(lst + q);
-                        if (j <= i || is_excluded(ex, j)) continue;
-                        const float4 pj = __ldcg(a.pos + j);
-                        const float3 d = min_image(mk3(p.x - pj.x, p.y - pj.y, p.z - pj.z), a.L, a.invL);
-                        const float r2 = dot(d, d);
-                        if (r2 < a.rlist2) fn(j, r2);
-                    }
+        if (lane < 27) {
+            const int cx = cell_coord(p.x, a.invL.x, a.nc.x), cy = cell_coord(p.y, a.invL.y, a.nc.y),
+                      cz = cell_coord(p.z, a.invL.z, a.nc.z);
+            const int x = (cx + lane % 3 - 1 + a.nc.x) % a.nc.x;
+            const int y = (cy + (lane / 3) % 3 - 1 + a.nc.y) % a.nc.y;
+            const int z = (cz + lane / 9 - 1 + a.nc.z) % a.nc.z;
+            const int c = (z * a.nc.y + y) * a.nc.x + x;
+            n_l = min((int)__ldcg(counts + c), a.cell_cap);
+            cbase = c * a.cell_cap;
+        }
+    } else if (lane == 0) {
+        n_l = a.N - 1 - i;  // all j > i
+    }
+    int incl = n_l;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl_off = incl - n_l;
+    bool over = false;
+    for (int k0 = 0; k0 < total; k0 += 32) {
+        const int k = k0 + lane;
+        const int kk = min(k, total - 1);
+        // largest lane l < 27 whose range starts at or before kk (a non-empty cell)
+        int lo = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int cand = lo + step;
+            const int e = __shfl_sync(0xffffffffu, excl_off, cand & 31);
+            if (cand < 27 && e <= kk) lo = cand;
+        }
+        const int start = __shfl_sync(0xffffffffu, excl_off, lo);
+        const int cb = __shfl_sync(0xffffffffu, cbase, lo);
+        bool is_short = false, is_long = false;
+        int j = -1;
+        if (k < total) {
+            j = a.use_cells ? __ldcg(a.cell_list + cb + (kk - start)) : i + 1 + kk;
+            if (j > i && !is_excluded(ex, j)) {
+                const float4 pj = __ldcg(a.pos + j);
+                const float3 d = min_image(mk3(p.x - pj.x, p.y - pj.y, p.z - pj.z), a.L, a.invL);
+                const float r2 = dot(d, d);
+                if (r2 < a.rlist2) {
+                    is_short = r2 < a.rshort2;
+                    is_long = !is_short;
                 }
             }
         }
-    } else {
-        for (int j = i + 1; j < a.N; ++j) {
-            if (is_excluded(ex, j)) continue;
-            const float4 pj = __ldcg(a.pos + j);
-            const float3 d = min_image(mk3(p.x - pj.x, p.y - pj.y, p.z - pj.z), a.L, a.invL);
-            const float r2 = dot(d, d);
-            if (r2 < a.rlist2) fn(j, r2);
+        const unsigned ms = __ballot_sync(0xffffffffu, is_short), ml = __ballot_sync(0xffffffffu, is_long);
+        uint32_t bs = 0, bl = 0;
+        if (lane == 0) {
+            if (ms) bs = atomicAdd(&a.st->n_short, (uint32_t)__popc(ms));
+            if (ml) bl = atomicAdd(&a.st->n_long, (uint32_t)__popc(ml));
+        }
+        bs = __shfl_sync(0xffffffffu, bs, 0);
+        bl = __shfl_sync(0xffffffffu, bl, 0);
+        if (is_short) {
+            const uint32_t slot = bs + __popc(ms & lt_mask);
+            if (slot < (uint32_t)a.cap_short) a.pairs_short[slot] = make_int2(i, j);
+            else over = true;
+        }
+        if (is_long) {
+            const uint32_t slot = bl + __popc(ml & lt_mask);
+            if (slot < (uint32_t)a.cap_long) a.pairs_long[slot] = make_int2(i, j);
+            else over = true;
         }
     }
-}
-
-// warp-aggregated reservation of n slots in a global list
-__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t n)
-{
-    const int lane = threadIdx.x & 31;
-    uint32_t incl = n;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    uint32_t base = 0;
-    if (lane == 31 && total) base = atomicAdd(counter, total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    return base + incl - n;
-}
-
-// Particle i's pairs j > i from the cells of parity `par` (whole warps: the slots are
-// reserved with warp-aggregated atomics).
-__device__ __forceinline__ void nlist_pairs_body(const NlistArgs& a, int i, uint32_t par)
-{
-    const bool active = i < a.N;
-    const uint32_t* counts = a.cell_count + (size_t)par * a.n_cells;
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    uint32_t ns = 0, nl = 0;
-    if (active) {
-        p = __ldcg(a.pos + i);
-        for_each_candidate(a, i, p, counts, [&](int, float r2) {
-            if (r2 < a.rshort2) ++ns;
-            else ++nl;
-        });
-    }
-    const uint32_t bs = warp_reserve(&a.st->n_short, ns);
-    const uint32_t bl = warp_reserve(&a.st->n_long, nl);
-    if (!active) return;
-    uint32_t ks = bs, kl = bl;
-    bool over = false;
-    for_each_candidate(a, i, p, counts, [&](int j, float r2) {
-        if (r2 < a.rshort2) {
-            if (ks < (uint32_t)a.cap_short) a.pairs_short[ks] = make_int2(i, j);
-            else over = true;
-            ++ks;
-        } else {
-            if (kl < (uint32_t)a.cap_long) a.pairs_long[kl] = make_int2(i, j);
-            else over = true;
-            ++kl;
-        }
-    });
     if (over) atomicOr(&a.st->flags, kStPairOverflow);
-    if (i == 0) atomicAdd(&a.st->builds, 1u);
+    if (i == 0 && lane == 0) atomicAdd(&a.st->builds, 1u);
 }
 
 #ifndef OXG_DEVICE_FUNCTIONS_ONLY
+// One warp per particle (grid-stride over particles).
 __global__ void k_nlist_pairs(NlistArgs a)
 {
     if (!a.st->rebuild) return;
-    nlist_pairs_body(a, blockIdx.x * blockDim.x + threadIdx.x, a.st->gen & 1u);
+    const uint32_t par = a.st->gen & 1u;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = w; i < a.N; i += nw) nlist_pairs_warp(a, i, par);
 }
 #endif
 
@@ -1356,7 +1353,7 @@ __global__ void __launch_bounds__(256, 2) k_run(RunArgs a)
             nlist_zero_other(a.n, gthread, nthreads, par);
             for (int i = gthread; i < a.n.N; i += nthreads) nlist_bin_particle(a.n, i, par);
             if (!grid_barrier(a.bar)) break;
-            for (int base = gwarp * 32; base < a.n.N; base += nthreads) nlist_pairs_body(a.n, base + lane, par);
+            for (int i = gwarp; i < a.n.N; i += nwarps) nlist_pairs_warp(a.n, i, par);
             if (!grid_barrier(a.bar)) break;
             if (ld_volatile(&st->flags) & (kStCellOverflow | kStPairOverflow)) break;
         }
