@@ -449,13 +449,30 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--quick", action="store_true",
                     help="resident timing only (no fused / e2e / CPU legs); for profiling runs")
+    ap.add_argument("--leg", choices=["batched", "rna", "surrogate"],
+                    help="run one extension leg alone and print its numbers (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.leg:
+        run_leg(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
+
+
+def run_leg(args):
+    import torch
+    stream = torch.cuda.Stream()
+    if args.leg == "batched":
+        out = bench_batched(stream, steps=args.steps)
+    elif args.leg == "rna":
+        out = bench_rna(stream, steps=args.steps, warmup=args.warmup)
+    else:
+        big = build_system(n_dup=2500, n_bp=20, box=230.0, seed=5)
+        out = bench_surrogate(stream, big, steps=args.steps, warmup=args.warmup)
+    print(json.dumps({"leg": args.leg, **out}), flush=True)
 
 
 if __name__ == "__main__":

@@ -47,7 +47,7 @@ struct TileRep {
     float3 L, invL;
     float kT;
     uint32_t seed_lo, seed_hi;
-    int pad;
+    float rlist2;  // (largest cutoff of the replica's terms + skin)^2
 };
 
 struct BatchArgs {
@@ -74,6 +74,8 @@ struct BatchArgs {
     float4* accel;          // (F + F_bath) / m after the last step two
     float4* tnet;           // T + T_bath after the last step two
     int max_reps, tile_cap, qcap;
+    int plist_cap;          // tile pair-list capacity
+    float skin;             // pair-list skin (rebuilt after a move of skin / 2)
     double* energy;         // [replica][9] (compute mode)
     float4* force_out;      // compute mode (may be null)
     float4* torque_out;
@@ -90,13 +92,16 @@ struct Smem {
     int* rep_of;
     int* queue;  // kNQ * qcap entries: (i << 16) | j
     int* qcnt;
+    int* nl;       // [0] pairs in plist, -1 = no list (all pairs tested every step)
+    int* plist;    // tile pair list (pi << 16) | pj, pi < pj
+    float4* xref;  // positions at the last list build
     double* eacc;  // [max_reps][9]
 };
 
 __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~size_t(15); }
 
 __host__ __device__ inline size_t smem_bytes(int max_reps, int tile_cap, int qcap, int stride,
-                                             bool energy)
+                                             bool energy, int plist_cap)
 {
     size_t b = a16(sizeof(TileRep) * max_reps);
     b += a16((size_t)stride * max_reps);
@@ -105,6 +110,9 @@ __host__ __device__ inline size_t smem_bytes(int max_reps, int tile_cap, int qca
     b += a16(sizeof(int) * tile_cap);
     b += a16(sizeof(int) * (size_t)kNQ * qcap);
     b += 32;  // queue counters (8 ints, kNQ used)
+    b += 16;  // list counters
+    b += a16(sizeof(int) * (size_t)plist_cap);
+    b += sizeof(float4) * (size_t)tile_cap;
     if (energy) b += a16(sizeof(double) * 9 * max_reps);
     return b;
 }
@@ -139,6 +147,12 @@ __device__ inline Smem carve(unsigned char* base, const BatchArgs& a, bool energ
     o += a16(sizeof(int) * (size_t)kNQ * a.qcap);
     s.qcnt = reinterpret_cast<int*>(base + o);
     o += 32;
+    s.nl = reinterpret_cast<int*>(base + o);
+    o += 16;
+    s.plist = reinterpret_cast<int*>(base + o);
+    o += a16(sizeof(int) * (size_t)a.plist_cap);
+    s.xref = reinterpret_cast<float4*>(base + o);
+    o += sizeof(float4) * (size_t)a.tile_cap;
     s.eacc = energy ? reinterpret_cast<double*>(base + o) : nullptr;
     return s;
 }
@@ -223,6 +237,131 @@ __device__ __noinline__ void batch_heavy(const Smem& s, const BatchArgs& a, int 
     scatter_pair<ENERGY>(s, pi, pj, r, acc, e, term);
 }
 
+// Phase-A work of one pair (pi < pj) of replica r: the cheap terms (excluded volume,
+// Debye) inline, the zero-factor tests of the heavy ones, which are queued.
+template <bool ENERGY>
+__device__ __forceinline__ void pair_a(const Smem& s, const BatchArgs& a, int r, int pi, int pj)
+{
+    const TileRep& R = s.reps[r];
+    const int4 ex = s.ex[pi];
+    if (ex.x == pj || ex.y == pj || ex.z == pj || ex.w == pj) return;
+    const float3 dr = rep_delta(s, R, pi, pj);
+    const float rsq = dot(dr, dr);
+    ParamView P;
+    P.b = s.params + (size_t)r * a.param_bytes;
+    const ParamHeader& H = P.h();
+    if (!(rsq < H.rcutsq_max)) return;
+    const int pidx = __float_as_int(s.x[pi].w) * kMaxTypes + __float_as_int(s.x[pj].w);
+    const Frame fi = frame_of(s, pi), fj = frame_of(s, pj);
+    const float3 rc = -dr;
+    const uint32_t mask = a.mask;
+    PairAcc acc;
+    acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+    float ev = 0.f, ed = 0.f;
+    bool inl = false;
+    if (mask & (1u << kExcVol)) {
+        const DExcVol& pe = P.term<DExcVol>(kExcVol, pidx);
+        if (rsq < pe.rcutsq) {
+            ev = excvol_term(pe, rc, fi, fj, acc);
+            inl = true;
+        }
+    }
+    if (mask & (1u << kDebye)) {
+        const DDebye& pd = P.term<DDebye>(kDebye, pidx);
+        if (rsq < pd.rcutsq) {
+            const float ci = a.charge[R.pstart + pi - R.loff], cj = a.charge[R.pstart + pj - R.loff];
+            ed = debye_term(pd, rc, fi, fj, ci, cj, acc);
+            inl = true;
+        }
+    }
+    if (inl) {
+        scatter_pair<ENERGY>(s, pi, pj, r, acc, ev + ed, kExcVol);
+        if (ENERGY && ed != 0.f) {  // book the Debye part under its own term
+            atomicAdd(&s.eacc[r * 9 + kExcVol], -(double)ed);
+            atomicAdd(&s.eacc[r * 9 + kDebye], (double)ed);
+        }
+    }
+    bool want[kNQ] = {};
+    BBGeom g;
+    bool gv = false;
+    if (mask & (1u << kHBond)) {
+        const DHBond& ph = P.term<DHBond>(kHBond, pidx);
+        if (rsq < ph.rcutsq && H.hb_eps[pidx] != 0.f) {
+            gv = bb_geometry(rc, fi, fj, ph.base, g);
+            RadialF1 Rr{ph.f1, H.hb_eps[pidx], H.hb_shift[pidx]};
+            want[kQHB] = gv && bb_support<false>(g, ph.t1, ph.t23, ph.t4, ph.t78, true, Rr);
+        }
+    }
+    if (mask & (1u << kCross)) {
+        const DCross& pc = P.term<DCross>(kCross, pidx);
+        if (rsq < pc.rcutsq) {
+            if (!gv || !H.hb_cs_same_site) gv = bb_geometry(rc, fi, fj, pc.base, g);
+            RadialF2 Rr{pc.f2};
+            want[kQCS] = gv && bb_support<true>(g, pc.t1, pc.t23, pc.t4, pc.t78, pc.t4_enabled != 0, Rr);
+        }
+    }
+    if (mask & (1u << kHBCross)) {
+        const DHBCross& px = P.term<DHBCross>(kHBCross, pidx);
+        if (rsq < px.rcutsq && bb_geometry(rc, fi, fj, px.base, g)) {
+            RadialF1 R1{px.f1, H.hbx_eps[pidx], H.hbx_shift[pidx]};
+            RadialF2 R2{px.f2};
+            want[kQHBX] = bb_support<false>(g, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1) ||
+                          bb_support<true>(g, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2);
+        }
+    }
+    if (mask & (1u << kCoax)) {
+        const DCoax& pc = P.term<DCoax>(kCoax, pidx);
+        want[kQCX] = rsq < pc.rcutsq && coax_support(pc, rc, fi, fj);
+    }
+    for (int q = 0; q < kNQ; ++q) {
+        if (!want[q]) continue;
+        const int slot = atomicAdd(&s.qcnt[q], 1);
+        if (slot < a.qcap) s.queue[q * a.qcap + slot] = (pi << 16) | pj;
+        else batch_heavy<ENERGY>(s, a, q, pi, pj, r);  // queue full: evaluate here
+    }
+}
+
+// Pair k of the strictly upper triangles of the tile's replicas -> (replica, pi, pj).
+__device__ __forceinline__ void tri_pair(const Smem& s, int nrep, int k, int& r, int& pi, int& pj)
+{
+    r = 0;
+    while (r + 1 < nrep && k >= s.reps[r + 1].tri_off) ++r;
+    const TileRep& R = s.reps[r];
+    const int n = R.n;
+    const int t = k - R.tri_off;
+    // row i of the strictly upper triangle holding index t
+    int i = (int)((2.f * n - 1.f - sqrtf((2.f * n - 1.f) * (2.f * n - 1.f) - 8.f * t)) * 0.5f);
+    i = max(0, min(i, n - 2));
+    while (i > 0 && t < i * (2 * n - i - 1) / 2) --i;
+    while (i < n - 2 && t >= (i + 1) * (2 * n - i - 2) / 2) ++i;
+    const int j = t - i * (2 * n - i - 1) / 2 + i + 1;
+    pi = R.loff + i;
+    pj = R.loff + j;
+}
+
+// Tile pair list: every bond-excluded-free pair within its replica's r_list; the list
+// falls back to testing all pairs every step when it would exceed its capacity.
+__device__ void build_list(const Smem& s, const BatchArgs& a, int nrep, int np, int total_pairs)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (tid == 0) s.nl[0] = 0;
+    for (int p = tid; p < np; p += nt) s.xref[p] = s.x[p];
+    __syncthreads();
+    for (int k = tid; k < total_pairs; k += nt) {
+        int r, pi, pj;
+        tri_pair(s, nrep, k, r, pi, pj);
+        const int4 ex = s.ex[pi];
+        if (ex.x == pj || ex.y == pj || ex.z == pj || ex.w == pj) continue;
+        const float3 dr = rep_delta(s, s.reps[r], pi, pj);
+        if (!(dot(dr, dr) < s.reps[r].rlist2)) continue;
+        const int slot = atomicAdd(&s.nl[0], 1);
+        if (slot < a.plist_cap) s.plist[slot] = (pi << 16) | pj;
+    }
+    __syncthreads();
+    if (tid == 0 && s.nl[0] > a.plist_cap) s.nl[0] = -1;
+    __syncthreads();
+}
+
 // Forces of the whole tile into s.f / s.t (block-cooperative).
 template <bool ENERGY>
 __device__ void tile_forces(const Smem& s, const BatchArgs& a, int nrep, int np, int nb,
@@ -239,95 +378,19 @@ __device__ void tile_forces(const Smem& s, const BatchArgs& a, int nrep, int np,
     }
     if (tid < kNQ) s.qcnt[tid] = 0;
     __syncthreads();
-    // phase A: every pair of every replica of the tile
-    for (int k = tid; k < total_pairs; k += nt) {
-        int r = 0;
-        while (r + 1 < nrep && k >= s.reps[r + 1].tri_off) ++r;
-        const TileRep& R = s.reps[r];
-        const int n = R.n;
-        const int t = k - R.tri_off;
-        // row i of the strictly upper triangle holding index t
-        int i = (int)((2.f * n - 1.f - sqrtf((2.f * n - 1.f) * (2.f * n - 1.f) - 8.f * t)) * 0.5f);
-        i = max(0, min(i, n - 2));
-        while (i > 0 && t < i * (2 * n - i - 1) / 2) --i;
-        while (i < n - 2 && t >= (i + 1) * (2 * n - i - 2) / 2) ++i;
-        const int j = t - i * (2 * n - i - 1) / 2 + i + 1;
-        const int pi = R.loff + i, pj = R.loff + j;
-        const int4 ex = s.ex[pi];
-        if (ex.x == pj || ex.y == pj || ex.z == pj || ex.w == pj) continue;
-        const float3 dr = rep_delta(s, R, pi, pj);
-        const float rsq = dot(dr, dr);
-        ParamView P;
-        P.b = s.params + (size_t)r * a.param_bytes;
-        const ParamHeader& H = P.h();
-        if (!(rsq < H.rcutsq_max)) continue;
-        const int pidx = __float_as_int(s.x[pi].w) * kMaxTypes + __float_as_int(s.x[pj].w);
-        const Frame fi = frame_of(s, pi), fj = frame_of(s, pj);
-        const float3 rc = -dr;
-        const uint32_t mask = a.mask;
-        PairAcc acc;
-        acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
-        float ev = 0.f, ed = 0.f;
-        bool inl = false;
-        if (mask & (1u << kExcVol)) {
-            const DExcVol& pe = P.term<DExcVol>(kExcVol, pidx);
-            if (rsq < pe.rcutsq) {
-                ev = excvol_term(pe, rc, fi, fj, acc);
-                inl = true;
-            }
+    // phase A: the tile's pair list (or every pair of every replica of the tile)
+    const int npl = s.nl[0];
+    if (npl >= 0) {
+        for (int k = tid; k < npl; k += nt) {
+            const int v = s.plist[k];
+            const int pi = v >> 16, pj = v & 0xffff;
+            pair_a<ENERGY>(s, a, s.rep_of[pi], pi, pj);
         }
-        if (mask & (1u << kDebye)) {
-            const DDebye& pd = P.term<DDebye>(kDebye, pidx);
-            if (rsq < pd.rcutsq) {
-                const float ci = a.charge[R.pstart + i], cj = a.charge[R.pstart + j];
-                ed = debye_term(pd, rc, fi, fj, ci, cj, acc);
-                inl = true;
-            }
-        }
-        if (inl) {
-            scatter_pair<ENERGY>(s, pi, pj, r, acc, ev + ed, kExcVol);
-            if (ENERGY && ed != 0.f) {  // book the Debye part under its own term
-                atomicAdd(&s.eacc[r * 9 + kExcVol], -(double)ed);
-                atomicAdd(&s.eacc[r * 9 + kDebye], (double)ed);
-            }
-        }
-        bool want[kNQ] = {};
-        BBGeom g;
-        bool gv = false;
-        if (mask & (1u << kHBond)) {
-            const DHBond& ph = P.term<DHBond>(kHBond, pidx);
-            if (rsq < ph.rcutsq && H.hb_eps[pidx] != 0.f) {
-                gv = bb_geometry(rc, fi, fj, ph.base, g);
-                RadialF1 Rr{ph.f1, H.hb_eps[pidx], H.hb_shift[pidx]};
-                want[kQHB] = gv && bb_support<false>(g, ph.t1, ph.t23, ph.t4, ph.t78, true, Rr);
-            }
-        }
-        if (mask & (1u << kCross)) {
-            const DCross& pc = P.term<DCross>(kCross, pidx);
-            if (rsq < pc.rcutsq) {
-                if (!gv || !H.hb_cs_same_site) gv = bb_geometry(rc, fi, fj, pc.base, g);
-                RadialF2 Rr{pc.f2};
-                want[kQCS] = gv && bb_support<true>(g, pc.t1, pc.t23, pc.t4, pc.t78, pc.t4_enabled != 0, Rr);
-            }
-        }
-        if (mask & (1u << kHBCross)) {
-            const DHBCross& px = P.term<DHBCross>(kHBCross, pidx);
-            if (rsq < px.rcutsq && bb_geometry(rc, fi, fj, px.base, g)) {
-                RadialF1 R1{px.f1, H.hbx_eps[pidx], H.hbx_shift[pidx]};
-                RadialF2 R2{px.f2};
-                want[kQHBX] = bb_support<false>(g, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1) ||
-                              bb_support<true>(g, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2);
-            }
-        }
-        if (mask & (1u << kCoax)) {
-            const DCoax& pc = P.term<DCoax>(kCoax, pidx);
-            want[kQCX] = rsq < pc.rcutsq && coax_support(pc, rc, fi, fj);
-        }
-        for (int q = 0; q < kNQ; ++q) {
-            if (!want[q]) continue;
-            const int slot = atomicAdd(&s.qcnt[q], 1);
-            if (slot < a.qcap) s.queue[q * a.qcap + slot] = (pi << 16) | pj;
-            else batch_heavy<ENERGY>(s, a, q, pi, pj, r);  // queue full: evaluate here
+    } else {
+        for (int k = tid; k < total_pairs; k += nt) {
+            int r, pi, pj;
+            tri_pair(s, nrep, k, r, pi, pj);
+            pair_a<ENERGY>(s, a, r, pi, pj);
         }
     }
     __syncthreads();
@@ -398,7 +461,7 @@ __global__ void __launch_bounds__(256) k_batch(BatchArgs a)
             R.kT = box.w;
             R.seed_lo = sd.x;
             R.seed_hi = sd.y;
-            R.pad = 0;
+            R.rlist2 = 0.f;
             s.reps[r] = R;
             loff += info.y;
             boff += info.w;
@@ -435,6 +498,21 @@ __global__ void __launch_bounds__(256) k_batch(BatchArgs a)
     if (ENERGY)
         for (int k = tid; k < 9 * nrep; k += nt) s.eacc[k] = 0.0;
     __syncthreads();
+    if (tid < nrep) {
+        ParamView P;
+        P.b = s.params + (size_t)tid * a.param_bytes;
+        const float rl = sqrtf(P.h().rcutsq_max) + a.skin;
+        s.reps[tid].rlist2 = rl * rl;
+    }
+    __syncthreads();
+    build_list(s, a, nrep, np, total_pairs);
+    const float half_skin2 = 0.25f * a.skin * a.skin;
+    auto moved_far = [&](int p) {
+        const TileRep& R = s.reps[s.rep_of[p]];
+        const float4 x = s.x[p], x0 = s.xref[p];
+        const float3 d = min_image(mk3(x.x - x0.x, x.y - x0.y, x.z - x0.z), R.L, R.invL);
+        return dot(d, d) > half_skin2;
+    };
 
     if (a.nsteps == 0 || !a.resume) tile_forces<ENERGY>(s, a, nrep, np, nb, total_pairs);
     if (a.nsteps == 0) {  // compute mode: forces and energies out
@@ -473,7 +551,9 @@ __global__ void __launch_bounds__(256) k_batch(BatchArgs a)
         s.q[p] = st.q;
         s.p[p] = st.p;
     }
-    __syncthreads();
+    bool far = false;
+    for (int p = tid; p < np; p += nt) far |= moved_far(p);
+    if (__syncthreads_or(far)) build_list(s, a, nrep, np, total_pairs);
     for (int step = 0; step < a.nsteps; ++step) {
         tile_forces<false>(s, a, nrep, np, nb, total_pairs);
         const unsigned long long ts = a.step0 + (unsigned long long)step + 1ull;
@@ -499,6 +579,9 @@ __global__ void __launch_bounds__(256) k_batch(BatchArgs a)
             s.p[p] = st.p;
         }
         __syncthreads();
+        bool far_s = false;
+        for (int p = tid; p < np; p += nt) far_s |= moved_far(p);
+        if (__syncthreads_or(far_s) && !last) build_list(s, a, nrep, np, total_pairs);
     }
     // write the state back
     for (int r = 0; r < nrep; ++r) {
@@ -672,6 +755,8 @@ BatchArgs batch_args(oxg_batch* b, int nsteps, bool resume, float4* fout, float4
     a.max_reps = b->max_reps;
     a.tile_cap = b->tile_cap;
     a.qcap = b->qcap;
+    a.plist_cap = 32 * b->tile_cap;
+    a.skin = 0.4f;
     a.energy = b->energy;
     a.force_out = fout;
     a.torque_out = tout;
@@ -682,7 +767,7 @@ BatchArgs batch_args(oxg_batch* b, int nsteps, bool resume, float4* fout, float4
 int launch_batch(oxg_batch* b, int nsteps, bool resume, bool energy, float4* fout, float4* tout)
 {
     const BatchArgs a = batch_args(b, nsteps, resume, fout, tout);
-    const size_t sm = smem_bytes(b->max_reps, b->tile_cap, b->qcap, b->param_bytes, energy);
+    const size_t sm = smem_bytes(b->max_reps, b->tile_cap, b->qcap, b->param_bytes, energy, 32 * b->tile_cap);
     if (sm > 227 * 1024)
         return internal_set_error(OXG_ERR_CAPACITY, "tile needs " + std::to_string(sm) + " bytes of shared memory");
     if (energy) {
@@ -1010,7 +1095,7 @@ int oxg_batch_tune(oxg_batch* b, int trial_steps, int* tile_out, int* threads_ou
             if (th > 2 * cap) continue;
             b->threads = th;
             if ((rc = build_tiles(b, cap))) break;
-            const size_t sm = smem_bytes(b->max_reps, b->tile_cap, b->qcap, b->param_bytes, false);
+            const size_t sm = smem_bytes(b->max_reps, b->tile_cap, b->qcap, b->param_bytes, false, 32 * b->tile_cap);
             if (sm > 227 * 1024) continue;
             launch_batch(b, 2, false, false, nullptr, nullptr);  // warm-up
             cudaEventRecord(e0, b->stream);
