@@ -101,6 +101,22 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
+class nvtx:
+    """NVTX range around a timed region (ncu --nvtx --nvtx-include "<name>/" selects the
+    kernels launched inside it)."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        import torch
+        torch.cuda.nvtx.range_push(self.name)
+
+    def __exit__(self, *a):
+        import torch
+        torch.cuda.nvtx.range_pop()
+
+
 def build_system(n_dup=200, n_bp=20, box=100.0, seed=2):
     from oxdna import io
     return io.duplex_system(n_dup, n_bp, box, seed=seed)
@@ -164,7 +180,8 @@ def bench_batched(stream, steps=2000, loop_steps=20, n_rep=512, seed=4):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    b.run(steps)
+    with nvtx("batched_timed"):
+        b.run(steps)
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1)
@@ -204,7 +221,8 @@ def bench_rna(stream, steps=2000, warmup=100):
     sim.operations.integrator = runtime.md.Integrator(dt=0.002, integrate_rotational_dof=True,
                                                       forces=forces, methods=[lang])
     sim.run(0)
-    ms = time_resident(sim, steps, warmup, stream)
+    with nvtx("rna_timed"):
+        ms = time_resident(sim, steps, warmup, stream)
     return {"workload": "oxRNA2 64 hairpins x 48 nt (3072 nt), box 80, 310.15 K, 1 M, dt 0.002",
             "steps_per_s": steps / (ms * 1e-3)}
 
@@ -228,7 +246,9 @@ def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epoc
     net = surrogate.Network(seed=0)
     net.fit_normalization(f[tr], e[tr])
     t0 = time.perf_counter()
-    net.train(f[tr].contiguous(), e[tr].contiguous(), epochs=epochs, batch=4096, lr=3e-3, lr_end=3e-5)
+    with nvtx("surrogate_train"):
+        net.train(f[tr].contiguous(), e[tr].contiguous(), epochs=epochs, batch=4096, lr=3e-3,
+                  lr_end=3e-5)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     d = net.energies(f[hold]) - e[hold]
@@ -241,7 +261,8 @@ def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epoc
         sim.run(0)
         if mode == "surrogate":
             sim.set_surrogate(net, run=True, compute=False, audit_every=100, audit_fraction=0.01, tol=0.5)
-        ms = time_resident(sim, steps, warmup, stream)
+        with nvtx(mode + "_timed"):
+            ms = time_resident(sim, steps, warmup, stream)
         out[mode + "_steps_per_s"] = steps / (ms * 1e-3)
         if mode == "surrogate":
             st = sim.surrogate_stats()
@@ -322,7 +343,8 @@ def run_ours(args):
     sim.run(args.warmup)
     sim.run_kernel_timing(reset=True)
     with ClockSampler(local) as clk:
-        ms = time_resident(sim, args.steps, 0, stream)
+        with nvtx("timed"):
+            ms = time_resident(sim, args.steps, 0, stream)
     k_ms, k_launches, k_steps = sim.run_kernel_timing(reset=True)
     torch.cuda.synchronize()
     ms = replicas.max_over_ranks(ms, dist)
