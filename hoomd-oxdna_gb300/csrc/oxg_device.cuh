@@ -62,6 +62,13 @@ OXG_HD float3 body_to_lab(const Frame& f, const float* s)
 // ---------------------------------------------------------------- numerics (L1)
 // src/OxDNANumerics.h:194-198
 OXG_HD float clamp_cos(float c) { return c > 1.f ? 1.f : (c < -1.f ? -1.f : c); }
+// sin(acos(c)) = sqrt((1 - c)(1 + c)): 1 - c (or 1 + c) is exact in FP32 for |c| >= 1/2,
+// so this is as accurate as sinf(acosf(c)) and does not wait for the acos.
+OXG_HD float sin_of_acos(float c)
+{
+    const float cc = clamp_cos(c);
+    return sqrtf(fmaxf(0.f, (1.f - cc) * (1.f + cc)));
+}
 
 // src/OxDNANumerics.h:201-215
 OXG_HD float f4_angle(float t, const F4& p)
@@ -87,6 +94,20 @@ OXG_HD float f4_dsin(float t, float st, const F4& p)
     if (!(d < p.tc)) return 0.f;
     if (d > p.ts) return m * 2.f * p.b * (d - p.tc) / st;
     if (st * st > 1e-8f) return -m * 2.f * p.a * d / st;
+    return -m * 2.f * p.a;
+}
+// The same with 1 / sin(theta) supplied (one reciprocal shared by an angle's branches).
+OXG_HD float f4_dsin_inv(float t, float st, float inv_st, const F4& p)
+{
+    float d = t - p.t0;
+    float m = 1.f;
+    if (d < 0.f) {
+        d = -d;
+        m = -1.f;
+    }
+    if (!(d < p.tc)) return 0.f;
+    if (d > p.ts) return m * 2.f * p.b * (d - p.tc) * inv_st;
+    if (st * st > 1e-8f) return -m * 2.f * p.a * d * inv_st;
     return -m * 2.f * p.a;
 }
 // cos(theta) in the open support interval of f4 (or, symmetrised, of f4(pi - theta))
@@ -221,7 +242,7 @@ OXG_HD void angle_of(float c, float3 u, float3 v, const F4& t, float& th, float&
         th = atan2f(st, c);
     } else {
         th = acosf(clamp_cos(c));
-        st = sinf(th);
+        st = sin_of_acos(c);
     }
 }
 
@@ -234,11 +255,12 @@ OXG_HD Ang angular(float cost, float3 u, float3 v, const F4& t, float sign)
     angle_of(cost, u, v, t, th, st);
     Ang a;
     a.val = f4_angle(th, t);
-    float d = f4_dsin(th, st, t);
+    const float inv_st = 1.f / st;
+    float d = f4_dsin_inv(th, st, inv_st, t);
     if (SYM) {
         const float thn = kPi - th;
         a.val += f4_angle(thn, t);
-        d -= f4_dsin(thn, st, t);
+        d -= f4_dsin_inv(thn, st, inv_st, t);
     }
     a.dsin = sign * d;
     return a;
@@ -580,8 +602,8 @@ OXG_HD float stacking_dna(const DBonded& p, float3 Rc, const Frame& fA,
     const float f5p1 = f5_val(cp1, p.p1), f5p2 = f5_val(cp2, p.p1);
     const float es = f1 * f4t4 * f4t5 * f4t6 * f5p1 * f5p2;
     if (es == 0.f) return 0.f;
-    const float f4t4D = f4_dsin(th4, sinf(th4), p.t4), f4t5D = f4_dsin(th5, sinf(th5), p.t5),
-                f4t6D = f4_dsin(th6, sinf(th6), p.t5);
+    const float f4t4D = f4_dsin(th4, sin_of_acos(c4), p.t4), f4t5D = f4_dsin(th5, sin_of_acos(-c5), p.t5),
+                f4t6D = f4_dsin(th6, sin_of_acos(c6), p.t5);
     const float f5p1D = f5_deriv(cp1, p.p1), f5p2D = f5_deriv(cp2, p.p1);
 
     float3 force = rsd * (-(f1D * f4t4 * f4t5 * f4t6 * f5p1 * f5p2));
@@ -678,8 +700,8 @@ OXG_HD float stacking_rna(const DBonded& p, float3 Rc, const Frame& fA,
     const float f5p1 = f5_val(cp1, p.p1), f5p2 = f5_val(cp2, p.p1);
     const float es = f1 * f4t5 * f4t6 * f4B1 * f4B2 * f5p1 * f5p2;
     if (es == 0.f) return 0.f;
-    const float f4t5D = f4_dsin(th5, sinf(th5), p.t5), f4t6D = f4_dsin(th6, sinf(th6), p.t5);
-    const float f4B1D = f4_dsin(thB1, sinf(thB1), p.tB1), f4B2D = f4_dsin(thB2, sinf(thB2), p.tB2);
+    const float f4t5D = f4_dsin(th5, sin_of_acos(-c5), p.t5), f4t6D = f4_dsin(th6, sin_of_acos(c6), p.t5);
+    const float f4B1D = f4_dsin(thB1, sin_of_acos(cB1), p.tB1), f4B2D = f4_dsin(thB2, sin_of_acos(cB2), p.tB2);
     const float f5p1D = f5_deriv(cp1, p.p1), f5p2D = f5_deriv(cp2, p.p1);
 
     float3 force = rsd * (-(f1D * f4t5 * f4t6 * f4B1 * f4B2 * f5p1 * f5p2));

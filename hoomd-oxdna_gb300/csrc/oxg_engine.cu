@@ -1240,7 +1240,7 @@ __global__ void k_hbx_samples(ForceArgs a, int max_n, float* feats, float* energ
         PairIn p;
         bool bad = false;
         if (!load_short_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad)) continue;
-        const Frame fi = quat_frame(__ldcg(a.quat + p.i)), fj = quat_frame(__ldcg(a.quat + p.j));
+        const Frame fi = quat_frame(p.qi), fj = quat_frame(p.qj);
         const DHBCross& px = P.term<DHBCross>(kHBCross, p.pidx);
         BBGeom g;
         if (!bb_geometry(p.rc, fi, fj, px.base, g)) continue;

@@ -245,6 +245,7 @@ struct PairIn {
     float3 rc;  // r_j - r_i
     float rsq;
     float ci, cj;
+    float4 qi, qj;  // orientations (loaded with the positions: one L2 round trip)
 };
 
 __device__ __forceinline__ bool load_short_pair(const ForceArgs& a, int w, int n_types, PairIn& p,
@@ -253,8 +254,12 @@ __device__ __forceinline__ bool load_short_pair(const ForceArgs& a, int w, int n
     const int2 pr = __ldcg(a.pairs_short + w);
     p.i = pr.x;
     p.j = pr.y;
+    // every load of the pair issued at once (one L2 round trip)
     const float4 pi = __ldcg(a.pos + p.i), pj = __ldcg(a.pos + p.j);
-    const float3 dr = min_image(pair_delta(pi, __ldcg(a.pos_lo + p.i), pj, __ldcg(a.pos_lo + p.j)), a.L, a.invL);
+    const float4 li = __ldcg(a.pos_lo + p.i), lj = __ldcg(a.pos_lo + p.j);
+    p.qi = __ldcg(a.quat + p.i);
+    p.qj = __ldcg(a.quat + p.j);
+    const float3 dr = min_image(pair_delta(pi, li, pj, lj), a.L, a.invL);
     p.rc = -dr;
     p.rsq = dot(dr, dr);
     const int ti = type_of(pi), tj = type_of(pj);
@@ -287,7 +292,7 @@ __device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamVie
     PairIn p;
     bool dummy = false;
     if (!load_short_pair(a, w, H.n_types, p, dummy)) return;
-    const Frame fi = quat_frame(__ldcg(a.quat + p.i)), fj = quat_frame(__ldcg(a.quat + p.j));
+    const Frame fi = quat_frame(p.qi), fj = quat_frame(p.qj);
     PairAcc acc;
     acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
     float e = 0.f;
@@ -358,7 +363,7 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
         bool want[kNQ] = {};
         PairIn p;
         if (w < n_short && load_short_pair(a, w, n_types, p, bad_type) && p.rsq < H.rcutsq_max) {
-            const Frame fi = quat_frame(__ldcg(a.quat + p.i)), fj = quat_frame(__ldcg(a.quat + p.j));
+            const Frame fi = quat_frame(p.qi), fj = quat_frame(p.qj);
             PairAcc acc;
             acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
             float e_inline = 0.f;
@@ -435,19 +440,21 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
     for (int w = tid; w < n_long && long_mask; w += nthreads) {
         const int2 pr = __ldcg(a.pairs_long + w);
         const int i = pr.x, j = pr.y;
+        // every load of the pair issued at once (one L2 round trip)
         const float4 pi = __ldcg(a.pos + i), pj = __ldcg(a.pos + j);
+        const float4 li = __ldcg(a.pos_lo + i), lj = __ldcg(a.pos_lo + j);
+        const float4 qi = __ldcg(a.quat + i), qj = __ldcg(a.quat + j);
+        const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
         const int ti = type_of(pi), tj = type_of(pj);
         if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
             bad_type = true;
             continue;
         }
-        const float3 dr = min_image(pair_delta(pi, __ldcg(a.pos_lo + i), pj, __ldcg(a.pos_lo + j)), a.L, a.invL);
+        const float3 dr = min_image(pair_delta(pi, li, pj, lj), a.L, a.invL);
         PairAcc acc;
         acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
         float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
-        if (eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), __ldcg(a.quat + i), __ldcg(a.quat + j), ci,
-                      cj, acc, E)) {
+        if (eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), qi, qj, ci, cj, acc, E)) {
             if (ENERGY) eacc[kDebye] += (double)E[kDebye];
             scatter<ENERGY>(a, i, j, acc, E[kDebye]);
         }
@@ -547,8 +554,8 @@ __device__ __noinline__ void surrogate_segment(const ForceArgs& a, const ParamVi
             bool bad = false;
             valid = load_short_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad);
             if (valid) {
-                fi = quat_frame(__ldcg(a.quat + p.i));
-                fj = quat_frame(__ldcg(a.quat + p.j));
+                fi = quat_frame(p.qi);
+                fj = quat_frame(p.qj);
                 valid = bb_geometry(p.rc, fi, fj, P.term<DHBCross>(kHBCross, p.pidx).base, g);
             }
             if (valid) {
