@@ -73,10 +73,11 @@ OXG_HD float sin_of_acos(float c)
 // src/OxDNANumerics.h:201-215
 OXG_HD float f4_angle(float t, const F4& p)
 {
+    // both non-zero branches computed and selected (no divergence; NaN d gives 0)
     const float d = fabsf(t - p.t0);
-    if (!(d < p.tc)) return 0.f;
-    if (d > p.ts) return p.b * (p.tc - d) * (p.tc - d);
-    return 1.f - p.a * d * d;
+    const float e = p.tc - d;
+    const float smooth = p.b * e * e, core = 1.f - p.a * d * d;
+    return d < p.tc ? (d > p.ts ? smooth : core) : 0.f;
 }
 // (d f4 / d theta) / sin(theta); src/OxDNANumerics.h:218-244, with sin(theta) passed in.
 // Callers compute sin(theta) once per angle and pass sin(pi - theta) = sin(theta) and
@@ -99,16 +100,13 @@ OXG_HD float f4_dsin(float t, float st, const F4& p)
 // The same with 1 / sin(theta) supplied (one reciprocal shared by an angle's branches).
 OXG_HD float f4_dsin_inv(float t, float st, float inv_st, const F4& p)
 {
-    float d = t - p.t0;
-    float m = 1.f;
-    if (d < 0.f) {
-        d = -d;
-        m = -1.f;
-    }
-    if (!(d < p.tc)) return 0.f;
-    if (d > p.ts) return m * 2.f * p.b * (d - p.tc) * inv_st;
-    if (st * st > 1e-8f) return -m * 2.f * p.a * d * inv_st;
-    return -m * 2.f * p.a;
+    // branch-free form of f4_dsin (same selections, same guard)
+    const float x = t - p.t0;
+    const float m = x < 0.f ? -1.f : 1.f;
+    const float d = fabsf(x);
+    const float smooth = m * 2.f * p.b * (d - p.tc) * inv_st;
+    const float core = st * st > 1e-8f ? -m * 2.f * p.a * d * inv_st : -m * 2.f * p.a;
+    return d < p.tc ? (d > p.ts ? smooth : core) : 0.f;
 }
 // cos(theta) in the open support interval of f4 (or, symmetrised, of f4(pi - theta))
 template <bool SYM>

@@ -443,7 +443,7 @@ struct oxg_system {
     uint32_t* cell_count = nullptr;
     int* cell_list = nullptr;
     int2 *pairs_short = nullptr, *pairs_long = nullptr;
-    int* queue = nullptr;  // kNQ deferred-term queues of cap_short entries
+    int2* queue = nullptr;  // kNQ deferred-term queues of cap_short pairs (i, j)
     long long cap_short = 0, cap_long = 0;
     float rlist2 = 0.f, rshort2 = 0.f;
     uint32_t nlist_mask = 0xffffffffu;  // term mask the current sizing was made for
@@ -1239,7 +1239,7 @@ __global__ void k_hbx_samples(ForceArgs a, int max_n, float* feats, float* energ
         const int q = it < n1 ? kQHBX : kQHBX0, k = it < n1 ? it : it - n1;
         PairIn p;
         bool bad = false;
-        if (!load_short_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad)) continue;
+        if (!load_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad)) continue;
         const Frame fi = quat_frame(p.qi), fj = quat_frame(p.qj);
         const DHBCross& px = P.term<DHBCross>(kHBCross, p.pidx);
         BBGeom g;
@@ -1402,7 +1402,7 @@ constexpr size_t kNaOffCellList = na_align(kNaOffCellCount + sizeof(uint32_t) * 
 constexpr size_t kNaOffShort = na_align(kNaOffCellList + sizeof(int) * (size_t)kNaMaxCells * kNaCellCap);
 constexpr size_t kNaOffLong = na_align(kNaOffShort + sizeof(int2) * kNaShortCap);
 constexpr size_t kNaOffQueue = na_align(kNaOffLong + sizeof(int2) * kNaLongCap);
-constexpr size_t kNaBytes = na_align(kNaOffQueue + sizeof(int) * kNQ * kNaShortCap);  // ~12.9 MB
+constexpr size_t kNaBytes = na_align(kNaOffQueue + sizeof(int2) * kNQ * kNaShortCap);  // ~18.1 MB
 
 }  // namespace
 
@@ -1591,7 +1591,7 @@ extern "C" int oxg_pair_forces_noalloc(oxg_context* c, uint32_t mask, int N,
     fa.cap_short = na.cap_short;
     fa.cap_long = na.cap_long;
     fa.advance_step = 0;
-    fa.queue = reinterpret_cast<int*>(scratch + kNaOffQueue);
+    fa.queue = reinterpret_cast<int2*>(scratch + kNaOffQueue);
     fa.L = na.L;
     fa.invL = na.invL;
     fa.force = reinterpret_cast<float4*>(force);

@@ -199,7 +199,7 @@ struct ForceArgs {
     DevStatus* st_rw;     // rebuild flag cleared here
     int cap_short, cap_long;  // list capacities (counts past them were not stored)
     int advance_step;     // MD step: advance the RNG step counter read by step two
-    int* queue;           // kNQ deferred-term queues of cap_short short-pair indices
+    int2* queue;          // kNQ deferred-term queues of cap_short pairs (i, j)
     float3 L, invL;
     float4* force;        // accumulated (pre-zeroed)
     float4* torque;
@@ -248,10 +248,9 @@ struct PairIn {
     float4 qi, qj;  // orientations (loaded with the positions: one L2 round trip)
 };
 
-__device__ __forceinline__ bool load_short_pair(const ForceArgs& a, int w, int n_types, PairIn& p,
-                                                bool& bad_type)
+__device__ __forceinline__ bool load_pair(const ForceArgs& a, int2 pr, int n_types, PairIn& p,
+                                          bool& bad_type)
 {
-    const int2 pr = __ldcg(a.pairs_short + w);
     p.i = pr.x;
     p.j = pr.y;
     // every load of the pair issued at once (one L2 round trip)
@@ -272,6 +271,11 @@ __device__ __forceinline__ bool load_short_pair(const ForceArgs& a, int w, int n
     p.cj = a.charge ? a.charge[p.j] : 1.f;
     return true;
 }
+__device__ __forceinline__ bool load_short_pair(const ForceArgs& a, int w, int n_types, PairIn& p,
+                                                bool& bad_type)
+{
+    return load_pair(a, __ldcg(a.pairs_short + w), n_types, p, bad_type);
+}
 
 template <bool ENERGY>
 __device__ __forceinline__ void scatter(const ForceArgs& a, int i, int j, const PairAcc& acc, float e)
@@ -285,13 +289,13 @@ __device__ __forceinline__ void scatter(const ForceArgs& a, int i, int j, const 
 
 // Full evaluation of one deferred term for short pair w (warp-uniform q).
 template <bool ENERGY>
-__device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamView& P, int q, int w,
+__device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamView& P, int q, int2 pr,
                                               double* eacc)
 {
     const ParamHeader& H = P.h();
     PairIn p;
     bool dummy = false;
-    if (!load_short_pair(a, w, H.n_types, p, dummy)) return;
+    if (!load_pair(a, pr, H.n_types, p, dummy)) return;
     const Frame fi = quat_frame(p.qi), fj = quat_frame(p.qj);
     PairAcc acc;
     acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
@@ -429,7 +433,7 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
                 uint32_t base_q = 0;
                 if (lane == leader) base_q = atomicAdd(&a.st_rw->qcount[q], (uint32_t)__popc(m));
                 base_q = __shfl_sync(0xffffffffu, base_q, leader);
-                if (want[q]) a.queue[(size_t)q * a.cap_short + base_q + __popc(m & lt_mask)] = w;
+                if (want[q]) a.queue[(size_t)q * a.cap_short + base_q + __popc(m & lt_mask)] = make_int2(p.i, p.j);
             }
         }
     }
@@ -552,7 +556,7 @@ __device__ __noinline__ void surrogate_segment(const ForceArgs& a, const ParamVi
         for (int f = 0; f < kMlpIn; ++f) x[f] = 0.f;
         if (valid) {
             bool bad = false;
-            valid = load_short_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad);
+            valid = load_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad);
             if (valid) {
                 fi = quat_frame(p.qi);
                 fj = quat_frame(p.qj);

@@ -369,7 +369,7 @@ int oxg_batch_compute(oxg_batch* b, uint32_t term_mask, int bonded, float* force
  * Same evaluation as the system engine's nonbonded forces (cell list with bond
  * exclusions, split pair lists, the fused force kernel), but every scratch buffer it
  * needs lives in one fixed-size static device array inside this library (about
- * 12.9 MB, held by every GPU that loads the library until the process exits). The
+ * 18.1 MB, held by every GPU that loads the library until the process exits). The
  * call allocates nothing: no cudaMalloc, cudaFree or allocating library routine.
  *
  * Inputs (device): pos_type[4*N] (x, y, z, type as the float's int bits), quat[4*N],
