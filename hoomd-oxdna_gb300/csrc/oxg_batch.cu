@@ -414,7 +414,7 @@ __device__ void tile_forces(const Smem& s, const BatchArgs& a, int nrep, int np,
             const float3 Rcf = rep_delta(s, R, B, A);
             const float4 qA = s.q[A], qB = s.q[B];
             BondAcc acc;
-            bonded_pair(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
+            bonded_pair<false>(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
                         make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
                         __float_as_int(s.x[A].w), __float_as_int(s.x[B].w), acc);
             const float eh = ENERGY ? (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2])) : 0.f;

@@ -733,6 +733,12 @@ OXG_HD float stacking_rna(const DBonded& p, float3 Rc, const Frame& fA,
 // One bond (A, B = A's 5' neighbour): FENE in FP64, bonded excluded volume and
 // stacking in FP32. src/OxDNABondedKernel.h:357-431. Rc = r_B - r_A in double;
 // qA, qB the quaternions (promoted to double for FENE).
+// FULL64: the BACK sites of FENE are rotated in FP64 too (the evaluator-level drop-in,
+// whose Rc is exact in double). The engine's Rc comes from FP32 double-float position
+// differences (~1e-7 absolute), which FP32 rotations of the BACK sites match, so there
+// FULL64 = false rotates in FP32 and keeps FP64 for the FENE scalar arithmetic itself
+// (|r|, r - r0, log(1 - dr^2 / delta^2), the restoring force): a third of the FP64 work.
+template <bool FULL64 = true>
 OXG_HD void bonded_pair(const DBonded& p, double3 Rc, double4_32a qA,
                                             double4_32a qB, int tA, int tB, BondAcc& acc)
 {
@@ -754,8 +760,24 @@ OXG_HD void bonded_pair(const DBonded& p, double3 Rc, double4_32a qA,
         r.z = ss * v[2] + 2.0 * s * (x * v[1] - y * v[0]) + 2.0 * ud * z;
         return r;
     };
-    const double3 bA = rot_d(qA, p.back_site), bB = rot_d(qB, p.back_site);
-    const double rbx = Rc.x + bB.x - bA.x, rby = Rc.y + bB.y - bA.y, rbz = Rc.z + bB.z - bA.z;
+    const Frame fA = quat_frame(make_float4((float)qA.x, (float)qA.y, (float)qA.z, (float)qA.w));
+    const Frame fB = quat_frame(make_float4((float)qB.x, (float)qB.y, (float)qB.z, (float)qB.w));
+    const float3 Rcf = mk3((float)Rc.x, (float)Rc.y, (float)Rc.z);
+    const float3 backA = body_to_lab(fA, p.back), backB = body_to_lab(fB, p.back);
+    double3 bA, bB;
+    double rbx, rby, rbz;
+    if (FULL64) {
+        bA = rot_d(qA, p.back_site);
+        bB = rot_d(qB, p.back_site);
+        rbx = Rc.x + bB.x - bA.x;
+        rby = Rc.y + bB.y - bA.y;
+        rbz = Rc.z + bB.z - bA.z;
+    } else {
+        const float3 rb = Rcf + backB - backA;
+        rbx = rb.x;
+        rby = rb.y;
+        rbz = rb.z;
+    }
     const double rmod = sqrt(rbx * rbx + rby * rby + rbz * rbz);
     const double dr = rmod - p.r0_backbone;
     if (fabs(dr) >= p.delta_backbone) {
@@ -764,22 +786,23 @@ OXG_HD void bonded_pair(const DBonded& p, double3 Rc, double4_32a qA,
         acc.e[0] = -0.5 * p.eps_backbone * log(1.0 - dr * dr / p.delta2);
         const double pref = -(p.eps_backbone * dr / (p.delta2 - dr * dr)) / rmod;
         const double fx = pref * rbx, fy = pref * rby, fz = pref * rbz;
-        // torques: backA x (-f), backB x f
-        const double tAx = -(bA.y * fz - bA.z * fy), tAy = -(bA.z * fx - bA.x * fz),
-                     tAz = -(bA.x * fy - bA.y * fx);
-        const double tBx = bB.y * fz - bB.z * fy, tBy = bB.z * fx - bB.x * fz,
-                     tBz = bB.x * fy - bB.y * fx;
         acc.fB = mk3((float)fx, (float)fy, (float)fz);
-        acc.tA = mk3((float)tAx, (float)tAy, (float)tAz);
-        acc.tB = mk3((float)tBx, (float)tBy, (float)tBz);
+        if (FULL64) {
+            // torques: backA x (-f), backB x f
+            const double tAx = -(bA.y * fz - bA.z * fy), tAy = -(bA.z * fx - bA.x * fz),
+                         tAz = -(bA.x * fy - bA.y * fx);
+            const double tBx = bB.y * fz - bB.z * fy, tBy = bB.z * fx - bB.x * fz,
+                         tBz = bB.x * fy - bB.y * fx;
+            acc.tA = mk3((float)tAx, (float)tAy, (float)tAz);
+            acc.tB = mk3((float)tBx, (float)tBy, (float)tBz);
+        } else {
+            acc.tA = cross(backA, -acc.fB);
+            acc.tB = cross(backB, acc.fB);
+        }
         vir_acc(acc.vir, mk3((float)rbx, (float)rby, (float)rbz), acc.fB);
     }
 
     // --- bonded excluded volume + stacking, FP32 ---
-    const Frame fA = quat_frame(make_float4((float)qA.x, (float)qA.y, (float)qA.z, (float)qA.w));
-    const Frame fB = quat_frame(make_float4((float)qB.x, (float)qB.y, (float)qB.z, (float)qB.w));
-    const float3 Rcf = mk3((float)Rc.x, (float)Rc.y, (float)Rc.z);
-    const float3 backA = body_to_lab(fA, p.back), backB = body_to_lab(fB, p.back);
     const float3 baseA = body_to_lab(fA, p.base), baseB = body_to_lab(fB, p.base);
     float eb = 0.f;
 #pragma unroll

@@ -438,10 +438,17 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
         }
     }
 
-    // long-range pairs: Debye only (uniform, cheap)
+    // long-range pairs: Debye only (uniform, cheap), in units of 32. When the short units
+    // leave warps free (small systems), the long units go to those warps only (a short
+    // unit costs about as much as three or four long ones); otherwise round-robin.
     const uint32_t long_mask = mask & (1u << kDebye);
-    const int tid = gwarp * 32 + lane, nthreads = nwarps * 32;
-    for (int w = tid; w < n_long && long_mask; w += nthreads) {
+    const int n_su = (n_short + 31) >> 5, n_lu = (n_long + 31) >> 5;
+    const int free_w = nwarps - n_su;
+    const bool to_free = free_w > 0 && 4 * free_w >= n_lu;
+    const int v0 = to_free ? gwarp - n_su : gwarp, vstride = to_free ? free_w : nwarps;
+    for (int v = v0; v >= 0 && v < n_lu && long_mask; v += vstride) {
+        const int w = v * 32 + lane;
+        if (w >= n_long) continue;
         const int2 pr = __ldcg(a.pairs_long + w);
         const int i = pr.x, j = pr.y;
         // every load of the pair issued at once (one L2 round trip)
@@ -629,7 +636,7 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
         const float3 Rcf = min_image(pair_delta(pB, __ldcg(a.pos_lo + B), pA, __ldcg(a.pos_lo + A)), a.L, a.invL);
         const float4 qA = __ldcg(a.quat + A), qB = __ldcg(a.quat + B);
         BondAcc acc;
-        bonded_pair(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
+        bonded_pair<false>(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
                     make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
                     type_of(pA), type_of(pB), acc);
         float eh = 0.f;

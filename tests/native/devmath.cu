@@ -70,14 +70,18 @@ extern "C" int devmath_pair(int term, const void* pod, double rcut, const double
     return in ? 1 : 0;
 }
 
+// full64 = 1: the drop-in's all-FP64 FENE; 0: the engine's (FP32 BACK-site rotations).
 extern "C" void devmath_bonded(const oxg_bonded_params* p, const double* Rc, const double* qA,
                                const double* qB, int tA, int tB, double* FB, double* tauA,
-                               double* tauB, double* e, double* vir)
+                               double* tauB, double* e, double* vir, int full64)
 {
     const DBonded D = to_dev(*p);
     BondAcc acc;
-    bonded_pair(D, make_double3(Rc[0], Rc[1], Rc[2]), make_double4_32a(qA[0], qA[1], qA[2], qA[3]),
-                make_double4_32a(qB[0], qB[1], qB[2], qB[3]), tA, tB, acc);
+    const double3 R = make_double3(Rc[0], Rc[1], Rc[2]);
+    const double4_32a a4 = make_double4_32a(qA[0], qA[1], qA[2], qA[3]);
+    const double4_32a b4 = make_double4_32a(qB[0], qB[1], qB[2], qB[3]);
+    if (full64) bonded_pair<true>(D, R, a4, b4, tA, tB, acc);
+    else bonded_pair<false>(D, R, a4, b4, tA, tB, acc);
     FB[0] = acc.fB.x; FB[1] = acc.fB.y; FB[2] = acc.fB.z;
     tauA[0] = acc.tA.x; tauA[1] = acc.tA.y; tauA[2] = acc.tA.z;
     tauB[0] = acc.tB.x; tauB[1] = acc.tB.y; tauB[2] = acc.tB.z;

@@ -34,7 +34,7 @@ def devmath():
     L.devmath_pair.argtypes = [C.c_int, C.c_void_p, C.c_double, dp, dp, dp, C.c_double,
                                C.c_double, dp, dp, dp, dp]
     L.devmath_pair.restype = C.c_int
-    L.devmath_bonded.argtypes = [C.c_void_p, dp, dp, dp, C.c_int, C.c_int, dp, dp, dp, dp, dp]
+    L.devmath_bonded.argtypes = [C.c_void_p, dp, dp, dp, C.c_int, C.c_int, dp, dp, dp, dp, dp, C.c_int]
     L.devmath_mlp_map.argtypes = [dp] * 9
     L.devmath_mlp_map.restype = C.c_int
     return L
@@ -73,7 +73,8 @@ def test_fp32_pair_math(devmath, model, term):
 
 @pytest.mark.parametrize("model", ("dna1", "dna2", "rna2"))
 @pytest.mark.parametrize("avg", ("avg", "seq"))
-def test_fp32_bonded_math(devmath, model, avg):
+@pytest.mark.parametrize("full64", (1, 0))
+def test_fp32_bonded_math(devmath, model, avg, full64):
     from oxdna import _abi
     d = golden(f"bonds_{model}.npz")
     _, bonded = model_forces(model, average=(avg == "avg"))
@@ -85,7 +86,7 @@ def test_fp32_bonded_math(devmath, model, avg):
         devmath.devmath_bonded(C.byref(pod), _p(d[f"{avg}/Rc"][k]), _p(d[f"{avg}/qA"][k]),
                                _p(d[f"{avg}/qB"][k]), int(d[f"{avg}/types"][k][0]),
                                int(d[f"{avg}/types"][k][1]), *(x.ctypes.data_as(C.POINTER(C.c_double))
-                                                               for x in (FB, tA, tB, e, v)))
+                                                               for x in (FB, tA, tB, e, v)), full64)
         for key, val in zip(out, (FB, tA, tB, e)):
             out[key].append(val)
     ok = d[f"{avg}/ref64/energy"][:, 0] < 1e12
