@@ -1078,10 +1078,11 @@ __device__ __forceinline__ float4 perm(int k, float4 a)
     if (k == 2) return make_float4(-a.z, -a.w, a.x, a.y);
     return make_float4(-a.w, a.z, -a.y, a.x);
 }
-__device__ __forceinline__ void free_rotor(int k, float h, float I, float4& p, float4& q)
+// q4I = 1 / (4 I) of the axis (a multiplication on the dependency chain, not a division)
+__device__ __forceinline__ void free_rotor(int k, float h, float q4I, float4& p, float4& q)
 {
     const float4 pq = perm(k, q);
-    const float phi = (p.x * pq.x + p.y * pq.y + p.z * pq.z + p.w * pq.w) / (4.f * I);
+    const float phi = (p.x * pq.x + p.y * pq.y + p.z * pq.z + p.w * pq.w) * q4I;
     float s, c;
     sincosf(h * phi, &s, &c);
     const float4 pp = perm(k, p);
@@ -1127,11 +1128,12 @@ __device__ __forceinline__ bool step_one_pure(PState& s, float4 ac, float4 tn, f
     p.y += dt * dq.y;
     p.z += dt * dq.z;
     p.w += dt * dq.w;
-    free_rotor(3, 0.5f * dt, inertia.z, p, q);
-    free_rotor(2, 0.5f * dt, inertia.y, p, q);
-    free_rotor(1, dt, inertia.x, p, q);
-    free_rotor(2, 0.5f * dt, inertia.y, p, q);
-    free_rotor(3, 0.5f * dt, inertia.z, p, q);
+    const float q4x = 0.25f / inertia.x, q4y = 0.25f / inertia.y, q4z = 0.25f / inertia.z;
+    free_rotor(3, 0.5f * dt, q4z, p, q);
+    free_rotor(2, 0.5f * dt, q4y, p, q);
+    free_rotor(1, dt, q4x, p, q);
+    free_rotor(2, 0.5f * dt, q4y, p, q);
+    free_rotor(3, 0.5f * dt, q4z, p, q);
     const float nq = rsqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
     s.q = make_float4(q.x * nq, q.y * nq, q.z * nq, q.w * nq);
     s.p = p;
@@ -1173,11 +1175,11 @@ __device__ __forceinline__ void step_two_pure(PState& s, float4 F, float4 T, uin
     const float u4 = (float)r1[3] * 2.3283064365386963e-10f;
     const float ra = sqrtf(-2.f * logf(fminf(u1, 1.f))), rb = sqrtf(-2.f * logf(fminf(u3, 1.f)));
     float s2a, c2a, s2b, c2b;
-    sincosf(2.f * kPi * u2, &s2a, &c2a);
-    sincosf(2.f * kPi * u4, &s2b, &c2b);
-    const float3 bt = mk3(ra * c2a * cr - gamma_r * sx / inertia.x,
-                          ra * s2a * cr - gamma_r * sy / inertia.y,
-                          rb * c2b * cr - gamma_r * sz / inertia.z);
+    sincospif(2.f * u2, &s2a, &c2a);
+    sincospif(2.f * u4, &s2b, &c2b);
+    const float3 bt = mk3(ra * c2a * cr - gamma_r * sx * (1.f / inertia.x),
+                          ra * s2a * cr - gamma_r * sy * (1.f / inertia.y),
+                          rb * c2b * cr - gamma_r * sz * (1.f / inertia.z));
     const Frame fq = quat_frame(q);
     const float3 btl = fq.a1 * bt.x + fq.a2 * bt.y + fq.a3 * bt.z;
     tn = make_float4(T.x + btl.x, T.y + btl.y, T.z + btl.z, 0.f);
