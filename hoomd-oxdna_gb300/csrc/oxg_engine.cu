@@ -1052,24 +1052,35 @@ static int launch_run(oxg_system* s, int bodies, bool closing)
     return OXG_OK;
 }
 
-// Bodies of a run on the persistent kernel, in launches of up to `chunk` bodies, each
-// from a checkpoint it is replayed from (with a forced rebuild into grown lists) when
-// a neighbour-list capacity overflowed.
-static int run_persistent(oxg_system* s, long bodies)
+// A run of n steps on the persistent kernel, in launches of up to `chunk` step bodies.
+// The first launch is preceded by prepRun (fresh neighbour list, forces, a = F/m, as
+// HOOMD computes the net force at the start of every run() call) and the first step
+// one. Every launch starts from a checkpoint of the state and is followed by the one
+// host synchronisation of the chunk (the status read); after a neighbour-list overflow
+// the lists grow and the chunk (with its prepRun, for the first) is replayed.
+static int run_persistent(oxg_system* s, long nsteps)
 {
     const int chunk = 2000;
     long done = 0;
     int retries = 0, rc;
     DevStatus d;
-    while (done < bodies) {
-        const int todo = (int)std::min<long>(chunk, bodies - done);
-        const bool closing = done + todo == bodies;
+    if (!s->ev_run[0]) {
+        OXG_CUDA(cudaEventCreate(&s->ev_run[0]));
+        OXG_CUDA(cudaEventCreate(&s->ev_run[1]));
+    }
+    while (done < nsteps) {
+        const int todo = (int)std::min<long>(chunk, nsteps - done);
+        const bool closing = done + todo == nsteps;
+        const unsigned long long step0 = s->timestep + (unsigned long long)done;
         if ((rc = checkpoint(s, false))) return rc;
-        DevStatus before;
-        if ((rc = read_status(s, &before))) return rc;
-        if (!s->ev_run[0]) {
-            OXG_CUDA(cudaEventCreate(&s->ev_run[0]));
-            OXG_CUDA(cudaEventCreate(&s->ev_run[1]));
+        if (done == 0) {
+            k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0);
+            OXG_CUDA(cudaMemsetAsync(s->force, 0, sizeof(float4) * s->N, s->stream));
+            OXG_CUDA(cudaMemsetAsync(s->torque, 0, sizeof(float4) * s->N, s->stream));
+            if ((rc = launch_nlist_forces(s, s->run_mask, s->run_bonded, false))) return rc;
+            const IntegArgs ia = integ_args(s);
+            k_prep_accel<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
+            if ((rc = enqueue_step_one(s))) return rc;
         }
         OXG_CUDA(cudaEventRecord(s->ev_run[0], s->stream));
         if ((rc = launch_run(s, todo, closing))) return rc;
@@ -1088,10 +1099,8 @@ static int run_persistent(oxg_system* s, long bodies)
             bool grew = false;
             if ((rc = grow_for(s, d, &grew))) return rc;
             if ((rc = checkpoint(s, true))) return rc;
-            OXG_CUDA(cudaMemcpyAsync(&s->st->step, &before.step, sizeof(unsigned long long),
-                                     cudaMemcpyHostToDevice, s->stream));
-            OXG_CUDA(cudaMemsetAsync(s->st->qcount, 0, sizeof(s->st->qcount), s->stream));
-            if ((rc = clear_flags(s)) || (rc = set_rebuild(s))) return rc;
+            k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0);  // step, flags, rebuild, queues
+            OXG_CUDA(cudaGetLastError());
             continue;
         }
         done += todo;
@@ -1132,6 +1141,11 @@ int oxg_system_run(oxg_system* s, long nsteps)
         if (!s->ctx->bonded_set[t]) return set_err(OXG_ERR_NO_PARAMS, "bond type without parameters");
     int rc = sys_setup_nlist(s, s->run_mask, false);
     if (rc) return rc;
+    if (s->persistent && nsteps > 0) {
+        if ((rc = run_persistent(s, nsteps))) return rc;
+        OXG_CUDA(cudaStreamSynchronize(s->stream));
+        return OXG_OK;
+    }
     // the RNG counter continues from the system's timestep
     OXG_CUDA(cudaMemcpyAsync(&s->st->step, &s->timestep, sizeof(unsigned long long),
                              cudaMemcpyHostToDevice, s->stream));
@@ -1141,11 +1155,6 @@ int oxg_system_run(oxg_system* s, long nsteps)
         return OXG_OK;
     }
     if ((rc = enqueue_step_one(s))) return rc;
-    if (s->persistent) {
-        if ((rc = run_persistent(s, nsteps))) return rc;
-        OXG_CUDA(cudaStreamSynchronize(s->stream));
-        return OXG_OK;
-    }
     // nsteps - 1 fused bodies in graph chunks, then the closing body with step two.
     // Chunk boundaries sit after a step one; on a list overflow the chunk is replayed
     // from its checkpoint with a forced neighbour-list rebuild.

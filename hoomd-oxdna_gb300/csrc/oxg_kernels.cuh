@@ -1281,6 +1281,18 @@ __global__ void k_step_two_one(IntegArgs a)
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&a.st->flags, kStNonFinite);
 }
 
+// Start (or replay) of a run on the device: the RNG step counter, cleared flags, a
+// forced neighbour-list rebuild and empty queues (no host-to-device copies needed).
+__global__ void k_begin_run(DevStatus* st, unsigned long long step)
+{
+    if (threadIdx.x == 0) {
+        st->step = step;
+        st->flags = 0u;
+        st->rebuild = 1u;
+    }
+    if (threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
+}
+
 // prepRun: accelerations from the forces alone (no bath), as HOOMD does at run start.
 __global__ void k_prep_accel(IntegArgs a)
 {
