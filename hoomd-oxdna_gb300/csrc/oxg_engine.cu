@@ -469,6 +469,7 @@ struct oxg_system {
     // persistent run kernel
     GridBarrier* bar = nullptr;
     int grid_run = 0, grid_run_surr = 0;
+    bool lists_valid = false;  // pair lists built for the current positions' reference
     cudaEvent_t ev_run[2] = {nullptr, nullptr};  // around each run-kernel launch
     double run_kernel_ms = 0.0;
     long long run_kernel_launches = 0, run_kernel_bodies = 0;
@@ -487,6 +488,7 @@ namespace {
 
 int sys_alloc_nlist(oxg_system* s)
 {
+    s->lists_valid = false;  // the next run must build them
     dfree(s->cell_count);
     dfree(s->cell_list);
     dfree(s->pairs_short);
@@ -1074,7 +1076,13 @@ static int run_persistent(oxg_system* s, long nsteps)
         const unsigned long long step0 = s->timestep + (unsigned long long)done;
         if ((rc = checkpoint(s, false))) return rc;
         if (done == 0) {
-            k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0);
+            // a rebuild only if the lists are new or a particle moved half the buffer since
+            // they were built (e.g. a state pushed from the host)
+            k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0, s->lists_valid ? 0u : 1u);
+            if (s->lists_valid) {
+                const IntegArgs ia = integ_args(s);
+                k_check_moved<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
+            }
             OXG_CUDA(cudaMemsetAsync(s->force, 0, sizeof(float4) * s->N, s->stream));
             OXG_CUDA(cudaMemsetAsync(s->torque, 0, sizeof(float4) * s->N, s->stream));
             if ((rc = launch_nlist_forces(s, s->run_mask, s->run_bonded, false))) return rc;
@@ -1099,12 +1107,13 @@ static int run_persistent(oxg_system* s, long nsteps)
             bool grew = false;
             if ((rc = grow_for(s, d, &grew))) return rc;
             if ((rc = checkpoint(s, true))) return rc;
-            k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0);  // step, flags, rebuild, queues
+            k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0, 1u);  // step, flags, rebuild, queues
             OXG_CUDA(cudaGetLastError());
             continue;
         }
         done += todo;
         s->steps_run += todo;
+        s->lists_valid = true;
     }
     s->timestep = d.step;
     return OXG_OK;

@@ -1283,14 +1283,28 @@ __global__ void k_step_two_one(IntegArgs a)
 
 // Start (or replay) of a run on the device: the RNG step counter, cleared flags, a
 // forced neighbour-list rebuild and empty queues (no host-to-device copies needed).
-__global__ void k_begin_run(DevStatus* st, unsigned long long step)
+__global__ void k_begin_run(DevStatus* st, unsigned long long step, uint32_t rebuild)
 {
     if (threadIdx.x == 0) {
         st->step = step;
         st->flags = 0u;
-        st->rebuild = 1u;
+        st->rebuild = rebuild;
     }
     if (threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
+}
+
+// Flags a neighbour-list rebuild if a particle is more than half the buffer away from
+// its position at the last build.
+__global__ void k_check_moved(IntegArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool far = false;
+    if (i < a.N) {
+        const float4 x = a.pos[i], r = a.pos_ref[i];
+        const float3 d = min_image(mk3(x.x - r.x, x.y - r.y, x.z - r.z), a.L, a.invL);
+        far = !(dot(d, d) <= a.half_buf2);
+    }
+    if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&a.st->rebuild, 1u);
 }
 
 // prepRun: accelerations from the forces alone (no bath), as HOOMD does at run start.
