@@ -278,6 +278,36 @@ def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epoc
     return out
 
 
+FLOP_COUNTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                           "flop_counts.json")
+
+
+def compute_roofline(ms_per_step, stream, workload="8000nt"):
+    """The MD step against the pipes that bound it: the reference's FP32 operation count
+    per step (flop census of its own evaluator and bonded arithmetic at the workload's
+    initial snapshot) over the run kernel's event-timed step time, against the FP32 FMA
+    and special-function throughput measured on this device by the library's
+    microbenchmarks (oxg_device_peaks)."""
+    from oxdna import runtime
+    with open(FLOP_COUNTS) as fh:
+        census = json.load(fh)["workloads"][workload]
+    fp32_gflops, sfu_gops = runtime.device_peaks(stream.cuda_stream)
+    t = ms_per_step * 1e-3
+    flops = census["flops_per_step"]
+    special = sum(census["special_per_step"].values())
+    achieved = flops / t / 1e12
+    sfu = special / t / 1e9
+    return {"bound": "fp32", "achieved": achieved, "peak": fp32_gflops / 1e3, "unit": "TFLOP/s",
+            "frac": achieved / (fp32_gflops / 1e3), "peak_kind": "measured (oxg_device_peaks FMA "
+            "microbenchmark on this device)", "flops_per_step": flops,
+            "special": {"achieved": sfu, "peak": sfu_gops, "unit": "Gop/s", "frac": sfu / sfu_gops,
+                        "ops_per_step": special, "per_step": census["special_per_step"],
+                        "note": "each div / sqrt / exp / acos / sin call counted as one "
+                                "special-function op (acos and div also cost FMA-pipe work)"},
+            "source": "tests/golden/flop_counts.json (reference headers compiled with an "
+                      "operation-counting ForceReal; flops = add + mul, FMA = 2)"}
+
+
 def cpu_baseline(sysarr, seconds=12.0, max_steps=400, threads=None):
     """The oracle port (FP64 C, OpenMP) running Langevin steps on the host cores."""
     from oracle import oracle as O
@@ -374,6 +404,7 @@ def run_ours(args):
     steps_per_launch = k_steps / max(k_launches, 1)
     hbm, peak_kind = _peaks()
     achieved = alg_bytes_step * steps_per_launch / (kernel_ms * 1e-3) / 1e9
+    compute = compute_roofline(kernel_ms / steps_per_launch, stream)
 
     # --- fused=True variant (HBondCross) ---------------------------------------
     sim_f, _ = make_sim(sysarr, fused=True, seed=1 + rank, stream=stream.cuda_stream)
@@ -460,6 +491,7 @@ def run_ours(args):
                      "alg_bytes_per_step": alg_bytes_step,
                      "note": "latency-bound, not HBM-bound: the 8000-nt working set (~5 MB) "
                              "is L2-resident"},
+        "roofline_compute": compute,
         "cpu_baseline": cb, "e2e": e2e,
         "gpu_launches": blocks * 9,
         "clocks": clk.summary(),

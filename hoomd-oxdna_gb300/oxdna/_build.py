@@ -1,8 +1,8 @@
 """Build recipe of the native library ``liboxdna_gb300.so`` (sm_103a only).
 
-The CUDA sources under ``csrc/`` form one translation unit (the kernels are headers
-included by the engine) compiled by nvcc straight into a shared library next to
-this package, so the library that gets loaded is the in-tree one.
+The CUDA sources under ``csrc/`` (kernels are headers included by the engine and
+batch units) are compiled unit by unit in parallel and linked by nvcc into a shared
+library next to this package, so the library that gets loaded is the in-tree one.
 """
 
 import os
@@ -37,18 +37,41 @@ def stale():
 
 
 def build(force=False, verbose=False):
-    """Compile the library if any source is newer than it. Returns the path."""
+    """Compile the library if any source is newer than it. Returns the path.
+
+    Each .cu unit is compiled to an object by its own nvcc process (in parallel), then
+    the objects are linked into the shared library."""
     if not force and not stale():
         return LIB
     units = [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith(".cu")]
-    tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc(), *NVCC_FLAGS, "-o", tmp, *units]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
-    if verbose:
-        print(r.stdout + r.stderr)
-    os.replace(tmp, LIB)
+    tag = ".tmp%d" % os.getpid()
+    objdir = os.path.join(PKG, "_obj")
+    os.makedirs(objdir, exist_ok=True)
+    objs = [os.path.join(objdir, os.path.basename(u)[:-3] + tag + ".o") for u in units]
+    compile_flags = [f for f in NVCC_FLAGS if f != "-shared"]
+    procs = [(subprocess.Popen([nvcc(), *compile_flags, "-c", "-o", o, u], stdout=subprocess.PIPE,
+                               stderr=subprocess.STDOUT, text=True), u) for u, o in zip(units, objs)]
+    logs, failed = [], []
+    for p, u in procs:
+        out, _ = p.communicate()
+        logs.append(out)
+        if p.returncode != 0:
+            failed.append((u, out))
+    try:
+        if failed:
+            raise RuntimeError("nvcc failed:\n" + "\n".join(f"{u}:\n{out}" for u, out in failed))
+        tmp = LIB + tag
+        cmd = [nvcc(), ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", tmp, *objs]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc link failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+        if verbose:
+            print("".join(logs) + r.stdout + r.stderr)
+        os.replace(tmp, LIB)
+    finally:
+        for o in objs:
+            if os.path.exists(o):
+                os.remove(o)
     return LIB
 
 

@@ -477,3 +477,11 @@ class Simulation:
         out = (C.c_int64 * 5)()
         _abi.check(L.oxg_system_stats(self._sys, out, 5), "oxg_system_stats")
         return dict(steps=out[0], nlist_builds=out[1], pairs_short=out[2], pairs_long=out[3])
+
+
+def device_peaks(stream=None):
+    """(FP32 GFLOP/s, special-function Gop/s) of the current device, measured by the
+    library's microbenchmark kernels (oxg_device_peaks)."""
+    out = (C.c_double * 2)()
+    _abi.check(_abi.lib().oxg_device_peaks(out, 2, C.c_void_p(stream or 0)), "oxg_device_peaks")
+    return out[0], out[1]

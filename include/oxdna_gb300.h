@@ -396,6 +396,13 @@ int oxg_pair_forces_noalloc(oxg_context* ctx, uint32_t term_mask, int N,
                             const float box[3], int n_bonds, const int32_t* bonds,
                             float* force, float* torque, double* term_energy, void* stream);
 
+/* Measured throughput of the current device's FP32 FMA pipe (out[0], GFLOP/s, an FMA
+ * counted as two flops) and special-function unit (out[1], reciprocal square roots in
+ * Gop/s): the denominators of the MD step's compute roofline. Runs two short
+ * microbenchmark kernels (a few ms each) on `stream` and synchronises. n: entries of
+ * `out` to fill (1 or 2). No counterpart in the reference: measurement support. */
+int oxg_device_peaks(double* out, int n, void* stream);
+
 /* Text of the last error raised on the calling thread (CUDA error string etc.). */
 const char* oxg_last_error(void);
 /* Version / build string of the loaded library. */

@@ -7,7 +7,8 @@
   ``/root/reference/src``) together with the clean-room HOOMD stand-ins in
   ``oracle/ref_shim`` into ``oracle/_ref/libref64.so`` (ForceReal = double) and
   ``oracle/_ref/libref32.so`` (ForceReal = float, the reference's mixed-precision
-  GPU arithmetic emulated on the host). Nothing is written outside ``oracle/_ref``;
+  GPU arithmetic emulated on the host) and ``oracle/_ref/librefcount.so`` (ForceReal
+  counts its operations: the flop census). Nothing is written outside ``oracle/_ref``;
   the reference sources are only read. Skipped when the reference tree is absent.
 """
 
@@ -65,9 +66,10 @@ def build_ref(force=False):
     src = os.path.join(HERE, "ref_wrap.cpp")
     shim = os.path.join(HERE, "ref_shim")
     deps = [src, os.path.join(shim, "hoomd", "HOOMDMath.h"),
-            os.path.join(shim, "hoomd", "VectorMath.h")]
+            os.path.join(shim, "hoomd", "VectorMath.h"), os.path.join(shim, "oxref_count.h")]
     out = []
-    for tag, defs in (("64", []), ("32", ["-DHOOMD_HAS_FORCEREAL"])):
+    for tag, defs in (("64", []), ("32", ["-DHOOMD_HAS_FORCEREAL"]),
+                      ("count", ["-DHOOMD_HAS_FORCEREAL", "-DOXREF_COUNTING"])):
         so = os.path.join(REF_DIR, "libref%s.so" % tag)
         if force or _stale(so, deps):
             tmp = so + ".tmp%d" % os.getpid()

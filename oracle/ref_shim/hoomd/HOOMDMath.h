@@ -4,14 +4,18 @@
  * oracle pin (HOOMD-blue itself is not available). Only what those headers use:
  * Scalar (double), Scalar2/3/4, make_scalar3/4, __scalar_as_int / __int_as_scalar.
  * With HOOMD_HAS_FORCEREAL defined, ForceReal is float (the mixed-precision build
- * the reference ships its GPU numbers with); otherwise MixedPrecisionCompat.h
- * aliases ForceReal to Scalar.
+ * the reference ships its GPU numbers with), or with OXREF_COUNTING also defined the
+ * operation-counting real of oxref_count.h; otherwise MixedPrecisionCompat.h aliases
+ * ForceReal to Scalar.
  */
 #ifndef OXREF_SHIM_HOOMDMATH_H
 #define OXREF_SHIM_HOOMDMATH_H
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
+#ifdef OXREF_COUNTING
+#include "../oxref_count.h"
+#endif
 
 namespace hoomd
 {
@@ -46,17 +50,21 @@ inline Scalar __int_as_scalar(int a)
     return r;
 }
 #ifdef HOOMD_HAS_FORCEREAL
+#ifdef OXREF_COUNTING
+typedef oxref::Counted ForceReal;  /* the flop census: every ForceReal operation counted */
+#else
 typedef float ForceReal;
-struct ForceReal2 { float x, y; };
-struct ForceReal3 { float x, y, z; };
-struct ForceReal4 { float x, y, z, w; };
-inline ForceReal3 make_forcereal3(float x, float y, float z)
+#endif
+struct ForceReal2 { ForceReal x, y; };
+struct ForceReal3 { ForceReal x, y, z; };
+struct ForceReal4 { ForceReal x, y, z, w; };
+inline ForceReal3 make_forcereal3(ForceReal x, ForceReal y, ForceReal z)
 {
     ForceReal3 r;
     r.x = x; r.y = y; r.z = z;
     return r;
 }
-inline ForceReal4 make_forcereal4(float x, float y, float z, float w)
+inline ForceReal4 make_forcereal4(ForceReal x, ForceReal y, ForceReal z, ForceReal w)
 {
     ForceReal4 r;
     r.x = x; r.y = y; r.z = z; r.w = w;

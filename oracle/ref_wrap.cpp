@@ -4,10 +4,11 @@
  * oracle/_ref/ (never committed). TEST INFRASTRUCTURE ONLY: it pins the C oracle
  * (oracle/oxdna_oracle.c) and generates the golden fixtures in tests/golden/.
  *
- * Built twice: FP64 (HOOMD_HAS_FORCEREAL undefined, ForceReal == Scalar == double:
- * the reference's upstream-HOOMD arithmetic) and FP32 (HOOMD_HAS_FORCEREAL defined,
+ * Built three times: FP64 (HOOMD_HAS_FORCEREAL undefined, ForceReal == Scalar == double:
+ * the reference's upstream-HOOMD arithmetic), FP32 (HOOMD_HAS_FORCEREAL defined,
  * ForceReal == float: the reference's mixed-precision GPU arithmetic emulated on the
- * host, src/MixedPrecisionCompat.h:20-35).
+ * host, src/MixedPrecisionCompat.h:20-35) and the flop census (OXREF_COUNTING:
+ * ForceReal counts its operations, ref_shim/oxref_count.h).
  *
  * Each ref_* function converts this project's POD parameter structs into the
  * reference param_type (same fields) and calls evaluate() / oxdna_bonded_pair().
@@ -259,6 +260,22 @@ int run_eval(const P& p, const double dr[3], const double qi[4], const double qj
 extern "C" {
 
 int ref_is_fp32(void) { return sizeof(ForceReal) == 4; }
+
+#ifdef OXREF_COUNTING
+// flop census: the operation tallies since the last reset, in the order of oxref_count.h
+// (add, mul, div, sqrt, exp, log, acos, sin, cos)
+int ref_count_n(void) { return oxref::kNCount; }
+void ref_count_get(unsigned long long* out)
+{
+    for (int k = 0; k < oxref::kNCount; ++k)
+        out[k] = oxref::op_counts()[k];
+}
+void ref_count_reset(void)
+{
+    for (int k = 0; k < oxref::kNCount; ++k)
+        oxref::op_counts()[k] = 0;
+}
+#endif
 
 int ref_excvol(const oxg_excvol_params* p, const double dr[3], const double qi[4],
                const double qj[4], double rcutsq, double f[3], double* e, double ti[3],
