@@ -738,7 +738,9 @@ OXG_HD float stacking_rna(const DBonded& p, float3 Rc, const Frame& fA,
 // differences (~1e-7 absolute), which FP32 rotations of the BACK sites match, so there
 // FULL64 = false rotates in FP32 and keeps FP64 for the FENE scalar arithmetic itself
 // (|r|, r - r0, log(1 - dr^2 / delta^2), the restoring force): a third of the FP64 work.
-template <bool FULL64 = true>
+// PART: 0 the whole bond; 1 FENE + bonded excluded volume; 2 stacking alone (two lanes
+// evaluating parts 1 and 2 of a bond sum to part 0).
+template <bool FULL64 = true, int PART = 0>
 OXG_HD void bonded_pair(const DBonded& p, double3 Rc, double4_32a qA,
                                             double4_32a qB, int tA, int tB, BondAcc& acc)
 {
@@ -763,6 +765,12 @@ OXG_HD void bonded_pair(const DBonded& p, double3 Rc, double4_32a qA,
     const Frame fA = quat_frame(make_float4((float)qA.x, (float)qA.y, (float)qA.z, (float)qA.w));
     const Frame fB = quat_frame(make_float4((float)qB.x, (float)qB.y, (float)qB.z, (float)qB.w));
     const float3 Rcf = mk3((float)Rc.x, (float)Rc.y, (float)Rc.z);
+    if (PART == 2) {
+        if (p.stacking_enabled)
+            acc.e[2] = p.rna_stacking ? stacking_rna(p, Rcf, fA, fB, tA, tB, acc)
+                                      : stacking_dna(p, Rcf, fA, fB, tA, tB, acc);
+        return;
+    }
     const float3 backA = body_to_lab(fA, p.back), backB = body_to_lab(fB, p.back);
     double3 bA, bB;
     double rbx, rby, rbz;
@@ -819,7 +827,7 @@ OXG_HD void bonded_pair(const DBonded& p, double3 Rc, double4_32a qA,
         vir_acc(acc.vir, r, f);
     }
     acc.e[1] = eb;
-    if (p.stacking_enabled) {
+    if (PART == 0 && p.stacking_enabled) {
         acc.e[2] = p.rna_stacking ? stacking_rna(p, Rcf, fA, fB, tA, tB, acc)
                                   : stacking_dna(p, Rcf, fA, fB, tA, tB, acc);
     }

@@ -780,6 +780,7 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
         (rc = dalloc(&s->ck_angmom, N)) || (rc = dalloc(&s->bar, 1)) || (rc = dalloc(&s->audit, 1)))
         return fail(rc);
     cudaMemset(s->audit, 0, sizeof(SurrogateAudit));
+    cudaMemset(s->bar, 0, sizeof(GridBarrier));
     if (const char* m = std::getenv("OXG_RUN_MODE")) s->persistent = std::string(m) != "graph";
     if (cudaMallocHost((void**)&s->st_host, sizeof(DevStatus)) != cudaSuccess)
         return fail(set_err(OXG_ERR_CUDA, "cudaMallocHost failed"));
@@ -825,6 +826,87 @@ int oxg_system_destroy(oxg_system* s)
     return OXG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Device-accessible address of page-locked, mapped host memory (cudaHostAlloc, torch's
+// pin_memory), or null for any other pointer: a state copy from or to such memory runs
+// as one kernel reading or writing host memory directly instead of five copies.
+const void* mapped_alias(const void* p)
+{
+    if (!p) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    return at.devicePointer;
+}
+
+struct StateCopy {
+    const float4* src[5];
+    float4* dst[5];
+    int N;
+};
+
+// One thread per particle and array: the five state arrays in one launch.
+__global__ void k_state_copy(StateCopy c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.N) return;
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        if (c.src[k]) c.dst[k][i] = c.src[k][i];
+}
+
+// The state arrays between host and device: one kernel when every host array given is
+// mapped page-locked memory, else one copy per array. Synchronises.
+int state_transfer(oxg_system* s, const float* const host[5], float4* const dev[5], bool to_device)
+{
+    StateCopy c;
+    c.N = s->N;
+    bool mapped = true;
+    int n = 0;
+    for (int k = 0; k < 5; ++k) {
+        c.src[k] = nullptr;
+        c.dst[k] = nullptr;
+        if (!host[k]) continue;
+        ++n;
+        const void* alias = mapped_alias(host[k]);
+        if (!alias) mapped = false;
+        if (to_device) {
+            c.src[k] = static_cast<const float4*>(alias);
+            c.dst[k] = dev[k];
+        } else {
+            c.src[k] = dev[k];
+            c.dst[k] = static_cast<float4*>(const_cast<void*>(alias));
+        }
+    }
+    if (n == 0) {
+        OXG_CUDA(cudaStreamSynchronize(s->stream));
+        return OXG_OK;
+    }
+    const size_t b4 = sizeof(float4) * s->N;
+    if (mapped && s->N > 0) {
+        k_state_copy<<<(s->N + 255) / 256, 256, 0, s->stream>>>(c);
+        OXG_CUDA(cudaGetLastError());
+    } else {
+        for (int k = 0; k < 5; ++k) {
+            if (!host[k]) continue;
+            if (to_device) OXG_CUDA(cudaMemcpyAsync(dev[k], host[k], b4, cudaMemcpyHostToDevice, s->stream));
+            else OXG_CUDA(cudaMemcpyAsync(const_cast<float*>(host[k]), dev[k], b4, cudaMemcpyDeviceToHost, s->stream));
+        }
+    }
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    return OXG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int oxg_system_set_stream(oxg_system* s, void* stream)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
@@ -847,30 +929,21 @@ int oxg_system_set_state(oxg_system* s, const float* pos_type, const float* pos_
                 return set_err(OXG_ERR_BAD_INDEX, "particle " + std::to_string(i) + " has type " +
                                                       std::to_string(t) + " outside the context's types");
         }
-        OXG_CUDA(cudaMemcpyAsync(s->pos, pos_type, b4, cudaMemcpyHostToDevice, s->stream));
         if (!pos_lo) OXG_CUDA(cudaMemsetAsync(s->pos_lo, 0, b4, s->stream));
     }
-    if (pos_lo) OXG_CUDA(cudaMemcpyAsync(s->pos_lo, pos_lo, b4, cudaMemcpyHostToDevice, s->stream));
-    if (quat) OXG_CUDA(cudaMemcpyAsync(s->quat, quat, b4, cudaMemcpyHostToDevice, s->stream));
-    if (vel) OXG_CUDA(cudaMemcpyAsync(s->vel, vel, b4, cudaMemcpyHostToDevice, s->stream));
-    if (angmom) OXG_CUDA(cudaMemcpyAsync(s->angmom, angmom, b4, cudaMemcpyHostToDevice, s->stream));
     if (charge) OXG_CUDA(cudaMemcpyAsync(s->charge, charge, sizeof(float) * s->N, cudaMemcpyHostToDevice, s->stream));
-    OXG_CUDA(cudaStreamSynchronize(s->stream));
-    return OXG_OK;
+    const float* const host[5] = {pos_type, pos_lo, quat, vel, angmom};
+    float4* const dev[5] = {s->pos, s->pos_lo, s->quat, s->vel, s->angmom};
+    return state_transfer(s, host, dev, true);
 }
 
 int oxg_system_get_state(oxg_system* s, float* pos_type, float* pos_lo, float* quat, float* vel,
                          float* angmom)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
-    const size_t b4 = sizeof(float4) * s->N;
-    if (pos_type) OXG_CUDA(cudaMemcpyAsync(pos_type, s->pos, b4, cudaMemcpyDeviceToHost, s->stream));
-    if (pos_lo) OXG_CUDA(cudaMemcpyAsync(pos_lo, s->pos_lo, b4, cudaMemcpyDeviceToHost, s->stream));
-    if (quat) OXG_CUDA(cudaMemcpyAsync(quat, s->quat, b4, cudaMemcpyDeviceToHost, s->stream));
-    if (vel) OXG_CUDA(cudaMemcpyAsync(vel, s->vel, b4, cudaMemcpyDeviceToHost, s->stream));
-    if (angmom) OXG_CUDA(cudaMemcpyAsync(angmom, s->angmom, b4, cudaMemcpyDeviceToHost, s->stream));
-    OXG_CUDA(cudaStreamSynchronize(s->stream));
-    return OXG_OK;
+    const float* const host[5] = {pos_type, pos_lo, quat, vel, angmom};
+    float4* const dev[5] = {s->pos, s->pos_lo, s->quat, s->vel, s->angmom};
+    return state_transfer(s, host, dev, false);
 }
 
 int oxg_system_device_state(oxg_system* s, float** pos_type, float** pos_lo, float** quat,
@@ -1027,8 +1100,10 @@ static int checkpoint(oxg_system* s, bool restore)
     return OXG_OK;
 }
 
-// The persistent run kernel: one cooperative launch of `bodies` step bodies.
-static int launch_run(oxg_system* s, int bodies, bool closing)
+// The persistent run kernel: one cooperative launch of `bodies` step bodies, preceded
+// by the run start (prepRun) when `prologue` (see k_run).
+static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = false,
+                      unsigned long long step0 = 0, bool rebuild0 = false)
 {
     const int block_bytes = s->ctx->block_bytes;
     RunArgs ra;
@@ -1048,18 +1123,29 @@ static int launch_run(oxg_system* s, int bodies, bool closing)
     ra.bar = s->bar;
     ra.bodies = bodies;
     ra.closing = closing ? 1 : 0;
-    OXG_CUDA(cudaMemsetAsync(s->bar, 0, sizeof(GridBarrier), s->stream));
+    ra.prologue = prologue ? 1 : 0;
+    ra.rebuild0 = rebuild0 ? 1u : 0u;
+    ra.step0 = step0;
+    ra.ck[0] = s->ck_pos;
+    ra.ck[1] = s->ck_pos_lo;
+    ra.ck[2] = s->ck_quat;
+    ra.ck[3] = s->ck_vel;
+    ra.ck[4] = s->ck_angmom;
+    // the barrier word needs no reset between launches: every completed barrier adds
+    // exactly 2^31 (it is cleared at allocation and after a launch that gave up)
     void* kargs[] = {&ra};
     OXG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), kargs, (size_t)block_bytes, s->stream));
     return OXG_OK;
 }
 
 // A run of n steps on the persistent kernel, in launches of up to `chunk` step bodies.
-// The first launch is preceded by prepRun (fresh neighbour list, forces, a = F/m, as
+// The first launch starts with prepRun (neighbour list if stale, forces, a = F/m, as
 // HOOMD computes the net force at the start of every run() call) and the first step
-// one. Every launch starts from a checkpoint of the state and is followed by the one
-// host synchronisation of the chunk (the status read); after a neighbour-list overflow
-// the lists grow and the chunk (with its prepRun, for the first) is replayed.
+// one, inside the kernel, so a run() call costs one launch and one synchronisation.
+// Every launch starts from a checkpoint of the state (taken by the first launch
+// itself) and is followed by the one host synchronisation of the chunk (the status
+// read); after a neighbour-list overflow the lists grow and the chunk (with its
+// prepRun, for the first) is replayed.
 static int run_persistent(oxg_system* s, long nsteps)
 {
     const int chunk = 2000;
@@ -1074,24 +1160,12 @@ static int run_persistent(oxg_system* s, long nsteps)
         const int todo = (int)std::min<long>(chunk, nsteps - done);
         const bool closing = done + todo == nsteps;
         const unsigned long long step0 = s->timestep + (unsigned long long)done;
-        if ((rc = checkpoint(s, false))) return rc;
-        if (done == 0) {
-            // a rebuild only if the lists are new or a particle moved half the buffer since
-            // they were built (e.g. a state pushed from the host)
-            k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0, s->lists_valid ? 0u : 1u);
-            if (s->lists_valid) {
-                const IntegArgs ia = integ_args(s);
-                k_check_moved<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
-            }
-            OXG_CUDA(cudaMemsetAsync(s->force, 0, sizeof(float4) * s->N, s->stream));
-            OXG_CUDA(cudaMemsetAsync(s->torque, 0, sizeof(float4) * s->N, s->stream));
-            if ((rc = launch_nlist_forces(s, s->run_mask, s->run_bonded, false))) return rc;
-            const IntegArgs ia = integ_args(s);
-            k_prep_accel<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
-            if ((rc = enqueue_step_one(s))) return rc;
-        }
+        // the first launch checkpoints the state itself (a rebuild only if the lists are
+        // new or a particle moved half the buffer since they were built)
+        const bool first = done == 0;
+        if (!first && (rc = checkpoint(s, false))) return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[0], s->stream));
-        if ((rc = launch_run(s, todo, closing))) return rc;
+        if ((rc = launch_run(s, todo, closing, first, step0, !s->lists_valid))) return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
         if ((rc = read_status(s, &d))) return rc;
         float ms = 0.f;
@@ -1100,15 +1174,21 @@ static int run_persistent(oxg_system* s, long nsteps)
             s->run_kernel_launches += 1;
             s->run_kernel_bodies += todo;
         }
-        if (d.flags & kStBarrierTimeout) return set_err(OXG_ERR_TIMEOUT, "a grid barrier wait of the run kernel gave up");
+        if (d.flags & kStBarrierTimeout) {
+            cudaMemsetAsync(s->bar, 0, sizeof(GridBarrier), s->stream);
+            return set_err(OXG_ERR_TIMEOUT, "a grid barrier wait of the run kernel gave up");
+        }
         if (d.flags & kStNonFinite) return set_err(OXG_ERR_NONFINITE, "non-finite positions or orientations");
         if (d.flags & (kStCellOverflow | kStPairOverflow)) {
             if (++retries > 8) return set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
             bool grew = false;
             if ((rc = grow_for(s, d, &grew))) return rc;
             if ((rc = checkpoint(s, true))) return rc;
-            k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0, 1u);  // step, flags, rebuild, queues
-            OXG_CUDA(cudaGetLastError());
+            s->lists_valid = false;  // the replayed prepRun rebuilds
+            if (!first) {
+                k_begin_run<<<1, 32, 0, s->stream>>>(s->st, step0, 1u);  // step, flags, rebuild, queues
+                OXG_CUDA(cudaGetLastError());
+            }
             continue;
         }
         done += todo;

@@ -39,7 +39,7 @@ struct DevStatus {
     uint32_t n_long;       // long-range pair count
     uint32_t builds;       // neighbour list builds so far
     uint32_t max_cell;     // largest cell occupancy seen
-    uint32_t pad;
+    uint32_t moved;        // run start: a particle moved half the buffer since the last build
     unsigned long long step;  // current timestep (RNG counter)
     uint32_t qcount[8];    // deferred-term queue lengths, kNQ used (k_forces_a -> k_forces_b)
 };
@@ -287,10 +287,11 @@ __device__ __forceinline__ void scatter(const ForceArgs& a, int i, int j, const 
     atomicAdd(a.torque + j, make_float4(acc.tj.x, acc.tj.y, acc.tj.z, 0.f));
 }
 
-// Full evaluation of one deferred term for short pair w (warp-uniform q).
+// Full evaluation of one deferred term for short pair w (warp-uniform q). part (fused
+// HB + CS pairs only): 0 both terms, 1 the HB term, 2 the CS term.
 template <bool ENERGY>
 __device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamView& P, int q, int2 pr,
-                                              double* eacc)
+                                              double* eacc, int part = 0)
 {
     const ParamHeader& H = P.h();
     PairIn p;
@@ -319,10 +320,14 @@ __device__ __forceinline__ void eval_deferred(const ForceArgs& a, const ParamVie
         term = kHBCross;
         const DHBCross& px = P.term<DHBCross>(kHBCross, p.pidx);
         if (bb_geometry(p.rc, fi, fj, px.base, g)) {
-            RadialF1 R1{px.f1, H.hbx_eps[p.pidx], H.hbx_shift[p.pidx]};
-            e = bb_term<false>(g, fi, fj, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1, acc);
-            RadialF2 R2{px.f2};
-            e += bb_term<true>(g, fi, fj, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2, acc);
+            if (part != 2) {
+                RadialF1 R1{px.f1, H.hbx_eps[p.pidx], H.hbx_shift[p.pidx]};
+                e = bb_term<false>(g, fi, fj, px.hb_t1, px.hb_t23, px.hb_t4, px.hb_t78, true, R1, acc);
+            }
+            if (part != 1) {
+                RadialF2 R2{px.f2};
+                e += bb_term<true>(g, fi, fj, px.cs_t1, px.cs_t23, px.cs_t4, px.cs_t78, true, R2, acc);
+            }
         }
     } else {
         term = kCoax;
@@ -592,8 +597,43 @@ __device__ __noinline__ void surrogate_segment(const ForceArgs& a, const ParamVi
     }
 }
 
-// Warp `gwarp` of `nwarps` over the segments [HB | CS | HB+CS | coax | bonds], each
-// padded to whole warps: every warp evaluates 32 items of one term.
+// One bond (part: 0 whole, 1 FENE + bonded excluded volume, 2 stacking).
+template <bool ENERGY>
+__device__ __forceinline__ void eval_bond(const ForceArgs& a, const ParamView& P, int k, int n_types,
+                                          double* eacc, bool& bad_type, int part)
+{
+    const int4 bd = a.bonds[k];
+    const int A = bd.x, B = bd.y;
+    const float4 pA = __ldcg(a.pos + A), pB = __ldcg(a.pos + B);
+    if ((unsigned)type_of(pA) >= (unsigned)n_types || (unsigned)type_of(pB) >= (unsigned)n_types) {
+        bad_type = true;
+        return;
+    }
+    const float3 Rcf = min_image(pair_delta(pB, __ldcg(a.pos_lo + B), pA, __ldcg(a.pos_lo + A)), a.L, a.invL);
+    const float4 qA = __ldcg(a.quat + A), qB = __ldcg(a.quat + B);
+    const double3 Rc = make_double3(Rcf.x, Rcf.y, Rcf.z);
+    const double4_32a dA = make_double4_32a(qA.x, qA.y, qA.z, qA.w), dB = make_double4_32a(qB.x, qB.y, qB.z, qB.w);
+    BondAcc acc;
+    if (part == 1) bonded_pair<false, 1>(P.bonded(bd.z), Rc, dA, dB, type_of(pA), type_of(pB), acc);
+    else if (part == 2) bonded_pair<false, 2>(P.bonded(bd.z), Rc, dA, dB, type_of(pA), type_of(pB), acc);
+    else bonded_pair<false>(P.bonded(bd.z), Rc, dA, dB, type_of(pA), type_of(pB), acc);
+    float eh = 0.f;
+    if (ENERGY) {
+        eacc[kNTerms + 0] += acc.e[0];
+        eacc[kNTerms + 1] += acc.e[1];
+        eacc[kNTerms + 2] += acc.e[2];
+        eh = (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2]));
+    }
+    atomicAdd(a.force + A, make_float4(-acc.fB.x, -acc.fB.y, -acc.fB.z, eh));
+    atomicAdd(a.force + B, make_float4(acc.fB.x, acc.fB.y, acc.fB.z, eh));
+    atomicAdd(a.torque + A, make_float4(acc.tA.x, acc.tA.y, acc.tA.z, 0.f));
+    atomicAdd(a.torque + B, make_float4(acc.tB.x, acc.tB.y, acc.tB.z, 0.f));
+}
+
+// Warp `gwarp` of `nwarps` over the segments [HB | CS | HB+CS | coax | HB+CS (other) |
+// bonds], each padded to whole warps: every warp evaluates 32 items of one term.
+// (Evaluating the bonds on two lanes each, FENE + bonded excluded volume | stacking,
+// shortens their chains but not the phase: the HB and cross-stacking items are as long.)
 template <bool ENERGY, bool SURR = false>
 __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamView& P, int gwarp,
                                               int nwarps, double* eacc, bool& bad_type)
@@ -622,34 +662,8 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
         }
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
-        if (q < kNQ) {
-            eval_deferred<ENERGY>(a, P, q, __ldcg(a.queue + (size_t)q * a.cap_short + k), eacc);
-            continue;
-        }
-        const int4 bd = a.bonds[k];
-        const int A = bd.x, B = bd.y;
-        const float4 pA = __ldcg(a.pos + A), pB = __ldcg(a.pos + B);
-        if ((unsigned)type_of(pA) >= (unsigned)n_types || (unsigned)type_of(pB) >= (unsigned)n_types) {
-            bad_type = true;
-            continue;
-        }
-        const float3 Rcf = min_image(pair_delta(pB, __ldcg(a.pos_lo + B), pA, __ldcg(a.pos_lo + A)), a.L, a.invL);
-        const float4 qA = __ldcg(a.quat + A), qB = __ldcg(a.quat + B);
-        BondAcc acc;
-        bonded_pair<false>(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
-                    make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
-                    type_of(pA), type_of(pB), acc);
-        float eh = 0.f;
-        if (ENERGY) {
-            eacc[kNTerms + 0] += acc.e[0];
-            eacc[kNTerms + 1] += acc.e[1];
-            eacc[kNTerms + 2] += acc.e[2];
-            eh = (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2]));
-        }
-        atomicAdd(a.force + A, make_float4(-acc.fB.x, -acc.fB.y, -acc.fB.z, eh));
-        atomicAdd(a.force + B, make_float4(acc.fB.x, acc.fB.y, acc.fB.z, eh));
-        atomicAdd(a.torque + A, make_float4(acc.tA.x, acc.tA.y, acc.tA.z, 0.f));
-        atomicAdd(a.torque + B, make_float4(acc.tB.x, acc.tB.y, acc.tB.z, 0.f));
+        if (q < kNQ) eval_deferred<ENERGY>(a, P, q, __ldcg(a.queue + (size_t)q * a.cap_short + k), eacc);
+        else eval_bond<ENERGY>(a, P, k, n_types, eacc, bad_type, 0);
     }
 }
 
@@ -1374,13 +1388,26 @@ struct RunArgs {
     GridBarrier* bar;
     int bodies;   // step bodies in this launch
     int closing;  // the last body is the run's last step (step two only)
+    // run start in the same launch (the first launch of a run() call):
+    int prologue;
+    uint32_t rebuild0;         // the lists are new: rebuild whatever the displacements
+    unsigned long long step0;  // the system's timestep (RNG counter)
+    float4* ck[5];             // checkpoint of pos, pos_lo, quat, vel, angmom for a replay
 };
+
+
 
 #ifndef OXG_DEVICE_FUNCTIONS_ONLY
 // Each body: [neighbour-list rebuild if flagged: bin | pairs] | forces part one |
 // forces part two | step two + step one of the next step. The rebuild flag is read by
 // every block right after a barrier and cleared one barrier later; a list overflow
 // ends the launch (the host grows the lists and replays from its checkpoint).
+//
+// The first launch of a run() call starts with the run start as body -1 (HOOMD's
+// prepRun): reset the step counter, flags and queues, checkpoint the state for a
+// replay, clear the accumulators and check the displacements since the last list
+// build | [rebuild if the lists are new or a particle moved half the buffer] | forces
+// of the current state, no step advance | a = F/m and step one of the first step.
 template <bool SURR>
 __global__ void __launch_bounds__(256, 2) k_run(RunArgs a)
 {
@@ -1392,8 +1419,37 @@ __global__ void __launch_bounds__(256, 2) k_run(RunArgs a)
     const int gthread = gwarp * 32 + lane, nthreads = nwarps * 32;
     double eacc[kNTerms + 3];  // unused: MD steps evaluate no energies
     bool bad_type = false;
-    for (int body = 0; body < a.bodies; ++body) {
-        const bool rebuild = ld_volatile(&st->rebuild) != 0u;
+    for (int body = a.prologue ? -1 : 0; body < a.bodies; ++body) {
+        const bool pro = body < 0;
+        bool rebuild;
+        if (pro) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                st->step = a.step0;
+                st->flags = 0u;
+                st->rebuild = 0u;
+            }
+            if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
+            const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+            bool far = false;
+            for (int i = gthread; i < a.g.N; i += nthreads) {
+                const float4 x = a.g.pos[i];
+                a.ck[0][i] = x;
+                a.ck[1][i] = a.g.pos_lo[i];
+                a.ck[2][i] = a.g.quat[i];
+                a.ck[3][i] = a.g.vel[i];
+                a.ck[4][i] = a.g.angmom[i];
+                a.g.force[i] = zero;
+                a.g.torque[i] = zero;
+                const float4 r = a.g.pos_ref[i];
+                const float3 d = min_image(mk3(x.x - r.x, x.y - r.y, x.z - r.z), a.g.L, a.g.invL);
+                far |= !(dot(d, d) <= a.g.half_buf2);
+            }
+            if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->moved, 1u);
+            if (!grid_barrier(a.bar)) break;
+            rebuild = a.rebuild0 != 0u || ld_volatile(&st->moved) != 0u;
+        } else {
+            rebuild = ld_volatile(&st->rebuild) != 0u;
+        }
         if (rebuild) {
             const uint32_t par = ld_volatile(&st->gen) & 1u;
             nlist_zero_other(a.n, gthread, nthreads, par);
@@ -1405,22 +1461,33 @@ __global__ void __launch_bounds__(256, 2) k_run(RunArgs a)
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             if (rebuild) st->gen += 1u;
-            st->step += 1ull;
+            if (!pro) st->step += 1ull;
         }
         forces_a_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
         if (!grid_barrier(a.bar)) break;
-        if (blockIdx.x == 0 && threadIdx.x == 0) st->rebuild = 0u;
+        if (!pro && blockIdx.x == 0 && threadIdx.x == 0) st->rebuild = 0u;
         forces_b_body<false, SURR>(a.f, P, gwarp, nwarps, eacc, bad_type);
         if (!grid_barrier(a.bar)) break;
-        // step two of this step (+ step one of the next)
+        // step two of this step (+ step one of the next); at run start a = F/m and
+        // step one of the first step
         const bool last = a.closing && body == a.bodies - 1;
         const unsigned long long step = *(const volatile unsigned long long*)&st->step;
-        if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
+        if (blockIdx.x == 0) {
+            if (threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
+            if (pro && threadIdx.x == 32) st->moved = 0u;  // read two barriers ago
+        }
         bool far = false, bad = false;
         for (int i = gthread; i < a.g.N; i += nthreads) {
             PState s = load_pstate(a.g, i);
             float4 ac, tn;
-            particle_step_two(a.g, i, step, s, ac, tn);
+            if (pro) {
+                const float4 F = __ldcg(a.g.force + i), T = __ldcg(a.g.torque + i);
+                const float minv = 1.f / s.v.w;
+                ac = make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f);
+                tn = make_float4(T.x, T.y, T.z, 0.f);
+            } else {
+                particle_step_two(a.g, i, step, s, ac, tn);
+            }
             if (last) {
                 a.g.vel[i] = s.v;
                 a.g.angmom[i] = s.p;

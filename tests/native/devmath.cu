@@ -80,7 +80,12 @@ extern "C" void devmath_bonded(const oxg_bonded_params* p, const double* Rc, con
     const double3 R = make_double3(Rc[0], Rc[1], Rc[2]);
     const double4_32a a4 = make_double4_32a(qA[0], qA[1], qA[2], qA[3]);
     const double4_32a b4 = make_double4_32a(qB[0], qB[1], qB[2], qB[3]);
-    if (full64) bonded_pair<true>(D, R, a4, b4, tA, tB, acc);
+    // full64: bit 0 the FP64 BACK-site rotations; bits 1-2 the part (0 whole bond,
+    // 1 FENE + bonded excluded volume, 2 stacking)
+    const int part = full64 >> 1;
+    if (part == 1) bonded_pair<false, 1>(D, R, a4, b4, tA, tB, acc);
+    else if (part == 2) bonded_pair<false, 2>(D, R, a4, b4, tA, tB, acc);
+    else if (full64 & 1) bonded_pair<true>(D, R, a4, b4, tA, tB, acc);
     else bonded_pair<false>(D, R, a4, b4, tA, tB, acc);
     FB[0] = acc.fB.x; FB[1] = acc.fB.y; FB[2] = acc.fB.z;
     tauA[0] = acc.tA.x; tauA[1] = acc.tA.y; tauA[2] = acc.tA.z;

@@ -98,6 +98,34 @@ def test_fp32_bonded_math(devmath, model, avg, full64):
     assert np.array_equal(e[:, 0] >= 1e12, ~ok)
 
 
+@pytest.mark.parametrize("model", ("dna1", "rna2"))
+def test_bond_parts_sum_to_whole_bond(devmath, model):
+    """The run kernel may evaluate a bond on two lanes (FENE + bonded excluded volume,
+    and stacking): the two parts add up to the whole bond."""
+    from oxdna import _abi
+    d = golden(f"bonds_{model}.npz")
+    _, bonded = model_forces(model, average=False)
+    pod = _abi.bonded_from_dict(bonded.params["backbone"])
+    n = len(d["seq/Rc"])
+    for k in range(n):
+        res = []
+        for mode in (0, 2, 4):
+            FB, tA, tB, e, v = (np.zeros(3), np.zeros(3), np.zeros(3), np.zeros(3), np.zeros(6))
+            devmath.devmath_bonded(C.byref(pod), _p(d["seq/Rc"][k]), _p(d["seq/qA"][k]),
+                                   _p(d["seq/qB"][k]), int(d["seq/types"][k][0]),
+                                   int(d["seq/types"][k][1]),
+                                   *(x.ctypes.data_as(C.POINTER(C.c_double)) for x in (FB, tA, tB, e, v)),
+                                   mode)
+            res.append((FB, tA, tB, e))
+        whole, p1, p2 = res
+        if whole[3][0] >= 1e12:
+            continue
+        assert p1[3][2] == 0.0 and p2[3][0] == 0.0 and p2[3][1] == 0.0
+        for w, a, b in zip(whole, p1, p2):
+            scale = max(np.abs(w).max(), 1.0)
+            assert np.abs(a + b - w).max() <= 1e-5 * scale, (k, w, a, b)
+
+
 def _qmul(a, b):
     w1, x1, y1, z1 = a
     w2, x2, y2, z2 = b
