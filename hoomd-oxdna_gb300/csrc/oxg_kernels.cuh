@@ -1345,13 +1345,21 @@ struct GridBarrier {
     uint32_t pad[30]; // a line of its own
 };
 
-constexpr long long kBarrierSpinLimit = 1LL << 22;  // polls of >= 0.1 us: about a second
+constexpr long long kBarrierSpinLimit = 1LL << 22;  // polls of an L2 round trip (~0.5 us): about 2 s
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 
 // Arrive-and-wait over all blocks of the launch. Block 0 adds 2^31 - (blocks - 1),
 // every other block 1, so bit 31 of the counter flips exactly when the last block
-// arrives (and the counter needs no reset). The fences on both sides make every write
-// before the barrier visible to every read after it. Returns false if the wait gave up
-// (after kBarrierSpinLimit polls) or another block did; the caller must then return.
+// arrives (and the counter needs no reset). The arrival is a release and the polls are
+// acquires (after the block's __syncthreads), so every write before the barrier is
+// visible to every read after it. Returns false if the wait gave up (after
+// kBarrierSpinLimit polls) or another block did; the caller must then return.
 __device__ __forceinline__ bool grid_barrier(GridBarrier* gb)
 {
     __shared__ int bar_ok;
@@ -1359,22 +1367,22 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier* gb)
     if (threadIdx.x == 0) {
         int ok = 1;
         const uint32_t add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
-        __threadfence();
-        const uint32_t old = atomicAdd(&gb->arrive, add);
+        uint32_t old;
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(&gb->arrive), "r"(add) : "memory");
         long long polls = 0;
-        while (((old ^ ld_volatile(&gb->arrive)) & 0x80000000u) == 0u) {
-            if (ld_volatile(&gb->abort)) {
-                ok = 0;
-                break;
+        while (((old ^ ld_acquire(&gb->arrive)) & 0x80000000u) == 0u) {
+            if ((++polls & 63) == 0) {  // the abort word and the limit every 64 polls
+                if (ld_volatile(&gb->abort)) {
+                    ok = 0;
+                    break;
+                }
+                if (polls > kBarrierSpinLimit) {
+                    atomicExch(&gb->abort, 1u);
+                    ok = 0;
+                    break;
+                }
             }
-            if (++polls > kBarrierSpinLimit) {
-                atomicExch(&gb->abort, 1u);
-                ok = 0;
-                break;
-            }
-            __nanosleep(32);
         }
-        __threadfence();
         bar_ok = ok;
     }
     __syncthreads();
