@@ -1114,9 +1114,9 @@ static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = f
     int& grid = surr ? s->grid_run_surr : s->grid_run;
     if (grid == 0) {
         int per_sm = 0;
-        OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, block_bytes));
+        OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRunThreads, block_bytes));
         if (per_sm < 1) return set_err(OXG_ERR_CUDA, "the run kernel does not fit on an SM");
-        grid = num_sms() * std::min(per_sm, 2);
+        grid = num_sms() * std::min(per_sm, 512 / kRunThreads);
     }
     ra.n = nlist_args(s);
     ra.g = integ_args(s);
@@ -1134,7 +1134,7 @@ static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = f
     // the barrier word needs no reset between launches: every completed barrier adds
     // exactly 2^31 (it is cleared at allocation and after a launch that gave up)
     void* kargs[] = {&ra};
-    OXG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), kargs, (size_t)block_bytes, s->stream));
+    OXG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kRunThreads), kargs, (size_t)block_bytes, s->stream));
     return OXG_OK;
 }
 

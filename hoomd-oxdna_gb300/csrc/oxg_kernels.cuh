@@ -1339,6 +1339,9 @@ __global__ void k_prep_accel(IntegArgs a)
 // the cooperative launch guarantees) meet at grid barriers between the phases, so the
 // code stays in the instruction caches and the parameters in shared memory for the
 // whole launch instead of being fetched again by five launches per step.
+#ifndef OXG_RUN_THREADS
+#define OXG_RUN_THREADS 256
+#endif
 struct GridBarrier {
     uint32_t arrive;  // bit 31 flips each time every block has arrived
     uint32_t abort;   // set by a block whose wait gave up: the others leave too
@@ -1416,8 +1419,9 @@ struct RunArgs {
 // replay, clear the accumulators and check the displacements since the last list
 // build | [rebuild if the lists are new or a particle moved half the buffer] | forces
 // of the current state, no step advance | a = F/m and step one of the first step.
+constexpr int kRunThreads = OXG_RUN_THREADS;  // threads per block of the run kernel
 template <bool SURR>
-__global__ void __launch_bounds__(256, 2) k_run(RunArgs a)
+__global__ void __launch_bounds__(kRunThreads, 512 / kRunThreads) k_run(RunArgs a)
 {
     const ParamView P = stage_params(a.f.params, a.f.param_bytes);
     DevStatus* st = a.f.st_rw;
