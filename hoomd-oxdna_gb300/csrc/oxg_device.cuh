@@ -17,6 +17,33 @@
 // Physics functions are host+device so that the exact FP32 arithmetic of the kernels
 // can also be exercised by the host-side numerics tests (tests/native/).
 #define OXG_HD __host__ __device__ __forceinline__
+// Shared (out-of-line) device code for the long per-pair evaluations: one copy of the
+// angle and BASE-BASE term code for every caller keeps the hot code small enough to
+// stay in the instruction caches when few warps run it once per step.
+#ifndef OXG_SHARED_ANGLES
+#define OXG_SHARED_ANGLES 1
+#endif
+#ifndef OXG_SHARED_STACKING
+#define OXG_SHARED_STACKING 0
+#endif
+#ifndef OXG_SHARED_TERMS
+#define OXG_SHARED_TERMS 0
+#endif
+#if OXG_SHARED_ANGLES
+#define OXG_HD_ANG static __host__ __device__ __noinline__
+#else
+#define OXG_HD_ANG OXG_HD
+#endif
+#if OXG_SHARED_STACKING
+#define OXG_HD_STACK static __host__ __device__ __noinline__
+#else
+#define OXG_HD_STACK OXG_HD
+#endif
+#if OXG_SHARED_TERMS
+#define OXG_HD_TERM static __host__ __device__ __noinline__
+#else
+#define OXG_HD_TERM OXG_HD
+#endif
 
 namespace oxg {
 
@@ -247,7 +274,7 @@ OXG_HD void angle_of(float c, float3 u, float3 v, const F4& t, float& th, float&
 // f4 value and torque coefficient of one angle; the reflected branch (SYM) reuses
 // pi - theta and sin(pi - theta) = sin(theta) (src/OxDNABaseBase.h:52-67).
 template <bool SYM>
-OXG_HD Ang angular(float cost, float3 u, float3 v, const F4& t, float sign)
+OXG_HD_ANG Ang angular(float cost, float3 u, float3 v, const F4& t, float sign)
 {
     float th, st;
     angle_of(cost, u, v, t, th, st);
@@ -314,7 +341,7 @@ OXG_HD bool bb_support(const BBGeom& g, const F4& t1, const F4& t23, const F4& t
 }
 
 template <bool SYM, class Radial>
-OXG_HD float bb_term(const BBGeom& g, const Frame& fi, const Frame& fj,
+OXG_HD_TERM float bb_term(const BBGeom& g, const Frame& fi, const Frame& fj,
                                          const F4& t1, const F4& t23, const F4& t4,
                                          const F4& t78, bool inc_t4, const Radial& R,
                                          PairAcc& acc)
@@ -386,7 +413,7 @@ OXG_HD bool coax_support(const DCoax& p, float3 rc, const Frame& fi, const Frame
            f4_support<true>(-dot(fj.a3, rsd), p.t56);
 }
 
-OXG_HD float coax_term(const DCoax& p, float3 rc, const Frame& fi,
+OXG_HD_TERM float coax_term(const DCoax& p, float3 rc, const Frame& fi,
                                            const Frame& fj, PairAcc& acc)
 {
     const float3 stack_i = body_to_lab(fi, p.stack), stack_j = body_to_lab(fj, p.stack);
@@ -570,7 +597,7 @@ OXG_HD void vir_acc(float* v, float3 r, float3 f)
 }
 
 // DNA stacking, oxDNA p = B, q = A (src/OxDNABondedKernel.h:69-231). Rc = r_B - r_A.
-OXG_HD float stacking_dna(const DBonded& p, float3 Rc, const Frame& fA,
+OXG_HD_STACK float stacking_dna(const DBonded& p, float3 Rc, const Frame& fA,
                                               const Frame& fB, int tA, int tB, BondAcc& acc)
 {
     const float3 a1 = fB.a1, a2 = fB.a2, a3 = fB.a3;
@@ -665,7 +692,7 @@ OXG_HD float stacking_dna(const DBonded& p, float3 Rc, const Frame& fA,
 }
 
 // RNA stacking, p = B, q = A (src/OxDNABondedKernel.h:238-353).
-OXG_HD float stacking_rna(const DBonded& p, float3 Rc, const Frame& fA,
+OXG_HD_STACK float stacking_rna(const DBonded& p, float3 Rc, const Frame& fA,
                                               const Frame& fB, int tA, int tB, BondAcc& acc)
 {
     const float3 a2 = fB.a2, a3 = fB.a3, b2 = fA.a2, b3 = fA.a3;
