@@ -15,8 +15,13 @@ LIB = os.path.join(PKG, "liboxdna_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+# FP32 division and square root to within 2 ulp (the hardware reciprocal / square-root
+# approximations) and denormals flushed: the per-pair dependency chains are what bound
+# the MD step, and the IEEE-rounded forms add a Newton step and a slow-path branch to
+# every division. FP64 arithmetic (FENE, energy sums) is unaffected.
 NVCC_FLAGS = [ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-shared", "--expt-relaxed-constexpr"]
+              "-shared", "--expt-relaxed-constexpr", "-ftz=true", "-prec-div=false",
+              "-prec-sqrt=false"]
 
 
 def sources():
