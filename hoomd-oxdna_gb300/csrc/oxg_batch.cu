@@ -188,7 +188,7 @@ __device__ inline void scatter_pair(const Smem& s, int pi, int pj, int r, const 
 __device__ inline float3 rep_delta(const Smem& s, const TileRep& R, int pi, int pj)
 {
     const float4 hi_i = s.x[pi], hi_j = s.x[pj], lo_i = s.xl[pi], lo_j = s.xl[pj];
-    return min_image(pair_delta(hi_i, lo_i, hi_j, lo_j), R.L, R.invL);
+    return image_delta(hi_i, lo_i, hi_j, lo_j, R.L, R.invL);
 }
 
 // the heavy term q of the tile pair (pi, pj) of replica r (block-cooperative caller)

@@ -5,7 +5,7 @@ Langevin / NO_SQUISH integrator (oracle trajectory, duplex stability, equipartit
 import numpy as np
 import pytest
 
-from _util import TOL_GPU
+from _util import TOL_GPU, maxrel
 
 pytestmark = pytest.mark.gpu
 
@@ -41,6 +41,12 @@ def test_8000nt_energies_match_oracle(native, oracle, fused):
     # Newton's third law on the summed GPU forces
     F = sum(sim._force_arrays(f)[0] for f in forces)
     assert np.linalg.norm(F.sum(axis=0)) < 1e-4 * np.abs(F).max() * np.sqrt(len(F))
+    # per-particle forces and torques (measured ~8e-6 / ~6e-6 max-norm relative; pairs
+    # across the periodic boundary included: ~2e-4 when the image shift rounded the
+    # position difference at the ulp of the box length)
+    T = sum(sim._force_arrays(f)[1] for f in forces)
+    assert maxrel(F, r["force"]) < 5e-5
+    assert maxrel(T, r["torque"]) < 5e-5
 
 
 def test_rna_hairpins_energies_match_oracle_and_run(native, oracle):
