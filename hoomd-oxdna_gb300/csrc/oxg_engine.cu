@@ -1116,7 +1116,7 @@ static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = f
         int per_sm = 0;
         OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRunThreads, block_bytes));
         if (per_sm < 1) return set_err(OXG_ERR_CUDA, "the run kernel does not fit on an SM");
-        grid = num_sms() * std::min(per_sm, 512 / kRunThreads);
+        grid = num_sms() * std::min(per_sm, OXG_RUN_BLOCKS_PER_SM);
     }
     ra.n = nlist_args(s);
     ra.g = integ_args(s);

@@ -288,12 +288,6 @@ __device__ __forceinline__ bool load_pair(const ForceArgs& a, int2 pr, int n_typ
     p.cj = a.charge ? a.charge[p.j] : 1.f;
     return true;
 }
-__device__ __forceinline__ bool load_short_pair(const ForceArgs& a, int w, int n_types, PairIn& p,
-                                                bool& bad_type)
-{
-    return load_pair(a, __ldcg(a.pairs_short + w), n_types, p, bad_type);
-}
-
 template <bool ENERGY>
 __device__ __forceinline__ void scatter(const ForceArgs& a, int i, int j, const PairAcc& acc, float e)
 {
@@ -384,11 +378,17 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint32_t mask = a.mask;
 
-    for (int base = gwarp * 32; base < n_short; base += nwarps * 32) {
+    // the next unit's pair entry is loaded one unit ahead (a warp takes several units
+    // of a large system: one L2 round trip of each unit's chain is hidden)
+    const int stride = nwarps * 32;
+    int2 next_pr = gwarp * 32 + lane < n_short ? __ldcg(a.pairs_short + gwarp * 32 + lane) : make_int2(0, 0);
+    for (int base = gwarp * 32; base < n_short; base += stride) {
         const int w = base + lane;
+        const int2 pr = next_pr;
+        if (w + stride < n_short) next_pr = __ldcg(a.pairs_short + w + stride);
         bool want[kNQ] = {};
         PairIn p;
-        if (w < n_short && load_short_pair(a, w, n_types, p, bad_type) && p.rsq < H.rcutsq_max) {
+        if (w < n_short && load_pair(a, pr, n_types, p, bad_type) && p.rsq < H.rcutsq_max) {
             const Frame fi = quat_frame(p.qi), fj = quat_frame(p.qj);
             PairAcc acc;
             acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
@@ -468,10 +468,12 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
     const int free_w = nwarps - n_su;
     const bool to_free = free_w > 0 && 4 * free_w >= n_lu;
     const int v0 = to_free ? gwarp - n_su : gwarp, vstride = to_free ? free_w : nwarps;
+    int2 next_lp = (v0 >= 0 && v0 * 32 + lane < n_long) ? __ldcg(a.pairs_long + v0 * 32 + lane) : make_int2(0, 0);
     for (int v = v0; v >= 0 && v < n_lu && long_mask; v += vstride) {
         const int w = v * 32 + lane;
+        const int2 pr = next_lp;
+        if (w + vstride * 32 < n_long) next_lp = __ldcg(a.pairs_long + w + vstride * 32);
         if (w >= n_long) continue;
-        const int2 pr = __ldcg(a.pairs_long + w);
         const int i = pr.x, j = pr.y;
         // every load of the pair issued at once (one L2 round trip)
         const float4 pi = __ldcg(a.pos + i), pj = __ldcg(a.pos + j);
@@ -1359,6 +1361,9 @@ __global__ void k_prep_accel(IntegArgs a)
 #ifndef OXG_RUN_THREADS
 #define OXG_RUN_THREADS 256
 #endif
+#ifndef OXG_RUN_BLOCKS_PER_SM
+#define OXG_RUN_BLOCKS_PER_SM (512 / OXG_RUN_THREADS)
+#endif
 struct GridBarrier {
     uint32_t arrive;  // bit 31 flips each time every block has arrived
     uint32_t abort;   // set by a block whose wait gave up: the others leave too
@@ -1438,7 +1443,7 @@ struct RunArgs {
 // of the current state, no step advance | a = F/m and step one of the first step.
 constexpr int kRunThreads = OXG_RUN_THREADS;  // threads per block of the run kernel
 template <bool SURR>
-__global__ void __launch_bounds__(kRunThreads, 512 / kRunThreads) k_run(RunArgs a)
+__global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunArgs a)
 {
     const ParamView P = stage_params(a.f.params, a.f.param_bytes);
     DevStatus* st = a.f.st_rw;
