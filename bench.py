@@ -510,7 +510,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--quick", action="store_true",
                     help="resident timing only (no fused / e2e / CPU legs); for profiling runs")
-    ap.add_argument("--leg", choices=["batched", "rna", "surrogate"],
+    ap.add_argument("--leg", choices=["batched", "rna", "surrogate", "nt100k"],
                     help="run one extension leg alone and print its numbers (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -530,6 +530,16 @@ def run_leg(args):
         out = bench_batched(stream, steps=args.steps)
     elif args.leg == "rna":
         out = bench_rna(stream, steps=args.steps, warmup=args.warmup)
+    elif args.leg == "nt100k":
+        big = build_system(n_dup=2500, n_bp=20, box=230.0, seed=5)
+        sim, _ = make_sim(big, fused=False, stream=stream.cuda_stream)
+        sim.run(0)
+        sim.run(args.warmup)
+        torch.cuda.synchronize()
+        with nvtx("timed"):
+            ms = time_resident(sim, args.steps, 0, stream, block=args.steps)
+        out = {"workload": "oxDNA2 2500 x 20 bp (100k nt), box 230, 296.15 K, 0.5 M, fused=False",
+               "steps_per_s": args.steps / (ms * 1e-3)}
     else:
         big = build_system(n_dup=2500, n_bp=20, box=230.0, seed=5)
         out = bench_surrogate(stream, big, steps=args.steps, warmup=args.warmup)
