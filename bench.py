@@ -451,6 +451,9 @@ def run_ours(args):
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cb = cpu_baseline(sysarr)
+        one = cpu_baseline(sysarr, seconds=8.0, max_steps=100, threads=1)
+        cb["single_core"] = {"value": one["value"], "unit": one["unit"], "cores": 1,
+                             "sample": one["sample"]}
     if rank != 0:
         dist.destroy_process_group()
         return
