@@ -963,7 +963,44 @@ __device__ __forceinline__ bool is_excluded(int4 e, int j) { return e.x == j || 
 // the 27 neighbour cells, a prefix sum flattens the candidates, and each round the 32
 // lanes test 32 candidates at once (cell of a candidate by binary search over the
 // prefix sums); found pairs are appended with one atomic per warp and list per round.
-__device__ __forceinline__ void nlist_pairs_warp(const NlistArgs& a, int i, uint32_t par)
+// Pairs found by a warp that handles many particles are staged in shared memory and
+// appended to the global lists in batches: one counter atomic per batch instead of one
+// per particle (100k particles: 200k same-address atomics per rebuild otherwise).
+constexpr int kPairStage = 128;  // entries per list per warp
+struct PairStage {
+    int2* s;      // short-pair staging buffer (kPairStage entries, shared memory)
+    int2* l;      // long-pair staging buffer
+    int ns, nl;   // staged entries (warp-uniform)
+};
+
+// Append the warp's staged pairs of one list to the global list (all lanes).
+__device__ __forceinline__ void stage_flush(const NlistArgs& a, int2* buf, int& n, uint32_t* counter,
+                                            int2* list, int cap, bool& over)
+{
+    if (n == 0) return;
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(counter, (uint32_t)n);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) {
+        if (base + (uint32_t)k < (uint32_t)cap) list[base + k] = buf[k];
+        else over = true;
+    }
+    __syncwarp();
+    n = 0;
+}
+
+__device__ __forceinline__ void stage_flush_all(const NlistArgs& a, PairStage& sg)
+{
+    bool over = false;
+    stage_flush(a, sg.s, sg.ns, &a.st->n_short, a.pairs_short, a.cap_short, over);
+    stage_flush(a, sg.l, sg.nl, &a.st->n_long, a.pairs_long, a.cap_long, over);
+    if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(&a.st->flags, kStPairOverflow);
+}
+
+__device__ __forceinline__ void nlist_pairs_warp(const NlistArgs& a, int i, uint32_t par,
+                                                 PairStage* sg = nullptr)
 {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -1022,6 +1059,18 @@ __device__ __forceinline__ void nlist_pairs_warp(const NlistArgs& a, int i, uint
             }
         }
         const unsigned ms = __ballot_sync(0xffffffffu, is_short), ml = __ballot_sync(0xffffffffu, is_long);
+        if (sg) {
+            if (sg->ns + __popc(ms) > kPairStage)
+                stage_flush(a, sg->s, sg->ns, &a.st->n_short, a.pairs_short, a.cap_short, over);
+            if (sg->nl + __popc(ml) > kPairStage)
+                stage_flush(a, sg->l, sg->nl, &a.st->n_long, a.pairs_long, a.cap_long, over);
+            if (is_short) sg->s[sg->ns + __popc(ms & lt_mask)] = make_int2(i, j);
+            if (is_long) sg->l[sg->nl + __popc(ml & lt_mask)] = make_int2(i, j);
+            sg->ns += __popc(ms);
+            sg->nl += __popc(ml);
+            __syncwarp();
+            continue;
+        }
         uint32_t bs = 0, bl = 0;
         if (lane == 0) {
             if (ms) bs = atomicAdd(&a.st->n_short, (uint32_t)__popc(ms));
@@ -1489,7 +1538,12 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             nlist_zero_other(a.n, gthread, nthreads, par);
             for (int i = gthread; i < a.n.N; i += nthreads) nlist_bin_particle(a.n, i, par);
             if (!grid_barrier(a.bar)) break;
-            for (int i = gwarp; i < a.n.N; i += nwarps) nlist_pairs_warp(a.n, i, par);
+            {
+                __shared__ int2 stage_buf[2][kRunThreads / 32][kPairStage];
+                PairStage sg{stage_buf[0][threadIdx.x >> 5], stage_buf[1][threadIdx.x >> 5], 0, 0};
+                for (int i = gwarp; i < a.n.N; i += nwarps) nlist_pairs_warp(a.n, i, par, &sg);
+                stage_flush_all(a.n, sg);
+            }
             if (!grid_barrier(a.bar)) break;
             if (ld_volatile(&st->flags) & (kStCellOverflow | kStPairOverflow)) break;
         }
