@@ -365,10 +365,28 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(co
 // Warp `gwarp` of `nwarps`: short-range pairs in units of 32 (cheap terms inline, heavy
 // ones queued), then the long-range pairs. Counters are read with volatile loads: the
 // persistent run kernel calls this after a neighbour-list rebuild in the same launch.
+// Phase A appends the heavy-term pairs of a block to shared-memory queues (shared
+// atomics) and copies them to the global queues at the end of the phase with one global
+// atomic per queue and block, instead of one same-address global atomic per warp, term
+// and unit. A reservation that does not fit goes to the global queue directly.
+constexpr int kBlockQ = 400;  // entries per queue and block
+struct BlockQueues {
+    uint32_t count[kNQ];  // reserved entries
+    uint32_t valid[kNQ];  // entries below this offset were all written
+    uint32_t base[kNQ];   // global offsets of the flush
+    int2 buf[kNQ][kBlockQ];
+};
+
 template <bool ENERGY>
 __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamView& P, int gwarp,
                                               int nwarps, double* eacc, bool& bad_type)
 {
+    __shared__ BlockQueues bq;
+    if (threadIdx.x < kNQ) {
+        bq.count[threadIdx.x] = 0u;
+        bq.valid[threadIdx.x] = (uint32_t)kBlockQ;
+    }
+    __syncthreads();
     const ParamHeader& H = P.h();
     // after an overflow the counters exceed the capacities; only stored pairs are read
     const int n_short = (int)min(ld_volatile(&a.st_rw->n_short), (uint32_t)a.cap_short);
@@ -452,10 +470,22 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
             const unsigned m = __ballot_sync(0xffffffffu, want[q]);
             if (m) {
                 const int leader = __ffs(m) - 1;
-                uint32_t base_q = 0;
-                if (lane == leader) base_q = atomicAdd(&a.st_rw->qcount[q], (uint32_t)__popc(m));
-                base_q = __shfl_sync(0xffffffffu, base_q, leader);
-                if (want[q]) a.queue[(size_t)q * a.cap_short + base_q + __popc(m & lt_mask)] = make_int2(p.i, p.j);
+                const uint32_t n = (uint32_t)__popc(m);
+                uint32_t off = 0;
+                if (lane == leader) {
+                    off = atomicAdd(&bq.count[q], n);
+                    if (off + n > (uint32_t)kBlockQ) {  // does not fit: straight to the global queue
+                        if (off < (uint32_t)kBlockQ) atomicMin(&bq.valid[q], off);
+                        off = 0x80000000u | atomicAdd(&a.st_rw->qcount[q], n);
+                    }
+                }
+                off = __shfl_sync(0xffffffffu, off, leader);
+                if (want[q]) {
+                    const int2 e = make_int2(p.i, p.j);
+                    const uint32_t k = (off & 0x7fffffffu) + __popc(m & lt_mask);
+                    if (off & 0x80000000u) a.queue[(size_t)q * a.cap_short + k] = e;
+                    else bq.buf[q][k] = e;
+                }
             }
         }
     }
@@ -493,6 +523,20 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
             if (ENERGY) eacc[kDebye] += (double)E[kDebye];
             scatter<ENERGY>(a, i, j, acc, E[kDebye]);
         }
+    }
+    // the block's staged heavy-term pairs to the global queues
+    __syncthreads();
+    if (threadIdx.x < kNQ) {
+        const uint32_t n = min(bq.count[threadIdx.x], bq.valid[threadIdx.x]);
+        bq.count[threadIdx.x] = n;
+        bq.base[threadIdx.x] = n ? atomicAdd(&a.st_rw->qcount[threadIdx.x], n) : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) {
+        const uint32_t n = bq.count[q], b = bq.base[q];
+        for (uint32_t k = threadIdx.x; k < n; k += blockDim.x)
+            if (b + k < (uint32_t)a.cap_short) a.queue[(size_t)q * a.cap_short + b + k] = bq.buf[q][k];
     }
 }
 
