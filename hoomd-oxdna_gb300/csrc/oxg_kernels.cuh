@@ -1232,6 +1232,7 @@ __device__ __forceinline__ void dd_advance(float& hi, float& lo, float d, float 
 // Per-particle integrator state (positions double-float).
 struct PState {
     float4 x, xl, v, q, p;  // x.w = type bits, v.w = mass
+    float4 ref;             // position at the last list build (the engine's step one)
 };
 
 // Step one with acceleration ac and net lab torque tn: v += dt/2 a; x += dt v
@@ -1329,6 +1330,7 @@ __device__ __forceinline__ PState load_pstate(const IntegArgs& a, int i)
     s.v = a.vel[i];
     s.q = a.quat[i];
     s.p = a.angmom[i];
+    s.ref = a.pos_ref[i];  // with the state loads: after the stores it would wait a round trip
     return s;
 }
 
@@ -1345,7 +1347,7 @@ __device__ __forceinline__ void particle_step_one(const IntegArgs& a, int i, PSt
     a.angmom[i] = s.p;
     a.force[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     a.torque[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 r = a.pos_ref[i];
+    const float4 r = s.ref;
     const float3 d = min_image(mk3(s.x.x - r.x, s.x.y - r.y, s.x.z - r.z), a.L, a.invL);
     far = dot(d, d) > a.half_buf2;
 }
