@@ -42,6 +42,9 @@ struct DevStatus {
     uint32_t moved;        // run start: a particle moved half the buffer since the last build
     unsigned long long step;  // current timestep (RNG counter)
     uint32_t qcount[8];    // deferred-term queue lengths, kNQ used (k_forces_a -> k_forces_b)
+    uint32_t qspill;       // run kernel: a block's shared-memory queue overflowed this step
+    uint32_t rb[2];        // run kernel: rebuild requests of the next bodies, by body parity
+    uint32_t pad2;
 };
 
 // ------------------------------------------------------------ parameter view
@@ -377,11 +380,19 @@ struct BlockQueues {
     int2 buf[kNQ][kBlockQ];
 };
 
-template <bool ENERGY>
+__device__ __forceinline__ BlockQueues& block_queues()
+{
+    __shared__ BlockQueues bq;
+    return bq;
+}
+
+// LOCAL: the block's heavy-term pairs stay in its shared-memory queues for
+// forces_b_local (the run kernel); otherwise they are copied to the global queues.
+template <bool ENERGY, bool LOCAL = false>
 __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamView& P, int gwarp,
                                               int nwarps, double* eacc, bool& bad_type)
 {
-    __shared__ BlockQueues bq;
+    BlockQueues& bq = block_queues();
     if (threadIdx.x < kNQ) {
         bq.count[threadIdx.x] = 0u;
         bq.valid[threadIdx.x] = (uint32_t)kBlockQ;
@@ -477,6 +488,7 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
                     if (off + n > (uint32_t)kBlockQ) {  // does not fit: straight to the global queue
                         if (off < (uint32_t)kBlockQ) atomicMin(&bq.valid[q], off);
                         off = 0x80000000u | atomicAdd(&a.st_rw->qcount[q], n);
+                        if (LOCAL) a.st_rw->qspill = 1u;
                     }
                 }
                 off = __shfl_sync(0xffffffffu, off, leader);
@@ -524,8 +536,13 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
             scatter<ENERGY>(a, i, j, acc, E[kDebye]);
         }
     }
-    // the block's staged heavy-term pairs to the global queues
     __syncthreads();
+    if (LOCAL) {  // the entries written, for forces_b_local after the block's barrier
+        if (threadIdx.x < kNQ) bq.count[threadIdx.x] = min(bq.count[threadIdx.x], bq.valid[threadIdx.x]);
+        __syncthreads();
+        return;
+    }
+    // the block's staged heavy-term pairs to the global queues
     if (threadIdx.x < kNQ) {
         const uint32_t n = min(bq.count[threadIdx.x], bq.valid[threadIdx.x]);
         bq.count[threadIdx.x] = n;
@@ -697,7 +714,7 @@ __device__ __forceinline__ void eval_bond(const ForceArgs& a, const ParamView& P
 // bonds], each padded to whole warps: every warp evaluates 32 items of one term.
 // (Evaluating the bonds on two lanes each, FENE + bonded excluded volume | stacking,
 // shortens their chains but not the phase: the HB and cross-stacking items are as long.)
-template <bool ENERGY, bool SURR = false>
+template <bool ENERGY, bool SURR = false, bool BONDS = true>
 __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamView& P, int gwarp,
                                               int nwarps, double* eacc, bool& bad_type)
 {
@@ -706,7 +723,7 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
     seg[0] = 0;
 #pragma unroll
     for (int q = 0; q < kNQ; ++q) cnt[q] = (int)min(ld_volatile(&a.st_rw->qcount[q]), (uint32_t)a.cap_short);
-    cnt[kNQ] = a.bonded ? a.n_bonds : 0;
+    cnt[kNQ] = (BONDS && a.bonded) ? a.n_bonds : 0;
 #pragma unroll
     for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
     const int lane = threadIdx.x & 31;
@@ -727,6 +744,36 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
         if (k >= cnt[q]) continue;
         if (q < kNQ) eval_deferred<ENERGY>(a, P, q, __ldcg(a.queue + (size_t)q * a.cap_short + k), eacc);
         else eval_bond<ENERGY>(a, P, k, n_types, eacc, bad_type, 0);
+    }
+}
+
+// Phase B of a block on its own shared-memory queues (filled by forces_a_body<.., true>
+// of the same block: no grid barrier between the phases) and its share of the bonds,
+// 32 items of one term per warp.
+template <bool ENERGY>
+__device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamView& P, double* eacc,
+                                               bool& bad_type)
+{
+    const BlockQueues& bq = block_queues();
+    const int n_types = P.h().n_types;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nb = a.bonded ? a.n_bonds : 0;
+    const int b0 = (int)((long long)nb * blockIdx.x / gridDim.x);
+    const int b1 = (int)((long long)nb * (blockIdx.x + 1) / gridDim.x);
+    int cnt[kNQ + 1], seg[kNQ + 2];
+    seg[0] = 0;
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) cnt[q] = (int)bq.count[q];
+    cnt[kNQ] = b1 - b0;
+#pragma unroll
+    for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
+    for (int wbase = w * 32; wbase < seg[kNQ + 1]; wbase += nw * 32) {
+        int q = 0;
+        while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
+        const int k = wbase - seg[q] + lane;
+        if (k >= cnt[q]) continue;
+        if (q < kNQ) eval_deferred<ENERGY>(a, P, q, bq.buf[q][k], eacc);
+        else eval_bond<ENERGY>(a, P, b0 + k, n_types, eacc, bad_type, 0);
     }
 }
 
@@ -1417,6 +1464,9 @@ __global__ void k_begin_run(DevStatus* st, unsigned long long step, uint32_t reb
         st->step = step;
         st->flags = 0u;
         st->rebuild = rebuild;
+        st->qspill = 0u;
+        st->rb[0] = 0u;
+        st->rb[1] = 0u;
     }
     if (threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
 }
@@ -1556,6 +1606,9 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 st->step = a.step0;
                 st->flags = 0u;
                 st->rebuild = 0u;
+                st->qspill = 0u;
+                st->rb[0] = 0u;
+                st->rb[1] = 0u;
             }
             if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
             const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1577,7 +1630,9 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             if (!grid_barrier(a.bar)) break;
             rebuild = a.rebuild0 != 0u || ld_volatile(&st->moved) != 0u;
         } else {
-            rebuild = ld_volatile(&st->rebuild) != 0u;
+            // rebuild requests: body 0 reads the one left by the run start or the previous
+            // launch, body b > 0 the one the step phase of body b - 1 left in rb[b & 1]
+            rebuild = ld_volatile(body == 0 ? &st->rebuild : &st->rb[body & 1]) != 0u;
         }
         if (rebuild) {
             const uint32_t par = ld_volatile(&st->gen) & 1u;
@@ -1597,11 +1652,28 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             if (rebuild) st->gen += 1u;
             if (!pro) st->step += 1ull;
         }
-        forces_a_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
-        if (!grid_barrier(a.bar)) break;
-        if (!pro && blockIdx.x == 0 && threadIdx.x == 0) st->rebuild = 0u;
-        forces_b_body<false, SURR>(a.f, P, gwarp, nwarps, eacc, bad_type);
-        if (!grid_barrier(a.bar)) break;
+        if constexpr (SURR) {
+            // the surrogate evaluates whole warps of one pair class from the global queues
+            forces_a_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+            if (!grid_barrier(a.bar)) break;
+            forces_b_body<false, SURR>(a.f, P, gwarp, nwarps, eacc, bad_type);
+            if (!grid_barrier(a.bar)) break;
+        } else {
+            // phase B on the block's own queues: a block barrier, not a grid barrier
+            forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type);
+            forces_b_local<false>(a.f, P, eacc, bad_type);
+            if (!grid_barrier(a.bar)) break;
+            if (ld_volatile(&st->qspill)) {  // pairs that did not fit a block's queues
+                forces_b_body<false, false, false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+                if (!grid_barrier(a.bar)) break;
+                if (blockIdx.x == 0 && threadIdx.x == 0) st->qspill = 0u;  // read a barrier ago
+            }
+        }
+        // every block read this body's rebuild request before the last barrier
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            if (body == 0) st->rebuild = 0u;
+            else if (body > 0) st->rb[body & 1] = 0u;
+        }
         // step two of this step (+ step one of the next); at run start a = F/m and
         // step one of the first step
         const bool last = a.closing && body == a.bodies - 1;
@@ -1634,9 +1706,17 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 bad |= b1;
             }
         }
-        if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->rebuild, 1u);
+        // the next body's rebuild request: the run start's to st->rebuild (read by body 0),
+        // body b's to rb[(b + 1) & 1] (cleared by body b - 1 after its force barrier)
+        if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(pro ? &st->rebuild : &st->rb[(body + 1) & 1], 1u);
         if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
         if (!grid_barrier(a.bar)) break;
+        if (body == a.bodies - 1 && blockIdx.x == 0 && threadIdx.x == 0) {
+            // completed: hand the pending request to the next launch (or per-step kernels)
+            st->rebuild = ld_volatile(&st->rb[a.bodies & 1]);
+            st->rb[0] = 0u;
+            st->rb[1] = 0u;
+        }
     }
     if (__syncthreads_or(bad_type) && threadIdx.x == 0) atomicOr(&st->flags, kStBadIndex);
     if (threadIdx.x == 0 && ld_volatile(&a.bar->abort)) atomicOr(&st->flags, kStBarrierTimeout);
