@@ -474,6 +474,7 @@ struct oxg_system {
     double run_kernel_ms = 0.0;
     long long run_kernel_launches = 0, run_kernel_bodies = 0;
     bool persistent = true;
+    int block_q = kBlockQ;  // phase-A per-block queue entries (OXG_BLOCK_QUEUE test hook)
     // learned surrogate of the fused HB + cross-stacking term
     const MlpDev* mlp = nullptr;
     SurrogateAudit* audit = nullptr;
@@ -585,6 +586,7 @@ ForceArgs force_args(oxg_system* s, uint32_t mask, int bonded)
     a.param_bytes = s->ctx->block_bytes;
     a.mask = mask;
     a.bonded = bonded && s->n_bonds > 0;
+    a.block_q = s->block_q;
     a.N = s->N;
     a.n_bonds = s->n_bonds;
     a.pos = s->pos;
@@ -782,6 +784,8 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
     cudaMemset(s->audit, 0, sizeof(SurrogateAudit));
     cudaMemset(s->bar, 0, sizeof(GridBarrier));
     if (const char* m = std::getenv("OXG_RUN_MODE")) s->persistent = std::string(m) != "graph";
+    // test hook: a smaller per-block queue in phase A exercises the spill path
+    if (const char* m = std::getenv("OXG_BLOCK_QUEUE")) s->block_q = std::max(0, std::min(kBlockQ, std::atoi(m)));
     if (cudaMallocHost((void**)&s->st_host, sizeof(DevStatus)) != cudaSuccess)
         return fail(set_err(OXG_ERR_CUDA, "cudaMallocHost failed"));
     cudaMemcpy(s->bonds, bnd.data(), sizeof(int4) * bnd.size(), cudaMemcpyHostToDevice);

@@ -231,6 +231,9 @@ struct ForceArgs {
     uint32_t audit_every = 0;  // steps between audits (0: never)
     uint32_t audit_mod = 100;  // one queued pair in audit_mod is audited
     float audit_tol = 0.f;     // largest accepted |E_surrogate - E_plain| of one pair
+    // entries per heavy-term queue a block keeps in shared memory in phase A (at most
+    // kBlockQ; lowered only to exercise the path of pairs that do not fit)
+    int block_q = 400;
 };
 
 // Statistics of the audits of the surrogate by the plain evaluator; `disabled` is the
@@ -372,7 +375,7 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(co
 // atomics) and copies them to the global queues at the end of the phase with one global
 // atomic per queue and block, instead of one same-address global atomic per warp, term
 // and unit. A reservation that does not fit goes to the global queue directly.
-constexpr int kBlockQ = 400;  // entries per queue and block
+constexpr int kBlockQ = 400;  // entries per queue and block (the largest ForceArgs::block_q)
 struct BlockQueues {
     uint32_t count[kNQ];  // reserved entries
     uint32_t valid[kNQ];  // entries below this offset were all written
@@ -393,9 +396,10 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
                                               int nwarps, double* eacc, bool& bad_type)
 {
     BlockQueues& bq = block_queues();
+    const uint32_t qcap = (uint32_t)min(max(a.block_q, 0), kBlockQ);
     if (threadIdx.x < kNQ) {
         bq.count[threadIdx.x] = 0u;
-        bq.valid[threadIdx.x] = (uint32_t)kBlockQ;
+        bq.valid[threadIdx.x] = qcap;
     }
     __syncthreads();
     const ParamHeader& H = P.h();
@@ -485,8 +489,8 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
                 uint32_t off = 0;
                 if (lane == leader) {
                     off = atomicAdd(&bq.count[q], n);
-                    if (off + n > (uint32_t)kBlockQ) {  // does not fit: straight to the global queue
-                        if (off < (uint32_t)kBlockQ) atomicMin(&bq.valid[q], off);
+                    if (off + n > qcap) {  // does not fit: straight to the global queue
+                        if (off < qcap) atomicMin(&bq.valid[q], off);
                         off = 0x80000000u | atomicAdd(&a.st_rw->qcount[q], n);
                         if (LOCAL) a.st_rw->qspill = 1u;
                     }

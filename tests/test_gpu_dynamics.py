@@ -75,13 +75,17 @@ def test_rna_hairpins_energies_match_oracle_and_run(native, oracle):
     assert b.stacking_energy < 0.0
 
 
-@pytest.mark.parametrize("mode", ["persistent", "graph"])
+@pytest.mark.parametrize("mode", ["persistent", "graph", "persistent-spill"])
 def test_short_trajectory_tracks_oracle(native, oracle, monkeypatch, mode):
     """Same counter-based RNG on both sides: 20 Langevin steps agree closely, on the
-    persistent run kernel and on the per-step kernels replayed from a CUDA graph."""
+    persistent run kernel, on the per-step kernels replayed from a CUDA graph, and on
+    the run kernel with its per-block phase-A queues cut to 3 pairs (the pairs that do
+    not fit go through the global queues after the force barrier)."""
     from oxdna import io
     from oxdna.model import dna1, dna2
-    monkeypatch.setenv("OXG_RUN_MODE", mode)
+    monkeypatch.setenv("OXG_RUN_MODE", mode.split("-")[0])
+    if mode.endswith("spill"):  # per-block phase-A queues of 3 pairs: most pairs spill
+        monkeypatch.setenv("OXG_BLOCK_QUEUE", "3")
     s = io.duplex_system(8, 20, 40.0, seed=1)
     kT = dna1.kT_from_temperature(296.15)
     forces, _ = dna2.forces()
