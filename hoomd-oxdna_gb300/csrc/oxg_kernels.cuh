@@ -1323,10 +1323,16 @@ __device__ __forceinline__ bool step_one_pure(PState& s, float4 ac, float4 tn, f
 // n*sqrt(2 gamma_r kT/dt) - gamma_r L/I, n standard normal; a = (F + F_bath)/m;
 // v += dt/2 a; tnet = T + R(q) T_bath; p += dt q*(0, t_body). The Philox counter is
 // (tag, step, stream) under the key (seed_lo, seed_hi).
-__device__ __forceinline__ void step_two_pure(PState& s, float4 F, float4 T, uint32_t tag,
-                                              unsigned long long step, uint32_t seed_lo,
-                                              uint32_t seed_hi, float dt, float kT, float gamma,
-                                              float gamma_r, float3 inertia, float4& ac, float4& tn)
+// The Langevin bath noise of one particle and step: translational u * sqrt(6 gamma kT/dt)
+// (u uniform in [-1, 1)) and rotational n * sqrt(2 gamma_r kT/dt) (n standard normal,
+// Box-Muller). It depends on the tag, step and seed alone, so the run kernel computes it
+// while it waits at the force barrier.
+struct LangevinNoise {
+    float3 t, r;
+};
+__device__ __forceinline__ LangevinNoise langevin_noise(uint32_t tag, unsigned long long step, uint32_t seed_lo,
+                                                        uint32_t seed_hi, float dt, float kT, float gamma,
+                                                        float gamma_r)
 {
     uint32_t r0[4] = {tag, (uint32_t)step, (uint32_t)(step >> 32), 0u};
     uint32_t r1[4] = {tag, (uint32_t)step, (uint32_t)(step >> 32), 1u};
@@ -1334,18 +1340,10 @@ __device__ __forceinline__ void step_two_pure(PState& s, float4 F, float4 T, uin
     philox4x32(r1, seed_lo, seed_hi);
     const float ct = sqrtf(6.f * gamma * kT / dt);
     const float cr = sqrtf(2.f * gamma_r * kT / dt);
-    const float minv = 1.f / s.v.w;
     const float inv31 = 1.f / 2147483648.f;
-    ac.x = (F.x + (float)(int32_t)r0[0] * inv31 * ct - gamma * s.v.x) * minv;
-    ac.y = (F.y + (float)(int32_t)r0[1] * inv31 * ct - gamma * s.v.y) * minv;
-    ac.z = (F.z + (float)(int32_t)r0[2] * inv31 * ct - gamma * s.v.z) * minv;
-    ac.w = 0.f;
-    const float4 q = s.q;
-    float4 p = s.p;
-    // s = (1/2 conj(q) p).v : body-frame angular momentum
-    const float sx = 0.5f * (q.x * p.y - p.x * q.y - (q.z * p.w - q.w * p.z));
-    const float sy = 0.5f * (q.x * p.z - p.x * q.z - (q.w * p.y - q.y * p.w));
-    const float sz = 0.5f * (q.x * p.w - p.x * q.w - (q.y * p.z - q.z * p.y));
+    LangevinNoise n;
+    n.t = mk3((float)(int32_t)r0[0] * inv31 * ct, (float)(int32_t)r0[1] * inv31 * ct,
+              (float)(int32_t)r0[2] * inv31 * ct);
     // Box-Muller on two word pairs
     const float u1 = ((float)r1[0] + 1.f) * 2.3283064365386963e-10f;
     const float u2 = (float)r1[1] * 2.3283064365386963e-10f;
@@ -1355,9 +1353,28 @@ __device__ __forceinline__ void step_two_pure(PState& s, float4 F, float4 T, uin
     float s2a, c2a, s2b, c2b;
     sincospif(2.f * u2, &s2a, &c2a);
     sincospif(2.f * u4, &s2b, &c2b);
-    const float3 bt = mk3(ra * c2a * cr - gamma_r * sx * (1.f / inertia.x),
-                          ra * s2a * cr - gamma_r * sy * (1.f / inertia.y),
-                          rb * c2b * cr - gamma_r * sz * (1.f / inertia.z));
+    n.r = mk3(ra * c2a * cr, ra * s2a * cr, rb * c2b * cr);
+    return n;
+}
+
+// Step two with the particle's bath noise n: a = (F + F_bath)/m with F_bath = n.t -
+// gamma v; tnet = T + R(q) (n.r - gamma_r L/I); v += dt/2 a; p += dt q*(0, t_body).
+__device__ __forceinline__ void step_two_noise(PState& s, float4 F, float4 T, const LangevinNoise& n, float dt,
+                                               float gamma, float gamma_r, float3 inertia, float4& ac, float4& tn)
+{
+    const float minv = 1.f / s.v.w;
+    ac.x = (F.x + n.t.x - gamma * s.v.x) * minv;
+    ac.y = (F.y + n.t.y - gamma * s.v.y) * minv;
+    ac.z = (F.z + n.t.z - gamma * s.v.z) * minv;
+    ac.w = 0.f;
+    const float4 q = s.q;
+    float4 p = s.p;
+    // s = (1/2 conj(q) p).v : body-frame angular momentum
+    const float sx = 0.5f * (q.x * p.y - p.x * q.y - (q.z * p.w - q.w * p.z));
+    const float sy = 0.5f * (q.x * p.z - p.x * q.z - (q.w * p.y - q.y * p.w));
+    const float sz = 0.5f * (q.x * p.w - p.x * q.w - (q.y * p.z - q.z * p.y));
+    const float3 bt = mk3(n.r.x - gamma_r * sx * (1.f / inertia.x), n.r.y - gamma_r * sy * (1.f / inertia.y),
+                          n.r.z - gamma_r * sz * (1.f / inertia.z));
     const Frame fq = quat_frame(q);
     const float3 btl = fq.a1 * bt.x + fq.a2 * bt.y + fq.a3 * bt.z;
     tn = make_float4(T.x + btl.x, T.y + btl.y, T.z + btl.z, 0.f);
@@ -1371,6 +1388,15 @@ __device__ __forceinline__ void step_two_pure(PState& s, float4 F, float4 T, uin
     p.z += dt * dq.z;
     p.w += dt * dq.w;
     s.p = p;
+}
+
+__device__ __forceinline__ void step_two_pure(PState& s, float4 F, float4 T, uint32_t tag,
+                                              unsigned long long step, uint32_t seed_lo,
+                                              uint32_t seed_hi, float dt, float kT, float gamma,
+                                              float gamma_r, float3 inertia, float4& ac, float4& tn)
+{
+    const LangevinNoise n = langevin_noise(tag, step, seed_lo, seed_hi, dt, kT, gamma, gamma_r);
+    step_two_noise(s, F, T, n, dt, gamma, gamma_r, inertia, ac, tn);
 }
 
 __device__ __forceinline__ PState load_pstate(const IntegArgs& a, int i)
@@ -1528,21 +1554,28 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p)
     return v;
 }
 
-// Arrive-and-wait over all blocks of the launch. Block 0 adds 2^31 - (blocks - 1),
-// every other block 1, so bit 31 of the counter flips exactly when the last block
-// arrives (and the counter needs no reset). The arrival is a release and the polls are
-// acquires (after the block's __syncthreads), so every write before the barrier is
-// visible to every read after it. Returns false if the wait gave up (after
-// kBarrierSpinLimit polls) or another block did; the caller must then return.
-__device__ __forceinline__ bool grid_barrier(GridBarrier* gb)
+// Arrive at the grid barrier (the whole block); the returned token (thread 0) is the
+// counter before this block's arrival. Work that does not depend on the other blocks
+// may run between grid_arrive and grid_wait.
+__device__ __forceinline__ uint32_t grid_arrive(GridBarrier* gb)
+{
+    __syncthreads();
+    uint32_t old = 0u;
+    if (threadIdx.x == 0) {
+        const uint32_t add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(&gb->arrive), "r"(add) : "memory");
+    }
+    return old;
+}
+
+// Wait until every block has arrived (bit 31 of the counter differs from the token's).
+// Returns false if the wait gave up (after kBarrierSpinLimit polls) or another block
+// did; the caller must then return.
+__device__ __forceinline__ bool grid_wait(GridBarrier* gb, uint32_t old)
 {
     __shared__ int bar_ok;
-    __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        const uint32_t add = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
-        uint32_t old;
-        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(&gb->arrive), "r"(add) : "memory");
         long long polls = 0;
         while (((old ^ ld_acquire(&gb->arrive)) & 0x80000000u) == 0u) {
             if ((++polls & 63) == 0) {  // the abort word and the limit every 64 polls
@@ -1561,6 +1594,16 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier* gb)
     }
     __syncthreads();
     return bar_ok != 0;
+}
+
+// Arrive-and-wait over all blocks of the launch. Block 0 adds 2^31 - (blocks - 1),
+// every other block 1, so bit 31 of the counter flips exactly when the last block
+// arrives (and the counter needs no reset). The arrival is a release and the polls are
+// acquires (after the block's __syncthreads), so every write before the barrier is
+// visible to every read after it.
+__device__ __forceinline__ bool grid_barrier(GridBarrier* gb)
+{
+    return grid_wait(gb, grid_arrive(gb));
 }
 
 struct RunArgs {
@@ -1602,6 +1645,8 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     const int gthread = gwarp * 32 + lane, nthreads = nwarps * 32;
     double eacc[kNTerms + 3];  // unused: MD steps evaluate no energies
     bool bad_type = false;
+    // the RNG step of body b is step_base + b + 1 (block 0 advances st->step to match)
+    const unsigned long long step_base = a.prologue ? a.step0 : *(const volatile unsigned long long*)&st->step;
     for (int body = a.prologue ? -1 : 0; body < a.bodies; ++body) {
         const bool pro = body < 0;
         bool rebuild;
@@ -1656,17 +1701,30 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             if (rebuild) st->gen += 1u;
             if (!pro) st->step += 1ull;
         }
+        // this thread's first particle's bath noise for step two, computed between its
+        // block's arrival at the force barrier and the barrier's release
+        const unsigned long long step = step_base + (unsigned long long)(body + 1);
+        LangevinNoise nz;
+        const bool have_nz = !pro && gthread < a.g.N;
         if constexpr (SURR) {
             // the surrogate evaluates whole warps of one pair class from the global queues
             forces_a_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
             if (!grid_barrier(a.bar)) break;
             forces_b_body<false, SURR>(a.f, P, gwarp, nwarps, eacc, bad_type);
-            if (!grid_barrier(a.bar)) break;
+            const uint32_t tok = grid_arrive(a.bar);
+            if (have_nz)
+                nz = langevin_noise((uint32_t)gthread, step, a.g.seed_lo, a.g.seed_hi, a.g.dt, a.g.kT, a.g.gamma,
+                                    a.g.gamma_r);
+            if (!grid_wait(a.bar, tok)) break;
         } else {
             // phase B on the block's own queues: a block barrier, not a grid barrier
             forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type);
             forces_b_local<false>(a.f, P, eacc, bad_type);
-            if (!grid_barrier(a.bar)) break;
+            const uint32_t tok = grid_arrive(a.bar);
+            if (have_nz)
+                nz = langevin_noise((uint32_t)gthread, step, a.g.seed_lo, a.g.seed_hi, a.g.dt, a.g.kT, a.g.gamma,
+                                    a.g.gamma_r);
+            if (!grid_wait(a.bar, tok)) break;
             if (ld_volatile(&st->qspill)) {  // pairs that did not fit a block's queues
                 forces_b_body<false, false, false>(a.f, P, gwarp, nwarps, eacc, bad_type);
                 if (!grid_barrier(a.bar)) break;
@@ -1681,7 +1739,6 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         // step two of this step (+ step one of the next); at run start a = F/m and
         // step one of the first step
         const bool last = a.closing && body == a.bodies - 1;
-        const unsigned long long step = *(const volatile unsigned long long*)&st->step;
         if (blockIdx.x == 0) {
             if (threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
             if (pro && threadIdx.x == 32) st->moved = 0u;  // read two barriers ago
@@ -1695,6 +1752,9 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 const float minv = 1.f / s.v.w;
                 ac = make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f);
                 tn = make_float4(T.x, T.y, T.z, 0.f);
+            } else if (have_nz && i == gthread) {
+                step_two_noise(s, __ldcg(a.g.force + i), __ldcg(a.g.torque + i), nz, a.g.dt, a.g.gamma,
+                               a.g.gamma_r, a.g.inertia, ac, tn);
             } else {
                 particle_step_two(a.g, i, step, s, ac, tn);
             }
