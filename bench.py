@@ -433,19 +433,31 @@ def run_ours(args):
     hp, hl, hq, hv, ha = pin(), pin(), pin(), pin(), pin()
     sim.pull_state_arrays(hp, hl, hq, hv, ha)
     e2e_steps = max(20, min(200, args.steps // 50))
+    for _ in range(3):  # warm-up of the call sequence
+        sim.run_state_arrays(1, hp, hl, hq, hv, ha)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        sim.push_state_arrays(hp, hl, hq, hv, ha)   # H2D: this step's inputs
-        sim.run(1)
-        sim.pull_state_arrays(hp, hl, hq, hv, ha)   # D2H: this step's result
+        # H2D: this step's inputs, one MD step, D2H: this step's result, in one call
+        sim.run_state_arrays(1, hp, hl, hq, hv, ha)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = replicas.max_over_ranks(e2e_s, dist)
+    # the same through three calls (state push, run, state pull)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.push_state_arrays(hp, hl, hq, hv, ha)
+        sim.run(1)
+        sim.pull_state_arrays(hp, hl, hq, hv, ha)
+    torch.cuda.synchronize()
+    e2e3_s = replicas.max_over_ranks(time.perf_counter() - t0, dist)
     e2e = {"value": world * e2e_steps / e2e_s, "unit": "steps/s",
            "h2d_bytes_per_step": 5 * 16 * n, "d2h_bytes_per_step": 5 * 16 * n,
-           "path": "Simulation.push_state_arrays -> run(1) -> pull_state_arrays "
-                   "(oxg_system_set_state / oxg_system_run / oxg_system_get_state)"}
+           "path": "Simulation.run_state_arrays(1, pinned host arrays) (oxg_system_run_host: a copy "
+                   "kernel reads the host state, the run kernel steps, a copy kernel writes it back)",
+           "three_calls_steps_per_s": world * e2e_steps / e2e3_s,
+           "three_calls_path": "push_state_arrays -> run(1) -> pull_state_arrays"}
 
     # --- CPU baseline (rank 0, N = 1 only) --------------------------------------
     cb = None

@@ -1104,6 +1104,22 @@ static int checkpoint(oxg_system* s, bool restore)
     return OXG_OK;
 }
 
+// Host-driven runs: the five state arrays between the device and mapped page-locked host
+// arrays (device aliases) in one kernel on the system's stream.
+static int copy_state_async(oxg_system* s, float4* const* host, bool to_device)
+{
+    StateCopy c;
+    c.N = s->N;
+    float4* const dev[5] = {s->pos, s->pos_lo, s->quat, s->vel, s->angmom};
+    for (int k = 0; k < 5; ++k) {
+        c.src[k] = to_device ? host[k] : dev[k];
+        c.dst[k] = to_device ? dev[k] : host[k];
+    }
+    k_state_copy<<<(s->N + 255) / 256, 256, 0, s->stream>>>(c);
+    OXG_CUDA(cudaGetLastError());
+    return OXG_OK;
+}
+
 // The persistent run kernel: one cooperative launch of `bodies` step bodies, preceded
 // by the run start (prepRun) when `prologue` (see k_run).
 static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = false,
@@ -1150,7 +1166,8 @@ static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = f
 // itself) and is followed by the one host synchronisation of the chunk (the status
 // read); after a neighbour-list overflow the lists grow and the chunk (with its
 // prepRun, for the first) is replayed.
-static int run_persistent(oxg_system* s, long nsteps)
+static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin = nullptr,
+                          float4* const* hout = nullptr)
 {
     const int chunk = 2000;
     long done = 0;
@@ -1160,6 +1177,7 @@ static int run_persistent(oxg_system* s, long nsteps)
         OXG_CUDA(cudaEventCreate(&s->ev_run[0]));
         OXG_CUDA(cudaEventCreate(&s->ev_run[1]));
     }
+    if (hin && (rc = copy_state_async(s, const_cast<float4* const*>(hin), true))) return rc;
     while (done < nsteps) {
         const int todo = (int)std::min<long>(chunk, nsteps - done);
         const bool closing = done + todo == nsteps;
@@ -1170,6 +1188,7 @@ static int run_persistent(oxg_system* s, long nsteps)
         if (!first && (rc = checkpoint(s, false))) return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[0], s->stream));
         if ((rc = launch_run(s, todo, closing, first, step0, !s->lists_valid))) return rc;
+        if (closing && hout && (rc = copy_state_async(s, hout, false))) return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
         if ((rc = read_status(s, &d))) return rc;
         float ms = 0.f;
@@ -1224,6 +1243,16 @@ static int prep_run(oxg_system* s)
     k_prep_accel<<<(s->N + 255) / 256, 256, 0, s->stream>>>(ia);
     OXG_CUDA(cudaGetLastError());
     return OXG_OK;
+}
+
+// device aliases of mapped page-locked host arrays (all or none); see state_transfer
+static bool mapped_state(const float* const host[5], float4* dev[5])
+{
+    for (int k = 0; k < 5; ++k) {
+        dev[k] = static_cast<float4*>(const_cast<void*>(mapped_alias(host[k])));
+        if (!dev[k]) return false;
+    }
+    return true;
 }
 
 int oxg_system_run(oxg_system* s, long nsteps)
@@ -1413,6 +1442,37 @@ int oxg_system_hbx_samples(oxg_system* s, int max_n, float* feats, float* energy
     cudaStreamSynchronize(s->stream);
     dfree(counter);
     return rc;
+}
+
+int oxg_system_run_host(oxg_system* s, long nsteps, float* pos_type, float* pos_lo, float* quat, float* vel,
+                        float* angmom)
+{
+    if (!s || nsteps < 1 || !pos_type || !pos_lo || !quat || !vel || !angmom)
+        return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (!s->integ_set) return set_err(OXG_ERR_INVALID_ARG, "integrator not set");
+    for (int i = 0; i < s->N; ++i) {
+        int t;
+        std::memcpy(&t, pos_type + 4 * (size_t)i + 3, sizeof(int));
+        if (t < 0 || t >= s->ctx->n_types)
+            return set_err(OXG_ERR_BAD_INDEX, "particle " + std::to_string(i) + " has type " +
+                                                  std::to_string(t) + " outside the context's types");
+    }
+    const float* const host[5] = {pos_type, pos_lo, quat, vel, angmom};
+    float4* dev[5];
+    int rc;
+    if (!s->persistent || !mapped_state(host, dev)) {  // per-call transfers
+        if ((rc = oxg_system_set_state(s, pos_type, pos_lo, quat, vel, angmom, nullptr))) return rc;
+        if ((rc = oxg_system_run(s, nsteps))) return rc;
+        return oxg_system_get_state(s, pos_type, pos_lo, quat, vel, angmom);
+    }
+    for (int t = 0; t < s->ctx->n_bond_types && s->run_bonded; ++t)
+        if (!s->ctx->bonded_set[t]) return set_err(OXG_ERR_NO_PARAMS, "bond type without parameters");
+    if ((rc = sys_setup_nlist(s, s->run_mask, false))) return rc;
+    // copy kernels move the state from the host arrays before the run launch and back
+    // after it, all on the stream, then one synchronisation
+    if ((rc = run_persistent(s, nsteps, dev, dev))) return rc;
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    return OXG_OK;
 }
 
 int oxg_system_run_timing(oxg_system* s, double* out, int n, int reset)

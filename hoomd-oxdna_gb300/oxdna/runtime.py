@@ -333,6 +333,23 @@ class Simulation:
         _abi.check(L.oxg_system_set_state(self._sys, ptr(pos_type), ptr(pos_lo), ptr(quat),
                                           ptr(vel), ptr(angmom), None), "oxg_system_set_state")
 
+    def run_state_arrays(self, steps, pos_type, pos_lo, quat, vel, angmom):
+        """push_state_arrays + run(steps) + pull_state_arrays in one call: the state is
+        read from the host float32 (N, 4) arrays and the final state written back into
+        them. With page-locked arrays (torch ``pin_memory()``) a copy kernel on each side
+        of the run launch moves the state over the host link: one synchronisation per
+        call."""
+        self._attach()
+        self._cache = {}
+        L = _abi.lib()
+        steps = int(steps)
+        if steps < 1 or self._langevin is None:
+            raise ValueError("run_state_arrays needs steps >= 1 and a Langevin method")
+        ptr = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
+        _abi.check(L.oxg_system_run_host(self._sys, steps, ptr(pos_type), ptr(pos_lo), ptr(quat),
+                                         ptr(vel), ptr(angmom)), "oxg_system_run_host")
+        self.timestep += steps
+
     def pull_state_arrays(self, pos_type, pos_lo, quat, vel, angmom):
         """Copy the device state into host float32 (N, 4) arrays."""
         L = _abi.lib()

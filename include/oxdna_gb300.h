@@ -261,6 +261,15 @@ int oxg_system_set_integrator(oxg_system* sys, double dt, double kT, double gamm
                               int bonded);
 /* Advance nsteps steps. Steps are replayed from a captured CUDA graph. */
 int oxg_system_run(oxg_system* sys, long nsteps);
+/* One call for host-driven loops: load the state from the host arrays (pos_type,
+ * pos_lo, quat, vel, angmom: float[4*N] each, as oxg_system_set_state), run nsteps >= 1
+ * steps, and write the final state back into the same arrays. With page-locked, mapped
+ * host arrays (cudaHostAlloc, torch pin_memory) on the persistent run kernel, one copy
+ * kernel on each side of the run launch reads and writes the host arrays directly (one
+ * synchronisation per call); otherwise set_state, run and get_state. No counterpart in
+ * the reference (HOOMD keeps the state on the device between calls). */
+int oxg_system_run_host(oxg_system* sys, long nsteps, float* pos_type, float* pos_lo, float* quat,
+                        float* vel, float* angmom);
 /* Per-term energies at the current state (device reduction, FP64) into host arrays. */
 int oxg_system_energies(oxg_system* sys, double* pair_energy, double* bonded_energy);
 /* Counters: index 0 steps run, 1 neighbour-list builds, 2 pair-list entries (short),

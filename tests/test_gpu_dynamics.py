@@ -201,3 +201,48 @@ def test_state_push_pull_pinned_and_pageable(native):
     for a, b in zip(*out):
         assert np.allclose(a, b, rtol=1e-5, atol=1e-5)
     assert not np.array_equal(out[0][0], pinned[0])
+
+
+@pytest.mark.parametrize("memory", ["pinned", "pageable"])
+def test_run_state_arrays_matches_push_run_pull(native, memory):
+    """oxg_system_run_host (one call: state in, n steps, state out) against
+    push_state_arrays + run + pull_state_arrays on a twin system (same seed and
+    timestep): with page-locked arrays copy kernels on either side of the run launch
+    move the state, with pageable arrays the call falls back to the three steps."""
+    import torch
+    from oxdna import io
+    from oxdna.model import dna1, dna2
+    s = io.duplex_system(8, 20, 40.0, seed=4)
+    forces, _ = dna2.forces()
+    kT = dna1.kT_from_temperature(296.15)
+    a = _sim(io.system_snapshot(s), forces, dt=0.003, kT=kT, seed=9)
+    b = _sim(io.system_snapshot(s), forces, dt=0.003, kT=kT, seed=9)
+    a.run(5)
+    b.run(5)
+    n = len(s["pos"])
+    if memory == "pinned":
+        alloc = lambda: torch.zeros((n, 4), dtype=torch.float32).pin_memory().numpy()  # noqa: E731
+    else:
+        alloc = lambda: np.zeros((n, 4), np.float32)  # noqa: E731
+    st_a = [alloc() for _ in range(5)]
+    a.pull_state_arrays(*st_a)
+    rng = np.random.Generator(np.random.PCG64(2))
+    st_a[3][:, :3] += rng.normal(0, 0.05, (n, 3)).astype(np.float32)  # a host-side change
+    st_b = [x.copy() for x in st_a]
+    for _ in range(3):
+        a.run_state_arrays(4, *st_a)
+        b.push_state_arrays(*st_b)
+        b.run(4)
+        b.pull_state_arrays(*st_b)
+    assert a.timestep == b.timestep
+    for x, y in zip(st_a, st_b):
+        assert np.allclose(x, y, rtol=1e-5, atol=1e-5)
+    # the device state is the returned state: a plain run continues from it
+    a.run(2)
+    b.run(2)
+    pa = [np.zeros((n, 4), np.float32) for _ in range(5)]
+    pb = [np.zeros((n, 4), np.float32) for _ in range(5)]
+    a.pull_state_arrays(*pa)
+    b.pull_state_arrays(*pb)
+    for x, y in zip(pa, pb):
+        assert np.allclose(x, y, rtol=1e-5, atol=1e-5)
