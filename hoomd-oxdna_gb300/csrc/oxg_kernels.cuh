@@ -1623,10 +1623,13 @@ struct RunArgs {
 
 
 #ifndef OXG_DEVICE_FUNCTIONS_ONLY
-// Each body: [neighbour-list rebuild if flagged: bin | pairs] | forces part one |
-// forces part two | step two + step one of the next step. The rebuild flag is read by
-// every block right after a barrier and cleared one barrier later; a list overflow
-// ends the launch (the host grows the lists and replays from its checkpoint).
+// Each body: [neighbour-list rebuild if flagged: bin | pairs] | forces: each block's
+// phase A, then (a block barrier) its phase B on the pairs it queued and its slice of
+// the bonds [| pairs that did not fit a block's queues, by every block] | step two +
+// step one of the next step. Grid barriers separate the brackets. A body's rebuild
+// request is read by every block before the force barrier and cleared after it (the
+// requests alternate between two words by body parity); a list overflow ends the
+// launch (the host grows the lists and replays from its checkpoint).
 //
 // The first launch of a run() call starts with the run start as body -1 (HOOMD's
 // prepRun): reset the step counter, flags and queues, checkpoint the state for a
