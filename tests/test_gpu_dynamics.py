@@ -246,3 +246,27 @@ def test_run_state_arrays_matches_push_run_pull(native, memory):
     b.pull_state_arrays(*pb)
     for x, y in zip(pa, pb):
         assert np.allclose(x, y, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_run_kernel_forces_match_oracle(native, oracle, fused):
+    """The run kernel's own force evaluation (the run start's and the step's: phase A and
+    the block-local phase B) checked through one noiseless Langevin step of the 8000-nt
+    system: with kT = 0 the velocity and angular momentum after the step are
+    deterministic sums of the forces and torques of the start and end positions, so they
+    match the FP64 oracle's step to FP32 rounding."""
+    from oxdna import io
+    from oxdna.model import dna2
+    s = io.duplex_system(200, 20, 100.0, seed=2)
+    forces, _ = dna2.forces(fused=fused)
+    sim = _sim(io.system_snapshot(s), forces, dt=0.003, kT=0.0, seed=3)
+    sim.run(1)
+    snap = sim.state.get_snapshot()
+    model = oracle.Model(forces, io.DNA_BASES)
+    o = oracle.System(s["pos"], s["quat"], s["typeid"], s["box"], s["bonds"])
+    n = len(s["pos"])
+    import os
+    _, vel, am = oracle.langevin(model, o, np.zeros((n, 3)), np.zeros((n, 4)), steps=1, dt=0.003,
+                                 kT=0.0, seed=3, threads=os.cpu_count())
+    assert maxrel(snap.particles.velocity, vel) < 1e-4
+    assert maxrel(snap.particles.angmom, am) < 1e-4
