@@ -630,7 +630,7 @@ __device__ __forceinline__ bool audit_pick(int k, unsigned long long step, uint3
 // torques from the gradient. On audit steps a hashed 1 / audit_mod of the pairs is also
 // evaluated by the plain evaluator.
 template <bool ENERGY>
-__device__ __noinline__ void surrogate_segment(const ForceArgs& a, const ParamView& P, int q, int kbase,
+__device__ __noinline__ void surrogate_segment(const int2* qbuf, const ForceArgs& a, const ParamView& P, int q, int kbase,
                                                int cnt, double* eacc)
 {
     const int lane = threadIdx.x & 31;
@@ -652,7 +652,7 @@ __device__ __noinline__ void surrogate_segment(const ForceArgs& a, const ParamVi
         for (int f = 0; f < kMlpIn; ++f) x[f] = 0.f;
         if (valid) {
             bool bad = false;
-            valid = load_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad);
+            valid = load_pair(a, qbuf[k], H.n_types, p, bad);
             if (valid) {
                 fi = quat_frame(p.qi);
                 fj = quat_frame(p.qj);
@@ -740,7 +740,7 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
         while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
         if constexpr (SURR) {
             if (surrogate && (q == kQHBX || q == kQHBX0)) {
-                surrogate_segment<ENERGY>(a, P, q, wbase - seg[q], cnt[q], eacc);
+                surrogate_segment<ENERGY>(a.queue + (size_t)q * a.cap_short, a, P, q, wbase - seg[q], cnt[q], eacc);
                 continue;
             }
         }
@@ -754,11 +754,13 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
 // Phase B of a block on its own shared-memory queues (filled by forces_a_body<.., true>
 // of the same block: no grid barrier between the phases) and its share of the bonds,
 // 32 items of one term per warp.
-template <bool ENERGY>
+template <bool ENERGY, bool SURR = false>
 __device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamView& P, double* eacc,
                                                bool& bad_type)
 {
-    const BlockQueues& bq = block_queues();
+    BlockQueues& bq = block_queues();
+    bool surrogate = false;  // the surrogate takes whole warps of one pair class
+    if constexpr (SURR) surrogate = a.mlp != nullptr && __shfl_sync(0xffffffffu, ld_volatile(&a.audit->disabled), 0) == 0u;
     const int n_types = P.h().n_types;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nb = a.bonded ? a.n_bonds : 0;
@@ -774,6 +776,12 @@ __device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamVi
     for (int wbase = w * 32; wbase < seg[kNQ + 1]; wbase += nw * 32) {
         int q = 0;
         while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
+        if constexpr (SURR) {
+            if (surrogate && (q == kQHBX || q == kQHBX0)) {
+                surrogate_segment<ENERGY>(bq.buf[q], a, P, q, wbase - seg[q], cnt[q], eacc);
+                continue;
+            }
+        }
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
         if (q < kNQ) eval_deferred<ENERGY>(a, P, q, bq.buf[q][k], eacc);
@@ -1709,27 +1717,17 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         const unsigned long long step = step_base + (unsigned long long)(body + 1);
         LangevinNoise nz;
         const bool have_nz = !pro && gthread < a.g.N;
-        if constexpr (SURR) {
-            // the surrogate evaluates whole warps of one pair class from the global queues
-            forces_a_body<false>(a.f, P, gwarp, nwarps, eacc, bad_type);
-            if (!grid_barrier(a.bar)) break;
-            forces_b_body<false, SURR>(a.f, P, gwarp, nwarps, eacc, bad_type);
-            const uint32_t tok = grid_arrive(a.bar);
-            if (have_nz)
-                nz = langevin_noise((uint32_t)gthread, step, a.g.seed_lo, a.g.seed_hi, a.g.dt, a.g.kT, a.g.gamma,
-                                    a.g.gamma_r);
-            if (!grid_wait(a.bar, tok)) break;
-        } else {
+        {
             // phase B on the block's own queues: a block barrier, not a grid barrier
             forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type);
-            forces_b_local<false>(a.f, P, eacc, bad_type);
+            forces_b_local<false, SURR>(a.f, P, eacc, bad_type);
             const uint32_t tok = grid_arrive(a.bar);
             if (have_nz)
                 nz = langevin_noise((uint32_t)gthread, step, a.g.seed_lo, a.g.seed_hi, a.g.dt, a.g.kT, a.g.gamma,
                                     a.g.gamma_r);
             if (!grid_wait(a.bar, tok)) break;
             if (ld_volatile(&st->qspill)) {  // pairs that did not fit a block's queues
-                forces_b_body<false, false, false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+                forces_b_body<false, SURR, false>(a.f, P, gwarp, nwarps, eacc, bad_type);
                 if (!grid_barrier(a.bar)) break;
                 if (blockIdx.x == 0 && threadIdx.x == 0) st->qspill = 0u;  // read a barrier ago
             }
