@@ -495,7 +495,7 @@ def run_ours(args):
         # set is loaded into L2 once per launch and then stays there, so the launch's
         # DRAM traffic does not grow with its steps.
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": 2.575e6,
+                     "frac": achieved / hbm, "traffic": 2.273e6,
                      "traffic_note": "DRAM bytes per launch (ncu); algorithmic bytes are "
                                      "per step and are served from L2",
                      "peak_kind": peak_kind,
