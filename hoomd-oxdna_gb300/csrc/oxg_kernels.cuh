@@ -391,9 +391,12 @@ __device__ __forceinline__ BlockQueues& block_queues()
 
 // LOCAL: the block's heavy-term pairs stay in its shared-memory queues for
 // forces_b_local (the run kernel); otherwise they are copied to the global queues.
+// n_short_known / n_long_known: the stored pair counts when the caller has them (the run
+// kernel keeps them between rebuilds), else negative: read from the status block.
 template <bool ENERGY, bool LOCAL = false>
 __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamView& P, int gwarp,
-                                              int nwarps, double* eacc, bool& bad_type)
+                                              int nwarps, double* eacc, bool& bad_type,
+                                              int n_short_known = -1, int n_long_known = -1)
 {
     BlockQueues& bq = block_queues();
     const uint32_t qcap = (uint32_t)min(max(a.block_q, 0), kBlockQ);
@@ -404,8 +407,10 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
     __syncthreads();
     const ParamHeader& H = P.h();
     // after an overflow the counters exceed the capacities; only stored pairs are read
-    const int n_short = (int)min(ld_volatile(&a.st_rw->n_short), (uint32_t)a.cap_short);
-    const int n_long = (int)min(ld_volatile(&a.st_rw->n_long), (uint32_t)a.cap_long);
+    const int n_short = n_short_known >= 0 ? n_short_known
+                                           : (int)min(ld_volatile(&a.st_rw->n_short), (uint32_t)a.cap_short);
+    const int n_long = n_long_known >= 0 ? n_long_known
+                                         : (int)min(ld_volatile(&a.st_rw->n_long), (uint32_t)a.cap_long);
     const int n_types = H.n_types;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -1658,6 +1663,8 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     bool bad_type = false;
     // the RNG step of body b is step_base + b + 1 (block 0 advances st->step to match)
     const unsigned long long step_base = a.prologue ? a.step0 : *(const volatile unsigned long long*)&st->step;
+    // the stored pair counts, read once after each list build (they change only there)
+    int ns_known = -1, nl_known = -1;
     for (int body = a.prologue ? -1 : 0; body < a.bodies; ++body) {
         const bool pro = body < 0;
         bool rebuild;
@@ -1708,6 +1715,10 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             if (!grid_barrier(a.bar)) break;
             if (ld_volatile(&st->flags) & (kStCellOverflow | kStPairOverflow)) break;
         }
+        if (rebuild || ns_known < 0) {
+            ns_known = (int)min(ld_volatile(&st->n_short), (uint32_t)a.f.cap_short);
+            nl_known = (int)min(ld_volatile(&st->n_long), (uint32_t)a.f.cap_long);
+        }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             if (rebuild) st->gen += 1u;
             if (!pro) st->step += 1ull;
@@ -1719,7 +1730,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         const bool have_nz = !pro && gthread < a.g.N;
         {
             // phase B on the block's own queues: a block barrier, not a grid barrier
-            forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type);
+            forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type, ns_known, nl_known);
             forces_b_local<false, SURR>(a.f, P, eacc, bad_type);
             const uint32_t tok = grid_arrive(a.bar);
             if (have_nz)
