@@ -259,7 +259,11 @@ int oxg_system_compute(oxg_system* sys, uint32_t term_mask, int bonded,
 int oxg_system_set_integrator(oxg_system* sys, double dt, double kT, double gamma,
                               double gamma_r, uint64_t seed, uint32_t term_mask,
                               int bonded);
-/* Advance nsteps steps. Steps are replayed from a captured CUDA graph. */
+/* Advance nsteps steps (HOOMD run(): forces of the current state first, as prepRun).
+ * By default one cooperative launch of the persistent run kernel per 2000 steps, one
+ * synchronisation per launch; with OXG_RUN_MODE=graph in the environment at system
+ * creation, per-step kernels replayed from captured CUDA graphs. On a neighbour-list
+ * overflow the lists grow and the launch is replayed from its checkpoint. */
 int oxg_system_run(oxg_system* sys, long nsteps);
 /* One call for host-driven loops: load the state from the host arrays (pos_type,
  * pos_lo, quat, vel, angmom: float[4*N] each, as oxg_system_set_state), run nsteps >= 1
