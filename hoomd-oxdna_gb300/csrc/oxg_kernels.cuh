@@ -688,10 +688,9 @@ __device__ __noinline__ void surrogate_segment(const int2* qbuf, const ForceArgs
 
 // One bond (part: 0 whole, 1 FENE + bonded excluded volume, 2 stacking).
 template <bool ENERGY>
-__device__ __forceinline__ void eval_bond(const ForceArgs& a, const ParamView& P, int k, int n_types,
+__device__ __forceinline__ void eval_bond(const ForceArgs& a, const ParamView& P, int4 bd, int n_types,
                                           double* eacc, bool& bad_type, int part)
 {
-    const int4 bd = a.bonds[k];
     const int A = bd.x, B = bd.y;
     const float4 pA = __ldcg(a.pos + A), pB = __ldcg(a.pos + B);
     if ((unsigned)type_of(pA) >= (unsigned)n_types || (unsigned)type_of(pB) >= (unsigned)n_types) {
@@ -752,16 +751,18 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
         if (q < kNQ) eval_deferred<ENERGY>(a, P, q, __ldcg(a.queue + (size_t)q * a.cap_short + k), eacc);
-        else eval_bond<ENERGY>(a, P, k, n_types, eacc, bad_type, 0);
+        else eval_bond<ENERGY>(a, P, a.bonds[k], n_types, eacc, bad_type, 0);
     }
 }
 
 // Phase B of a block on its own shared-memory queues (filled by forces_a_body<.., true>
 // of the same block: no grid barrier between the phases) and its share of the bonds,
 // 32 items of one term per warp.
+// bond_stage: the block's slice of the bonds in shared memory (or null: read the global
+// table). The slice is [n_bonds * block / grid, n_bonds * (block + 1) / grid).
 template <bool ENERGY, bool SURR = false>
 __device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamView& P, double* eacc,
-                                               bool& bad_type)
+                                               bool& bad_type, const int4* bond_stage = nullptr)
 {
     BlockQueues& bq = block_queues();
     bool surrogate = false;  // the surrogate takes whole warps of one pair class
@@ -790,7 +791,7 @@ __device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamVi
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
         if (q < kNQ) eval_deferred<ENERGY>(a, P, q, bq.buf[q][k], eacc);
-        else eval_bond<ENERGY>(a, P, b0 + k, n_types, eacc, bad_type, 0);
+        else eval_bond<ENERGY>(a, P, bond_stage ? bond_stage[k] : a.bonds[b0 + k], n_types, eacc, bad_type, 0);
     }
 }
 
@@ -1650,6 +1651,7 @@ struct RunArgs {
 // build | [rebuild if the lists are new or a particle moved half the buffer] | forces
 // of the current state, no step advance | a = F/m and step one of the first step.
 constexpr int kRunThreads = OXG_RUN_THREADS;  // threads per block of the run kernel
+constexpr int kBondStage = 512;               // bonds a block stages in shared memory
 template <bool SURR>
 __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunArgs a)
 {
@@ -1665,6 +1667,18 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     const unsigned long long step_base = a.prologue ? a.step0 : *(const volatile unsigned long long*)&st->step;
     // the stored pair counts, read once after each list build (they change only there)
     int ns_known = -1, nl_known = -1;
+    // the block's slice of the (constant) bond table, staged once per launch when it fits
+    __shared__ int4 bond_stage[kBondStage];
+    const int4* bonds_here = nullptr;
+    {
+        const int nb = a.f.bonded ? a.f.n_bonds : 0;
+        const int bb0 = (int)((long long)nb * blockIdx.x / gridDim.x);
+        const int bb1 = (int)((long long)nb * (blockIdx.x + 1) / gridDim.x);
+        if (bb1 - bb0 <= kBondStage) {
+            for (int k = threadIdx.x; k < bb1 - bb0; k += blockDim.x) bond_stage[k] = a.f.bonds[bb0 + k];
+            bonds_here = bond_stage;  // read after phase A's first block barrier
+        }
+    }
     for (int body = a.prologue ? -1 : 0; body < a.bodies; ++body) {
         const bool pro = body < 0;
         bool rebuild;
@@ -1731,7 +1745,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         {
             // phase B on the block's own queues: a block barrier, not a grid barrier
             forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type, ns_known, nl_known);
-            forces_b_local<false, SURR>(a.f, P, eacc, bad_type);
+            forces_b_local<false, SURR>(a.f, P, eacc, bad_type, bonds_here);
             const uint32_t tok = grid_arrive(a.bar);
             if (have_nz)
                 nz = langevin_noise((uint32_t)gthread, step, a.g.seed_lo, a.g.seed_hi, a.g.dt, a.g.kT, a.g.gamma,
