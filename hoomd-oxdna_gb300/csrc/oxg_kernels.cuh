@@ -371,6 +371,18 @@ __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(co
 // Warp `gwarp` of `nwarps`: short-range pairs in units of 32 (cheap terms inline, heavy
 // ones queued), then the long-range pairs. Counters are read with volatile loads: the
 // persistent run kernel calls this after a neighbour-list rebuild in the same launch.
+// The long-pair units of warp gwarp: v0, v0 + vstride, ... When the short units leave
+// warps free (small systems) the long units go to those warps only (a short unit costs
+// about as much as three or four long ones); otherwise round-robin over all warps.
+__device__ __forceinline__ void long_units(int gwarp, int nwarps, int n_short, int n_long, int& v0, int& vstride)
+{
+    const int n_su = (n_short + 31) >> 5, n_lu = (n_long + 31) >> 5;
+    const int free_w = nwarps - n_su;
+    const bool to_free = free_w > 0 && 4 * free_w >= n_lu;
+    v0 = to_free ? gwarp - n_su : gwarp;
+    vstride = to_free ? free_w : nwarps;
+}
+
 // Phase A appends the heavy-term pairs of a block to shared-memory queues (shared
 // atomics) and copies them to the global queues at the end of the phase with one global
 // atomic per queue and block, instead of one same-address global atomic per warp, term
@@ -393,10 +405,13 @@ __device__ __forceinline__ BlockQueues& block_queues()
 // forces_b_local (the run kernel); otherwise they are copied to the global queues.
 // n_short_known / n_long_known: the stored pair counts when the caller has them (the run
 // kernel keeps them between rebuilds), else negative: read from the status block.
+// first: this thread's first short- and long-pair entries when the caller keeps them
+// (with the counts), else null.
 template <bool ENERGY, bool LOCAL = false>
 __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamView& P, int gwarp,
                                               int nwarps, double* eacc, bool& bad_type,
-                                              int n_short_known = -1, int n_long_known = -1)
+                                              int n_short_known = -1, int n_long_known = -1,
+                                              const int2* first = nullptr)
 {
     BlockQueues& bq = block_queues();
     const uint32_t qcap = (uint32_t)min(max(a.block_q, 0), kBlockQ);
@@ -419,7 +434,8 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
     // the next unit's pair entry is loaded one unit ahead (a warp takes several units
     // of a large system: one L2 round trip of each unit's chain is hidden)
     const int stride = nwarps * 32;
-    int2 next_pr = gwarp * 32 + lane < n_short ? __ldcg(a.pairs_short + gwarp * 32 + lane) : make_int2(0, 0);
+    int2 next_pr = first ? first[0]
+                         : (gwarp * 32 + lane < n_short ? __ldcg(a.pairs_short + gwarp * 32 + lane) : make_int2(0, 0));
     for (int base = gwarp * 32; base < n_short; base += stride) {
         const int w = base + lane;
         const int2 pr = next_pr;
@@ -515,11 +531,11 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
     // leave warps free (small systems), the long units go to those warps only (a short
     // unit costs about as much as three or four long ones); otherwise round-robin.
     const uint32_t long_mask = mask & (1u << kDebye);
-    const int n_su = (n_short + 31) >> 5, n_lu = (n_long + 31) >> 5;
-    const int free_w = nwarps - n_su;
-    const bool to_free = free_w > 0 && 4 * free_w >= n_lu;
-    const int v0 = to_free ? gwarp - n_su : gwarp, vstride = to_free ? free_w : nwarps;
-    int2 next_lp = (v0 >= 0 && v0 * 32 + lane < n_long) ? __ldcg(a.pairs_long + v0 * 32 + lane) : make_int2(0, 0);
+    int v0, vstride;
+    long_units(gwarp, nwarps, n_short, n_long, v0, vstride);
+    const int n_lu = (n_long + 31) >> 5;
+    int2 next_lp = first ? first[1]
+                         : ((v0 >= 0 && v0 * 32 + lane < n_long) ? __ldcg(a.pairs_long + v0 * 32 + lane) : make_int2(0, 0));
     for (int v = v0; v >= 0 && v < n_lu && long_mask; v += vstride) {
         const int w = v * 32 + lane;
         const int2 pr = next_lp;
@@ -1665,8 +1681,10 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     bool bad_type = false;
     // the RNG step of body b is step_base + b + 1 (block 0 advances st->step to match)
     const unsigned long long step_base = a.prologue ? a.step0 : *(const volatile unsigned long long*)&st->step;
-    // the stored pair counts, read once after each list build (they change only there)
+    // the stored pair counts and this thread's first short- and long-pair entries, read
+    // once after each list build (they change only there)
     int ns_known = -1, nl_known = -1;
+    int2 first_pair[2];
     // the block's slice of the (constant) bond table, staged once per launch when it fits
     __shared__ int4 bond_stage[kBondStage];
     const int4* bonds_here = nullptr;
@@ -1732,6 +1750,11 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         if (rebuild || ns_known < 0) {
             ns_known = (int)min(ld_volatile(&st->n_short), (uint32_t)a.f.cap_short);
             nl_known = (int)min(ld_volatile(&st->n_long), (uint32_t)a.f.cap_long);
+            first_pair[0] = gwarp * 32 + lane < ns_known ? __ldcg(a.f.pairs_short + gwarp * 32 + lane) : make_int2(0, 0);
+            int v0, vstride;
+            long_units(gwarp, nwarps, ns_known, nl_known, v0, vstride);
+            first_pair[1] = (v0 >= 0 && v0 * 32 + lane < nl_known) ? __ldcg(a.f.pairs_long + v0 * 32 + lane)
+                                                                   : make_int2(0, 0);
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             if (rebuild) st->gen += 1u;
@@ -1744,7 +1767,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         const bool have_nz = !pro && gthread < a.g.N;
         {
             // phase B on the block's own queues: a block barrier, not a grid barrier
-            forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type, ns_known, nl_known);
+            forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type, ns_known, nl_known, first_pair);
             forces_b_local<false, SURR>(a.f, P, eacc, bad_type, bonds_here);
             const uint32_t tok = grid_arrive(a.bar);
             if (have_nz)
