@@ -8,7 +8,7 @@ from the network's analytic input gradient. BF16 weights on the tensor cores, FP
 accumulation; trained by the library's own kernels on samples the plain evaluator
 produces along its own trajectories. The reference has no learned part: this is an
 extension, used only while audits by the plain evaluator keep its per-pair error under
-a tolerance (the plain evaluator stays the fallback and the judge).
+a tolerance (the plain evaluator stays the fallback and the yardstick).
 
 Device buffers are torch CUDA tensors (plumbing only); every computation runs in
 ``liboxdna_gb300.so``.

@@ -8,7 +8,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 TERMS = ("oxdna_excvol", "oxdna_hbond", "oxdna_crossstacking", "oxdna_hbondcross",
          "oxdna_coaxstacking", "oxdna_debye")
 
-# Parity tolerance of the FP32 GPU path against the FP64 reference (spec:
+# Parity tolerance of the FP32 GPU path against the FP64 reference (the required
 # 1e-4 relative), as a set-level max-norm relative error: max|x - x_ref| / max|x_ref|
 # over all samples of one term. Per-pair relative errors are not meaningful where the
 # reference force is ~0 (ideal geometries), where even the reference's own FP32 build

@@ -55,7 +55,7 @@ def test_abi_struct_conversion():
 
 
 def test_debye_parameters():
-    """dna2.debye_params at 296.15 K, 0.5 M: lambda 0.50815, rc 2.2867 (SURVEY config 1)."""
+    """dna2.debye_params at 296.15 K, 0.5 M: lambda 0.50815, rc 2.2867 (the 320-nt configuration)."""
     from oxdna.model import dna2
     mk, pref, b, rc, rhigh = dna2.debye_params(296.15, 0.5)
     assert abs(-1.0 / mk - 0.50815) < 1e-4 and abs(rc - 2.2867) < 1e-3
