@@ -1087,7 +1087,8 @@ __device__ __forceinline__ bool is_excluded(int4 e, int j) { return e.x == j || 
 // `par`, found by a whole warp (i warp-uniform): lanes 0..26 take the member counts of
 // the 27 neighbour cells, a prefix sum flattens the candidates, and each round the 32
 // lanes test 32 candidates at once (cell of a candidate by binary search over the
-// prefix sums); found pairs are appended with one atomic per warp and list per round.
+// prefix sums); found pairs are appended with one atomic per warp and list per round,
+// or staged (below) when the warp handles many particles.
 // Pairs found by a warp that handles many particles are staged in shared memory and
 // appended to the global lists in batches: one counter atomic per batch instead of one
 // per particle (100k particles: 200k same-address atomics per rebuild otherwise).

@@ -1,7 +1,7 @@
 /*
  * oxdna_oracle.h - FP64 CPU oracle for the oxDNA force hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This is the checker: a plain-C, all-double restatement
+ * TEST INFRASTRUCTURE ONLY. This is the oracle: a plain-C, all-double restatement
  * of the reference plugin's per-pair evaluators, its bonded kernel and the HOOMD
  * driver semantics around them (minimum image, per-type-pair cutoffs, 0.5*E split,
  * Newton's third law, bond exclusions, Langevin + NO_SQUISH). Only the test suite,
