@@ -1644,10 +1644,10 @@ struct RunArgs {
     GridBarrier* bar;
     int bodies;   // step bodies in this launch
     int closing;  // the last body is the run's last step (step two only)
+    unsigned long long step0;  // the system's timestep at the launch (RNG counter), every launch
     // run start in the same launch (the first launch of a run() call):
     int prologue;
     uint32_t rebuild0;         // the lists are new: rebuild whatever the displacements
-    unsigned long long step0;  // the system's timestep (RNG counter)
     float4* ck[5];             // checkpoint of pos, pos_lo, quat, vel, angmom for a replay
 };
 
@@ -1680,8 +1680,10 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     const int gthread = gwarp * 32 + lane, nthreads = nwarps * 32;
     double eacc[kNTerms + 3];  // unused: MD steps evaluate no energies
     bool bad_type = false;
-    // the RNG step of body b is step_base + b + 1 (block 0 advances st->step to match)
-    const unsigned long long step_base = a.prologue ? a.step0 : *(const volatile unsigned long long*)&st->step;
+    // the RNG step of body b is step0 + b + 1 (block 0 advances st->step to match); the
+    // host passes step0 to every launch: reading st->step here would race with block 0's
+    // first increment in a block that starts late
+    const unsigned long long step_base = a.step0;
     // the stored pair counts and this thread's first short- and long-pair entries, read
     // once after each list build (they change only there)
     int ns_known = -1, nl_known = -1;
