@@ -26,42 +26,84 @@ def base_typeid(letter):
     return DNA_BASES.index(BASE_ALIAS.get(letter, letter))
 
 
+def _fields(fh):
+    """(line number, fields) of the non-blank lines of an open text file."""
+    for k, line in enumerate(fh, start=1):
+        f = line.split()
+        if f:
+            yield k, f
+
+
 def read_topology(top_path):
-    """Parse an oxDNA .top file: n, n_strands, strand, base, n3, n5."""
+    """Parse an oxDNA .top file (oxdna/io.py:32-52).
+
+    Header ``N n_strands``, then one line per nucleotide ``strand base n3 n5`` (-1 where
+    there is no neighbour). Returns a dict with ``n``, ``n_strands``, ``strand``,
+    ``base`` (letters), ``n3`` and ``n5``. A short file, a malformed line or a
+    neighbour index outside [-1, N) raises ``ValueError`` naming the line.
+    """
     with open(top_path) as fh:
-        n, n_strands = (int(x) for x in fh.readline().split()[:2])
-        strand = np.empty(n, dtype=int)
-        n3 = np.empty(n, dtype=int)
-        n5 = np.empty(n, dtype=int)
-        base = []
-        for i in range(n):
-            parts = fh.readline().split()
-            strand[i] = int(parts[0])
-            base.append(parts[1])
-            n3[i] = int(parts[2])
-            n5[i] = int(parts[3])
-    return dict(n=n, n_strands=n_strands, strand=strand, base=base, n3=n3, n5=n5)
+        lines = _fields(fh)
+        try:
+            k, head = next(lines)
+        except StopIteration:
+            raise ValueError(f"{top_path}: empty topology") from None
+        n, n_strands = int(head[0]), int(head[1])
+        body = [(k, f) for _, (k, f) in zip(range(n), lines)]
+    if len(body) < n:
+        raise ValueError(f"{top_path}: the header announces {n} nucleotides, the file lists {len(body)}")
+    for k, f in body:
+        if len(f) < 4:
+            raise ValueError(f"{top_path}:{k}: expected 'strand base n3 n5', got {' '.join(f)!r}")
+    strand = np.array([int(f[0]) for _, f in body], dtype=int)
+    base = [f[1] for _, f in body]
+    links = np.array([(int(f[2]), int(f[3])) for _, f in body], dtype=int).reshape(n, 2)
+    bad = np.flatnonzero((links < -1).any(axis=1) | (links >= n).any(axis=1))
+    if len(bad):
+        k = body[bad[0]][0]
+        raise ValueError(f"{top_path}:{k}: neighbour index outside [-1, {n})")
+    return dict(n=n, n_strands=n_strands, strand=strand, base=base,
+                n3=links[:, 0].copy(), n5=links[:, 1].copy())
 
 
 def iter_conf_frames(conf_path):
-    """Yield (t, box, arr) per frame; arr rows are com(3) a1(3) a3(3) v(3) L(3)."""
+    """Yield (t, box, arr) per frame of an oxDNA configuration or trajectory
+    (oxdna/io.py:55-76), reading one frame at a time.
+
+    A frame is ``t = T``, ``b = Lx Ly Lz``, ``E = ...`` and then one line per
+    nucleotide; ``arr`` rows are com(3) a1(3) a3(3) v(3) L(3). Lines with fewer than
+    nine numbers are skipped; a row without velocities gets zeros there.
+    """
+    def frame(t, box, rows):
+        arr = np.zeros((len(rows), 15))
+        for r, f in enumerate(rows):
+            m = min(len(f), 15)
+            arr[r, :m] = [float(x) for x in f[:m]]
+        return t, box, arr
+
+    t = box = None
+    rows = []
+    skip = 0
     with open(conf_path) as fh:
-        lines = fh.readlines()
-    i = 0
-    while i < len(lines):
-        if not lines[i].startswith("t ="):
-            i += 1
-            continue
-        t = float(lines[i].split("=")[1])
-        box = np.array(lines[i + 1].split("=")[1].split(), dtype=float)
-        i += 3
-        rows = []
-        while i < len(lines) and not lines[i].startswith("t ="):
-            s = lines[i].split()
-            if len(s) >= 9:
-                rows.append([float(x) for x in s[:15]])
-            i += 1
-        yield t, box, np.array(rows, dtype=float)
+        for line in fh:
+            if line.startswith("t ="):
+                if t is not None:
+                    yield frame(t, box, rows)
+                t, box, rows, skip = float(line.split("=", 1)[1]), None, [], 2
+                continue
+            if t is None:
+                continue
+            if skip:
+                # the two header lines after 't =': the box, then the energies
+                if box is None:
+                    box = np.array(line.split("=", 1)[1].split(), dtype=float)
+                skip -= 1
+                continue
+            f = line.split()
+            if len(f) >= 9:
+                rows.append(f)
+    if t is not None:
+        yield frame(t, box, rows)
 
 
 def quat_to_matrix(q):
@@ -82,27 +124,35 @@ def quat_to_matrix(q):
 
 
 def matrix_to_quaternion(R):
-    """Rotation matrices (..., 3, 3) -> unit (w, x, y, z), Shepperd's branch choice."""
+    """Rotation matrices (..., 3, 3) -> unit (w, x, y, z), vectorised.
+
+    The entries of the symmetric matrix K = 4 q q^T are linear in R: the diagonal is
+    1 + tr R with the signs of (w, x, y, z), the off-diagonal the sums and differences
+    of R's mirrored entries. q is the row of K through a large diagonal entry, divided
+    by 2 sqrt(K_kk). The row is picked with Shepperd's rule (w when tr R > 0, else the
+    largest diagonal of R), as the reference does (oxdna/io.py:79-114), so the sign of
+    q (the chosen component positive) is the reference's too.
+    """
     R = np.asarray(R, dtype=float)
-    flat = R.reshape(-1, 3, 3)
-    out = np.empty((flat.shape[0], 4))
-    for k, M in enumerate(flat):
-        tr = M[0, 0] + M[1, 1] + M[2, 2]
-        if tr > 0.0:
-            s = 2.0 * math.sqrt(tr + 1.0)
-            q = (0.25 * s, (M[2, 1] - M[1, 2]) / s, (M[0, 2] - M[2, 0]) / s, (M[1, 0] - M[0, 1]) / s)
-        elif M[0, 0] > M[1, 1] and M[0, 0] > M[2, 2]:
-            s = 2.0 * math.sqrt(1.0 + M[0, 0] - M[1, 1] - M[2, 2])
-            q = ((M[2, 1] - M[1, 2]) / s, 0.25 * s, (M[0, 1] + M[1, 0]) / s, (M[0, 2] + M[2, 0]) / s)
-        elif M[1, 1] > M[2, 2]:
-            s = 2.0 * math.sqrt(1.0 + M[1, 1] - M[0, 0] - M[2, 2])
-            q = ((M[0, 2] - M[2, 0]) / s, (M[0, 1] + M[1, 0]) / s, 0.25 * s, (M[1, 2] + M[2, 1]) / s)
-        else:
-            s = 2.0 * math.sqrt(1.0 + M[2, 2] - M[0, 0] - M[1, 1])
-            q = ((M[1, 0] - M[0, 1]) / s, (M[0, 2] + M[2, 0]) / s, (M[1, 2] + M[2, 1]) / s, 0.25 * s)
-        q = np.array(q)
-        out[k] = q / np.linalg.norm(q)
-    return out.reshape(R.shape[:-2] + (4,))
+    M = R.reshape(-1, 3, 3)
+    m00, m11, m22 = M[:, 0, 0], M[:, 1, 1], M[:, 2, 2]
+    K = np.empty((len(M), 4, 4))
+    K[:, 0, 0] = 1.0 + m00 + m11 + m22
+    K[:, 1, 1] = 1.0 + m00 - m11 - m22
+    K[:, 2, 2] = 1.0 - m00 + m11 - m22
+    K[:, 3, 3] = 1.0 - m00 - m11 + m22
+    for a, b, v in ((0, 1, M[:, 2, 1] - M[:, 1, 2]), (0, 2, M[:, 0, 2] - M[:, 2, 0]),
+                    (0, 3, M[:, 1, 0] - M[:, 0, 1]), (1, 2, M[:, 0, 1] + M[:, 1, 0]),
+                    (1, 3, M[:, 0, 2] + M[:, 2, 0]), (2, 3, M[:, 1, 2] + M[:, 2, 1])):
+        K[:, a, b] = K[:, b, a] = v
+    tr = m00 + m11 + m22
+    k = np.where(tr > 0.0, 0, np.where((m00 > m11) & (m00 > m22), 1, np.where(m11 > m22, 2, 3)))
+    rows = np.arange(len(M))
+    s = 2.0 * np.sqrt(K[rows, k, k])
+    q = K[rows, k, :] / s[:, None]
+    q[rows, k] = 0.25 * s
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return q.reshape(R.shape[:-2] + (4,))
 
 
 def orientations_to_quaternions(a1, a3, check=True):
@@ -120,6 +170,12 @@ def orientations_to_quaternions(a1, a3, check=True):
             i = int(np.argmax(err))
             raise ValueError(f"quaternion convention check failed at nucleotide {i}: {err[i]:.2e}")
     return q
+
+
+def quaternions_to_orientations(q):
+    """(w, x, y, z) -> (a1, a3) = (rotate(q, e_x), rotate(q, e_z)): the inverse map."""
+    R = quat_to_matrix(q)
+    return R[..., :, 0], R[..., :, 2]
 
 
 def terminal_charges(top, end_charge=0.5, interior_charge=1.0):
@@ -159,15 +215,79 @@ def snapshot_from_arrays(positions, quaternions, typeids, box, bonds=None, types
 
 
 def build_snapshot(top_path, conf_path, frame=0, bond_type="backbone", half_charged_ends=False):
-    """Snapshot from an oxDNA topology + configuration frame (io.py:196-241)."""
+    """Snapshot from an oxDNA topology + configuration frame (io.py:196-241).
+
+    Positions move from oxDNA's [0, L) box to HOOMD's origin-centred one; backbone
+    bonds are (i, n5[i]), one per 5' link.
+    """
     top = read_topology(top_path)
-    _, box, arr = list(iter_conf_frames(conf_path))[frame]
+    for k, (_, box, arr) in enumerate(iter_conf_frames(conf_path)):
+        if k == frame:
+            break
+    else:
+        raise ValueError(f"{conf_path}: no frame {frame}")
+    if len(arr) != top["n"]:
+        raise ValueError(f"{conf_path}: frame {frame} has {len(arr)} nucleotides, "
+                         f"the topology {top['n']}")
     q = orientations_to_quaternions(arr[:, 3:6], arr[:, 6:9])
     typeids = [base_typeid(b) for b in top["base"]]
-    bonds = [(i, int(top["n5"][i])) for i in range(top["n"]) if top["n5"][i] >= 0]
+    n5 = top["n5"]
+    bonds = [(int(i), int(n5[i])) for i in np.flatnonzero(n5 >= 0)]
     charges = terminal_charges(top) if half_charged_ends else np.ones(top["n"])
     return snapshot_from_arrays(arr[:, 0:3] - box / 2.0, q, typeids, box, bonds=bonds,
                                 bond_type=bond_type, charges=charges)
+
+
+def topology_from_bonds(n, bonds, typeids):
+    """(strand, base, n3, n5) of n nucleotides whose backbone bonds (A, B) link A to its
+    5' neighbour B, the convention of :func:`build_snapshot`; strands are numbered from
+    1 in order of their 3' ends."""
+    n3 = np.full(n, -1, dtype=int)
+    n5 = np.full(n, -1, dtype=int)
+    for a, b in bonds:
+        if n5[a] >= 0 or n3[b] >= 0:
+            raise ValueError(f"nucleotide {a} or {b} has two backbone bonds in one direction")
+        n5[a], n3[b] = b, a
+    strand = np.zeros(n, dtype=int)
+    sid = 0
+    for start in list(np.flatnonzero(n3 < 0)) + list(range(n)):
+        if strand[start]:
+            continue
+        sid += 1  # a 3' end, then what is left: circular strands
+        i = start
+        while i >= 0 and not strand[i]:
+            strand[i] = sid
+            i = n5[i]
+    base = [DNA_BASES[int(t)] for t in typeids]
+    return strand, base, n3, n5
+
+
+def write_topology(top_path, strand, base, n3, n5):
+    """Write an oxDNA .top file (the format :func:`read_topology` reads)."""
+    n = len(base)
+    with open(top_path, "w") as fh:
+        fh.write(f"{n} {len(set(int(x) for x in strand))}\n")
+        for i in range(n):
+            fh.write(f"{int(strand[i])} {base[i]} {int(n3[i])} {int(n5[i])}\n")
+
+
+def write_conf(conf_path, positions, quaternions, box, t=0, velocities=None, angular=None,
+               energies=(0.0, 0.0, 0.0), append=False):
+    """Write one frame of an oxDNA configuration (the format :func:`iter_conf_frames`
+    reads): HOOMD's origin-centred positions move to [0, L), orientations become
+    (a1, a3). ``append`` adds the frame to a trajectory file."""
+    box = np.asarray(box, float)[:3]
+    pos = np.asarray(positions, float) + box / 2.0
+    a1, a3 = quaternions_to_orientations(quaternions)
+    n = len(pos)
+    v = np.zeros((n, 3)) if velocities is None else np.asarray(velocities, float)
+    L = np.zeros((n, 3)) if angular is None else np.asarray(angular, float)
+    cols = np.hstack([pos, a1, a3, v, L])
+    with open(conf_path, "a" if append else "w") as fh:
+        fh.write(f"t = {t}\n")
+        fh.write("b = " + " ".join(repr(float(x)) for x in box) + "\n")
+        fh.write("E = " + " ".join(repr(float(x)) for x in energies) + "\n")
+        np.savetxt(fh, cols, fmt="%.17g")
 
 
 # ------------------------------------------------------------------ synthetic builders
