@@ -12,6 +12,6 @@ from . import forces  # noqa: F401
 from . import runtime  # noqa: F401
 from . import model  # noqa: F401
 
-version = "1.0.0"
+from .version import version  # noqa: F401
 
 __all__ = ["io", "forces", "model", "runtime", "version"]
