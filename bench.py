@@ -160,14 +160,15 @@ def time_resident(sim, steps, warmup, stream, block=1000):
     return total_ms
 
 
-def bench_batched(stream, steps=2000, loop_steps=20, n_rep=512, seed=4):
+def bench_batched(stream, steps=2000, loop_steps=20, n_rep=512, seed=4, hairpin_fraction=0.0):
     """512 independent duplex replicas (12-64 bp, box 30, 290-340 K): aggregate
     nt*steps/s of the batched engine (autotuned tile shape, one persistent launch per
-    5000 steps) against looping the single-system engine over the replicas."""
+    5000 steps) against looping the single-system engine over the replicas. With
+    hairpin_fraction > 0 that fraction of the replicas are hairpins of the same size."""
     import torch
 
     from oxdna import replicas
-    work = replicas.replica_workload(n_rep, seed=seed)
+    work = replicas.replica_workload(n_rep, seed=seed, hairpin_fraction=hairpin_fraction)
     sims = [replicas.replica_simulation(s, T, seed=100 + r) for r, (s, T) in enumerate(work)]
     b = replicas.ReplicaBatch(sims, seed=100)
     b.set_stream(stream.cuda_stream)
@@ -196,7 +197,9 @@ def bench_batched(stream, steps=2000, loop_steps=20, n_rep=512, seed=4):
     e1.record(stream)
     e1.synchronize()
     ms_loop = e0.elapsed_time(e1)
-    return {"workload": f"{n_rep} replicas x one duplex of 12-64 bp ({n_total} nt), box 30, "
+    kind = (f"one duplex of 12-64 bp or ({hairpin_fraction:.0%}) a hairpin of the same size"
+            if hairpin_fraction > 0 else "one duplex of 12-64 bp")
+    return {"workload": f"{n_rep} replicas x {kind} ({n_total} nt), box 30, "
                         "290-340 K, 0.5 M, Langevin dt 0.003",
             "n_nt": n_total, "steps": steps, "tile_particles": tile, "threads": threads,
             "replica_steps_per_s": steps / (ms * 1e-3),
@@ -526,6 +529,8 @@ def main():
                     help="resident timing only (no fused / e2e / CPU legs); for profiling runs")
     ap.add_argument("--leg", choices=["batched", "rna", "surrogate", "nt100k"],
                     help="run one extension leg alone and print its numbers (profiling runs)")
+    ap.add_argument("--hairpin-fraction", type=float, default=0.0,
+                    help="--leg batched: fraction of the replicas that are hairpins")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -541,7 +546,7 @@ def run_leg(args):
     import torch
     stream = torch.cuda.Stream()
     if args.leg == "batched":
-        out = bench_batched(stream, steps=args.steps)
+        out = bench_batched(stream, steps=args.steps, hairpin_fraction=args.hairpin_fraction)
     elif args.leg == "rna":
         out = bench_rna(stream, steps=args.steps, warmup=args.warmup)
     elif args.leg == "nt100k":

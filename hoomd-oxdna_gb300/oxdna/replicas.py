@@ -191,18 +191,35 @@ class ReplicaBatch:
 
 
 def replica_workload(n_replicas=512, bp_range=(12, 64), box_len=30.0, t_range=(290.0, 340.0),
-                     seed=4):
-    """Independent duplex replicas: replica r is one random-sequence B-form duplex of
-    uniform-random length in bp_range (inclusive) in its own periodic cube of side
-    box_len, at a temperature uniform in t_range (K). Returns a list of
-    (system arrays as from ``io.duplex_system``, temperature)."""
+                     seed=4, hairpin_fraction=0.0, hairpin_loop=8):
+    """Independent replicas: replica r is one random-sequence B-form duplex of
+    uniform-random length n in bp_range (inclusive) in its own periodic cube of side
+    box_len, at a temperature uniform in t_range (K). With ``hairpin_fraction`` > 0 that
+    fraction of the replicas (chosen at random) are instead single-strand hairpins of
+    the same 2n nucleotides: a stem of n - hairpin_loop/2 base pairs closed by a loop
+    of hairpin_loop nucleotides, started as an extended helix. The duplex draws do not
+    depend on ``hairpin_fraction``, so the default reproduces the all-duplex workload.
+    Returns a list of (system arrays as from ``io.duplex_system``, temperature)."""
     from . import io
     rng = np.random.Generator(np.random.PCG64(seed))
     lengths = rng.integers(bp_range[0], bp_range[1] + 1, size=n_replicas)
     temps = rng.uniform(t_range[0], t_range[1], size=n_replicas)
     seeds = rng.integers(1, 2 ** 31 - 1, size=n_replicas)
-    return [(io.duplex_system(1, int(n), box_len, seed=int(s)), float(t))
-            for n, t, s in zip(lengths, temps, seeds)]
+    hairpin = np.zeros(n_replicas, bool)
+    if hairpin_fraction > 0.0:
+        if hairpin_loop < 2 or hairpin_loop % 2 or 2 * bp_range[0] - hairpin_loop < 4:
+            raise ValueError("hairpin_loop must be even, >= 2, and leave a stem of >= 2 bp")
+        pick = np.random.Generator(np.random.PCG64(seed + 1))
+        hairpin = pick.random(n_replicas) < hairpin_fraction
+    out = []
+    for n, t, s, h in zip(lengths, temps, seeds, hairpin):
+        if h:
+            stem = int(n) - hairpin_loop // 2
+            out.append((io.hairpin_system(1, stem=stem, loop=hairpin_loop, box_len=box_len,
+                                          seed=int(s)), float(t)))
+        else:
+            out.append((io.duplex_system(1, int(n), box_len, seed=int(s)), float(t)))
+    return out
 
 
 def replica_simulation(system, temperature, salt=0.5, dt=0.003, seed=1, fused=False):

@@ -89,6 +89,31 @@ def test_quaternion_roundtrip():
     assert np.allclose(np.abs(np.einsum("ij,ij->i", q, q2)), 1.0, atol=1e-12)
 
 
+def test_replica_workload_hairpins():
+    from oxdna import replicas
+    base = replicas.replica_workload(40, seed=9)
+    mixed = replicas.replica_workload(40, seed=9, hairpin_fraction=0.5)
+    assert replicas.replica_workload(40, seed=9, hairpin_fraction=0.0)[7][0]["pos"].tolist() == \
+        base[7][0]["pos"].tolist()
+    n_hairpins = 0
+    for (d, td), (m, tm) in zip(base, mixed):
+        assert td == tm and len(d["pos"]) == len(m["pos"])  # same size and temperature
+        strands = len(m["pos"]) - len(m["bonds"])
+        assert strands in (1, 2)
+        if strands == 1:
+            n_hairpins += 1
+            n = len(m["pos"])
+            t = m["typeid"]
+            stem = n // 2 - 4
+            # 5'-stem, 8-nt loop, complementary stem-3': paired bases sum to 3
+            assert all(t[k] + t[n - 1 - k] == 3 for k in range(stem))
+        else:
+            assert d["pos"].tolist() == m["pos"].tolist()
+    assert 10 <= n_hairpins <= 30
+    with pytest.raises(ValueError):
+        replicas.replica_workload(4, hairpin_fraction=0.5, hairpin_loop=7)
+
+
 def test_replica_sharding():
     from oxdna import replicas
     shards = [replicas.shard(103, r, 4) for r in range(4)]
