@@ -229,6 +229,29 @@ def bench_rna(stream, steps=2000, warmup=100):
             "steps_per_s": steps / (ms * 1e-3)}
 
 
+def bench_tiled(stream, steps=10000, warmup=500, copies=8):
+    """The layout of the reference's own benchmark (bench/benchmark.py): one 8-bp duplex
+    (its 16-nt simple-helix; here an ideal helix with a seeded sequence, the data file
+    being absent) tiled on an 8^3 grid of spacing 8 = 8192 nt in a box of 64, oxDNA2 at
+    296.15 K, 0.5 M, Langevin dt 0.003; steps/s unfused and fused."""
+    import torch
+
+    from oxdna import io
+    sysarr = io.tiled_duplex_system(copies)
+    out = {"workload": f"oxDNA2 {copies}^3 x 8-bp duplex ({len(sysarr['pos'])} nt), box "
+                       f"{copies * 8}, 296.15 K, 0.5 M, dt 0.003 (the reference benchmark's tiling)"}
+    for fused in (False, True):
+        sim, _ = make_sim(sysarr, fused=fused, stream=stream.cuda_stream)
+        sim.run(0)
+        sim.run(warmup)
+        torch.cuda.synchronize()
+        with nvtx("timed"):
+            ms = time_resident(sim, steps, 0, stream)
+        out[("fused" if fused else "unfused") + "_steps_per_s"] = steps / (ms * 1e-3)
+        del sim
+    return out
+
+
 def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epochs=15):
     """The learned HB + cross-stacking surrogate on the 100k-nt system (2500 x 20 bp, box
     230, forces(fused=True)): trained here by the library's kernels on 4M pair geometries
@@ -527,7 +550,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--quick", action="store_true",
                     help="resident timing only (no fused / e2e / CPU legs); for profiling runs")
-    ap.add_argument("--leg", choices=["batched", "rna", "surrogate", "nt100k"],
+    ap.add_argument("--leg", choices=["batched", "rna", "surrogate", "nt100k", "tiled"],
                     help="run one extension leg alone and print its numbers (profiling runs)")
     ap.add_argument("--hairpin-fraction", type=float, default=0.0,
                     help="--leg batched: fraction of the replicas that are hairpins")
@@ -549,6 +572,8 @@ def run_leg(args):
         out = bench_batched(stream, steps=args.steps, hairpin_fraction=args.hairpin_fraction)
     elif args.leg == "rna":
         out = bench_rna(stream, steps=args.steps, warmup=args.warmup)
+    elif args.leg == "tiled":
+        out = bench_tiled(stream, steps=args.steps, warmup=args.warmup)
     elif args.leg == "nt100k":
         big = build_system(n_dup=2500, n_bp=20, box=230.0, seed=5)
         sim, _ = make_sim(big, fused=False, stream=stream.cuda_stream)

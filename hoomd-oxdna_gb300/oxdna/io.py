@@ -445,6 +445,31 @@ def hairpin_system(n_hairpins, stem=16, loop=16, box_len=80.0, seed=1, min_dist=
     return pack_molecules(mols, box_len, rng, min_dist=min_dist)
 
 
+def tiled_duplex_system(copies, n_bp=8, spacing=8.0, seed=1):
+    """One ideal duplex of n_bp base pairs (seeded random sequence) repeated, with the
+    same orientation, at the centres of a copies^3 grid of cells of side ``spacing``:
+    the layout of the reference's benchmark (bench/benchmark.py:22-52, which tiles
+    its 16-nt simple-helix duplex, 8 bp, spacing 8; copies = 8 gives 8192 nt in a
+    box of 64). Each copy is centred on its COM, so the copies are ``spacing`` apart."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pos0, a10, a30, t0, b0, e0 = duplex(random_sequence(rng, n_bp))
+    pos0 = pos0 - pos0.mean(axis=0)
+    n0 = len(pos0)
+    L = copies * float(spacing)
+    g = (np.arange(copies) + 0.5) * spacing - L / 2.0
+    shifts = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3)
+    m = len(shifts)
+    pos = (pos0[None, :, :] + shifts[:, None, :]).reshape(-1, 3)
+    a1 = np.tile(a10, (m, 1))
+    a3 = np.tile(a30, (m, 1))
+    b0 = np.asarray(b0, dtype=int)
+    bonds = (b0[None, :, :] + (n0 * np.arange(m))[:, None, None]).reshape(-1, 2)
+    return SystemArrays(pos=pos, quat=orientations_to_quaternions(a1, a3),
+                        typeid=np.tile(t0, m), box=np.array([L, L, L]),
+                        bonds=[tuple(b) for b in bonds.tolist()], ends=np.tile(e0, m),
+                        molecule=np.repeat(np.arange(m), n0), charge=np.ones(m * n0))
+
+
 def system_snapshot(sysarr, half_charged_ends=False):
     charges = np.where(sysarr["ends"], 0.5, 1.0) if half_charged_ends else sysarr["charge"]
     return snapshot_from_arrays(sysarr["pos"], sysarr["quat"], sysarr["typeid"], sysarr["box"],

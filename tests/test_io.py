@@ -143,3 +143,23 @@ def test_malformed_topology(tmp_path):
     top.write_text("2 1\n\n1 A -1 1\n\n1 U 0 -1\n")
     t = io.read_topology(top)
     assert t["base"] == ["A", "U"] and io.base_typeid(t["base"][1]) == 3
+
+
+def test_tiled_duplex_system_layout():
+    from oxdna.model import dna2
+    s = io.tiled_duplex_system(8)
+    n = len(s["pos"])
+    assert n == 8192 and np.all(s["box"] == 64.0) and len(s["bonds"]) == 512 * 14
+    b = np.asarray(s["bonds"])
+    r = np.linalg.norm(s["pos"][b[:, 1]] - s["pos"][b[:, 0]], axis=1)
+    assert np.all(np.abs(r - dna2.FENE_R0) < 0.25)
+    # every copy identical up to its grid shift, inside the box, 8 apart
+    p = s["pos"].reshape(512, 16, 3)
+    shift = p - p[:1]
+    assert np.abs(shift - shift[:, :1]).max() < 1e-12
+    assert np.all(np.abs(s["pos"]) < 32.0)
+    com = p.mean(axis=1)
+    d = np.linalg.norm(com[:, None] - com[None], axis=-1) + 1e9 * np.eye(512)
+    assert abs(d.min() - 8.0) < 1e-9
+    t = s["typeid"][:16]
+    assert all(t[k] + t[15 - k] == 3 for k in range(8))
