@@ -34,10 +34,9 @@ def test_param_dict_validation():
         f.params[("A", "A")] = dict(back_site=(0, 0, 0), debye=(1, 2, 3, 4, 5), bogus=1)
     c = dna2.coaxial_stacking(nl)
     assert c.params[("A", "C")]["f5_phi4"] == (0.0,) * 4 and c.params[("A", "C")]["rna_coax"] is False
+    from oxdna.forces import ExcludedVolume
     with pytest.raises(ValueError):
-        dna2.ExcludedVolume if False else None
-        from oxdna.forces import ExcludedVolume
-        ExcludedVolume(nl, 2.0, mode="shift")
+        ExcludedVolume(nl, 2.0, mode="shift")  # the evaluators implement no energy shift
 
 
 def test_abi_struct_conversion():
@@ -138,3 +137,35 @@ def test_library_exports_every_header_symbol():
         assert hasattr(L, n), n
     assert set(names) == set(_abi.EXPORTS)
     assert b"sm_103a" in _abi.lib().oxg_version()
+
+
+def test_abi_rejects_null_handles_without_touching_the_device():
+    """Every entry point checks its handle and pointers before any device work: called
+    with a null handle (and zero / null for the rest) each returns OXG_ERR_INVALID_ARG
+    with a message, the destroy calls accept null (OXG_OK), and the status strings
+    name every code (the reference's std::runtime_error throws become status codes)."""
+    from oxdna import _abi
+    L = _abi.lib()
+    ints = (C.c_int32, C.c_uint32, C.c_long, C.c_uint64, C.c_int)
+    for name in _abi.EXPORTS:
+        if name in ("oxg_last_error", "oxg_version", "oxg_status_string"):
+            continue
+        fn = getattr(L, name)
+        args = [0 if t in ints else 0.0 if t in (C.c_double, C.c_float) else None
+                for t in fn.argtypes]
+        rc = fn(*args)
+        if name.endswith("_destroy"):
+            assert rc == 0, name
+        else:
+            assert rc == 1, (name, rc)
+            assert L.oxg_last_error(), name
+    names = {L.oxg_status_string(k).decode() for k in range(9)}
+    assert len(names) == 9 and "unknown status" not in names
+    assert L.oxg_status_string(99) == b"unknown status"
+    # out-of-range sizes are rejected before the device is looked at
+    h = C.c_void_p()
+    assert L.oxg_create(C.byref(h), 0, 1) == 1 and not h.value
+    assert L.oxg_create(C.byref(h), 5, 1) == 1 and not h.value
+    assert L.oxg_create(C.byref(h), 4, -1) == 1 and not h.value
+    with pytest.raises(_abi.OxgError, match="status 1"):
+        _abi.check(L.oxg_system_run(None, 10), "oxg_system_run")
