@@ -20,15 +20,9 @@ def _system(oracle):
     return g, g["pos"].copy(), g["quat"].copy()
 
 
-@pytest.mark.parametrize("what", list(TERMS) + ["bonded"])
-def test_finite_difference_force_and_torque(oracle, what):
-    from oxdna import io
-    g, pos, quat = _system(oracle)
-    pair, bonded = model_forces("dna2")
-    model = oracle.Model(pair + [bonded], io.DNA_BASES)
-    mask = 0 if what == "bonded" else 1 << TERMS.index(what)
-    use_bonded = what == "bonded"
-
+def _fd_check(oracle, model, g, pos, quat, mask, use_bonded, label):
+    """Forces and torques against central differences of the energy for the three
+    most-forced particles (displacements along x, y, z; rotations about x, y, z)."""
     def run(p, q):
         s = oracle.System(p, q, g["typeid"], g["box"], g["bonds"], g["charge"])
         r = oracle.forces(model, s, mask=mask, bonded=use_bonded)
@@ -38,7 +32,7 @@ def test_finite_difference_force_and_torque(oracle, what):
     e0, r0 = run(pos, quat)
     F, T = r0["force"], r0["torque"]
     if np.abs(F).max() == 0.0:
-        pytest.skip(f"{what} is zero on this configuration")
+        pytest.skip(f"{label} is zero on this configuration")
     # Newton's third law (_helpers.py:156-157)
     assert np.linalg.norm(F.sum(axis=0)) < 1e-9 * (1 + np.abs(F).max())
     for i in np.argsort(-np.linalg.norm(F, axis=1))[:3]:
@@ -57,6 +51,43 @@ def test_finite_difference_force_and_torque(oracle, what):
             qp[i] = _quat_mul(np.r_[np.cos(-h / 2), np.sin(-h / 2) * axis], quat[i])
             em = run(pos, qp)[0]
             assert abs(-(ep - em) / (2 * h) - T[i, k]) < 1e-5 * max(1.0, abs(T[i, k]))
+    return e0
+
+
+@pytest.mark.parametrize("what", [t for t in TERMS if t != "oxdna_coaxstacking"] + ["bonded"])
+def test_finite_difference_force_and_torque(oracle, what):
+    from oxdna import io
+    g, pos, quat = _system(oracle)
+    pair, bonded = model_forces("dna2")
+    model = oracle.Model(pair + [bonded], io.DNA_BASES)
+    mask = 0 if what == "bonded" else 1 << TERMS.index(what)
+    _fd_check(oracle, model, g, pos, quat, mask, what == "bonded", what)
+
+
+@pytest.mark.parametrize("model_name", ["dna1", "dna2", "rna2"])
+def test_finite_difference_coax_on_nicked_duplex(oracle, model_name):
+    """Coaxial stacking, which is zero inside an intact duplex: a 20-bp duplex whose
+    first strand is nicked between nucleotides 9 and 10 (no backbone bond, so the pair
+    is no longer excluded and the two stack coaxially); the reference checks the same
+    term on its two-duplex simple-coax case (pytest/test_coaxstacking.py:26-31,
+    pytest/test_rna2.py:86-145). Positions and orientations are perturbed: in the ideal
+    helix the a3 axes of a strand are exactly parallel, theta4 = 0, a cone point of the
+    oxRNA2 theta4 factor (its theta0 is 0.151), where the energy has no derivative."""
+    from oxdna import io
+    s = io.duplex_system(1, 20, 30.0, seed=7)
+    g = dict(typeid=s["typeid"], box=s["box"], charge=s["charge"],
+             bonds=[b for b in s["bonds"] if b != (9, 10)])
+    rng = np.random.default_rng(2)
+    pos = s["pos"] + rng.normal(0, 0.02, s["pos"].shape)
+    quat = s["quat"].copy()
+    for k in range(len(quat)):
+        ax = rng.normal(size=3)
+        ang = rng.normal(0, 0.05)
+        quat[k] = _quat_mul(np.r_[np.cos(ang / 2), np.sin(ang / 2) * ax / np.linalg.norm(ax)], quat[k])
+    pair, bonded = model_forces(model_name)
+    model = oracle.Model(pair + [bonded], io.DNA_BASES)
+    e = _fd_check(oracle, model, g, pos, quat, 1 << TERMS.index("oxdna_coaxstacking"), False, "coax")
+    assert e < -0.1  # the nick's neighbours are stacked
 
 
 @pytest.mark.parametrize("model_name", ["dna1", "dna2"])
