@@ -1533,6 +1533,52 @@ int oxg_system_stats(oxg_system* s, int64_t* out, int n)
 
 }  // extern "C"
 
+// =================================================================== bounded-wait self-test
+namespace {
+// One grid barrier of the run kernel's kind (grid_arrive / grid_wait) over the launch's
+// blocks, of which block `skip_block` (none if negative) never arrives: the others then
+// poll until the barrier's poll limit, the first to reach it sets the abort word, and
+// all return. ok_out[b]: 1 passed the barrier, 0 gave up, -1 skipped it.
+__global__ void k_barrier_selftest(GridBarrier* gb, int skip_block, int* ok_out)
+{
+    if ((int)blockIdx.x == skip_block) {
+        if (threadIdx.x == 0) ok_out[blockIdx.x] = -1;
+        return;
+    }
+    const uint32_t old = grid_arrive(gb);
+    const bool ok = grid_wait(gb, old);
+    if (threadIdx.x == 0) ok_out[blockIdx.x] = ok ? 1 : 0;
+}
+}  // namespace
+
+extern "C" int oxg_selftest_barrier(int n_blocks, int skip_block, int* results, void* stream)
+{
+    if (n_blocks < 2 || n_blocks > 64 || skip_block >= n_blocks || !results)
+        return set_err(OXG_ERR_INVALID_ARG, "n_blocks must be 2..64, skip_block < n_blocks, results non-null");
+    if (n_blocks > num_sms()) return set_err(OXG_ERR_INVALID_ARG, "more blocks than SMs");
+    cudaStream_t s = (cudaStream_t)stream;
+    GridBarrier* gb = nullptr;
+    int* d_ok = nullptr;
+    int rc = dalloc(&gb, 1);
+    if (!rc) rc = dalloc(&d_ok, (size_t)n_blocks);
+    if (!rc) {
+        cudaError_t e = cudaMemsetAsync(gb, 0, sizeof(GridBarrier), s);
+        if (e == cudaSuccess) {
+            void* kargs[] = {&gb, &skip_block, &d_ok};
+            e = cudaLaunchCooperativeKernel((const void*)k_barrier_selftest, dim3(n_blocks), dim3(32), kargs, 0, s);
+        }
+        GridBarrier h;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(results, d_ok, sizeof(int) * n_blocks, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h, gb, sizeof(GridBarrier), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) rc = set_err(OXG_ERR_CUDA, std::string("barrier self-test: ") + cudaGetErrorString(e));
+        else if (h.abort) rc = set_err(OXG_ERR_TIMEOUT, "a grid barrier wait gave up (self-test)");
+    }
+    dfree(gb);
+    dfree(d_ok);
+    return rc;
+}
+
 // =================================================================== allocation-free
 // oxg_pair_forces_noalloc: the system engine's nonbonded evaluation (cell list, split
 // pair lists, fused force kernel) for callers that cannot allocate GPU memory. All of
