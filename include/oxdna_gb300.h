@@ -419,7 +419,7 @@ int oxg_device_peaks(double* out, int n, void* stream);
 /* Bounded-wait self-test of the run kernel's grid barrier: one cooperative launch of
  * n_blocks (2..64, at most the SM count) blocks meets at one barrier, except block
  * skip_block (none if negative), which never arrives. The others then give up after
- * the barrier's poll limit (about 2 s) and the call returns OXG_ERR_TIMEOUT, the status
+ * the barrier's poll limit (about 1 s on a GB300) and the call returns OXG_ERR_TIMEOUT, the status
  * the run entry points return when a run kernel's barrier gives up; with no skipped
  * block it returns OXG_OK. results[b] (host, n_blocks entries): 1 passed the barrier,
  * 0 gave up, -1 skipped. The context stays usable either way. Failure-handling test
