@@ -971,6 +971,13 @@ int oxg_system_set_nlist_buffer(oxg_system* s, double buffer)
     return OXG_OK;
 }
 
+int oxg_system_set_timestep(oxg_system* s, uint64_t step)
+{
+    if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    s->timestep = step;  // the next run's RNG steps continue from here
+    return OXG_OK;
+}
+
 static int system_compute_impl(oxg_system* s, uint32_t mask, int bonded)
 {
     int rc = sys_setup_nlist(s, mask, false);

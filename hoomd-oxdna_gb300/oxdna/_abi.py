@@ -244,6 +244,7 @@ EXPORTS = [
     "oxg_mlp_set_normalization", "oxg_mlp_gradient", "oxg_mlp_train_step", "oxg_mlp_predict",
     "oxg_system_set_surrogate", "oxg_system_surrogate_stats", "oxg_system_hbx_samples",
     "oxg_system_run_timing", "oxg_device_peaks", "oxg_system_run_host", "oxg_selftest_barrier",
+    "oxg_system_set_timestep",
 ]
 
 MLP_PARAMS = 9480  # OXG_MLP_PARAMS
@@ -297,6 +298,7 @@ def lib():
         "oxg_system_device_state": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
                                      C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)], i32),
         "oxg_system_set_nlist_buffer": ([vp, f64], i32),
+        "oxg_system_set_timestep": ([vp, C.c_uint64], i32),
         "oxg_system_compute": ([vp, u32, i32, vp, vp, vp, vp], i32),
         "oxg_system_set_integrator": ([vp, f64, f64, f64, f64, C.c_uint64, u32, i32], i32),
         "oxg_system_run": ([vp, C.c_long], i32),

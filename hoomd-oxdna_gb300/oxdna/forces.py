@@ -69,7 +69,8 @@ class TypeParameterDict:
         return ((k, dict(v)) for k, v in self._data.items())
 
     def _on_change(self):
-        pass
+        # a simulation compares this against the value it attached with
+        self._version = getattr(self, "_version", 0) + 1
 
 
 F = float

@@ -67,6 +67,7 @@ class _Bonds:
 class _Configuration:
     def __init__(self):
         self.box = [1.0, 1.0, 1.0, 0.0, 0.0, 0.0]
+        self.step = 0  # the simulation timestep the snapshot was taken at
 
 
 class _Communicator:
@@ -82,6 +83,44 @@ class Snapshot:
         self.bonds = _Bonds()
         self.configuration = _Configuration()
         self.communicator = _Communicator()
+
+
+_PARTICLE_FIELDS = ("position", "typeid", "mass", "moment_inertia", "orientation", "charge",
+                    "velocity", "angmom", "image")
+
+
+def write_snapshot(snap, path):
+    """Save a snapshot as a .npz file (numpy appends the suffix if missing): every
+    particle, bond and box field and the timestep, bit for bit. With
+    ``sim.state.get_snapshot()`` this is a checkpoint; :func:`read_snapshot` and
+    ``create_state_from_snapshot`` resume from it, the bath noise continuing from the
+    saved timestep."""
+    p, b, c = snap.particles, snap.bonds, snap.configuration
+    arrays = {k: np.asarray(getattr(p, k)) for k in _PARTICLE_FIELDS}
+    np.savez(path, N=np.int64(p.N), types=np.array(list(p.types), dtype=str),
+             bond_N=np.int64(b.N), bond_types=np.array(list(b.types), dtype=str),
+             bond_group=np.asarray(b.group), bond_typeid=np.asarray(b.typeid),
+             box=np.asarray(c.box, dtype=np.float64),
+             step=np.uint64(int(getattr(c, "step", 0) or 0)), **arrays)
+
+
+def read_snapshot(path):
+    """The snapshot written by :func:`write_snapshot`."""
+    with np.load(path) as z:
+        snap = Snapshot()
+        p = snap.particles
+        p.N = int(z["N"])
+        p.types = [str(t) for t in z["types"]]
+        for k in _PARTICLE_FIELDS:
+            getattr(p, k)[:] = z[k]
+        snap.bonds.N = int(z["bond_N"])
+        snap.bonds.types = [str(t) for t in z["bond_types"]]
+        if snap.bonds.N:
+            snap.bonds.group[:] = z["bond_group"]
+            snap.bonds.typeid[:] = z["bond_typeid"]
+        snap.configuration.box = [float(x) for x in z["box"]]
+        snap.configuration.step = int(z["step"])
+    return snap
 
 
 # --------------------------------------------------------------------- devices etc.
@@ -188,6 +227,8 @@ class Simulation:
         self._attached = False
         self._cache = {}
         self._stream = None
+        self._fkey = self._ikey = None
+        self._surrogate_args = None
 
     def set_stream(self, handle):
         """Run every later engine call on this CUDA stream (a cudaStream_t handle,
@@ -203,14 +244,63 @@ class Simulation:
             raise RuntimeError("state already created")
         self._snap = snap
         self.state = _State(self)
+        # HOOMD restores the timestep from the snapshot; the bath noise of step t depends
+        # only on (seed, t, particle), so a restored run continues the noise stream
+        self.timestep = int(getattr(snap.configuration, "step", 0) or 0)
 
     def _types(self):
         return list(self._snap.particles.types)
 
     def _detach(self):
+        """Drop the native context and system; the device state comes back into the
+        snapshot first, so the next attach continues from it (as HOOMD keeps the state
+        when the integrator or the forces change)."""
+        if self._attached and self._sys:
+            self._snap = self._pull_snapshot()
         self._free()
         self._attached = False
         self._cache = {}
+
+    def _forces_key(self):
+        """What the native context was built from: the integrator, its methods, and per
+        force its identity, parameter versions, cutoffs and list buffer."""
+        integ = self.operations.integrator
+        if integ is None:
+            return None
+        fk = tuple((id(f), getattr(f.params, "_version", 0),
+                    getattr(getattr(f, "r_cut", None), "_version", 0),
+                    getattr(f, "default_r_cut", None),
+                    getattr(getattr(f, "nlist", None), "buffer", None)) for f in integ.forces)
+        return (id(integ), fk, tuple(id(m) for m in integ.methods),
+                integ.integrate_rotational_dof)
+
+    def _integ_key(self):
+        integ = self.operations.integrator
+        lang = self._langevin
+        if lang is None:
+            return (integ.dt,)
+        return (integ.dt, lang.kT, lang.default_gamma, tuple(lang.default_gamma_r))
+
+    def _send_integrator(self):
+        integ = self.operations.integrator
+        if self._langevin is not None:
+            _abi.check(_abi.lib().oxg_system_set_integrator(
+                self._sys, integ.dt, self._langevin.kT, self._langevin.default_gamma,
+                self._langevin.default_gamma_r[0], self.seed, self._mask,
+                1 if self._bonded else 0), "oxg_system_set_integrator")
+        self._ikey = self._integ_key()
+
+    def _sync(self):
+        """Attach, or bring the attached engine up to date with the Python objects: a
+        changed force set, force parameters or cutoffs rebuild the native context and
+        system with the state carried over; a changed dt, kT or gamma is passed on."""
+        if self._attached:
+            if self._forces_key() != self._fkey:
+                self._detach()
+            elif self._integ_key() != self._ikey:
+                self._send_integrator()
+                self._cache = {}
+        self._attach()
 
     def _free(self):
         L = _abi.lib()
@@ -319,12 +409,13 @@ class Simulation:
         if self._nlist is not None:
             _abi.check(L.oxg_system_set_nlist_buffer(sys_, self._nlist.buffer), "set buffer")
         self._push_state()
-        if self._langevin is not None:
-            _abi.check(L.oxg_system_set_integrator(
-                sys_, integ.dt, self._langevin.kT, self._langevin.default_gamma,
-                self._langevin.default_gamma_r[0], self.seed, self._mask,
-                1 if self._bonded else 0), "oxg_system_set_integrator")
+        self._send_integrator()
+        if self.timestep:
+            _abi.check(L.oxg_system_set_timestep(sys_, int(self.timestep)), "oxg_system_set_timestep")
+        self._fkey = self._forces_key()
         self._attached = True
+        if getattr(self, "_surrogate_args", None) is not None:
+            self._apply_surrogate(*self._surrogate_args)
 
     def push_state_arrays(self, pos_type, pos_lo, quat, vel, angmom):
         """Copy host float32 (N, 4) arrays (pinned or not) into the device state."""
@@ -339,7 +430,7 @@ class Simulation:
         them. With page-locked arrays (torch ``pin_memory()``) a copy kernel on each side
         of the run launch moves the state over the host link: one synchronisation per
         call."""
-        self._attach()
+        self._sync()
         self._cache = {}
         L = _abi.lib()
         steps = int(steps)
@@ -388,6 +479,7 @@ class Simulation:
     def _pull_snapshot(self):
         import copy
         snap = copy.deepcopy(self._snap)
+        snap.configuration.step = int(self.timestep)
         if not self._attached:
             return snap
         L = _abi.lib()
@@ -409,7 +501,7 @@ class Simulation:
 
     # -- running -------------------------------------------------------------
     def run(self, steps):
-        self._attach()
+        self._sync()
         self._cache = {}
         L = _abi.lib()
         steps = int(steps)
@@ -462,7 +554,10 @@ class Simulation:
         also evaluated by the plain evaluator; a pair energy error above tol switches
         the surrogate off for the rest of the simulation. network=None restores the
         plain evaluator."""
-        self._attach()
+        self._sync()
+        self._apply_surrogate(network, run, compute, audit_every, audit_fraction, tol)
+
+    def _apply_surrogate(self, network, run, compute, audit_every, audit_fraction, tol):
         flags = (_abi.SURROGATE_RUN if run else 0) | (_abi.SURROGATE_COMPUTE if compute else 0)
         mod = max(1, int(round(1.0 / audit_fraction))) if audit_fraction > 0 else 1
         every = int(audit_every) if audit_fraction > 0 else 0
@@ -470,6 +565,9 @@ class Simulation:
             self._sys, network.handle if network is not None else None,
             flags if network is not None else 0, every, mod, float(tol)), "oxg_system_set_surrogate")
         self._surrogate = network
+        # kept so that a rebuilt native system (after a parameter change) gets it again
+        self._surrogate_args = ((network, run, compute, audit_every, audit_fraction, tol)
+                                if network is not None else None)
         self._cache = {}
 
     def surrogate_stats(self):

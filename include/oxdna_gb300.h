@@ -247,6 +247,10 @@ int oxg_system_device_state(oxg_system* sys, float** pos_type, float** pos_lo, f
                             float** vel, float** angmom, float** charge);
 /* Neighbour-list skin (HOOMD Cell nlist buffer, default 0.4). */
 int oxg_system_set_nlist_buffer(oxg_system* sys, double buffer);
+/* The system's timestep (0 after creation; every run advances it). The bath noise of
+ * step t depends only on (seed, t, particle), so a state restored with its timestep
+ * continues the noise stream: HOOMD's Simulation timestep restored from a snapshot. */
+int oxg_system_set_timestep(oxg_system* sys, uint64_t step);
 /* Evaluate forces at the current state: pair terms in term_mask plus (if bonded != 0)
  * the bonded force. Outputs are host arrays (any may be NULL): force/torque 4*N floats,
  * pair_energy OXG_N_PAIR_TERMS doubles, bonded_energy 3 doubles. */

@@ -169,3 +169,58 @@ def test_abi_rejects_null_handles_without_touching_the_device():
     assert L.oxg_create(C.byref(h), 4, -1) == 1 and not h.value
     with pytest.raises(_abi.OxgError, match="status 1"):
         _abi.check(L.oxg_system_run(None, 10), "oxg_system_run")
+
+
+def test_snapshot_checkpoint_round_trip(tmp_path):
+    """write_snapshot / read_snapshot keep every field bit for bit, and a simulation
+    created from the snapshot takes its timestep (the noise counter of a resumed run)."""
+    from oxdna import io, runtime
+    s = io.duplex_system(3, 10, 20.0, seed=5)
+    snap = io.system_snapshot(s, half_charged_ends=True)
+    rng = np.random.default_rng(1)
+    snap.particles.velocity[:] = rng.normal(size=(snap.particles.N, 3))
+    snap.particles.angmom[:] = rng.normal(size=(snap.particles.N, 4))
+    snap.configuration.step = 123456789012
+    runtime.write_snapshot(snap, tmp_path / "ck.npz")
+    back = runtime.read_snapshot(tmp_path / "ck.npz")
+    for k in ("position", "typeid", "mass", "moment_inertia", "orientation", "charge",
+              "velocity", "angmom", "image"):
+        a, b = getattr(snap.particles, k), getattr(back.particles, k)
+        assert a.dtype == b.dtype and np.array_equal(a, b), k
+    assert back.particles.types == snap.particles.types
+    assert np.array_equal(back.bonds.group, snap.bonds.group) and back.bonds.types == ["backbone"]
+    assert back.configuration.box == snap.configuration.box
+    assert back.configuration.step == 123456789012
+    sim = runtime.Simulation(device=runtime.device.GPU(), seed=3)
+    sim.create_state_from_snapshot(back)
+    assert sim.timestep == 123456789012
+    assert sim.state.get_snapshot().configuration.step == 123456789012
+
+
+def test_engine_sync_keys_follow_parameter_changes():
+    """The attached engine is rebuilt when a force's parameters, cutoffs or the force
+    set change, and only re-sent the integrator when dt / kT / gamma change (the keys
+    are plain Python; nothing here touches the device)."""
+    from oxdna import io, runtime
+    from oxdna.model import dna1, dna2
+    forces, _ = dna2.forces()
+    sim = runtime.Simulation(device=runtime.device.GPU(), seed=3)
+    sim.create_state_from_snapshot(io.system_snapshot(io.duplex_system(1, 8, 20.0)))
+    lang = runtime.md.methods.Langevin(filter=runtime.filter.All(), kT=dna1.kT_from_temperature(300))
+    sim.operations.integrator = runtime.md.Integrator(dt=0.003, integrate_rotational_dof=True,
+                                                      forces=forces, methods=[lang])
+    sim._langevin = lang
+    k0, i0 = sim._forces_key(), sim._integ_key()
+    assert sim._forces_key() == k0
+    hb = forces[2]
+    hb.params[("A", "T")] = dict(hb.params[("A", "T")], eps=1.0)
+    k1 = sim._forces_key()
+    assert k1 != k0
+    forces[1].r_cut[("A", "A")] = dict(r_cut=1.9)
+    assert sim._forces_key() != k1
+    assert sim._integ_key() == i0
+    k2 = sim._forces_key()
+    lang.kT = 0.2
+    assert sim._integ_key() != i0 and sim._forces_key() == k2
+    sim.operations.integrator.forces.append(dna2.debye_huckel(forces[1].nlist))
+    assert sim._forces_key()[1] != k1[1]
