@@ -10,6 +10,15 @@ evaluates every attached force in one fused GPU launch per step.
 
 from . import _abi
 
+# Counts every change of a force's parameters, cutoffs or attributes (and, through
+# oxdna.runtime, of integrators, Langevin methods and their force lists): an attached
+# simulation compares its full description only when this has moved since it looked.
+_changes = [0]
+
+
+def _changed():
+    _changes[0] += 1
+
 
 class TypeParameterDict:
     """Per-type (len_keys=1) or per-unordered-type-pair (len_keys=2) parameter dict
@@ -71,6 +80,7 @@ class TypeParameterDict:
     def _on_change(self):
         # a simulation compares this against the value it attached with
         self._version = getattr(self, "_version", 0) + 1
+        _changed()
 
 
 F = float
@@ -84,6 +94,11 @@ class _Force:
 
     def __init__(self):
         self._simulation = None
+
+    def __setattr__(self, name, value):
+        object.__setattr__(self, name, value)
+        if not name.startswith("_"):
+            _changed()
 
     def _sim(self):
         if self._simulation is None:

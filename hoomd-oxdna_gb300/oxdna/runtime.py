@@ -4,9 +4,9 @@ The reference plugin runs inside HOOMD-blue; this package stands that runtime in
 with the subset the reference's model files, tests and benchmark use
 (``hoomd.Simulation``, ``Snapshot``, ``md.Integrator``, ``md.methods.Langevin``,
 ``md.nlist.Cell``, ``filter.All``, ``device.GPU``). Everything it runs goes through
-the native library: the state lives on the GPU, and each step (neighbour list,
-every attached force in one fused kernel, Langevin + NO_SQUISH) is replayed from a
-captured CUDA graph.
+the native library: the state lives on the GPU, and a run() call is one launch of
+the persistent step kernel (neighbour list, every attached force, Langevin +
+NO_SQUISH for each step).
 """
 
 import ctypes as C
@@ -15,6 +15,7 @@ import types as _types
 import numpy as np
 
 from . import _abi
+from . import forces as _forces_mod
 from .forces import OxDNABonded, _PairForce
 
 
@@ -144,7 +145,33 @@ class _All:
 filter = _types.SimpleNamespace(All=_All)
 
 
-class _Cell:
+class _Tracked:
+    """Attribute changes count as changes of the simulation description."""
+
+    def __setattr__(self, name, value):
+        object.__setattr__(self, name, value)
+        _forces_mod._changed()
+
+
+class _ChangeList(list):
+    """A list whose mutations count as changes (an integrator's forces and methods)."""
+
+
+def _counting(name):
+    def method(self, *a, **k):
+        out = getattr(list, name)(self, *a, **k)
+        _forces_mod._changed()
+        return out
+    method.__name__ = name
+    return method
+
+
+for _name in ("append", "extend", "insert", "remove", "pop", "clear", "sort", "reverse",
+              "__setitem__", "__delitem__", "__iadd__"):
+    setattr(_ChangeList, _name, _counting(_name))
+
+
+class _Cell(_Tracked):
     """Cell neighbour list: radius max(r_cut) + buffer, bond exclusions."""
 
     def __init__(self, buffer=0.4, exclusions=("bond",)):
@@ -154,7 +181,7 @@ class _Cell:
             raise ValueError("oxDNA forces require exclusions=('bond',)")
 
 
-class _Langevin:
+class _Langevin(_Tracked):
     def __init__(self, filter=None, kT=1.0, default_gamma=1.0, default_gamma_r=(1.0, 1.0, 1.0)):
         self.filter = filter
         self.kT = float(kT)
@@ -165,12 +192,17 @@ class _Langevin:
         self.default_gamma_r = g
 
 
-class _Integrator:
+class _Integrator(_Tracked):
     def __init__(self, dt, integrate_rotational_dof=False, forces=(), methods=()):
         self.dt = float(dt)
         self.integrate_rotational_dof = bool(integrate_rotational_dof)
-        self.forces = list(forces)
-        self.methods = list(methods)
+        self.forces = forces
+        self.methods = methods
+
+    def __setattr__(self, name, value):
+        if name in ("forces", "methods"):
+            value = _ChangeList(value)
+        super().__setattr__(name, value)
 
 
 md = _types.SimpleNamespace(
@@ -228,6 +260,7 @@ class Simulation:
         self._cache = {}
         self._stream = None
         self._fkey = self._ikey = None
+        self._seen = -1
         self._surrogate_args = None
 
     def set_stream(self, handle):
@@ -294,7 +327,8 @@ class Simulation:
         """Attach, or bring the attached engine up to date with the Python objects: a
         changed force set, force parameters or cutoffs rebuild the native context and
         system with the state carried over; a changed dt, kT or gamma is passed on."""
-        if self._attached:
+        if self._attached and _forces_mod._changes[0] != self._seen:
+            self._seen = _forces_mod._changes[0]
             if self._forces_key() != self._fkey:
                 self._detach()
             elif self._integ_key() != self._ikey:
@@ -413,6 +447,7 @@ class Simulation:
         if self.timestep:
             _abi.check(L.oxg_system_set_timestep(sys_, int(self.timestep)), "oxg_system_set_timestep")
         self._fkey = self._forces_key()
+        self._seen = _forces_mod._changes[0]
         self._attached = True
         if getattr(self, "_surrogate_args", None) is not None:
             self._apply_surrogate(*self._surrogate_args)

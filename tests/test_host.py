@@ -220,7 +220,12 @@ def test_engine_sync_keys_follow_parameter_changes():
     assert sim._forces_key() != k1
     assert sim._integ_key() == i0
     k2 = sim._forces_key()
+    from oxdna import forces as F
+    c0 = F._changes[0]
     lang.kT = 0.2
+    assert F._changes[0] > c0  # the cheap test run() makes first
     assert sim._integ_key() != i0 and sim._forces_key() == k2
+    c1 = F._changes[0]
     sim.operations.integrator.forces.append(dna2.debye_huckel(forces[1].nlist))
+    assert F._changes[0] > c1
     assert sim._forces_key()[1] != k1[1]
