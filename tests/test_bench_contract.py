@@ -1,0 +1,43 @@
+"""The benchmark's reference arm runs on the host cores only, so its one-line JSON
+contract is checked here: the keys and types every line carries, the reference arm's
+own fields, and that a rank other than 0 prints nothing."""
+
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(env_extra):
+    env = dict(os.environ, **env_extra)
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--steps", "3", "--warmup", "3"], cwd=ROOT, env=env,
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    return [ln for ln in out.stdout.splitlines() if ln.strip()]
+
+
+def test_reference_arm_prints_one_contract_line():
+    lines = _run({"RANK": "0", "WORLD_SIZE": "1", "LOCAL_RANK": "0"})
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key, typ in (("metric", str), ("value", float), ("unit", str), ("n_gpus", int),
+                     ("steps", int), ("warmup", int), ("ms_per_step", float),
+                     ("higher_is_better", bool), ("scaling", str), ("dtype", str),
+                     ("data", str), ("config", dict), ("cpu_baseline", dict), ("e2e", dict)):
+        assert isinstance(d[key], typ), key
+    assert d["impl"] == "reference" and d["vs_baseline"] is None
+    assert d["unit"] == "steps/s" and d["higher_is_better"] is True and d["value"] > 0
+    assert d["steps"] == 3 and d["warmup"] == 3 and d["n_gpus"] == 1
+    assert abs(d["ms_per_step"] - 1e3 / d["value"]) < 1e-9 * d["ms_per_step"]
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert cb["sample"] and "workload" in d["config"]
+    assert d["e2e"] == {"value": d["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    assert _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
