@@ -117,6 +117,12 @@ class _Force:
     def torques(self):
         return self._sim()._force_arrays(self)[1]
 
+    @property
+    def energies(self):
+        """Per-particle energies (HOOMD's Force.energies): half of each pair's or bond's
+        energy on each of its two particles, so they sum to ``energy``."""
+        return self._sim()._force_arrays(self)[2]
+
 
 class OxDNABonded(_Force):
     """FENE backbone, bonded excluded volume and (optional) DNA/RNA stacking between
