@@ -78,6 +78,10 @@ class _FakeLib:
         self.calls.append(("run", s.value, n))
         return 0
 
+    def oxg_system_set_surrogate(self, s, mlp, flags, every, mod, tol):
+        self.calls.append(("set_surrogate", s.value, mlp, flags))
+        return 0
+
     def __getattr__(self, name):  # parameter setters, buffer, stream
         if not name.startswith("oxg_"):
             raise AttributeError(name)
@@ -198,3 +202,22 @@ def test_integrator_swap_keeps_the_state(fake):
                           moved[0][:, :3].astype(np.float64) + moved[1][:, :3])
     assert np.array_equal(st[2], moved[2])
     assert fake.systems[h1]["integ"][0] == 0.002 and fake.systems[h1]["integ"][1] == 0.11
+
+
+def test_surrogate_is_reapplied_after_a_rebuild(fake):
+    import types
+    sim, forces, lang = _sim()
+    net = types.SimpleNamespace(handle=C.c_void_p(4242))
+    sim.set_surrogate(net, run=True, compute=False)
+    h0 = [c for c in fake.calls if c[0] == "system_create"][-1][1]
+    assert ("set_surrogate", h0) == fake.calls[-1][:2]
+    forces[1].params[("A", "A")] = dict(forces[1].params[("A", "A")])  # a parameter write
+    sim.run(1)
+    h1 = [c for c in fake.calls if c[0] == "system_create"][-1][1]
+    assert h1 != h0
+    assert [c for c in fake.calls if c[0] == "set_surrogate" and c[1] == h1]
+    sim.set_surrogate(None)
+    n0 = len(fake.calls)
+    forces[1].params[("A", "A")] = dict(forces[1].params[("A", "A")])
+    sim.run(1)
+    assert "set_surrogate" not in _kinds(fake, n0)  # switched off: not reapplied
