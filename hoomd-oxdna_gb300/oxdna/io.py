@@ -48,6 +48,8 @@ def read_topology(top_path):
             k, head = next(lines)
         except StopIteration:
             raise ValueError(f"{top_path}: empty topology") from None
+        if len(head) < 2:
+            raise ValueError(f"{top_path}:{k}: expected the header 'N n_strands'")
         n, n_strands = int(head[0]), int(head[1])
         body = [(k, f) for _, (k, f) in zip(range(n), lines)]
     if len(body) < n:

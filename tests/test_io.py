@@ -139,6 +139,9 @@ def test_malformed_topology(tmp_path):
     top.write_text("2 1\n1 A -1\n1 G 0 -1\n")
     with pytest.raises(ValueError, match=r"bad.top:2: expected"):
         io.read_topology(top)
+    top.write_text("2\n1 A -1 1\n1 G 0 -1\n")
+    with pytest.raises(ValueError, match=r"bad.top:1: expected the header"):
+        io.read_topology(top)
     # blank lines between records are tolerated
     top.write_text("2 1\n\n1 A -1 1\n\n1 U 0 -1\n")
     t = io.read_topology(top)
