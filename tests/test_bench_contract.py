@@ -41,3 +41,24 @@ def test_reference_arm_prints_one_contract_line():
 
 def test_reference_arm_other_ranks_exit_quietly():
     assert _run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
+
+
+def test_compute_roofline_arithmetic(monkeypatch):
+    """The compute roofline of the bench line: the flop census per step over the step
+    time against the measured FP32 and special-function peaks (replaced here by fixed
+    numbers; nothing touches a device)."""
+    import types
+
+    import bench  # the repository root is on the path (conftest)
+    from oxdna import runtime
+    monkeypatch.setattr(runtime, "device_peaks", lambda stream=None: (60_000.0, 8_000.0))
+    r = bench.compute_roofline(0.016, types.SimpleNamespace(cuda_stream=None))
+    census = json.load(open(bench.FLOP_COUNTS))["workloads"]["8000nt"]
+    assert r["flops_per_step"] == census["flops_per_step"] > 0
+    assert abs(r["achieved"] - census["flops_per_step"] / 0.016e-3 / 1e12) < 1e-12
+    assert r["peak"] == 60.0 and r["unit"] == "TFLOP/s"
+    assert abs(r["frac"] - r["achieved"] / 60.0) < 1e-15
+    sp = r["special"]
+    assert sp["ops_per_step"] == sum(census["special_per_step"].values())
+    assert abs(sp["frac"] - sp["achieved"] / 8_000.0) < 1e-15
+    assert 0.0 < r["frac"] < 1.0 and 0.0 < sp["frac"] < 1.0
