@@ -166,3 +166,34 @@ def test_tiled_duplex_system_layout():
     assert abs(d.min() - 8.0) < 1e-9
     t = s["typeid"][:16]
     assert all(t[k] + t[15 - k] == 3 for k in range(8))
+
+
+def test_against_the_reference_io(tmp_path):
+    """The reference's own io.py on the same inputs (tests/golden/io_golden.npz, from
+    make_io_golden.py): quaternions of every branch (the same sign), the topology and
+    both configuration frames, and build_snapshot with and without half-charged ends."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "io_golden.npz"))
+    q = io.orientations_to_quaternions(g["frames/a1"], g["frames/a3"])
+    assert np.abs(q - g["frames/quat"]).max() < 1e-14
+    top, conf = tmp_path / "s.top", tmp_path / "s.conf"
+    top.write_text(str(g["files/top"]))
+    conf.write_text(str(g["files/conf"]))
+    t = io.read_topology(top)
+    for k in ("strand", "n3", "n5"):
+        assert np.array_equal(t[k], g[f"top/{k}"]), k
+    assert t["base"] == list(g["top/base"])
+    frames = list(io.iter_conf_frames(conf))
+    assert np.array_equal([f[0] for f in frames], g["conf/t"])
+    assert np.array_equal([f[1] for f in frames], g["conf/box"])
+    assert np.array_equal(np.array([f[2] for f in frames]), g["conf/arr"])
+    for tag, half in (("plain", False), ("half", True)):
+        for frame in (0, 1):
+            s = io.build_snapshot(top, conf, frame=frame, half_charged_ends=half)
+            key = f"snap/{tag}/{frame}"
+            assert np.array_equal(s.particles.position, g[key + "/position"])
+            assert np.abs(s.particles.orientation - g[key + "/orientation"]).max() < 1e-14
+            assert np.array_equal(s.particles.typeid, g[key + "/typeid"])
+            assert np.array_equal(s.particles.charge, g[key + "/charge"])
+            assert np.array_equal(s.bonds.group, g[key + "/bonds"])
+            assert np.array_equal(np.asarray(s.configuration.box, float), g[key + "/box"])
