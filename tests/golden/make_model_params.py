@@ -101,6 +101,14 @@ def _is_type_spec(v):
     return isinstance(v, tuple) and len(v) > 0 and all(isinstance(x, type) for x in v)
 
 
+def _shape(v):
+    """A spec entry as text: 'float', 'bool', or a list of those for a tuple."""
+    if isinstance(v, tuple):
+        return [_shape(x) for x in v]
+    t = v if isinstance(v, type) else type(v)
+    return t.__name__
+
+
 def _plain(v):
     if isinstance(v, (list, tuple)):
         return [_plain(x) for x in v]
@@ -129,9 +137,11 @@ def main(ref_root):
             defaults = {p: _plain(v) for p, v in spec.get("_defaults", {}).items()}
             defaults.update({p: _plain(v) for p, v in spec.items()
                              if p != "_defaults" and not _is_type_spec(v)})
+            shape = {p: _shape(v) for p, v in spec.items() if p != "_defaults"}
             entry["forces"].append({"class": type(f).__name__,
                                     "default_r_cut": getattr(f, "default_r_cut", None),
-                                    "params": params, "defaults": defaults})
+                                    "params": params, "defaults": defaults, "spec": shape,
+                                    "len_keys": f._typeparams["params"].param_dict.len_keys})
         out.append(entry)
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "model_params.json")
     with open(path, "w") as fh:

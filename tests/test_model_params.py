@@ -38,6 +38,13 @@ def test_model_parameters_match_the_reference(case):
     assert [type(f).__name__ for f in forces] == [g["class"] for g in case["forces"]]
     for f, g in zip(forces, case["forces"]):
         name = g["class"]
+        # the parameter declaration: the same keys, kinds and tuple widths, keyed the
+        # same way, and the same keys optional
+        def shape(v):
+            return [shape(x) for x in v] if isinstance(v, tuple) else v.__name__
+        assert {p: shape(v) for p, v in f.params._spec.items()} == g["spec"], name
+        assert f.params._len_keys == g["len_keys"], name
+        assert set(f.params._defaults) == set(g["defaults"]), name
         if g["default_r_cut"] is not None:
             assert math.isclose(f.default_r_cut, g["default_r_cut"], rel_tol=1e-14), name
         for key, ref in g["params"].items():
