@@ -255,7 +255,50 @@ int run_eval(const P& p, const double dr[3], const double qi[4], const double qj
     *e = E;
     return 1;
 }
+// The reference's own dict -> param_type constructor beside this project's route
+// (dict -> POD struct -> cvt), both serialised by the reference's own toPython() /
+// asDict(): the caller compares the two dicts. Called through ctypes.PyDLL (GIL held).
+template <class T, class POD> PyObject* pair_dicts(PyObject* d, const void* pod)
+{
+    pybind11::dict v = pybind11::reinterpret_borrow<pybind11::dict>(pybind11::handle(d));
+    T a(v, false);
+    T b = cvt(static_cast<const POD*>(pod));
+    return pybind11::make_tuple(a.toPython(), b.toPython()).release().ptr();
+}
 } // namespace
+
+extern "C" PyObject* ref_param_dicts(int term, PyObject* d, const void* pod)
+{
+    try
+        {
+        switch (term)
+            {
+        case 0: return pair_dicts<OxDNAExcVolParams, oxg_excvol_params>(d, pod);
+        case 1: return pair_dicts<OxDNAHBondParams, oxg_hbond_params>(d, pod);
+        case 2: return pair_dicts<OxDNACrossStackingParams, oxg_cross_params>(d, pod);
+        case 3: return pair_dicts<OxDNAHBondCrossParams, oxg_hbondcross_params>(d, pod);
+        case 4: return pair_dicts<OxDNACoaxStackingParams, oxg_coax_params>(d, pod);
+        case 5: return pair_dicts<OxDNADebyeParams, oxg_debye_params>(d, pod);
+        case 6:
+            {
+            pybind11::dict v = pybind11::reinterpret_borrow<pybind11::dict>(pybind11::handle(d));
+            oxdna_bonded_params a(v);
+            oxdna_bonded_params b = cvt(static_cast<const oxg_bonded_params*>(pod));
+            return pybind11::make_tuple(a.asDict(), b.asDict()).release().ptr();
+            }
+            }
+        PyErr_SetString(PyExc_ValueError, "term must be 0..6");
+        }
+    catch (pybind11::error_already_set& e)
+        {
+        e.restore();
+        }
+    catch (const std::exception& e)
+        {
+        PyErr_SetString(PyExc_RuntimeError, e.what());
+        }
+    return nullptr;
+}
 
 extern "C" {
 

@@ -74,3 +74,43 @@ def test_system_driver_matches_reference(oracle):
         assert maxrel(r["bonded_energy"], g["bonded/energy"]) < TOL_ORACLE
         assert maxrel(r["force"], g["bonded/force"]) < TOL_ORACLE
         assert maxrel(r["torque"], g["bonded/torque"]) < TOL_ORACLE
+
+
+def test_parameter_structs_match_the_reference_constructors():
+    """This build's route from a parameter dict to the evaluators' param_type (dict ->
+    POD struct -> field copy in oracle/ref_wrap.cpp) against the reference's own
+    pybind11 dict constructors, both serialised by the reference's own toPython() /
+    asDict(), for every type pair and bond type of the three models. Needs the
+    reference-pin libraries (oracle/_ref, built where the reference tree is present).
+    Skipped fields: for DNA bonds the reference constructor leaves the oxRNA-only
+    stacking angles (stack_f4_tB1, stack_f4_tB2) uninitialised; they are never read."""
+    import ctypes as C
+    import os
+
+    from oxdna import _abi
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "oracle", "_ref", "libref64.so")
+    if not os.path.exists(path):
+        pytest.skip("reference-pin libraries not built here")
+    fn = C.PyDLL(path).ref_param_dicts
+    fn.restype = C.py_object
+    fn.argtypes = [C.c_int, C.py_object, C.c_void_p]
+    n = 0
+    for model in MODELS:
+        for avg in (True, False):
+            pair, bonded = model_forces(model, average=avg)
+            for t, f in enumerate(pair):
+                for key, d in f.params.items():
+                    p = _abi.FROM_DICT[t](d)
+                    ref, ours = fn(t, dict(d), C.addressof(p))
+                    assert ref == ours, (model, t, key)
+                    n += 1
+            for key, d in bonded.params.items():
+                p = _abi.bonded_from_dict(d)
+                ref, ours = fn(6, dict(d), C.addressof(p))
+                skip = set() if d.get("stack_rna") else {"stack_f4_tB1", "stack_f4_tB2"}
+                assert set(ref) == set(ours)
+                for k in set(ref) - skip:
+                    assert ref[k] == ours[k], (model, key, k)
+                n += 1
+    assert n > 300
