@@ -229,3 +229,23 @@ def test_engine_sync_keys_follow_parameter_changes():
     sim.operations.integrator.forces.append(dna2.debye_huckel(forces[1].nlist))
     assert F._changes[0] > c1
     assert sim._forces_key()[1] != k1[1]
+
+
+def test_header_is_plain_c99_and_cxx(tmp_path):
+    """include/oxdna_gb300.h compiles as strict C99 and as C++17 with every entry point
+    it declares referenced: what a cgo, N-API or ctypes binding author includes."""
+    import shutil
+    import subprocess
+    names = _header_functions()
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "oxdna_gb300.h"\n'
+                   "typedef void (*fn)(void);\n"
+                   "fn table[] = {" + ", ".join(f"(fn){n}" for n in names) + "};\n"
+                   "int main(void) { return table[0] == 0; }\n")
+    inc = os.path.join(ROOT, "include")
+    for cmd in (["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only"],
+                ["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", "c++"]):
+        if shutil.which(cmd[0]) is None:
+            pytest.skip(f"{cmd[0]} not available")
+        out = subprocess.run(cmd + ["-I", inc, str(src)], capture_output=True, text=True)
+        assert out.returncode == 0, out.stderr
