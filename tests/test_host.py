@@ -249,3 +249,27 @@ def test_header_is_plain_c99_and_cxx(tmp_path):
             pytest.skip(f"{cmd[0]} not available")
         out = subprocess.run(cmd + ["-I", inc, str(src)], capture_output=True, text=True)
         assert out.returncode == 0, out.stderr
+
+
+def test_no_cpu_fallback_without_a_gpu():
+    """Without a CUDA device the product path fails loudly: the native context cannot
+    be created and run() raises the library's CUDA error instead of computing on the
+    host (there is no CPU path); a CPU device is refused outright."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from oxdna import _abi, io, runtime
+    from oxdna.model import dna1, dna2
+    with pytest.raises(RuntimeError, match="GPU only"):
+        runtime.device.CPU()
+    forces, _ = dna2.forces()
+    sim = runtime.Simulation(device=runtime.device.GPU(), seed=1)
+    sim.create_state_from_snapshot(io.system_snapshot(io.duplex_system(1, 6, 20.0)))
+    lang = runtime.md.methods.Langevin(filter=runtime.filter.All(), kT=dna1.kT_from_temperature(300))
+    sim.operations.integrator = runtime.md.Integrator(dt=0.003, integrate_rotational_dof=True,
+                                                      forces=forces, methods=[lang])
+    with pytest.raises(_abi.OxgError) as err:
+        sim.run(10)
+    assert err.value.code == 2 and "CUDA" in str(err.value)
+    with pytest.raises(RuntimeError, match="not attached"):
+        forces[1].energy
