@@ -1627,20 +1627,43 @@ namespace {
 
 std::mutex g_na_mutex;
 void* g_na_ptr[256];  // device address of g_noalloc_scratch, per device ordinal
+void* g_na_ctx[256];  // the driver context that address belongs to
 
-// Set-up, once per device with that device current: the symbol's device address.
+// The current driver context (cuCtxGetCurrent through the runtime's entry-point query,
+// so the library needs no link against the driver library); null if unavailable.
+void* current_driver_context()
+{
+    using CtxGetCurrent = int (*)(void**);
+    static CtxGetCurrent fn = []() -> CtxGetCurrent {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<CtxGetCurrent>(f);
+    }();
+    void* ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+// Set-up, once per device with that device current: the symbol's device address. The
+// address is looked up again when the device's context has changed since (after a
+// cudaDeviceReset the module is loaded again, possibly at another address).
 int noalloc_scratch(unsigned char** out)
 {
     int dev = 0;
     OXG_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 256) return set_err(OXG_ERR_INVALID_ARG, "device ordinal out of range");
+    void* const ctx = current_driver_context();  // null before the runtime's first call on this thread
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
+    if (!g_na_ptr[dev] || !ctx || ctx != g_na_ctx[dev]) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess)
             return set_err(OXG_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
         g_na_ptr[dev] = p;
+        g_na_ctx[dev] = current_driver_context();  // current now: the lookup initialised it
     }
     *out = static_cast<unsigned char*>(g_na_ptr[dev]);
     return OXG_OK;
@@ -1686,8 +1709,13 @@ __global__ void k_noalloc_excl(int N, int n_bonds, const int* bonds, int4* excl,
     for (int pass = 0; pass < 2; ++pass) {
         int* e = reinterpret_cast<int*>(excl + (pass ? B : A));
         const int other = pass ? A : B;
+        // a bond listed twice (or as both (A, B) and (B, A)) takes one slot: a slot that
+        // already holds the partner counts as stored
         bool stored = false;
-        for (int k = 0; k < 4 && !stored; ++k) stored = atomicCAS(e + k, -1, other) == -1;
+        for (int k = 0; k < 4 && !stored; ++k) {
+            const int prev = atomicCAS(e + k, -1, other);
+            stored = prev == -1 || prev == other;
+        }
         if (!stored) atomicOr(&st->flags, kStExclOverflow);
     }
 }

@@ -186,10 +186,21 @@ class _Langevin(_Tracked):
         self.filter = filter
         self.kT = float(kT)
         self.default_gamma = float(default_gamma)
-        g = tuple(default_gamma_r) if hasattr(default_gamma_r, "__len__") else (default_gamma_r,) * 3
-        if len(set(g)) != 1:
-            raise ValueError("anisotropic gamma_r is not supported")
-        self.default_gamma_r = g
+        self.default_gamma_r = default_gamma_r
+
+    def __setattr__(self, name, value):
+        # every assignment, not only the constructor's, is normalised and checked: the
+        # engine takes one rotational drag coefficient (isotropic gamma_r)
+        if name == "default_gamma_r":
+            g = tuple(float(x) for x in value) if hasattr(value, "__len__") else (float(value),) * 3
+            if len(g) != 3:
+                raise ValueError("default_gamma_r needs 3 components (or one scalar)")
+            if len(set(g)) != 1:
+                raise ValueError("anisotropic gamma_r is not supported")
+            value = g
+        elif name in ("kT", "default_gamma"):
+            value = float(value)
+        super().__setattr__(name, value)
 
 
 class _Integrator(_Tracked):
@@ -242,6 +253,16 @@ class _State:
 # --------------------------------------------------------------------- simulation
 def _f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _check_unit_inertia(moment_inertia):
+    """The engine integrates every particle with the unit moment of inertia the oxDNA
+    builders set (reference io.py: moment_inertia = 1); any other value is refused
+    rather than ignored."""
+    mi = np.asarray(moment_inertia, dtype=np.float64)
+    if mi.size and not np.all(mi == 1.0):
+        raise ValueError("moment_inertia other than (1, 1, 1) is not supported: the engine "
+                         "integrates the rotations with unit moments of inertia")
 
 
 class Simulation:
@@ -497,6 +518,7 @@ class Simulation:
         angmom (float32, N x 4) and charge (N)."""
         p = self._snap.particles
         n = p.N
+        _check_unit_inertia(p.moment_inertia)
         pos = np.zeros((n, 4), np.float32)
         x = np.asarray(p.position, np.float64)
         pos[:, :3] = x
@@ -546,6 +568,7 @@ class Simulation:
 
     # -- read-outs -----------------------------------------------------------
     def _energies(self):
+        self._sync()  # a parameter changed since the last run is in effect for read-outs too
         if "energies" not in self._cache:
             L = _abi.lib()
             pe = (C.c_double * 6)()
@@ -565,6 +588,7 @@ class Simulation:
         return float(self._energies()[1][k])
 
     def _force_arrays(self, f):
+        self._sync()
         key = ("arrays", id(f))
         if key not in self._cache:
             L = _abi.lib()

@@ -22,6 +22,20 @@ def golden(name):
     return np.load(os.path.join(GOLDEN, name))
 
 
+# Pair-term golden cases (model, term id, "avg" | "seq"): every term with the
+# sequence-averaged parameters, plus the two terms whose parameters depend on the
+# sequence (hydrogen bonding and fused HB + cross-stacking: per-type-pair eps,
+# reference oxdna/model/dna1.py:186-194, dna2.py:117-121, rna2.py:147-152) with
+# average=False.
+SEQ_TERMS = (1, 3)
+PAIR_CASES = [(m, t, "avg") for m in ("dna1", "dna2", "rna2") for t in range(6)] + \
+             [(m, t, "seq") for m in ("dna1", "dna2", "rna2") for t in SEQ_TERMS]
+
+
+def pair_golden(model, avg):
+    return golden(f"pairs_{model}.npz" if avg == "avg" else f"pairs_{model}_seq.npz")
+
+
 def maxrel(x, ref):
     x = np.asarray(x, float)
     ref = np.asarray(ref, float)

@@ -14,6 +14,9 @@ writes are committed so that the tests run anywhere. Contents:
 * ``bonds_<model>.npz``  per-bond inputs and FP64/FP32 outputs of
   oxdna_bonded_pair (FENE, bonded excluded volume, DNA/RNA stacking), sequence-
   averaged and sequence-dependent, including stretched and broken bonds.
+* ``pairs_<model>_seq.npz``  as ``pairs_<model>.npz`` for the sequence-dependent
+  parameters (average=False) of the two terms that have them: hydrogen bonding and
+  fused HB + cross-stacking (per-type-pair eps).
 * ``system_dna2.npz``  per-term energies, per-particle forces and torques of the
   perturbed 320-nt oxDNA2 system, summed from reference per-pair calls with the
   HOOMD driver semantics (all unordered non-bonded pairs, dr = r_i - r_j minimum
@@ -78,8 +81,8 @@ def min_image(d, L=BOX):
     return d - L * np.round(d / L)
 
 
-def pair_samples(name, rng):
-    pair, _ = model_forces(name)
+def pair_samples(name, rng, average=True, terms=range(6)):
+    pair, _ = model_forces(name, average=average)
     base = io.duplex_system(8, 20, BOX, seed=1)
     geoms = [(base["pos"], base["quat"])]
     for sx, sa in ((0.03, 0.05), (0.08, 0.15), (0.15, 0.3)):
@@ -88,7 +91,7 @@ def pair_samples(name, rng):
     charges = np.where(base["ends"], 0.5, 1.0)
     r64, r32 = O.ref_lib(64), O.ref_lib(32)
     out = {}
-    for t in range(6):
+    for t in terms:
         f = pair[t]
         rows = []
         for gi, (pos, q) in enumerate(geoms):
@@ -239,6 +242,13 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"pairs_{name}.npz"), **pair_samples(name, rng))
         np.savez_compressed(os.path.join(HERE, f"bonds_{name}.npz"), **bond_samples(name, rng))
     np.savez_compressed(os.path.join(HERE, "system_dna2.npz"), **system_golden(rng))
+    # sequence-dependent hydrogen bonding (per-type-pair eps): the HB and fused HB +
+    # cross-stacking terms with average=False, from a stream of their own so the
+    # fixtures above do not change
+    rng_seq = np.random.default_rng(SEED + 1)
+    for name in ("dna1", "dna2", "rna2"):
+        np.savez_compressed(os.path.join(HERE, f"pairs_{name}_seq.npz"),
+                            **pair_samples(name, rng_seq, average=False, terms=(1, 3)))
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -9,7 +9,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from _util import TERMS, TOL_GPU, golden, maxrel, model_forces
+from _util import PAIR_CASES, TERMS, TOL_GPU, golden, maxrel, model_forces, pair_golden
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "native", "devmath.cu")
@@ -44,13 +44,12 @@ def _p(a):
     return np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.POINTER(C.c_double))
 
 
-@pytest.mark.parametrize("model", ("dna1", "dna2", "rna2"))
-@pytest.mark.parametrize("term", range(6))
-def test_fp32_pair_math(devmath, model, term):
+@pytest.mark.parametrize("model,term,avg", PAIR_CASES)
+def test_fp32_pair_math(devmath, model, term, avg):
     from oxdna import _abi, io
-    d = golden(f"pairs_{model}.npz")
+    d = pair_golden(model, avg)
     name = TERMS[term]
-    f = model_forces(model)[0][term]
+    f = model_forces(model, average=(avg == "avg"))[0][term]
     n = len(d[name + "/dr"])
     F, E, TI, TJ = np.zeros((n, 3)), np.zeros(n), np.zeros((n, 3)), np.zeros((n, 3))
     for k in range(n):

@@ -112,3 +112,30 @@ def test_replica_larger_than_tile_is_rejected(native):
     b, _ = _batch(work)
     with pytest.raises(_abi.OxgError, match="tile capacity"):
         b.set_tiling(64, 64)
+
+
+def test_mixed_duplexes_and_hairpins(native, oracle):
+    """Replicas of uneven size mixing duplexes and hairpins (half of them single-strand
+    hairpins of the same nucleotide count): per-replica energies against the FP64
+    oracle, then 20 steps that follow single-system runs with the same seeds."""
+    from oxdna import io, replicas
+    work = replicas.replica_workload(10, bp_range=(12, 40), seed=12, hairpin_fraction=0.5)
+    kinds = [len(s["bonds"]) == len(s["pos"]) - 1 for s, _ in work]  # one strand: a hairpin
+    assert any(kinds) and not all(kinds)
+    b, sims = _batch(work, seed=31)
+    _, _, e = b.compute()
+    for r, (s, _T) in enumerate(work):
+        model = oracle.Model(sims[r]._forces, io.DNA_BASES)
+        ref = oracle.forces(model, oracle.System(s["pos"], s["quat"], s["typeid"], s["box"],
+                                                 s["bonds"]))
+        want = np.concatenate([ref["pair_energy"], ref["bonded_energy"]])
+        assert np.abs(e[r] - want).max() <= TOL_GPU * np.abs(want).max(), (r, kinds[r])
+    b.run(20)
+    for r, sim in enumerate(sims):
+        sim.run(20)
+        x = b.positions(r)
+        p = sim.state.get_snapshot().particles.position
+        L = work[r][0]["box"][0]
+        d = x - p
+        d -= L * np.round(d / L)
+        assert np.abs(d).max() < 2e-3, (r, kinds[r])

@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from _util import TERMS, TOL_GPU, golden, maxrel, model_forces
+from _util import PAIR_CASES, TERMS, TOL_GPU, golden, maxrel, model_forces, pair_golden
 
 pytestmark = pytest.mark.gpu
 MODELS = ("dna1", "dna2", "rna2")
@@ -49,12 +49,11 @@ def _pair_snapshot(dr, qi, qj, types, charges, spacing=12.0):
     return io.snapshot_from_arrays(pos, q, ty, [L, L, L], charges=ch)
 
 
-@pytest.mark.parametrize("model", MODELS)
-@pytest.mark.parametrize("term", range(6))
-def test_engine_pair_terms_match_reference(native, model, term):
-    d = golden(f"pairs_{model}.npz")
+@pytest.mark.parametrize("model,term,avg", PAIR_CASES)
+def test_engine_pair_terms_match_reference(native, model, term, avg):
+    d = pair_golden(model, avg)
     name = TERMS[term]
-    f = model_forces(model)[0][term]
+    f = model_forces(model, average=(avg == "avg"))[0][term]
     snap = _pair_snapshot(d[name + "/dr"], d[name + "/qi"], d[name + "/qj"], d[name + "/types"],
                           d[name + "/charges"])
     sim = _sim(snap, [f])
@@ -189,14 +188,17 @@ def test_dropin_full_nlist_and_bonds(native, oracle):
     for t in (0, 1, 2, 3, 4, 5):
         force = torch.zeros((n, 4), dtype=torch.float32, device=dev)
         torque = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        virial = torch.zeros((6, n), dtype=torch.float32, device=dev)
         energy = torch.zeros(6, dtype=torch.float64, device=dev)
         _abi.check(L.oxg_pair_forces(ctx, 1 << t, n, ptr(pos_d), ptr(quat_d), ptr(ch_d), box,
                                      ptr(nn_d), ptr(fl_d), ptr(hd_d), ptr(force), ptr(torque),
-                                     None, ptr(energy), None), "pair_forces")
+                                     ptr(virial), ptr(energy), None), "pair_forces")
         _abi.check(L.oxg_context_status(ctx, 1), "status")
-        # oracle with the full-list semantics: particle i gets sum_j eval(i, j)
+        # oracle with the full-list semantics: particle i gets sum_j eval(i, j), and
+        # HOOMD's pair virial W_i = sum_j 0.5 * dr_ij (x) F_i (xx, xy, xz, yy, yz, zz)
         Fo = np.zeros((n, 3))
         To = np.zeros((n, 3))
+        Vo = np.zeros((6, n))
         Eo = 0.0
         f = pair[t]
         for i in range(n):
@@ -211,26 +213,43 @@ def test_dropin_full_nlist_and_bonds(native, oracle):
                                                     g["charge"][j])
                 Fo[i] += fi
                 To[i] += ti
+                Vo[:, i] += 0.5 * np.array([d[0] * fi[0], d[0] * fi[1], d[0] * fi[2],
+                                            d[1] * fi[1], d[1] * fi[2], d[2] * fi[2]])
                 Eo += 0.5 * e
         Fg = force.cpu().numpy()
         Tg = torque.cpu().numpy()
         if np.abs(Fo).max() > 0:
             assert maxrel(Fg[:, :3], Fo) < TOL_GPU, TERMS[t]
             assert maxrel(Tg[:, :3], To) < TOL_GPU, TERMS[t]
+            assert maxrel(virial.cpu().numpy(), Vo) < TOL_GPU, TERMS[t]
         assert abs(energy[t].item() - Eo) <= TOL_GPU * max(abs(Eo), 1e-6), TERMS[t]
     # bonded drop-in
     bonds = torch.tensor(np.c_[g["bonds"], np.zeros(len(g["bonds"]))].astype(np.int64),
                          device=dev).to(torch.int32)
     force = torch.zeros((n, 4), dtype=torch.float32, device=dev)
     torque = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    virial = torch.zeros((6, n), dtype=torch.float32, device=dev)
     split = torch.zeros(3, dtype=torch.float64, device=dev)
     _abi.check(L.oxg_bonded_forces(ctx, n, ptr(pos_d), ptr(quat_d), box, len(g["bonds"]),
-                                   ptr(bonds), ptr(force), ptr(torque), None, ptr(split), None),
-               "bonded_forces")
+                                   ptr(bonds), ptr(force), ptr(torque), ptr(virial), ptr(split),
+                                   None), "bonded_forces")
     _abi.check(L.oxg_context_status(ctx, 1), "status")
     assert maxrel(force.cpu().numpy()[:, :3], g["bonded/force"]) < TOL_GPU
     assert maxrel(torque.cpu().numpy()[:, :3], g["bonded/torque"]) < TOL_GPU
     assert maxrel(split.cpu().numpy(), g["bonded/energy"]) < TOL_GPU
+    # the bonded half virial (reference OxDNABondedKernel.h:48-58, written to both ends
+    # at OxDNABondedGPU.cu:120-121) from the oracle's bonded kernel, pinned to the
+    # reference's own by tests/test_oracle_pin.py
+    bp_o = _abi.bonded_from_dict(bonded.params["backbone"])
+    Vb = np.zeros((6, n))
+    for A, B in g["bonds"]:
+        Rc = g["pos"][B] - g["pos"][A]
+        Rc -= g["box"] * np.round(Rc / g["box"])
+        vir = oracle.eval_bonded(oracle.oracle_lib(), "oxo", bp_o, Rc, g["quat"][A], g["quat"][B],
+                                 g["typeid"][A], g["typeid"][B])[4]
+        Vb[:, A] += vir
+        Vb[:, B] += vir
+    assert maxrel(virial.cpu().numpy(), Vb) < TOL_GPU
     # an out-of-range neighbour index is skipped and reported, not dereferenced
     bad = fl_d.clone()
     bad[0] = n + 5

@@ -273,3 +273,36 @@ def test_no_cpu_fallback_without_a_gpu():
     assert err.value.code == 2 and "CUDA" in str(err.value)
     with pytest.raises(RuntimeError, match="not attached"):
         forces[1].energy
+
+
+def test_langevin_gamma_r_checked_on_every_assignment():
+    """default_gamma_r is normalised and checked when assigned after construction too:
+    the engine takes one isotropic rotational drag coefficient."""
+    from oxdna import runtime
+    lang = runtime.md.methods.Langevin(filter=runtime.filter.All(), kT=0.1)
+    assert lang.default_gamma_r == (1.0, 1.0, 1.0)
+    lang.default_gamma_r = 2
+    assert lang.default_gamma_r == (2.0, 2.0, 2.0)
+    lang.default_gamma_r = [3, 3, 3]
+    assert lang.default_gamma_r == (3.0, 3.0, 3.0)
+    with pytest.raises(ValueError, match="anisotropic"):
+        lang.default_gamma_r = (1, 2, 3)
+    with pytest.raises(ValueError, match="3 components"):
+        lang.default_gamma_r = (1, 1)
+    assert lang.default_gamma_r == (3.0, 3.0, 3.0)
+    with pytest.raises(ValueError, match="anisotropic"):
+        runtime.md.methods.Langevin(filter=runtime.filter.All(), kT=0.1, default_gamma_r=(1, 1, 2))
+
+
+def test_non_unit_moment_of_inertia_is_refused():
+    """The engine integrates rotations with unit moments of inertia (the value the oxDNA
+    builders set); a snapshot with other values is refused, not silently ignored."""
+    from oxdna import io, runtime
+    s = io.duplex_system(2, 8, 20.0, seed=1)
+    snap = io.system_snapshot(s)
+    sim = runtime.Simulation(device=runtime.device.GPU())
+    sim.create_state_from_snapshot(snap)
+    sim._state_arrays()  # unit inertia: accepted
+    snap.particles.moment_inertia[3] = (1.0, 2.0, 1.0)
+    with pytest.raises(ValueError, match="moment_inertia"):
+        sim._state_arrays()

@@ -4,18 +4,17 @@ tests/golden/make_golden.py from the reference headers compiled unchanged)."""
 import numpy as np
 import pytest
 
-from _util import TERMS, TOL_ORACLE, golden, maxrel, model_forces
+from _util import PAIR_CASES, TERMS, TOL_ORACLE, golden, maxrel, model_forces, pair_golden
 
 MODELS = ("dna1", "dna2", "rna2")
 
 
-@pytest.mark.parametrize("model", MODELS)
-@pytest.mark.parametrize("term", range(6))
-def test_pair_evaluators_match_reference(oracle, model, term):
+@pytest.mark.parametrize("model,term,avg", PAIR_CASES)
+def test_pair_evaluators_match_reference(oracle, model, term, avg):
     from oxdna import _abi, io
-    d = golden(f"pairs_{model}.npz")
+    d = pair_golden(model, avg)
     name = TERMS[term]
-    f = model_forces(model)[0][term]
+    f = model_forces(model, average=(avg == "avg"))[0][term]
     L = oracle.oracle_lib()
     n = len(d[name + "/dr"])
     got = {k: [] for k in ("flag", "force", "energy", "torque_i", "torque_j")}

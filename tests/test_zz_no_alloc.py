@@ -1,8 +1,10 @@
 """oxg_pair_forces_noalloc: the nonbonded evaluation for callers that cannot
 allocate GPU memory (a framework owning the whole device pool, or a host that forbids
 cudaMalloc inside its loop). It keeps all scratch in a fixed static device array, so
-it must give the same result as the allocating system engine, and a second call must
-not be disturbed by what the first left in that shared array.
+it must give the same result as the allocating system engine and as the FP64 oracle,
+a second call must not be disturbed by what the first left in that shared array, and a
+bond table that lists a bond twice must still fit the four exclusion slots a particle
+has.
 
 Collected last on purpose (file name), so a failing run that stops at the first
 failure has already run every other test."""
@@ -27,7 +29,7 @@ def _state(sysarr):
     return pos, pt, sysarr["quat"].astype(np.float32)
 
 
-def test_noalloc_matches_engine_on_two_calls(native):
+def test_noalloc_matches_engine_on_two_calls(native, oracle):
     import torch
 
     from oxdna import _abi, io, runtime
@@ -79,6 +81,25 @@ def test_noalloc_matches_engine_on_two_calls(native):
         for t in range(6):
             if (mask >> t) & 1:
                 assert abs(E[t] - e_ref[t]) <= TOL_GPU * max(abs(e_ref[t]), 1e-6), (call, t)
+    # directly against the FP64 oracle on the same (float32-rounded) inputs
+    model = oracle.Model(pair_forces, io.DNA_BASES)
+    r = oracle.forces(model, oracle.System(pos, q.astype(np.float64), s["typeid"], s["box"],
+                                           s["bonds"]), bonded=False)
+    assert maxrel(F[:, :3], r["force"]) < 5e-5
+    assert maxrel(T[:, :3], r["torque"]) < 5e-5
+    for t in range(6):
+        if (mask >> t) & 1:
+            ref = r["pair_energy"][t]
+            assert abs(E[t] - ref) <= TOL_GPU * max(abs(ref), 1e-6), t
+    # every bond listed twice, once reversed: duplicates take no extra exclusion slot
+    dup = np.concatenate([bonds, bonds[:, [1, 0, 2]]])
+    dup_d = torch.tensor(dup.astype(np.int64), device=dev).to(torch.int32)
+    force.fill_(float("nan"))
+    _abi.check(L.oxg_pair_forces_noalloc(sim._ctx, mask, n, ptr(pos_d), ptr(quat_d),
+                                         ptr(charge_d), box, len(dup), ptr(dup_d),
+                                         ptr(force), ptr(torque), None, None),
+               "oxg_pair_forces_noalloc with duplicated bonds")
+    assert maxrel(force.cpu().numpy()[:, :3], f_ref[:, :3]) < TOL_GPU
     # sizes beyond the fixed scratch are rejected before any GPU work
     big = L.oxg_pair_forces_noalloc(sim._ctx, mask, 8193, ptr(pos_d), ptr(quat_d), None, box, 0,
                                     None, ptr(force), ptr(torque), None, None)
