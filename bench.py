@@ -160,10 +160,11 @@ def time_resident(sim, steps, warmup, stream, block=1000):
     return total_ms
 
 
-def bench_batched(stream, steps=2000, loop_steps=20, n_rep=512, seed=4, hairpin_fraction=0.0):
+def bench_batched(stream, steps=2000, loop_steps=200, n_rep=512, seed=4, hairpin_fraction=0.0):
     """512 independent duplex replicas (12-64 bp, box 30, 290-340 K): aggregate
     nt*steps/s of the batched engine (autotuned tile shape, one persistent launch per
-    5000 steps) against looping the single-system engine over the replicas. With
+    5000 steps) against looping the single-system engine over the replicas (each
+    replica one run(loop_steps) call; skipped when loop_steps is 0). With
     hairpin_fraction > 0 that fraction of the replicas are hairpins of the same size."""
     import torch
 
@@ -186,27 +187,30 @@ def bench_batched(stream, steps=2000, loop_steps=20, n_rep=512, seed=4, hairpin_
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     n_total = b.N
-    # the same replicas, one oxg_system each, run one after another
-    for sim in sims:
-        sim.set_stream(stream.cuda_stream)
-        sim.run(loop_steps)  # attach + graph capture (untimed)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for sim in sims:
-        sim.run(loop_steps)
-    e1.record(stream)
-    e1.synchronize()
-    ms_loop = e0.elapsed_time(e1)
     kind = (f"one duplex of 12-64 bp or ({hairpin_fraction:.0%}) a hairpin of the same size"
             if hairpin_fraction > 0 else "one duplex of 12-64 bp")
-    return {"workload": f"{n_rep} replicas x {kind} ({n_total} nt), box 30, "
-                        "290-340 K, 0.5 M, Langevin dt 0.003",
-            "n_nt": n_total, "steps": steps, "tile_particles": tile, "threads": threads,
-            "replica_steps_per_s": steps / (ms * 1e-3),
-            "nt_steps_per_s": n_total * steps / (ms * 1e-3),
-            "looped_single_nt_steps_per_s": n_total * loop_steps / (ms_loop * 1e-3),
-            "speedup_vs_looped": (n_total * steps / ms) / (n_total * loop_steps / ms_loop),
-            "launches": (steps + 4999) // 5000}
+    out = {"workload": f"{n_rep} replicas x {kind} ({n_total} nt), box 30, "
+                       "290-340 K, 0.5 M, Langevin dt 0.003",
+           "n_nt": n_total, "steps": steps, "tile_particles": tile, "threads": threads,
+           "replica_steps_per_s": steps / (ms * 1e-3),
+           "nt_steps_per_s": n_total * steps / (ms * 1e-3),
+           "launches": (steps + 4999) // 5000}
+    if loop_steps > 0:
+        # the same replicas, one oxg_system each, run one after another
+        for sim in sims:
+            sim.set_stream(stream.cuda_stream)
+            sim.run(20)  # attach (untimed)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for sim in sims:
+            sim.run(loop_steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms_loop = e0.elapsed_time(e1)
+        out["looped_single_nt_steps_per_s"] = n_total * loop_steps / (ms_loop * 1e-3)
+        out["looped_single_steps_per_call"] = loop_steps
+        out["speedup_vs_looped"] = (n_total * steps / ms) / (n_total * loop_steps / ms_loop)
+    return out
 
 
 def bench_rna(stream, steps=2000, warmup=100):
@@ -241,13 +245,21 @@ def bench_tiled(stream, steps=10000, warmup=500, copies=8):
     out = {"workload": f"oxDNA2 {copies}^3 x 8-bp duplex ({len(sysarr['pos'])} nt), box "
                        f"{copies * 8}, 296.15 K, 0.5 M, dt 0.003 (the reference benchmark's tiling)"}
     for fused in (False, True):
+        tag = "fused" if fused else "unfused"
         sim, _ = make_sim(sysarr, fused=fused, stream=stream.cuda_stream)
         sim.run(0)
         sim.run(warmup)
         torch.cuda.synchronize()
         with nvtx("timed"):
             ms = time_resident(sim, steps, 0, stream)
-        out[("fused" if fused else "unfused") + "_steps_per_s"] = steps / (ms * 1e-3)
+        out[tag + "_steps_per_s"] = steps / (ms * 1e-3)
+        # timed as the reference's benchmark times it: run(20), run(0), then the host
+        # clock around one run(500) call
+        sim.run(20)
+        sim.run(0)
+        t0 = time.perf_counter()
+        sim.run(500)
+        out[tag + "_reference_style_steps_per_s"] = 500 / (time.perf_counter() - t0)
         del sim
     return out
 
@@ -300,6 +312,117 @@ def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epoc
             out["fused_term_energy_rel_error_vs_plain"] = abs(forces[2].energy - e_plain) / abs(e_plain)
         del sim
     out["speedup_vs_plain"] = out["surrogate_steps_per_s"] / out["plain_steps_per_s"]
+    return out
+
+
+def hoomd_full_nlist(pos, box, r_list, bonds):
+    """HOOMD's neighbour-list layout for N particles: a FULL list (each pair from both
+    ends, bonded pairs excluded) as n_neigh (uint32), nlist (uint32) and head_list
+    (uint64), built on the host with a periodic k-d tree."""
+    from scipy.spatial import cKDTree
+    L = float(box[0])
+    x = np.mod(np.asarray(pos, np.float64) + 0.5 * L, L)
+    pairs = cKDTree(x, boxsize=L).query_pairs(r_list, output_type="ndarray")
+    n = len(x)
+    key = lambda a, b: np.minimum(a, b).astype(np.int64) * n + np.maximum(a, b)  # noqa: E731
+    b = np.asarray(bonds, np.int64)
+    keep = ~np.isin(key(pairs[:, 0], pairs[:, 1]), key(b[:, 0], b[:, 1]))
+    pairs = pairs[keep]
+    i = np.concatenate([pairs[:, 0], pairs[:, 1]])
+    j = np.concatenate([pairs[:, 1], pairs[:, 0]])
+    order = np.lexsort((j, i))
+    i, j = i[order], j[order]
+    n_neigh = np.bincount(i, minlength=n).astype(np.uint32)
+    head = np.concatenate([[0], np.cumsum(n_neigh)[:-1]]).astype(np.uint64)
+    return n_neigh, j.astype(np.uint32), head
+
+
+def bench_dropin(stream, sysarr, calls=200):
+    """The evaluator-level entry points a HOOMD build would call in place of the
+    reference's kernels, on HOOMD-shaped buffers (Scalar4 double positions and
+    orientations, full neighbour list of radius max r_cut + 0.4, device arrays):
+    oxg_pair_forces for each of the five oxDNA2 terms of forces(fused=False) alone (the
+    reference runs one aniso launch per term) and for all five in one call, and
+    oxg_bonded_forces; microseconds per call from CUDA events over `calls` calls."""
+    import ctypes as C
+
+    import torch
+
+    from oxdna import _abi, io
+    from oxdna.model import dna2
+    L = _abi.lib()
+    forces, _ = dna2.forces(fused=False)
+    bonded, pair = forces[0], forces[1:]
+    n = len(sysarr["pos"])
+    ctx = C.c_void_p()
+    _abi.check(L.oxg_create(C.byref(ctx), 4, 1), "oxg_create")
+    setters = {_abi.EXCVOL: L.oxg_set_excvol_params, _abi.HBOND: L.oxg_set_hbond_params,
+               _abi.CROSS: L.oxg_set_cross_params, _abi.COAX: L.oxg_set_coax_params,
+               _abi.DEBYE: L.oxg_set_debye_params}
+    for f in pair:
+        for a in range(4):
+            for b in range(a, 4):
+                key = (io.DNA_BASES[a], io.DNA_BASES[b])
+                _abi.check(setters[f._term](ctx, a, b, C.byref(_abi.FROM_DICT[f._term](f.params[key])),
+                                            f.rcut_for(*key)), "set params")
+    bp = _abi.bonded_from_dict(bonded.params["backbone"])
+    _abi.check(L.oxg_set_bonded_params(ctx, 0, C.byref(bp)), "oxg_set_bonded_params")
+    dev = torch.device("cuda")
+    pt = np.zeros((n, 4))
+    pt[:, :3] = sysarr["pos"]
+    pt[:, 3] = sysarr["typeid"].astype(np.int64).view(np.float64)
+    r_list = max(f.default_r_cut for f in pair) + 0.4
+    nn, flat, head = hoomd_full_nlist(sysarr["pos"], sysarr["box"], r_list, sysarr["bonds"])
+    pos_d = torch.tensor(pt, dtype=torch.float64, device=dev)
+    quat_d = torch.tensor(sysarr["quat"], dtype=torch.float64, device=dev)
+    ch_d = torch.ones(n, dtype=torch.float64, device=dev)
+    nn_d = torch.tensor(nn.astype(np.int64), device=dev).to(torch.int32)
+    fl_d = torch.tensor(flat.astype(np.int64), device=dev).to(torch.int32)
+    hd_d = torch.tensor(head.astype(np.int64), device=dev)
+    bonds = np.zeros((len(sysarr["bonds"]), 3), np.int64)
+    bonds[:, :2] = sysarr["bonds"]
+    bonds_d = torch.tensor(bonds, device=dev).to(torch.int32)
+    force = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    torque = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    box = (C.c_float * 3)(*[float(x) for x in sysarr["box"]])
+    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    sh = C.c_void_p(stream.cuda_stream)
+
+    def timed(fn):
+        for _ in range(5):
+            fn()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(calls):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        _abi.check(L.oxg_context_status(ctx, 1), "oxg_context_status")
+        return a.elapsed_time(b) * 1e3 / calls
+
+    def pair_call(mask):
+        return lambda: _abi.check(L.oxg_pair_forces(ctx, mask, n, ptr(pos_d), ptr(quat_d), ptr(ch_d), box,
+                                                    ptr(nn_d), ptr(fl_d), ptr(hd_d), ptr(force),
+                                                    ptr(torque), None, None, sh), "oxg_pair_forces")
+
+    out = {"workload": f"oxDNA2 {n} nt (the headline system), HOOMD buffers: Scalar4 double "
+                       f"positions / orientations, full list r_list {r_list:.2f} "
+                       f"({int(nn.sum())} entries, {nn.mean():.1f} per particle)",
+           "calls": calls, "us_per_call": {}}
+    all_mask = 0
+    for f in pair:
+        all_mask |= 1 << f._term
+        out["us_per_call"][_abi.TERM_NAMES[f._term]] = timed(pair_call(1 << f._term))
+    out["us_per_call"]["all_five_terms_one_call"] = timed(pair_call(all_mask))
+    out["us_per_call"]["oxdna_bonded"] = timed(lambda: _abi.check(L.oxg_bonded_forces(
+        ctx, n, ptr(pos_d), ptr(quat_d), box, len(bonds), ptr(bonds_d), ptr(force), ptr(torque),
+        None, None, sh), "oxg_bonded_forces"))
+    per = out["us_per_call"]
+    out["us_per_step_one_launch_per_term"] = sum(per[_abi.TERM_NAMES[f._term]] for f in pair) + \
+        per["oxdna_bonded"]
+    out["us_per_step_all_terms_one_call"] = per["all_five_terms_one_call"] + per["oxdna_bonded"]
+    L.oxg_destroy(ctx)
     return out
 
 
@@ -364,16 +487,35 @@ def run_reference(args):
     sysarr = build_system()
     cb = cpu_baseline(sysarr, seconds=max(10.0, min(60.0, 0.02 * args.steps)),
                       max_steps=max(args.steps, 10))
+    cb["reference_build"] = ("oracle port: the reference's HOOMD build cannot be installed "
+                             "(no HOOMD-blue on this machine)")
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 / cb["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "reference_build": "oracle port (reference HOOMD "
-                       "build unavailable on this box)"},
+            "config": {"workload": WORKLOAD},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "k_run_8000nt.md")
+
+
+def profiled_traffic():
+    """DRAM bytes per run-kernel launch of the headline workload from the committed ncu
+    summary (its ``traffic_bytes_per_launch:`` line; dram__bytes_read.sum +
+    dram__bytes_write.sum of one launch). The working set (~5 MB) is read into L2 once
+    per launch and stays there, so the figure is per launch whatever its step count."""
+    try:
+        with open(PROFILE_TRAFFIC) as fh:
+            for line in fh:
+                if line.strip().startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
 
 
 def run_ours(args):
@@ -384,7 +526,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    from oxdna import _abi, replicas
+    from oxdna import replicas
     stream = torch.cuda.Stream()
     sysarr = build_system(seed=2 + rank)
     n = len(sysarr["pos"])
@@ -409,18 +551,19 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": steps_per_s, "unit": "steps/s",
                               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-                              "quick": True, "clocks": clk.summary()}), flush=True)
+                              "quick": True, "kernel_ms": k_ms, "kernel_launches": k_launches,
+                              "clocks": clk.summary()}), flush=True)
         if dist is not None:
             dist.destroy_process_group()
         return
 
     # --- roofline of the dominant kernel: the persistent run kernel k_run ----------
-    # Its launches (one per run() block of 1000 steps) were timed with CUDA events on
-    # the engine stream during the timed region. Algorithmic bytes per step: the pair
-    # lists (8 B / pair), the bonds (16 B / bond), per particle the position, low-order
-    # position, quaternion and charge reads (52 B), force and torque read-modify-write
-    # (64 B) and the integrator's state update (velocity, angular momentum read + write,
-    # position and quaternion writes: 96 B).
+    # Its launches (one per run() block of up to 1000 steps) were timed with CUDA events
+    # on the engine stream during the timed region. Algorithmic bytes per step: the
+    # pair lists (8 B / pair), the bonds (16 B / bond), per particle the position,
+    # low-order position, quaternion and charge reads (52 B), force and torque
+    # read-modify-write (64 B) and the integrator's state update (velocity, angular
+    # momentum read + write, position and quaternion writes: 96 B).
     st = sim.native_stats()
     pairs = st["pairs_short"] + st["pairs_long"]
     n_bonds = len(sysarr["bonds"])
@@ -430,28 +573,41 @@ def run_ours(args):
     hbm, peak_kind = _peaks()
     achieved = alg_bytes_step * steps_per_launch / (kernel_ms * 1e-3) / 1e9
     compute = compute_roofline(kernel_ms / steps_per_launch, stream)
+    # steady state of the same workload: one long run() (the per-call run start and the
+    # cold L2 after the flush amortised), beside the K-step figure above
+    steady_steps = 20000
+    ms_steady = time_resident(sim, steady_steps, 0, stream, block=steady_steps)
+    legs = {"steady_state_steps_per_s": steady_steps / (ms_steady * 1e-3),
+            "steady_state_note": f"one run({steady_steps}) call of the headline workload"}
 
     # --- fused=True variant (HBondCross) ---------------------------------------
     sim_f, _ = make_sim(sysarr, fused=True, seed=1 + rank, stream=stream.cuda_stream)
     sim_f.run(0)
-    ms_f = time_resident(sim_f, min(args.steps, 5000), args.warmup, stream)
-    fused_sps = min(args.steps, 5000) / (ms_f * 1e-3)
+    ms_f = time_resident(sim_f, 5000, 100, stream, block=5000)
+    legs["fused_true_steps_per_s"] = 5000 / (ms_f * 1e-3)
     del sim_f
+
+    # --- the reference benchmark's own layout (8^3 tiled 8-bp duplex, 8192 nt) ----
+    legs["tiled"] = bench_tiled(stream, steps=5000, warmup=200)
 
     # --- 100k nt (2500 x 20-bp duplexes, box 230): the plain path at the large size --
     big = build_system(n_dup=2500, n_bp=20, box=230.0, seed=5 + rank)
     sim_b, _ = make_sim(big, fused=False, seed=1 + rank, stream=stream.cuda_stream)
     sim_b.run(0)
-    nb_steps = min(args.steps, 2000)
-    ms_b = time_resident(sim_b, nb_steps, args.warmup, stream)
-    big_sps = nb_steps / (ms_b * 1e-3)
+    ms_b = time_resident(sim_b, 2000, 100, stream, block=2000)
     big_stats = sim_b.native_stats()
+    legs["nt100k"] = {"steps_per_s": 2000 / (ms_b * 1e-3),
+                      "nt_steps_per_s": 2000 / (ms_b * 1e-3) * len(big["pos"]),
+                      "pairs": [big_stats["pairs_short"], big_stats["pairs_long"]]}
     del sim_b
 
-    # --- batched replicas, RNA hairpins, learned surrogate ----------------------------
-    batched = bench_batched(stream, steps=min(args.steps, 2000))
-    rna = bench_rna(stream, steps=min(args.steps, 2000), warmup=args.warmup)
-    surr = bench_surrogate(stream, big, steps=min(args.steps, 1000), warmup=args.warmup)
+    # --- drop-in entry points, batched replicas, RNA hairpins, learned surrogate ------
+    legs["dropin"] = bench_dropin(stream, sysarr)
+    legs["batched"] = bench_batched(stream, steps=2000)
+    legs["batched_with_hairpins"] = bench_batched(stream, steps=2000, hairpin_fraction=0.5,
+                                                  loop_steps=0)
+    legs["rna_hairpins"] = bench_rna(stream, steps=2000, warmup=100)
+    legs["surrogate_100k"] = bench_surrogate(stream, big, steps=1000, warmup=100)
 
     # --- end to end through the public API with host buffers ----------------------
     pin = lambda: torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy()  # noqa: E731
@@ -494,35 +650,28 @@ def run_ours(args):
     if rank != 0:
         dist.destroy_process_group()
         return
-    # per run() block of 1000 steps: one persistent run-kernel launch (its first body
-    # is the run start: checkpoint, list check, prepRun forces, the first step one)
-    blocks = (args.steps + 999) // 1000
+    # one persistent run-kernel launch per run() block of up to 1000 steps (its first
+    # body is the run start: checkpoint, list check, prepRun forces, the first step one)
+    traffic = profiled_traffic()
     line = {
         "metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_nt": n, "bonds": n_bonds,
-                   "pairs_short": st["pairs_short"], "pairs_long": st["pairs_long"],
-                   "l2": "flushed (256 MB write) before every timed run() block of 1000 steps; "
-                         "within a block the ~5 MB working set stays L2-resident",
-                   "fused_true_steps_per_s": fused_sps,
-                   "nt100k_steps_per_s": big_sps,
-                   "nt100k_nt_steps_per_s": big_sps * len(big["pos"]),
-                   "nt100k_pairs": [big_stats["pairs_short"], big_stats["pairs_long"]],
-                   "batched": batched,
-                   "rna_hairpins": rna,
-                   "surrogate_100k": surr,
-                   "reference_published": "~4600 steps/s unfused, ~5000 fused (RTX 4090, "
-                                          "8192-nt tiled duplex, box 64; README.md:97-98)"},
-        # DRAM bytes of one launch of this workload's run kernel measured with ncu
-        # (dram__bytes_read.sum + dram__bytes_write.sum, a 200-step launch): the working
-        # set is loaded into L2 once per launch and then stays there, so the launch's
-        # DRAM traffic does not grow with its steps.
+        "config": {"workload": WORKLOAD},
+        "workload_detail": {"n_nt": n, "bonds": n_bonds, "pairs_short": st["pairs_short"],
+                            "pairs_long": st["pairs_long"],
+                            "l2": "flushed (256 MB write) before every timed run() block of up "
+                                  "to 1000 steps; within a block the ~5 MB working set stays "
+                                  "L2-resident"},
+        "legs": legs,
+        "reference_published": "~4600 steps/s unfused, ~5000 fused (RTX 4090, 8192-nt tiled "
+                               "duplex, box 64; README.md:97-98): compare legs.tiled",
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": 2.273e6,
-                     "traffic_note": "DRAM bytes per launch (ncu); algorithmic bytes are "
-                                     "per step and are served from L2",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "traffic_note": "DRAM bytes of one run-kernel launch of this workload "
+                                     "(ncu, profiles/k_run_8000nt.md); the algorithmic bytes "
+                                     "of its steps are served from L2",
                      "peak_kind": peak_kind,
                      "kernel": "k_run (persistent MD step kernel: nlist rebuild when flagged, "
                                "forces, Langevin + NO_SQUISH)",
@@ -532,7 +681,7 @@ def run_ours(args):
                              "is L2-resident"},
         "roofline_compute": compute,
         "cpu_baseline": cb, "e2e": e2e,
-        "gpu_launches": blocks,
+        "gpu_launches": k_launches,
         "clocks": clk.summary(),
         "nlist_builds": stats["nlist_builds"],
     }
