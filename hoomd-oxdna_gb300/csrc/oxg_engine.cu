@@ -1519,11 +1519,15 @@ int oxg_system_surrogate_stats(oxg_system* s, double* out, int n)
     OXG_CUDA(cudaMemcpyAsync(&h, s->audit, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
     OXG_CUDA(cudaStreamSynchronize(s->stream));
     const double na = h.n_audited ? (double)h.n_audited : 1.0;
-    const double v[9] = {(double)h.disabled, (double)h.n_audited, (double)h.n_over,
-                         std::sqrt(h.sum_sq_de / na), std::sqrt(h.sum_sq_e / na),
-                         std::sqrt(h.sum_sq_df / na), std::sqrt(h.sum_sq_f / na),
-                         (double)h.max_abs_de, (double)h.max_abs_df};
-    for (int k = 0; k < n && k < 9; ++k) out[k] = v[k];
+    const double mean = h.sum_de / na;
+    const double rel = h.sum_e != 0.0 ? h.sum_de / h.sum_e : 0.0;
+    const double rel_se =
+        h.sum_e != 0.0 ? std::sqrt(std::max(h.sum_sq_de / na - mean * mean, 0.0) * na) / std::fabs(h.sum_e) : 0.0;
+    const double v[11] = {(double)h.disabled, (double)h.n_audited, (double)h.n_over,
+                          std::sqrt(h.sum_sq_de / na), std::sqrt(h.sum_sq_e / na),
+                          std::sqrt(h.sum_sq_df / na), std::sqrt(h.sum_sq_f / na),
+                          (double)h.max_abs_de, (double)h.max_abs_df, rel, rel_se};
+    for (int k = 0; k < n && k < 11; ++k) out[k] = v[k];
     return OXG_OK;
 }
 

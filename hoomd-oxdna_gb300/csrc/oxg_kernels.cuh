@@ -230,24 +230,29 @@ struct ForceArgs {
     struct SurrogateAudit* audit = nullptr;
     uint32_t audit_every = 0;  // steps between audits (0: never)
     uint32_t audit_mod = 100;  // one queued pair in audit_mod is audited
-    float audit_tol = 0.f;     // largest accepted |E_surrogate - E_plain| of one pair
+    float audit_tol = 1e-4f;   // largest accepted relative error of the term's energy
     // entries per heavy-term queue a block keeps in shared memory in phase A (at most
     // kBlockQ; lowered only to exercise the path of pairs that do not fit)
     int block_q = 400;
 };
 
 // Statistics of the audits of the surrogate by the plain evaluator; `disabled` is the
-// kill switch the force kernels read (set by the first pair over the tolerance).
+// kill switch the force kernels read. The audited pairs are a hashed sample of the
+// term's pairs, so sum_de / sum_e estimates the relative error of the term's energy;
+// the switch trips when that estimate exceeds the tolerance by more than two standard
+// errors (at least kAuditMinPairs audited pairs).
 struct SurrogateAudit {
     uint32_t disabled;
     uint32_t n_audited;
-    uint32_t n_over;
+    uint32_t n_over;             // audits at which the test failed (the switch tripped)
     uint32_t pad;
     double sum_sq_de, sum_sq_e;  // pair energy error and reference
     double sum_sq_df, sum_sq_f;  // force (on i) error and reference
+    double sum_de, sum_e;        // signed sums of the pair energy error and reference
     float max_abs_de, max_abs_df;
     float pad2[2];
 };
+constexpr uint32_t kAuditMinPairs = 100;
 
 // The force evaluation is split in two launches so that the acos-heavy terms run with
 // every lane busy (whatever the system size):
@@ -625,17 +630,25 @@ static __device__ __noinline__ void surrogate_audit(const ForceArgs& a, const Pa
     const float3 df = acc_sur.fi - pa.fi;
     const float df2 = dot(df, df);
     SurrogateAudit* au = a.audit;
-    atomicAdd(&au->n_audited, 1u);
-    atomicAdd(&au->sum_sq_de, (double)de * de);
+    // the running sums including this pair (each field read as it was updated)
+    const uint32_t n = atomicAdd(&au->n_audited, 1u) + 1u;
+    const double sq = atomicAdd(&au->sum_sq_de, (double)de * de) + (double)de * de;
     atomicAdd(&au->sum_sq_e, (double)e * e);
     atomicAdd(&au->sum_sq_df, (double)df2);
     atomicAdd(&au->sum_sq_f, (double)dot(pa.fi, pa.fi));
+    const double sde = atomicAdd(&au->sum_de, (double)de) + (double)de;
+    const double se = atomicAdd(&au->sum_e, (double)e) + (double)e;
     // non-negative floats order like their bit patterns
     atomicMax(reinterpret_cast<int*>(&au->max_abs_de), __float_as_int(fabsf(de)));
     atomicMax(reinterpret_cast<int*>(&au->max_abs_df), __float_as_int(sqrtf(df2)));
-    if (!(fabsf(de) <= a.audit_tol)) {
-        atomicAdd(&au->n_over, 1u);
-        atomicExch(&au->disabled, 1u);
+    // kill switch: the sampled relative error of the term's energy over the tolerance by
+    // more than two standard errors (NaN errors trip it too)
+    if (n >= kAuditMinPairs && fabs(se) > 0.0) {
+        const double mean = sde / n;
+        const double se_rel = sqrt(fmax(sq / n - mean * mean, 0.0) * n) / fabs(se);
+        const double rel = fabs(sde) / fabs(se);
+        if (!(rel - 2.0 * se_rel <= (double)a.audit_tol) && atomicExch(&au->disabled, 1u) == 0u)
+            atomicAdd(&au->n_over, 1u);
     }
 }
 

@@ -606,13 +606,14 @@ class Simulation:
 
     # -- learned surrogate (extension; see oxdna.surrogate) ----------------------
     def set_surrogate(self, network, run=True, compute=False, audit_every=100,
-                      audit_fraction=0.01, tol=0.05):
+                      audit_fraction=0.01, tol=1e-4):
         """Evaluate the fused HB + cross-stacking term (forces(fused=True)) with a
         trained surrogate network in MD steps (run) and / or in energy and force
         read-outs (compute). Every audit_every steps about audit_fraction of the pairs is
-        also evaluated by the plain evaluator; a pair energy error above tol switches
-        the surrogate off for the rest of the simulation. network=None restores the
-        plain evaluator."""
+        also evaluated by the plain evaluator; when the audited sample shows the
+        relative error of the term's energy above tol (default 1e-4, the per-term
+        energy budget) by more than two standard errors, the surrogate is switched off
+        for the rest of the simulation. network=None restores the plain evaluator."""
         self._sync()
         self._apply_surrogate(network, run, compute, audit_every, audit_fraction, tol)
 
@@ -630,12 +631,14 @@ class Simulation:
         self._cache = {}
 
     def surrogate_stats(self):
-        """Audit statistics: disabled (the kill switch tripped), audited pairs, pairs
-        over tolerance, rms / max energy and force errors against the plain evaluator."""
-        out = (C.c_double * 9)()
-        _abi.check(_abi.lib().oxg_system_surrogate_stats(self._sys, out, 9), "oxg_system_surrogate_stats")
+        """Audit statistics: disabled (the kill switch tripped), audited pairs, audits
+        that tripped it, rms / max pair energy and force errors against the plain
+        evaluator, and the sampled relative error of the term's energy (rel_energy_error)
+        with its standard error (rel_energy_error_se)."""
+        out = (C.c_double * 11)()
+        _abi.check(_abi.lib().oxg_system_surrogate_stats(self._sys, out, 11), "oxg_system_surrogate_stats")
         keys = ("disabled", "n_audited", "n_over", "rms_de", "rms_e", "rms_df", "rms_f",
-                "max_abs_de", "max_abs_df")
+                "max_abs_de", "max_abs_df", "rel_energy_error", "rel_energy_error_se")
         return dict(zip(keys, list(out)))
 
     def run_kernel_timing(self, reset=False):

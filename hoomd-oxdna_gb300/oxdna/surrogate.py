@@ -7,8 +7,9 @@ base-base evaluator, src/OxDNABaseBase.h:74-121) to its energy. Forces and torqu
 from the network's analytic input gradient. BF16 weights on the tensor cores, FP32
 accumulation; trained by the library's own kernels on samples the plain evaluator
 produces along its own trajectories. The reference has no learned part: this is an
-extension, used only while audits by the plain evaluator keep its per-pair error under
-a tolerance (the plain evaluator stays the fallback and the yardstick).
+extension, used only while audits by the plain evaluator keep the sampled error of the
+term's energy under a tolerance (the plain evaluator stays the fallback and the
+yardstick).
 
 Device buffers are torch CUDA tensors (plumbing only); every computation runs in
 ``liboxdna_gb300.so``.
@@ -108,6 +109,25 @@ class Network:
             sd[sd < 1e-6] = 1.0
             es = float(e[m].std()) or 1.0
             self.set_normalization(c, x.mean(axis=0), sd, es, float(e[m].mean()))
+
+    def calibrate(self, feats, energy):
+        """Shift each class's output so that its mean pair-energy error over a data set
+        (the pair distribution the network will meet in MD) is zero: a systematic error
+        of the pair energies adds up over every pair of the term, random errors largely
+        cancel. Returns the per-class shifts applied."""
+        import torch
+        shifts = []
+        for c in (0, 1):
+            m = feats[:, 7] == c
+            if int(m.sum()) == 0 or self.norm[c] is None:
+                shifts.append(0.0)
+                continue
+            resid = (self.energies(feats[m].contiguous()) - energy[m]).to(torch.float64)
+            d = float(resid.mean())
+            mu, inv, es, sh = self.norm[c]
+            self.set_normalization(c, mu, 1.0 / inv, es, sh - d)
+            shifts.append(-d)
+        return shifts
 
     def gradient(self, cls, feats, target, idx):
         """Loss gradient (P floats) and sum of squared errors for a minibatch (torch

@@ -323,16 +323,21 @@ int oxg_mlp_predict(oxg_mlp* m, int cls, const float* feats, int n, float* y, fl
 /* Surrogate use by a system. flags: OXG_SURROGATE_RUN replaces the fused HB + cross-
  * stacking pairs of MD steps (oxg_system_run), OXG_SURROGATE_COMPUTE those of
  * oxg_system_compute. Every audit_every MD steps (0 = never) a hashed 1 / audit_mod of
- * the pairs is also evaluated by the plain evaluator; the first pair whose energy error
- * exceeds audit_tol switches the surrogate off (the plain evaluator takes over) until
- * the next set_surrogate. mlp = NULL or flags = 0 restores the plain evaluator. */
+ * the pairs is also evaluated by the plain evaluator. The audited pairs are a sample of
+ * the term's pairs, so (sum of the surrogate's pair energy errors) / (sum of the plain
+ * pair energies) over them estimates the relative error of the term's energy; once at
+ * least 100 pairs are audited, an estimate that exceeds audit_tol (a relative error,
+ * e.g. 1e-4) by more than two standard errors switches the surrogate off (the plain
+ * evaluator takes over) until the next set_surrogate. mlp = NULL or flags = 0 restores
+ * the plain evaluator. */
 #define OXG_SURROGATE_RUN 1
 #define OXG_SURROGATE_COMPUTE 2
 int oxg_system_set_surrogate(oxg_system* sys, const oxg_mlp* mlp, int flags, int audit_every,
                              int audit_mod, double audit_tol);
-/* out[0..8]: disabled, audited pairs, pairs over tolerance, rms energy error, rms
- * reference energy, rms force error, rms reference force, max |energy error|, max
- * |force error| */
+/* out[0..10]: disabled, audited pairs, audits that tripped the switch (0 or 1), rms
+ * pair energy error, rms reference pair energy, rms force error, rms reference force,
+ * max |pair energy error|, max |force error|, the sampled relative error of the term's
+ * energy (sum of errors / sum of reference energies) and its standard error */
 int oxg_system_surrogate_stats(oxg_system* sys, double* out, int n);
 /* Training samples from the system's current state: every fused HB + CS pair that
  * passes the zero-factor tests gives feats[8*k..] (7 features, class) and the plain
