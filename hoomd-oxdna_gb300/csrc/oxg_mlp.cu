@@ -17,6 +17,7 @@
 #include "../../include/oxdna_gb300.h"
 #include "oxg_internal.h"
 #include "oxg_mlp.cuh"
+#include "oxg_tc.cuh"
 
 using namespace oxg;
 
@@ -77,7 +78,215 @@ __global__ void k_mlp_pack_vec(const float* P, MlpDev* M)
     if (j == 0) V.b4 = W[P_B4];
 }
 
-// ------------------------------------------------------------------ training
+// ------------------------------------------------------------------ tcgen05 images
+// The six B operands of one class in the canonical K-major layout (oxg_tc.cuh), one
+// thread per element: forward F (n = output, k = input): W[n][k]; backward G (n = input,
+// k = output): W[k][n].
+__global__ void k_mlp_pack_tc(const float* P, MlpDev* M)
+{
+    const int per_class = 1024 + 4 * 4096 + 1024;
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= kMlpClasses * per_class) return;
+    const int cls = id / per_class;
+    int e = id % per_class;
+    const float* W = P + (size_t)cls * kMlpParams;
+    unsigned char* img = M->tcw[cls];
+    float v;
+    uint32_t off;
+    if (e < 1024) {  // F1: 64 x 16
+        const int n = e >> 4, k = e & 15;
+        v = W[P_W1 + n * 16 + k];
+        off = tc::kImgF1 + tc::kmaj_off(64, n, k);
+    } else if ((e -= 1024) < 4 * 4096) {
+        const int m = e >> 12, n = (e >> 6) & 63, k = e & 63;
+        const float* Wm = W + ((m == 0 || m == 3) ? P_W2 : P_W3);
+        const bool fwd = m < 2;
+        v = fwd ? Wm[n * 64 + k] : Wm[k * 64 + n];
+        const uint32_t base = m == 0 ? tc::kImgF2 : m == 1 ? tc::kImgF3 : m == 2 ? tc::kImgG3 : tc::kImgG2;
+        off = base + tc::kmaj_off(64, n, k);
+    } else {  // G1: 16 (inputs) x 64 (outputs)
+        e -= 4 * 4096;
+        const int n = e >> 6, k = e & 63;
+        v = W[P_W1 + k * 16 + n];
+        off = tc::kImgG1 + tc::kmaj_off(16, n, k);
+    }
+    *reinterpret_cast<__nv_bfloat16*>(img + off) = __float2bfloat16_rn(v);
+}
+
+// ------------------------------------------------------------------ tcgen05 tiles
+// A warpgroup (128 threads, thread = row) runs the network over 128 rows with the
+// GEMMs on the tensor cores: M = 128 rows, BF16 operands in shared memory, FP32
+// accumulators in tensor memory, read back a row per thread for the bias / SiLU
+// epilogues on the CUDA cores. Tensor-memory columns: D1 [0, 64), D2 [64, 128),
+// D3 [128, 192), D4 [192, 256) (the backward GEMMs), the input gradient in [0, 16)
+// once D1 is consumed.
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcX = 4096, kTcAct = 16384;  // A buffers: 128 x 16 and 128 x 64 BF16
+
+struct TcTile {
+    unsigned char* w;  // weight image of the class (36864 B)
+    unsigned char* x;  // 128 x 16 inputs
+    unsigned char* p;  // 128 x 64 activations / gradients (two buffers)
+    unsigned char* q;
+    uint32_t mbar;     // shared address of the MMA-completion mbarrier
+    uint32_t tmem;     // tensor-memory base of the tile's columns
+    int bar_id;        // named barrier of the warpgroup
+};
+
+__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+
+// Shared-memory writes of this warpgroup's threads become operands of an MMA issued next:
+// make them visible to the tensor cores, order earlier TMEM reads, and meet.
+__device__ __forceinline__ void tc_publish(const TcTile& t)
+{
+    tc::fence_smem_async();
+    tc::fence_before();
+    wg_sync(t.bar_id);
+}
+
+// One thread issues `steps` K = 16 MMAs D(tmem col) = A * B and commits them; then every
+// thread waits for the completion. Returns false if the wait gave up.
+__device__ __forceinline__ bool tc_gemm(const TcTile& t, uint32_t& phase, uint32_t dcol, const unsigned char* A,
+                                        int a_rows, const unsigned char* B, int b_rows, int n, int steps,
+                                        bool first_acc)
+{
+    if ((threadIdx.x & 127) == 0) {
+        tc::fence_after();
+        const uint32_t sa = tc::smem_addr(A), sb = tc::smem_addr(B), id = tc::idesc_bf16(128, n);
+        for (int j = 0; j < steps; ++j)
+            tc::mma(t.tmem + dcol, tc::op_desc(sa, a_rows, j), tc::op_desc(sb, b_rows, j), id,
+                    (first_acc || j > 0) ? 1u : 0u);
+        tc::commit(t.mbar);
+    }
+    const bool ok = tc::mbar_wait(t.mbar, phase);
+    phase ^= 1u;
+    tc::fence_after();
+    return ok;
+}
+
+__device__ __forceinline__ float silu_d(float z, float& h)
+{
+    const float sg = 1.f / (1.f + __expf(-z));
+    h = z * sg;
+    return sg * (1.f + z * (1.f - sg));
+}
+
+__device__ __forceinline__ void st_bf16(unsigned char* base, uint32_t off, float v)
+{
+    *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(v);
+}
+
+// This thread's row of D (64 columns from col) plus the bias: z; writes silu(z) as the
+// row of the next A operand (dst, if set) and as this row's column of a transposed
+// operand with tr_rows rows (dstT, if set).
+__device__ __forceinline__ void tc_bias_silu_row(uint32_t lane_t, uint32_t col, const float* b, unsigned char* dst,
+                                                 int row, unsigned char* dstT = nullptr, int tr_rows = 80)
+{
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float z[16], h[16];
+        tc::ld16(lane_t + col + 16 * c, z);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            (void)silu_d(z[e] + b[16 * c + e], h[e]);
+            if (dstT) st_bf16(dstT, tc::kmaj_off(tr_rows, 16 * c + e, row), h[e]);
+        }
+        if (dst) {
+            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c), h);
+            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c + 8), h + 8);
+        }
+    }
+}
+
+// dz = g * silu'(z) for this row: g from D4, z from the forward accumulator at zcol plus
+// the bias; written as the row of an A operand (dst, if set) and as this row's column of
+// a transposed operand of 128 rows (dstT, if set).
+__device__ __forceinline__ void tc_backprop_row(uint32_t lane_t, uint32_t zcol, const float* b, unsigned char* dst,
+                                                int row, unsigned char* dstT = nullptr)
+{
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float g[16], z[16], dz[16];
+        tc::ld16(lane_t + 192 + 16 * c, g);
+        tc::ld16(lane_t + zcol + 16 * c, z);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            float h;
+            dz[e] = g[e] * silu_d(z[e] + b[16 * c + e], h);
+            if (dstT) st_bf16(dstT, tc::kmaj_off(128, 16 * c + e, row), dz[e]);
+        }
+        if (dst) {
+            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c), dz);
+            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c + 8), dz + 8);
+        }
+    }
+}
+
+// Energy and input gradient of 128 rows: x (this thread's row, 7 normalised features;
+// zeros for an unused row) -> y and dy/dx'. Returns false if an MMA wait gave up.
+__device__ bool tc_rows128(const TcTile& t, uint32_t& phase, const MlpVec& V, const float* x, float& y, float* dydx)
+{
+    const int row = threadIdx.x & 127;
+    const uint32_t lane_t = t.tmem + ((uint32_t)(((threadIdx.x >> 5) & 3) * 32) << 16);
+    bool ok = true;
+    {
+        float xr[16];
+#pragma unroll
+        for (int f = 0; f < 16; ++f) xr[f] = f < kMlpIn ? x[f] : 0.f;
+        tc::st_row8(t.x, tc::kmaj_off(128, row, 0), xr);
+        tc::st_row8(t.x, tc::kmaj_off(128, row, 8), xr + 8);
+    }
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 0, t.x, 128, t.w + tc::kImgF1, 64, 64, 1, false);     // D1 = X F1
+    tc_bias_silu_row(lane_t, 0, V.b1, t.p, row);
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 64, t.p, 128, t.w + tc::kImgF2, 64, 64, 4, false);    // D2 = H1 F2
+    tc_bias_silu_row(lane_t, 64, V.b2, t.q, row);
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 128, t.q, 128, t.w + tc::kImgF3, 64, 64, 4, false);   // D3 = H2 F3
+    // output and dy/dz3 = w4 * silu'(z3)
+    float yy = V.b4;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float z[16], dz[16];
+        tc::ld16(lane_t + 128 + 16 * c, z);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            float h;
+            const float sp = silu_d(z[e] + V.b3[16 * c + e], h);
+            yy += h * V.w4[16 * c + e];
+            dz[e] = sp * V.w4[16 * c + e];
+        }
+        tc::st_row8(t.p, tc::kmaj_off(128, row, 16 * c), dz);
+        tc::st_row8(t.p, tc::kmaj_off(128, row, 16 * c + 8), dz + 8);
+    }
+    y = yy;
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 192, t.p, 128, t.w + tc::kImgG3, 64, 64, 4, false);   // dH2 = dZ3 G3
+    tc_backprop_row(lane_t, 64, V.b2, t.q, row);                                  // dZ2
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 192, t.q, 128, t.w + tc::kImgG2, 64, 64, 4, false);   // dH1 = dZ2 G2
+    tc_backprop_row(lane_t, 0, V.b1, t.p, row);                                   // dZ1
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 0, t.p, 128, t.w + tc::kImgG1, 16, 16, 4, false);     // dX = dZ1 G1
+    float dx[16];
+    tc::ld16(lane_t, dx);
+#pragma unroll
+    for (int f = 0; f < kMlpIn; ++f) dydx[f] = dx[f];
+    tc::fence_before();  // the next tile's MMAs overwrite these columns after a barrier
+    return ok;
+}
+
+// The class's weight image into shared memory (all threads of the block, 16-byte loads),
+// made visible to the tensor cores.
+__device__ __forceinline__ void tc_load_weights(unsigned char* dst, const unsigned char* src)
+{
+    for (int k = threadIdx.x; k < (int)(tc::kImgBytes / 16); k += blockDim.x)
+        reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(src)[k];
+    tc::fence_smem_async();
+}
+
+// ------------------------------------------------------------------ training (tcgen05)
 struct TrainArgs {
     const MlpDev* M;
     int cls;
@@ -87,226 +296,231 @@ struct TrainArgs {
     int nb;               // minibatch size
     float* grad;          // kMlpParams (this class), accumulated
     double* loss;         // sum of squared errors in normalised units, accumulated
+    uint32_t* err;        // set when an MMA wait gave up
 };
 
-constexpr int kTrainWarps = 4;
-// per-warp transposed activations [unit][sample] (BF16) used as the weight-gradient
-// GEMM operands, and the block's gradient accumulators
-struct TrainSmem {
-    __nv_bfloat16 xT[kTrainWarps][16][16];
-    __nv_bfloat16 h1T[kTrainWarps][64][16];
-    __nv_bfloat16 h2T[kTrainWarps][64][16];
-    __nv_bfloat16 dzT[kTrainWarps][64][16];
-    float g[kMlpParams];
-};
+// Shared-memory plan of the training kernel (bytes). Weight-gradient GEMMs contract over
+// the 128 samples of a tile: A = dZ^T (128 rows: the 64 units, then zeros), B = H^T (80
+// rows: the 64 inputs, a row of ones that yields the bias gradient, zeros) or X^T (32
+// rows: 16 inputs, ones, zeros). 32 KB of slack follow the last operand.
+constexpr uint32_t kTrW = 0, kTrX = 36864, kTrP = kTrX + kTcX, kTrQ = kTrP + kTcAct, kTrXT = kTrQ + kTcAct,
+                   kTrH1T = kTrXT + 32 * 128 * 2, kTrH2T = kTrH1T + 80 * 128 * 2, kTrDZT = kTrH2T + 80 * 128 * 2,
+                   kTrRed = kTrDZT + 128 * 128 * 2, kTrBytes = kTrRed + 4 * 65 * 4 + 32768;
+// tensor-memory columns of the weight gradients (after D1..D4)
+constexpr uint32_t kColDW3 = 256, kColDW2 = 336, kColDW1 = 416;
 
-__device__ __forceinline__ void store_T(__nv_bfloat16 (*T)[16], const float (*c)[4], int lane)
+// One minibatch: L = sum_s (y_s - y*_s)^2 / nb (normalised units) and its gradient with
+// respect to every parameter of the class, accumulated into a.grad. A block of 128
+// threads takes tiles of 128 samples; the weight gradients accumulate in tensor memory
+// over the block's tiles and are added to a.grad once at the end.
+__global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
 {
-    const int g = lane >> 2;
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) T[frag_col(nt, e, lane)][g + (e >> 1) * 8] = __float2bfloat16_rn(c[nt][e]);
-}
-
-__device__ __forceinline__ uint32_t ld2(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
-// dW[j][k] += sum_s dz[s][j] * h[s][k] for j < 64, k < 16 * NK (A = dz^T, B from h^T)
-template <int NT>
-__device__ __forceinline__ void weight_grad(const __nv_bfloat16 (*dzT)[16], const __nv_bfloat16 (*hT)[16],
-                                            float* gW, int in_dim, int lane)
-{
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int mt = 0; mt < 4; ++mt) {
-        const int j = mt * 16 + g;
-        const uint32_t a0 = ld2(&dzT[j][2 * t]), a1 = ld2(&dzT[j + 8][2 * t]);
-        const uint32_t a2 = ld2(&dzT[j][2 * t + 8]), a3 = ld2(&dzT[j + 8][2 * t + 8]);
-#pragma unroll
-        for (int nt = 0; nt < NT; ++nt) {
-            const int k = nt * 8 + g;
-            const uint2 b = make_uint2(ld2(&hT[k][2 * t]), ld2(&hT[k][2 * t + 8]));
-            float d[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_bf16(d, a0, a1, a2, a3, b);
-            const int c0 = nt * 8 + 2 * t;
-            atomicAdd(&gW[j * in_dim + c0], d[0]);
-            atomicAdd(&gW[j * in_dim + c0 + 1], d[1]);
-            atomicAdd(&gW[(j + 8) * in_dim + c0], d[2]);
-            atomicAdd(&gW[(j + 8) * in_dim + c0 + 1], d[3]);
-        }
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const MlpVec& V = a.M->vec[a.cls];
+    tc_load_weights(sm + kTrW, a.M->tcw[a.cls]);
+    // constant rows of the weight-gradient operands: ones (bias gradients) and zeros
+    st_bf16(sm + kTrXT, tc::kmaj_off(32, 16, tid), 1.f);
+    for (int r = 17; r < 32; ++r) st_bf16(sm + kTrXT, tc::kmaj_off(32, r, tid), 0.f);
+    st_bf16(sm + kTrH1T, tc::kmaj_off(80, 64, tid), 1.f);
+    st_bf16(sm + kTrH2T, tc::kmaj_off(80, 64, tid), 1.f);
+    for (int r = 65; r < 80; ++r) {
+        st_bf16(sm + kTrH1T, tc::kmaj_off(80, r, tid), 0.f);
+        st_bf16(sm + kTrH2T, tc::kmaj_off(80, r, tid), 0.f);
     }
-}
-
-// db[j] += sum over the 16 rows of the C fragments c
-__device__ __forceinline__ void bias_grad(const float (*c)[4], float* gb, int lane)
-{
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-        float v0 = c[nt][0] + c[nt][2], v1 = c[nt][1] + c[nt][3];
-#pragma unroll
-        for (int o = 4; o < 32; o <<= 1) {
-            v0 += __shfl_xor_sync(0xffffffffu, v0, o);
-            v1 += __shfl_xor_sync(0xffffffffu, v1, o);
-        }
-        if (lane < 4) {
-            atomicAdd(&gb[frag_col(nt, 0, lane)], v0);
-            atomicAdd(&gb[frag_col(nt, 1, lane)], v1);
-        }
-    }
-}
-
-// One minibatch: loss L = sum_s (y_s - y*_s)^2 / nb in normalised energy units and its
-// gradient with respect to every parameter of the class, accumulated into a.grad.
-__global__ void __launch_bounds__(kTrainWarps * 32) k_mlp_train(TrainArgs a)
-{
-    extern __shared__ float4 smem_train[];
-    TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_train);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) S.g[k] = 0.f;
-    const MlpDev& M = *a.M;
-    const MlpVec& V = M.vec[a.cls];
-    const uint2* F = &M.frag[a.cls][0][0];
+    for (int r = 64; r < 128; ++r) st_bf16(sm + kTrDZT, tc::kmaj_off(128, r, tid), 0.f);
+    float* red = reinterpret_cast<float*>(sm + kTrRed);
+    for (int k = tid; k < 4 * 65; k += 128) red[k] = 0.f;
+    if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_base), 512);
+    if (tid == 0) tc::mbar_init(tc::smem_addr(&mbar), 1);
+    tc::fence_smem_async();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    TcTile t;
+    t.w = sm + kTrW;
+    t.x = sm + kTrX;
+    t.p = sm + kTrP;
+    t.q = sm + kTrQ;
+    t.mbar = tc::smem_addr(&mbar);
+    t.tmem = tmem_base;
+    t.bar_id = 1;
+    const uint32_t lane_t = t.tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t phase = 0;
+    bool ok = true;
     double sse = 0.0;
-    __syncthreads();
-    const int chunks = (a.nb + 15) / 16;
-    for (int ch = blockIdx.x * kTrainWarps + w; ch < chunks; ch += gridDim.x * kTrainWarps) {
-        // row r = lane & 15: its sample, normalised features and target
-        const int r = lane & 15;
-        const int sidx = ch * 16 + r;
+    float gb4 = 0.f;
+    bool first = true;
+    const int tiles = (a.nb + kTcRows - 1) / kTcRows;
+    for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const int sidx = tile * kTcRows + tid;
         const bool valid = sidx < a.nb;
-        float x[kMlpIn], yt = 0.f;
+        float x[16], yt = 0.f;
+#pragma unroll
+        for (int f = 0; f < 16; ++f) x[f] = 0.f;
         if (valid) {
-            const int s = a.idx[sidx];
+            const int sI = a.idx[sidx];
 #pragma unroll
-            for (int f = 0; f < kMlpIn; ++f) x[f] = (a.feats[(size_t)s * 8 + f] - V.mu[f]) * V.inv_sd[f];
-            yt = (a.target[s] - V.e_shift) / V.e_scale;
-        } else {
-#pragma unroll
-            for (int f = 0; f < kMlpIn; ++f) x[f] = 0.f;
+            for (int f = 0; f < kMlpIn; ++f) x[f] = (a.feats[(size_t)sI * 8 + f] - V.mu[f]) * V.inv_sd[f];
+            yt = (a.target[sI] - V.e_shift) / V.e_scale;
         }
-        // x^T for the first layer's weight gradient (rows 7..15 zero)
-        if (lane < 16) {
+        tc::st_row8(t.x, tc::kmaj_off(128, tid, 0), x);
+        tc::st_row8(t.x, tc::kmaj_off(128, tid, 8), x + 8);
 #pragma unroll
-            for (int f = 0; f < 16; ++f) S.xT[w][f][r] = __float2bfloat16_rn(f < kMlpIn ? x[f] : 0.f);
-        }
-        // forward (as mlp_rows16)
-        float xg[kMlpIn], xg8[kMlpIn];
-#pragma unroll
-        for (int f = 0; f < kMlpIn; ++f) {
-            xg[f] = __shfl_sync(0xffffffffu, x[f], g);
-            xg8[f] = __shfl_sync(0xffffffffu, x[f], g + 8);
-        }
-        auto pick = [&](const float* v, int f) {
-            float q = 0.f;
-#pragma unroll
-            for (int k = 0; k < kMlpIn; ++k) q = (k == f) ? v[k] : q;
-            return q;
-        };
-        uint32_t A0[1][4];
-        A0[0][0] = pack_bf16(pick(xg, 2 * t), pick(xg, 2 * t + 1));
-        A0[0][1] = pack_bf16(pick(xg8, 2 * t), pick(xg8, 2 * t + 1));
-        A0[0][2] = 0u;
-        A0[0][3] = 0u;
-        float z1[8][4], s1[8][4], z2[8][4], s2[8][4], z3[8][4];
-        uint32_t A[4][4];
-        mlp_layer<1>(F + kFragF1 * 32, A0, z1, lane);
-        bias_silu(z1, s1, V.b1, lane);
-        store_T(S.h1T[w], z1, lane);
-        c_to_a(z1, A);
-        mlp_layer<4>(F + kFragF2 * 32, A, z2, lane);
-        bias_silu(z2, s2, V.b2, lane);
-        store_T(S.h2T[w], z2, lane);
-        c_to_a(z2, A);
-        mlp_layer<4>(F + kFragF3 * 32, A, z3, lane);
-        float s3[8][4];
-        bias_silu(z3, s3, V.b3, lane);
-        float yg = 0.f, yg8 = 0.f;
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const float w0 = V.w4[frag_col(nt, 0, lane)], w1 = V.w4[frag_col(nt, 1, lane)];
-            yg += z3[nt][0] * w0 + z3[nt][1] * w1;
-            yg8 += z3[nt][2] * w0 + z3[nt][3] * w1;
-        }
-        yg += __shfl_xor_sync(0xffffffffu, yg, 1);
-        yg += __shfl_xor_sync(0xffffffffu, yg, 2);
-        yg8 += __shfl_xor_sync(0xffffffffu, yg8, 1);
-        yg8 += __shfl_xor_sync(0xffffffffu, yg8, 2);
-        yg += V.b4;
-        yg8 += V.b4;
-        // dL/dy of rows g and g + 8
-        const float tg = __shfl_sync(0xffffffffu, yt, g), tg8 = __shfl_sync(0xffffffffu, yt, g + 8);
-        const bool vg = __shfl_sync(0xffffffffu, valid, g), vg8 = __shfl_sync(0xffffffffu, valid, g + 8);
-        const float dg = vg ? 2.f * (yg - tg) / (float)a.nb : 0.f;
-        const float dg8 = vg8 ? 2.f * (yg8 - tg8) / (float)a.nb : 0.f;
+        for (int f = 0; f < 16; ++f) st_bf16(sm + kTrXT, tc::kmaj_off(32, f, tid), x[f]);
+        // forward, keeping the activations' transposes for the weight gradients
+        tc_publish(t);
+        ok &= tc_gemm(t, phase, 0, t.x, 128, t.w + tc::kImgF1, 64, 64, 1, false);
+        tc_bias_silu_row(lane_t, 0, V.b1, t.p, tid, sm + kTrH1T, 80);
+        tc_publish(t);
+        ok &= tc_gemm(t, phase, 64, t.p, 128, t.w + tc::kImgF2, 64, 64, 4, false);
+        tc_bias_silu_row(lane_t, 64, V.b2, t.q, tid, sm + kTrH2T, 80);
+        tc_publish(t);
+        ok &= tc_gemm(t, phase, 128, t.q, 128, t.w + tc::kImgF3, 64, 64, 4, false);
+        // output, loss, dL/dy (first pass over z3); dz3 = dL/dy * w4 * silu'(z3) and the
+        // w4 gradient dL/dy * h3 (second pass; warp sums into the block's accumulators)
         {
-            // squared error: lanes with t == 0 hold rows g and g + 8
-            const float e0 = vg ? (yg - tg) : 0.f, e1 = vg8 ? (yg8 - tg8) : 0.f;
-            if (t == 0) sse += (double)e0 * e0 + (double)e1 * e1;
-        }
-        // output layer: dw4[j] = sum_s dL/dy_s h3[s][j]; db4 = sum_s dL/dy_s
+            float y = V.b4;
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            float v0 = dg * z3[nt][0] + dg8 * z3[nt][2], v1 = dg * z3[nt][1] + dg8 * z3[nt][3];
+            for (int c = 0; c < 4; ++c) {
+                float z[16];
+                tc::ld16(lane_t + 128 + 16 * c, z);
 #pragma unroll
-            for (int o = 4; o < 32; o <<= 1) {
-                v0 += __shfl_xor_sync(0xffffffffu, v0, o);
-                v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+                for (int e = 0; e < 16; ++e) {
+                    float h;
+                    (void)silu_d(z[e] + V.b3[16 * c + e], h);
+                    y += h * V.w4[16 * c + e];
+                }
             }
-            if (lane < 4) {
-                atomicAdd(&S.g[P_W4 + frag_col(nt, 0, lane)], v0);
-                atomicAdd(&S.g[P_W4 + frag_col(nt, 1, lane)], v1);
+            const float err = valid ? y - yt : 0.f;
+            sse += (double)err * err;
+            const float dy = 2.f * err / (float)a.nb;
+            gb4 += dy;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float z[16], dz[16];
+                tc::ld16(lane_t + 128 + 16 * c, z);
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int j = 16 * c + e;
+                    float h;
+                    const float sp = silu_d(z[e] + V.b3[j], h);
+                    dz[e] = dy * V.w4[j] * sp;
+                    st_bf16(sm + kTrDZT, tc::kmaj_off(128, j, tid), dz[e]);
+                    float v = dy * h;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0) red[warp * 65 + j] += v;
+                }
+                tc::st_row8(t.p, tc::kmaj_off(128, tid, 16 * c), dz);
+                tc::st_row8(t.p, tc::kmaj_off(128, tid, 16 * c + 8), dz + 8);
             }
         }
-        {
-            float v = (t == 0) ? dg + dg8 : 0.f;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) atomicAdd(&S.g[P_B4], v);
+        tc_publish(t);
+        // dH2 = dZ3 G3 and DW3 += dZ3^T H2 (with db3 in column 64)
+        if (tid == 0) {
+            tc::fence_after();
+            const uint32_t id64 = tc::idesc_bf16(128, 64), id80 = tc::idesc_bf16(128, 80);
+            const uint32_t sp_ = tc::smem_addr(t.p), sg = tc::smem_addr(t.w + tc::kImgG3);
+            const uint32_t sdz = tc::smem_addr(sm + kTrDZT), sh = tc::smem_addr(sm + kTrH2T);
+            for (int j = 0; j < 4; ++j) tc::mma(t.tmem + 192, tc::op_desc(sp_, 128, j), tc::op_desc(sg, 64, j), id64, j > 0);
+            for (int j = 0; j < 8; ++j)
+                tc::mma(t.tmem + kColDW3, tc::op_desc(sdz, 128, j), tc::op_desc(sh, 80, j), id80, (!first || j > 0));
+            tc::commit(t.mbar);
         }
-        // dz3 = dL/dy * w4 * silu'(z3)
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const float w0 = V.w4[frag_col(nt, 0, lane)], w1 = V.w4[frag_col(nt, 1, lane)];
-            s3[nt][0] *= dg * w0;
-            s3[nt][1] *= dg * w1;
-            s3[nt][2] *= dg8 * w0;
-            s3[nt][3] *= dg8 * w1;
+        ok &= tc::mbar_wait(t.mbar, phase);
+        phase ^= 1u;
+        tc::fence_after();
+        tc_backprop_row(lane_t, 64, V.b2, t.q, tid, sm + kTrDZT);  // dZ2 into Q and dZ2^T
+        tc_publish(t);
+        // dH1 = dZ2 G2 and DW2 += dZ2^T H1
+        if (tid == 0) {
+            tc::fence_after();
+            const uint32_t id64 = tc::idesc_bf16(128, 64), id80 = tc::idesc_bf16(128, 80);
+            const uint32_t sq = tc::smem_addr(t.q), sg = tc::smem_addr(t.w + tc::kImgG2);
+            const uint32_t sdz = tc::smem_addr(sm + kTrDZT), sh = tc::smem_addr(sm + kTrH1T);
+            for (int j = 0; j < 4; ++j) tc::mma(t.tmem + 192, tc::op_desc(sq, 128, j), tc::op_desc(sg, 64, j), id64, j > 0);
+            for (int j = 0; j < 8; ++j)
+                tc::mma(t.tmem + kColDW2, tc::op_desc(sdz, 128, j), tc::op_desc(sh, 80, j), id80, (!first || j > 0));
+            tc::commit(t.mbar);
         }
-        bias_grad(s3, S.g + P_B3, lane);
-        store_T(S.dzT[w], s3, lane);
-        __syncwarp();
-        weight_grad<8>(S.dzT[w], S.h2T[w], S.g + P_W3, 64, lane);
-        c_to_a(s3, A);
-        mlp_layer<4>(F + kFragG3 * 32, A, z2, lane);  // dL/dh2
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) s2[nt][e] *= z2[nt][e];
-        bias_grad(s2, S.g + P_B2, lane);
-        __syncwarp();
-        store_T(S.dzT[w], s2, lane);
-        __syncwarp();
-        weight_grad<8>(S.dzT[w], S.h1T[w], S.g + P_W2, 64, lane);
-        c_to_a(s2, A);
-        mlp_layer<4>(F + kFragG2 * 32, A, z1, lane);  // dL/dh1
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) s1[nt][e] *= z1[nt][e];
-        bias_grad(s1, S.g + P_B1, lane);
-        __syncwarp();
-        store_T(S.dzT[w], s1, lane);
-        __syncwarp();
-        weight_grad<2>(S.dzT[w], S.xT[w], S.g + P_W1, 16, lane);
-        __syncwarp();
+        ok &= tc::mbar_wait(t.mbar, phase);
+        phase ^= 1u;
+        tc::fence_after();
+        tc_backprop_row(lane_t, 0, V.b1, nullptr, tid, sm + kTrDZT);  // dZ1^T only (DW1 += dZ1^T X)
+        tc_publish(t);
+        if (tid == 0) {
+            tc::fence_after();
+            const uint32_t id32 = tc::idesc_bf16(128, 32);
+            const uint32_t sdz = tc::smem_addr(sm + kTrDZT), sx = tc::smem_addr(sm + kTrXT);
+            for (int j = 0; j < 8; ++j)
+                tc::mma(t.tmem + kColDW1, tc::op_desc(sdz, 128, j), tc::op_desc(sx, 32, j), id32, (!first || j > 0));
+            tc::commit(t.mbar);
+        }
+        ok &= tc::mbar_wait(t.mbar, phase);
+        phase ^= 1u;
+        tc::fence_after();
+        tc::fence_before();
+        ok = __syncthreads_and(ok) != 0;
+        tc::fence_after();
+        first = false;
     }
-    // loss and the block's gradient into the global accumulators
-    for (int o = 16; o > 0; o >>= 1) sse += __shfl_xor_sync(0xffffffffu, sse, o);
-    if (lane == 0 && sse != 0.0) atomicAdd(a.loss, sse);
+    // the block's gradients: weights (and b1..b3) from tensor memory, rows = units 0..63
+    if (!first && ok && warp < 2) {
+        const int j = tid;  // unit
+        float* g = a.grad;
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            float v[16];
+            tc::ld16(lane_t + kColDW3 + 16 * c, v);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int k = 16 * c + e;
+                if (k < 64) atomicAdd(g + P_W3 + j * 64 + k, v[e]);
+                else if (k == 64) atomicAdd(g + P_B3 + j, v[e]);
+            }
+            tc::ld16(lane_t + kColDW2 + 16 * c, v);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int k = 16 * c + e;
+                if (k < 64) atomicAdd(g + P_W2 + j * 64 + k, v[e]);
+                else if (k == 64) atomicAdd(g + P_B2 + j, v[e]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            float v[16];
+            tc::ld16(lane_t + kColDW1 + 16 * c, v);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int k = 16 * c + e;
+                if (k < kMlpIn) atomicAdd(g + P_W1 + j * 16 + k, v[e]);
+                else if (k == 16) atomicAdd(g + P_B1 + j, v[e]);
+            }
+        }
+    }
+    // b4 and the loss: warp sums, then the block's (w4's are in red already)
+    {
+        float v = gb4;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp * 65 + 64] = v;
+        for (int o = 16; o > 0; o >>= 1) sse += __shfl_xor_sync(0xffffffffu, sse, o);
+        if (lane == 0 && sse != 0.0) atomicAdd(a.loss, sse);
+    }
+    tc::fence_before();
     __syncthreads();
-    for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x)
-        if (S.g[k] != 0.f) atomicAdd(a.grad + k, S.g[k]);
+    if (tid < 65) {
+        const float v = red[tid] + red[65 + tid] + red[130 + tid] + red[195 + tid];
+        if (v != 0.f) atomicAdd(a.grad + (tid < 64 ? P_W4 + tid : P_B4), v);
+    }
+    if (warp == 0) {
+        tc::fence_after();
+        tc::tmem_dealloc(t.tmem, 512);
+    }
+    if (!ok && tid == 0) atomicOr(a.err, 1u);
 }
 
 // Adam on the masters of one class; zeroes the gradient. Input columns 7..15 of W1 stay 0.
@@ -325,33 +539,64 @@ __global__ void k_mlp_adam(float* P, float* G, float* m1, float* m2, int n, floa
     P[k] -= lr * (mk / c1) / (sqrtf(vk / c2) + eps);
 }
 
-// Network outputs for contiguous samples of one class (tests, audits): y and dy/dx' in
-// normalised units, one warp per 16 samples.
-__global__ void k_mlp_predict(const MlpDev* M, int cls, const float* feats, int n, float* y,
-                              float* dydx)
+// Network outputs for contiguous samples of one class (tests, calibration, audits): y
+// and dy/dx' in normalised units, 128 samples per tile on the tensor cores.
+constexpr uint32_t kPrW = 0, kPrX = 36864, kPrP = kPrX + kTcX, kPrQ = kPrP + kTcAct,
+                   kPrBytes = kPrQ + kTcAct + 32768;
+
+__global__ void __launch_bounds__(128) k_mlp_predict(const MlpDev* M, int cls, const float* feats, int n, float* y,
+                                                     float* dydx, uint32_t* err)
 {
-    const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const MlpVec& V = M->vec[cls];
-    for (int base = gw * 16; base < n; base += nw * 16) {
-        const int s = base + (lane & 15);
+    tc_load_weights(sm + kPrW, M->tcw[cls]);
+    if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_base), 256);
+    if (tid == 0) tc::mbar_init(tc::smem_addr(&mbar), 1);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    TcTile t;
+    t.w = sm + kPrW;
+    t.x = sm + kPrX;
+    t.p = sm + kPrP;
+    t.q = sm + kPrQ;
+    t.mbar = tc::smem_addr(&mbar);
+    t.tmem = tmem_base;
+    t.bar_id = 1;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int base = blockIdx.x * kTcRows; base < n && ok; base += gridDim.x * kTcRows) {
+        const int s = base + tid;
         float x[kMlpIn];
 #pragma unroll
         for (int f = 0; f < kMlpIn; ++f) x[f] = s < n ? (feats[(size_t)s * 8 + f] - V.mu[f]) * V.inv_sd[f] : 0.f;
         float yy, d[kMlpIn];
-        mlp_rows16(*M, cls, x, yy, d);
-        if (lane < 16 && s < n) {
+        ok &= tc_rows128(t, phase, V, x, yy, d);
+        if (s < n) {
             y[s] = yy;
 #pragma unroll
             for (int f = 0; f < kMlpIn; ++f) dydx[(size_t)s * kMlpIn + f] = d[f];
         }
+        ok = __syncthreads_and(ok) != 0;
+        tc::fence_after();
     }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after();
+        tc::tmem_dealloc(t.tmem, 256);
+    }
+    if (!ok && tid == 0) atomicOr(err, 1u);
 }
 
 }  // namespace
 
 struct oxg_mlp {
     MlpDev* dev = nullptr;
+    uint32_t* err = nullptr;  // set by a tensor-core kernel whose MMA wait gave up
     float* P = nullptr;   // masters, kMlpClasses * kMlpParams
     float* G = nullptr;   // gradients
     float* m1 = nullptr;  // Adam moments
@@ -363,10 +608,25 @@ struct oxg_mlp {
 
 namespace {
 
+// A tensor-core kernel reports an MMA wait that gave up through m->err (read after a
+// synchronisation, then cleared).
+int mlp_check_err(oxg_mlp* m)
+{
+    uint32_t e = 0;
+    MCUDA(cudaMemcpy(&e, m->err, sizeof(e), cudaMemcpyDeviceToHost));
+    if (e) {
+        MCUDA(cudaMemset(m->err, 0, sizeof(e)));
+        return internal_set_error(OXG_ERR_TIMEOUT, "a tensor-core MMA of the surrogate did not complete");
+    }
+    return OXG_OK;
+}
+
 int mlp_repack(oxg_mlp* m, cudaStream_t st)
 {
     const int n = kMlpClasses * kFragTiles * 32;
     k_mlp_pack<<<(n + 255) / 256, 256, 0, st>>>(m->P, m->dev);
+    const int nt = kMlpClasses * (1024 + 4 * 4096 + 1024);
+    k_mlp_pack_tc<<<(nt + 255) / 256, 256, 0, st>>>(m->P, m->dev);
     k_mlp_pack_vec<<<1, kMlpClasses * kMlpHid, 0, st>>>(m->P, m->dev);
     MCUDA(cudaGetLastError());
     return OXG_OK;
@@ -387,11 +647,13 @@ int oxg_mlp_create(oxg_mlp** out)
     const size_t np = (size_t)kMlpClasses * kMlpParams;
     if (cudaMalloc(&m->dev, sizeof(MlpDev)) != cudaSuccess || cudaMalloc(&m->P, np * 4) != cudaSuccess ||
         cudaMalloc(&m->G, np * 4) != cudaSuccess || cudaMalloc(&m->m1, np * 4) != cudaSuccess ||
-        cudaMalloc(&m->m2, np * 4) != cudaSuccess || cudaMalloc(&m->loss, sizeof(double)) != cudaSuccess) {
+        cudaMalloc(&m->m2, np * 4) != cudaSuccess || cudaMalloc(&m->loss, sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&m->err, sizeof(uint32_t)) != cudaSuccess) {
         oxg_mlp_destroy(m);
         return internal_set_error(OXG_ERR_CUDA, "cudaMalloc failed");
     }
     cudaMemset(m->dev, 0, sizeof(MlpDev));
+    cudaMemset(m->err, 0, sizeof(uint32_t));
     cudaMemset(m->P, 0, np * 4);
     cudaMemset(m->G, 0, np * 4);
     cudaMemset(m->m1, 0, np * 4);
@@ -421,6 +683,7 @@ int oxg_mlp_destroy(oxg_mlp* m)
     cudaFree(m->m1);
     cudaFree(m->m2);
     cudaFree(m->loss);
+    cudaFree(m->err);
     delete m;
     return OXG_OK;
 }
@@ -486,19 +749,23 @@ int oxg_mlp_gradient(oxg_mlp* m, int cls, const float* feats, const float* targe
     a.nb = nb;
     a.grad = m->G + (size_t)cls * kMlpParams;
     a.loss = m->loss;
+    a.err = m->err;
     MCUDA(cudaMemsetAsync(m->loss, 0, sizeof(double), st));
-    const int smem = (int)sizeof(TrainSmem);
+    const int smem = (int)kTrBytes;
     MCUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    const int chunks = (nb + 15) / 16;
-    const int blocks = std::max(1, std::min((chunks + kTrainWarps - 1) / kTrainWarps, 2 * internal_num_sms()));
-    k_mlp_train<<<blocks, kTrainWarps * 32, smem, st>>>(a);
+    const int tiles = (nb + kTcRows - 1) / kTcRows;
+    const int blocks = std::max(1, std::min(tiles, internal_num_sms()));
+    k_mlp_train<<<blocks, 128, smem, st>>>(a);
     MCUDA(cudaGetLastError());
     if (grad_host) {
         MCUDA(cudaMemcpyAsync(grad_host, a.grad, kMlpParams * 4, cudaMemcpyDeviceToHost, st));
         MCUDA(cudaMemsetAsync(a.grad, 0, kMlpParams * 4, st));
     }
     if (loss_host) MCUDA(cudaMemcpyAsync(loss_host, m->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
-    if (grad_host || loss_host) MCUDA(cudaStreamSynchronize(st));
+    if (grad_host || loss_host) {
+        MCUDA(cudaStreamSynchronize(st));
+        return mlp_check_err(m);
+    }
     return OXG_OK;
 }
 
@@ -524,12 +791,14 @@ int oxg_mlp_predict(oxg_mlp* m, int cls, const float* feats, int n, float* y, fl
         return internal_set_error(OXG_ERR_INVALID_ARG, "bad arguments");
     if (n == 0) return OXG_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    const int warps = (n + 15) / 16;
-    const int blocks = std::min((warps + 7) / 8, 8 * internal_num_sms());
-    k_mlp_predict<<<blocks, 256, 0, st>>>(m->dev, cls, feats, n, y, dydx);
+    const int smem = (int)kPrBytes;
+    MCUDA(cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const int tiles = (n + kTcRows - 1) / kTcRows;
+    const int blocks = std::min(tiles, 2 * internal_num_sms());
+    k_mlp_predict<<<blocks, 128, smem, st>>>(m->dev, cls, feats, n, y, dydx, m->err);
     MCUDA(cudaGetLastError());
     MCUDA(cudaStreamSynchronize(st));
-    return OXG_OK;
+    return mlp_check_err(m);
 }
 
 }  // extern "C"

@@ -38,10 +38,13 @@ struct MlpVec {
     float pad[11];
 };
 
-// Device image of the surrogate (both classes).
+// Device image of the surrogate (both classes): the mma fragments of the in-kernel
+// warp pass, the vectors, and the tcgen05 weight images (B operands of the six GEMMs
+// in the canonical K-major layout, oxg_tc.cuh).
 struct MlpDev {
     uint2 frag[kMlpClasses][kFragTiles][32];  // BF16x2 pairs (b0, b1) per lane
     MlpVec vec[kMlpClasses];
+    alignas(16) unsigned char tcw[kMlpClasses][36864];
 };
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)

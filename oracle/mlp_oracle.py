@@ -64,32 +64,37 @@ def loss_gradient(params, xn, yt):
     g = np.zeros(len(params))
     g[9408:9472] = dy @ c["h3"]
     g[9472] = dy.sum()
+    # the bias gradients are sums of the BF16 operands (a row of ones in the weight-
+    # gradient GEMM's B operand yields them)
     dz3 = dy[:, None] * w["w4"][None, :] * c["s3"]
-    g[9344:9408] = dz3.sum(0)
+    g[9344:9408] = bf16(dz3).sum(0)
     g[5248:9344] = (bf16(dz3).T @ c["h2b"]).ravel()
     dh2 = bf16(dz3) @ bf16(w["W3"])
     dz2 = dh2 * c["s2"]
-    g[5184:5248] = dz2.sum(0)
+    g[5184:5248] = bf16(dz2).sum(0)
     g[1088:5184] = (bf16(dz2).T @ c["h1b"]).ravel()
     dh1 = bf16(dz2) @ bf16(w["W2"])
     dz1 = dh1 * c["s1"]
-    g[1024:1088] = dz1.sum(0)
+    g[1024:1088] = bf16(dz1).sum(0)
     gw1 = np.zeros((64, 16))
     gw1[:, :N_IN] = bf16(dz1).T @ c["xb"]
     g[0:1024] = gw1.ravel()
     return g, float(((y - yt) ** 2).sum())
 
 
-def input_gradient(params, xn):
-    """y and dy/dxn of each sample as the inference pass (mlp_rows16) computes them:
-    SiLU derivatives of the first two layers rounded to BF16, every GEMM operand BF16."""
+def input_gradient(params, xn, round_silu_grad=False):
+    """y and dy/dxn of each sample as the inference passes compute them: every GEMM
+    operand BF16; the SiLU derivatives of the first two layers FP32 (the tensor-core
+    pass recomputes them from the accumulators kept in tensor memory) or, with
+    round_silu_grad, rounded to BF16 (the in-kernel warp pass keeps them packed)."""
     y, c = forward(params, xn)
     w = c["w"]
+    r = bf16 if round_silu_grad else (lambda v: v)
     dz3 = c["s3"] * w["w4"][None, :]
     dh2 = bf16(dz3) @ bf16(w["W3"])
-    dz2 = dh2 * bf16(c["s2"])
+    dz2 = dh2 * r(c["s2"])
     dh1 = bf16(dz2) @ bf16(w["W2"])
-    dz1 = dh1 * bf16(c["s1"])
+    dz1 = dh1 * r(c["s1"])
     dx = bf16(dz1) @ bf16(w["W1"])
     return y, dx
 

@@ -38,8 +38,9 @@ def _net(seed):
 
 
 def test_training_gradient_matches_oracle(native):
-    """k_mlp_train's loss gradient (every parameter block, both classes) against the
-    BF16-emulating numpy oracle on the same minibatch."""
+    """k_mlp_train's loss gradient (tcgen05 GEMMs; every parameter block, both classes)
+    against the BF16-emulating numpy oracle on the same minibatch (several 128-sample
+    tiles, the last one partial)."""
     import torch
     from oracle import mlp_oracle as M
     net, p = _net(3)
@@ -61,8 +62,8 @@ def test_training_gradient_matches_oracle(native):
 
 
 def test_inference_matches_oracle(native):
-    """mlp_rows16 (energy and input gradient, the pass the force kernels run) against the
-    oracle's emulation of the same BF16 rounding points."""
+    """k_mlp_predict (energy and input gradient of 128-row tiles on the tensor cores)
+    against the oracle's emulation of the same BF16 rounding points."""
     import torch
     from oracle import mlp_oracle as M
     net, p = _net(5)
