@@ -468,7 +468,7 @@ struct oxg_system {
     int grid_forces = 0;
     // persistent run kernel
     GridBarrier* bar = nullptr;
-    int grid_run = 0, grid_run_surr = 0;
+    int grid_run = 0;
     bool lists_valid = false;  // pair lists built for the current positions' reference
     cudaEvent_t ev_run[2] = {nullptr, nullptr};  // around each run-kernel launch
     double run_kernel_ms = 0.0;
@@ -658,6 +658,11 @@ int forces_grid(oxg_system* s)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forces_a<false>, 256, s->ctx->block_bytes);
         if (per_sm < 1) per_sm = 1;
         s->grid_forces = num_sms() * per_sm;
+        // the surrogate kernel's shared memory exceeds the default limit (set here, outside
+        // any stream capture)
+        const int smem = (int)surrogate_smem(kParamBlockMax);
+        cudaFuncSetAttribute(k_surrogate<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(k_surrogate<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     }
     return s->grid_forces;
 }
@@ -677,14 +682,17 @@ int launch_nlist_forces(oxg_system* s, uint32_t mask, int bonded, bool energy, b
     if (!md_step)  // MD steps: the integrator kernels reset the queue lengths
         OXG_CUDA(cudaMemsetAsync(s->st->qcount, 0, sizeof(s->st->qcount), s->stream));
     const bool surr = fa.mlp != nullptr;
+    // the surrogate's tiles on the tensor cores between the phases (two blocks per SM)
+    const uint32_t surr_smem = surrogate_smem(s->ctx->block_bytes);
+    const int surr_grid = 2 * num_sms();
     if (energy) {
         k_forces_a<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-        if (surr) k_forces_b<true, true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-        else k_forces_b<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+        if (surr) k_surrogate<true><<<surr_grid, kSurrThreads, surr_smem, s->stream>>>(fa);
+        k_forces_b<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
     } else {
         k_forces_a<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-        if (surr) k_forces_b<false, true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-        else k_forces_b<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+        if (surr) k_surrogate<false><<<surr_grid, kSurrThreads, surr_smem, s->stream>>>(fa);
+        k_forces_b<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
     }
     OXG_CUDA(cudaGetLastError());
     return OXG_OK;
@@ -1134,11 +1142,9 @@ static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = f
 {
     const int block_bytes = s->ctx->block_bytes;
     RunArgs ra;
-    ra.f = force_args(s, s->run_mask, s->run_bonded);
-    surrogate_args(s, ra.f, true);
-    const bool surr = ra.f.mlp != nullptr;
-    const void* fn = surr ? (const void*)k_run<true> : (const void*)k_run<false>;
-    int& grid = surr ? s->grid_run_surr : s->grid_run;
+    ra.f = force_args(s, s->run_mask, s->run_bonded);  // plain evaluators only
+    const void* fn = (const void*)k_run;
+    int& grid = s->grid_run;
     if (grid == 0) {
         int per_sm = 0;
         OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRunThreads, block_bytes));
@@ -1270,7 +1276,10 @@ int oxg_system_run(oxg_system* s, long nsteps)
         if (!s->ctx->bonded_set[t]) return set_err(OXG_ERR_NO_PARAMS, "bond type without parameters");
     int rc = sys_setup_nlist(s, s->run_mask, false);
     if (rc) return rc;
-    if (s->persistent && nsteps > 0) {
+    // MD steps with the surrogate take the per-step path (forces A | surrogate tiles on
+    // the tensor cores | forces B | integrator, replayed from a CUDA graph)
+    const bool surrogate_md = s->mlp && (s->surr_flags & OXG_SURROGATE_RUN) && ((s->run_mask >> kHBCross) & 1u);
+    if (s->persistent && nsteps > 0 && !surrogate_md) {
         if ((rc = run_persistent(s, nsteps))) return rc;
         OXG_CUDA(cudaStreamSynchronize(s->stream));
         return OXG_OK;
@@ -1313,6 +1322,7 @@ int oxg_system_run(oxg_system* s, long nsteps)
         DevStatus d;
         if ((rc = read_status(s, &d))) return rc;
         if (d.flags & kStNonFinite) return set_err(OXG_ERR_NONFINITE, "non-finite positions or orientations");
+        if (d.flags & kStBarrierTimeout) return set_err(OXG_ERR_TIMEOUT, "a tensor-core MMA of the surrogate did not complete");
         if (d.flags & (kStCellOverflow | kStPairOverflow)) {
             if (++retries > 8) return set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
             bool grew = false;
@@ -1336,6 +1346,7 @@ int oxg_system_run(oxg_system* s, long nsteps)
         DevStatus d;
         if ((rc = read_status(s, &d))) return rc;
         if (d.flags & kStNonFinite) return set_err(OXG_ERR_NONFINITE, "non-finite positions or orientations");
+        if (d.flags & kStBarrierTimeout) return set_err(OXG_ERR_TIMEOUT, "a tensor-core MMA of the surrogate did not complete");
         if (!(d.flags & (kStCellOverflow | kStPairOverflow))) {
             s->timestep = d.step;
             s->steps_run += 1;
@@ -1507,6 +1518,7 @@ int oxg_system_set_surrogate(oxg_system* s, const oxg_mlp* mlp, int flags, int a
     s->audit_every = (uint32_t)audit_every;
     s->audit_mod = (uint32_t)audit_mod;
     s->audit_tol = (float)audit_tol;
+    s->graph_key = ~0ull;  // the captured steps launch the surrogate kernel or not
     OXG_CUDA(cudaMemsetAsync(s->audit, 0, sizeof(SurrogateAudit), s->stream));
     OXG_CUDA(cudaStreamSynchronize(s->stream));
     return OXG_OK;
@@ -1523,7 +1535,7 @@ int oxg_system_surrogate_stats(oxg_system* s, double* out, int n)
     const double rel = h.sum_e != 0.0 ? h.sum_de / h.sum_e : 0.0;
     const double rel_se =
         h.sum_e != 0.0 ? std::sqrt(std::max(h.sum_sq_de / na - mean * mean, 0.0) * na) / std::fabs(h.sum_e) : 0.0;
-    const double v[11] = {(double)h.disabled, (double)h.n_audited, (double)h.n_over,
+    const double v[11] = {(double)(h.disabled | h.pending), (double)h.n_audited, (double)h.n_over,
                           std::sqrt(h.sum_sq_de / na), std::sqrt(h.sum_sq_e / na),
                           std::sqrt(h.sum_sq_df / na), std::sqrt(h.sum_sq_f / na),
                           (double)h.max_abs_de, (double)h.max_abs_df, rel, rel_se};

@@ -240,12 +240,14 @@ struct ForceArgs {
 // kill switch the force kernels read. The audited pairs are a hashed sample of the
 // term's pairs, so sum_de / sum_e estimates the relative error of the term's energy;
 // the switch trips when that estimate exceeds the tolerance by more than two standard
-// errors (at least kAuditMinPairs audited pairs).
+// errors (at least kAuditMinPairs audited pairs): the audit sets `pending`, and the
+// next step's forces A turns it into `disabled`, so every kernel of a step sees the
+// same switch.
 struct SurrogateAudit {
-    uint32_t disabled;
+    uint32_t disabled;           // read by the force kernels; set from `pending` at a step start
     uint32_t n_audited;
     uint32_t n_over;             // audits at which the test failed (the switch tripped)
-    uint32_t pad;
+    uint32_t pending;            // the test failed during this step
     double sum_sq_de, sum_sq_e;  // pair energy error and reference
     double sum_sq_df, sum_sq_f;  // force (on i) error and reference
     double sum_de, sum_e;        // signed sums of the pair energy error and reference
@@ -601,6 +603,8 @@ __global__ void __launch_bounds__(256) k_forces_a(ForceArgs a)
             a.st_rw->gen += 1u;
         }
         if (a.advance_step) a.st_rw->step += 1ull;
+        // a failed surrogate audit of the last step switches the surrogate off from here
+        if (a.audit && ld_volatile(&a.audit->pending)) a.audit->disabled = 1u;
     }
     double eacc[kNTerms + 3];
 #pragma unroll
@@ -647,7 +651,7 @@ static __device__ __noinline__ void surrogate_audit(const ForceArgs& a, const Pa
         const double mean = sde / n;
         const double se_rel = sqrt(fmax(sq / n - mean * mean, 0.0) * n) / fabs(se);
         const double rel = fabs(sde) / fabs(se);
-        if (!(rel - 2.0 * se_rel <= (double)a.audit_tol) && atomicExch(&au->disabled, 1u) == 0u)
+        if (!(rel - 2.0 * se_rel <= (double)a.audit_tol) && atomicExch(&au->pending, 1u) == 0u)
             atomicAdd(&au->n_over, 1u);
     }
 }
@@ -656,63 +660,6 @@ __device__ __forceinline__ bool audit_pick(int k, unsigned long long step, uint3
 {
     const uint32_t h = ((uint32_t)k * 2654435761u) ^ ((uint32_t)step * 40503u + 0x9e3779b9u);
     return (h % mod) == 0u;
-}
-
-// A warp over up to 32 queued fused HB + CS pairs of one class (q = kQHBX complementary,
-// kQHBX0 not), in two rows-of-16 passes through the network: features from the plain
-// evaluator's base-base geometry, energy and input gradient from the MLP, forces and
-// torques from the gradient. On audit steps a hashed 1 / audit_mod of the pairs is also
-// evaluated by the plain evaluator.
-template <bool ENERGY>
-__device__ __noinline__ void surrogate_segment(const int2* qbuf, const ForceArgs& a, const ParamView& P, int q, int kbase,
-                                               int cnt, double* eacc)
-{
-    const int lane = threadIdx.x & 31;
-    const ParamHeader& H = P.h();
-    const int cls = q == kQHBX ? 1 : 0;
-    const MlpVec& V = a.mlp->vec[cls];
-    const unsigned long long step = *(const volatile unsigned long long*)&a.st_rw->step;
-    const bool audit_step = a.audit_every != 0u && (step % a.audit_every) == 0ull;
-    for (int h = 0; h < 2; ++h) {
-        const int k0 = kbase + 16 * h;
-        if (k0 >= cnt) break;
-        const int k = k0 + (lane & 15);
-        bool valid = lane < 16 && k < cnt;
-        PairIn p;
-        BBGeom g;
-        Frame fi, fj;
-        float x[kMlpIn];
-#pragma unroll
-        for (int f = 0; f < kMlpIn; ++f) x[f] = 0.f;
-        if (valid) {
-            bool bad = false;
-            valid = load_pair(a, qbuf[k], H.n_types, p, bad);
-            if (valid) {
-                fi = quat_frame(p.qi);
-                fj = quat_frame(p.qj);
-                valid = bb_geometry(p.rc, fi, fj, P.term<DHBCross>(kHBCross, p.pidx).base, g);
-            }
-            if (valid) {
-                mlp_features(g, x);
-#pragma unroll
-                for (int f = 0; f < kMlpIn; ++f) x[f] = (x[f] - V.mu[f]) * V.inv_sd[f];
-            }
-        }
-        float y, dydx[kMlpIn];
-        mlp_rows16(*a.mlp, cls, x, y, dydx);
-        if (valid) {
-            const float e = V.e_scale * y + V.e_shift;
-            float dE[kMlpIn];
-#pragma unroll
-            for (int f = 0; f < kMlpIn; ++f) dE[f] = V.e_scale * dydx[f] * V.inv_sd[f];
-            PairAcc acc;
-            acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
-            mlp_grad_to_forces(g, fi, fj, dE, acc);
-            scatter<ENERGY>(a, p.i, p.j, acc, e);
-            if (ENERGY) eacc[kHBCross] += (double)e;
-            if (audit_step && audit_pick(k, step, a.audit_mod)) surrogate_audit(a, P, p.pidx, g, fi, fj, e, acc);
-        }
-    }
 }
 
 // One bond (part: 0 whole, 1 FENE + bonded excluded volume, 2 stacking).
@@ -751,7 +698,7 @@ __device__ __forceinline__ void eval_bond(const ForceArgs& a, const ParamView& P
 // bonds], each padded to whole warps: every warp evaluates 32 items of one term.
 // (Evaluating the bonds on two lanes each, FENE + bonded excluded volume | stacking,
 // shortens their chains but not the phase: the HB and cross-stacking items are as long.)
-template <bool ENERGY, bool SURR = false, bool BONDS = true>
+template <bool ENERGY, bool BONDS = true>
 __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamView& P, int gwarp,
                                               int nwarps, double* eacc, bool& bad_type)
 {
@@ -764,19 +711,13 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
 #pragma unroll
     for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
     const int lane = threadIdx.x & 31;
-    // the surrogate path is a separate instantiation: its registers would otherwise
-    // lower the occupancy of the plain kernels
-    bool surrogate = false;
-    if constexpr (SURR) surrogate = a.mlp != nullptr && __shfl_sync(0xffffffffu, ld_volatile(&a.audit->disabled), 0) == 0u;
+    // the fused HB + CS queues are the surrogate kernel's while it is switched on
+    if (a.mlp != nullptr && ld_volatile(&a.audit->disabled) == 0u) cnt[kQHBX] = cnt[kQHBX0] = 0;
+#pragma unroll
+    for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
     for (int wbase = gwarp * 32; wbase < seg[kNQ + 1]; wbase += nwarps * 32) {
         int q = 0;
         while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
-        if constexpr (SURR) {
-            if (surrogate && (q == kQHBX || q == kQHBX0)) {
-                surrogate_segment<ENERGY>(a.queue + (size_t)q * a.cap_short, a, P, q, wbase - seg[q], cnt[q], eacc);
-                continue;
-            }
-        }
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
         if (q < kNQ) eval_deferred<ENERGY>(a, P, q, __ldcg(a.queue + (size_t)q * a.cap_short + k), eacc);
@@ -789,13 +730,11 @@ __device__ __forceinline__ void forces_b_body(const ForceArgs& a, const ParamVie
 // 32 items of one term per warp.
 // bond_stage: the block's slice of the bonds in shared memory (or null: read the global
 // table). The slice is [n_bonds * block / grid, n_bonds * (block + 1) / grid).
-template <bool ENERGY, bool SURR = false>
+template <bool ENERGY>
 __device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamView& P, double* eacc,
                                                bool& bad_type, const int4* bond_stage = nullptr)
 {
     BlockQueues& bq = block_queues();
-    bool surrogate = false;  // the surrogate takes whole warps of one pair class
-    if constexpr (SURR) surrogate = a.mlp != nullptr && __shfl_sync(0xffffffffu, ld_volatile(&a.audit->disabled), 0) == 0u;
     const int n_types = P.h().n_types;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nb = a.bonded ? a.n_bonds : 0;
@@ -811,12 +750,6 @@ __device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamVi
     for (int wbase = w * 32; wbase < seg[kNQ + 1]; wbase += nw * 32) {
         int q = 0;
         while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
-        if constexpr (SURR) {
-            if (surrogate && (q == kQHBX || q == kQHBX0)) {
-                surrogate_segment<ENERGY>(bq.buf[q], a, P, q, wbase - seg[q], cnt[q], eacc);
-                continue;
-            }
-        }
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
         if (q < kNQ) eval_deferred<ENERGY>(a, P, q, bq.buf[q][k], eacc);
@@ -824,7 +757,7 @@ __device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamVi
     }
 }
 
-template <bool ENERGY, bool SURR = false>
+template <bool ENERGY>
 __global__ void __launch_bounds__(256) k_forces_b(ForceArgs a)
 {
     const ParamView P = stage_params(a.params, a.param_bytes);
@@ -832,9 +765,123 @@ __global__ void __launch_bounds__(256) k_forces_b(ForceArgs a)
 #pragma unroll
     for (int t = 0; t < kNTerms + 3; ++t) eacc[t] = 0.0;
     bool bad_type = false;
-    forces_b_body<ENERGY, SURR>(a, P, spread_warp(), (gridDim.x * blockDim.x) >> 5, eacc, bad_type);
+    forces_b_body<ENERGY>(a, P, spread_warp(), (gridDim.x * blockDim.x) >> 5, eacc, bad_type);
     reduce_energies<ENERGY>(a, eacc);
     if (bad_type) atomicOr(&a.st_rw->flags, kStBadIndex);
+}
+
+// ------------------------------------------------------ surrogate (tcgen05)
+// The queued fused HB + cross-stacking pairs of both classes through the surrogate
+// network on the tensor cores, 128 pairs per tile, a pair per thread of a 128-thread
+// block: features from the plain evaluator's base-base geometry, energy and input
+// gradient from the network (tc_rows128), forces and torques from the gradient,
+// scattered like the plain evaluator's; on audit steps a hashed sample of the pairs is
+// also evaluated by the plain evaluator. It runs between forces A (which queued the
+// pairs) and forces B (which leaves these queues to it while the surrogate is on).
+// Dynamic shared memory: the parameter block, then one class's weight image and the
+// tile's operand buffers; blocks take tiles [class 1 | class 0] round robin and load the
+// weights of a class when they first meet it.
+constexpr int kSurrThreads = 128;
+constexpr uint32_t kSurrW = 0, kSurrX = tc::kImgBytes, kSurrP = kSurrX + kTcX, kSurrQ = kSurrP + kTcAct,
+                   kSurrBuf = kSurrQ + kTcAct;
+// at least 80 KB per block so that at most two blocks (2 x 256 tensor-memory columns) share an SM
+__host__ __device__ constexpr uint32_t surrogate_smem(int param_bytes)
+{
+    const uint32_t need = (((uint32_t)param_bytes + 1023u) & ~1023u) + kSurrBuf;
+    return need > 81920u ? need : 81920u;
+}
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(kSurrThreads) k_surrogate(ForceArgs a)
+{
+    const ParamView P = stage_params(a.params, a.param_bytes);
+    extern __shared__ float4 smem_params[];
+    unsigned char* buf = reinterpret_cast<unsigned char*>(smem_params) + (((uint32_t)a.param_bytes + 1023u) & ~1023u);
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    if (ld_volatile(&a.audit->disabled)) return;  // switched off (constant during the step)
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const ParamHeader& H = P.h();
+    const int n1 = (int)min(ld_volatile(&a.st_rw->qcount[kQHBX]), (uint32_t)a.cap_short);
+    const int n0 = (int)min(ld_volatile(&a.st_rw->qcount[kQHBX0]), (uint32_t)a.cap_short);
+    const int t1 = (n1 + kTcRows - 1) / kTcRows, t0 = (n0 + kTcRows - 1) / kTcRows;
+    if ((int)blockIdx.x >= t1 + t0) return;
+    if (warp == 0) tc::tmem_alloc(tc::smem_addr(&tmem_base), 256);
+    if (tid == 0) tc::mbar_init(tc::smem_addr(&mbar), 1);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    TcTile t;
+    t.w = buf + kSurrW;
+    t.x = buf + kSurrX;
+    t.p = buf + kSurrP;
+    t.q = buf + kSurrQ;
+    t.mbar = tc::smem_addr(&mbar);
+    t.tmem = tmem_base;
+    t.bar_id = 1;
+    const unsigned long long step = *(const volatile unsigned long long*)&a.st_rw->step;
+    const bool audit_step = a.audit_every != 0u && (step % a.audit_every) == 0ull;
+    double eacc[kNTerms + 3];
+#pragma unroll
+    for (int k = 0; k < kNTerms + 3; ++k) eacc[k] = 0.0;
+    uint32_t phase = 0;
+    int loaded = -1;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < t1 + t0 && ok; tile += gridDim.x) {
+        const int cls = tile < t1 ? 1 : 0;
+        const int q = cls ? kQHBX : kQHBX0;
+        const int k = (cls ? tile : tile - t1) * kTcRows + tid;
+        if (cls != loaded) {  // block-uniform; the previous tile's MMAs have completed
+            tc_load_weights(t.w, a.mlp->tcw[cls]);
+            loaded = cls;
+        }
+        const MlpVec& V = a.mlp->vec[cls];
+        PairIn p;
+        BBGeom g;
+        Frame fi, fj;
+        float x[kMlpIn];
+#pragma unroll
+        for (int f = 0; f < kMlpIn; ++f) x[f] = 0.f;
+        bool valid = k < (cls ? n1 : n0);
+        if (valid) {
+            bool bad = false;
+            valid = load_pair(a, __ldcg(a.queue + (size_t)q * a.cap_short + k), H.n_types, p, bad);
+            if (valid) {
+                fi = quat_frame(p.qi);
+                fj = quat_frame(p.qj);
+                valid = bb_geometry(p.rc, fi, fj, P.term<DHBCross>(kHBCross, p.pidx).base, g);
+            }
+            if (valid) {
+                mlp_features(g, x);
+#pragma unroll
+                for (int f = 0; f < kMlpIn; ++f) x[f] = (x[f] - V.mu[f]) * V.inv_sd[f];
+            }
+        }
+        float y, dydx[kMlpIn];
+        ok &= tc_rows128(t, phase, V, x, y, dydx);
+        if (valid) {
+            const float e = V.e_scale * y + V.e_shift;
+            float dE[kMlpIn];
+#pragma unroll
+            for (int f = 0; f < kMlpIn; ++f) dE[f] = V.e_scale * dydx[f] * V.inv_sd[f];
+            PairAcc acc;
+            acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+            mlp_grad_to_forces(g, fi, fj, dE, acc);
+            scatter<ENERGY>(a, p.i, p.j, acc, e);
+            if (ENERGY) eacc[kHBCross] += (double)e;
+            if (audit_step && audit_pick(k, step, a.audit_mod)) surrogate_audit(a, P, p.pidx, g, fi, fj, e, acc);
+        }
+        ok = __syncthreads_and(ok) != 0;
+        tc::fence_after();
+    }
+    reduce_energies<ENERGY>(a, eacc);
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after();
+        tc::tmem_dealloc(t.tmem, 256);
+    }
+    if (!ok && tid == 0) atomicOr(&a.st_rw->flags, kStBarrierTimeout);
 }
 
 // --------------------------------------------------- drop-in: HOOMD full nlist
@@ -1682,7 +1729,6 @@ struct RunArgs {
 // of the current state, no step advance | a = F/m and step one of the first step.
 constexpr int kRunThreads = OXG_RUN_THREADS;  // threads per block of the run kernel
 constexpr int kBondStage = 512;               // bonds a block stages in shared memory
-template <bool SURR>
 __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunArgs a)
 {
     const ParamView P = stage_params(a.f.params, a.f.param_bytes);
@@ -1784,14 +1830,14 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         {
             // phase B on the block's own queues: a block barrier, not a grid barrier
             forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type, ns_known, nl_known, first_pair);
-            forces_b_local<false, SURR>(a.f, P, eacc, bad_type, bonds_here);
+            forces_b_local<false>(a.f, P, eacc, bad_type, bonds_here);
             const uint32_t tok = grid_arrive(a.bar);
             if (have_nz)
                 nz = langevin_noise((uint32_t)gthread, step, a.g.seed_lo, a.g.seed_hi, a.g.dt, a.g.kT, a.g.gamma,
                                     a.g.gamma_r);
             if (!grid_wait(a.bar, tok)) break;
             if (ld_volatile(&st->qspill)) {  // pairs that did not fit a block's queues
-                forces_b_body<false, SURR, false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+                forces_b_body<false, false>(a.f, P, gwarp, nwarps, eacc, bad_type);
                 if (!grid_barrier(a.bar)) break;
                 if (blockIdx.x == 0 && threadIdx.x == 0) st->qspill = 0u;  // read a barrier ago
             }

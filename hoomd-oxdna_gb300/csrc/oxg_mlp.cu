@@ -1,12 +1,13 @@
-// oxg_mlp.cu - the HB + cross-stacking surrogate: training-data sampling from the plain
-// evaluator, hand-written training kernels (forward, loss, backward to the weights on
-// BF16 tensor cores with FP32 accumulation, Adam) and the inference image the force
-// kernels use.
+// oxg_mlp.cu - the HB + cross-stacking surrogate: hand-written training kernels (forward,
+// loss, backward to the weights with every GEMM on the tcgen05 tensor cores, BF16
+// operands and FP32 accumulation in tensor memory; Adam), batch inference, and the
+// device image the force kernels use.
 //
 // FP32 master parameters of one class (flat, kMlpParams floats): W1[64][16] (input
 // columns 7..15 stay zero), b1[64], W2[64][64], b2[64], W3[64][64], b3[64], w4[64], b4.
-// Weight matrices are [out][in]. The device image (MlpDev) holds BF16 copies in per-lane
-// mma fragment order, rebuilt from the masters after every optimiser step.
+// Weight matrices are [out][in]. The device image (MlpDev) holds BF16 copies as the six
+// GEMMs' B operands in the canonical K-major layout, rebuilt from the masters after
+// every optimiser step.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -36,33 +37,6 @@ static_assert(kMlpParams == OXG_MLP_PARAMS, "header and kernels disagree on the 
     } while (0)
 
 // ------------------------------------------------------------------ packing
-// frag[cls][tile][lane] from the FP32 masters (one thread per (cls, tile, lane)).
-__global__ void k_mlp_pack(const float* P, MlpDev* M)
-{
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= kMlpClasses * kFragTiles * 32) return;
-    const int lane = id & 31, tile = (id >> 5) % kFragTiles, cls = id / (kFragTiles * 32);
-    const float* W = P + (size_t)cls * kMlpParams;
-    const int g = lane >> 2, t = lane & 3;
-    // B[k][n] element for a tile: forward B[k = in][n = out] = W[out][in];
-    // backward B[k = out][n = in] = W[out][in]
-    float e[4];
-    int kt, nt;
-    const float* Wm;
-    int in_dim;
-    bool fwd;
-    if (tile < kFragF2) { kt = 0; nt = tile; Wm = W + P_W1; in_dim = 16; fwd = true; }
-    else if (tile < kFragF3) { kt = (tile - kFragF2) / 8; nt = (tile - kFragF2) % 8; Wm = W + P_W2; in_dim = 64; fwd = true; }
-    else if (tile < kFragG3) { kt = (tile - kFragF3) / 8; nt = (tile - kFragF3) % 8; Wm = W + P_W3; in_dim = 64; fwd = true; }
-    else if (tile < kFragG2) { kt = (tile - kFragG3) / 8; nt = (tile - kFragG3) % 8; Wm = W + P_W3; in_dim = 64; fwd = false; }
-    else if (tile < kFragG1) { kt = (tile - kFragG2) / 8; nt = (tile - kFragG2) % 8; Wm = W + P_W2; in_dim = 64; fwd = false; }
-    else { kt = (tile - kFragG1) / 2; nt = (tile - kFragG1) % 2; Wm = W + P_W1; in_dim = 16; fwd = false; }
-    const int n = nt * 8 + g;
-    const int ks[4] = {kt * 16 + 2 * t, kt * 16 + 2 * t + 1, kt * 16 + 2 * t + 8, kt * 16 + 2 * t + 9};
-    for (int q = 0; q < 4; ++q) e[q] = fwd ? Wm[n * in_dim + ks[q]] : Wm[ks[q] * in_dim + n];
-    M->frag[cls][tile][lane] = make_uint2(pack_bf16(e[0], e[1]), pack_bf16(e[2], e[3]));
-}
-
 // vectors (biases, w4, b4) of both classes; the normalisation is set separately
 __global__ void k_mlp_pack_vec(const float* P, MlpDev* M)
 {
@@ -111,179 +85,6 @@ __global__ void k_mlp_pack_tc(const float* P, MlpDev* M)
         off = tc::kImgG1 + tc::kmaj_off(16, n, k);
     }
     *reinterpret_cast<__nv_bfloat16*>(img + off) = __float2bfloat16_rn(v);
-}
-
-// ------------------------------------------------------------------ tcgen05 tiles
-// A warpgroup (128 threads, thread = row) runs the network over 128 rows with the
-// GEMMs on the tensor cores: M = 128 rows, BF16 operands in shared memory, FP32
-// accumulators in tensor memory, read back a row per thread for the bias / SiLU
-// epilogues on the CUDA cores. Tensor-memory columns: D1 [0, 64), D2 [64, 128),
-// D3 [128, 192), D4 [192, 256) (the backward GEMMs), the input gradient in [0, 16)
-// once D1 is consumed.
-constexpr int kTcRows = 128;
-constexpr uint32_t kTcX = 4096, kTcAct = 16384;  // A buffers: 128 x 16 and 128 x 64 BF16
-
-struct TcTile {
-    unsigned char* w;  // weight image of the class (36864 B)
-    unsigned char* x;  // 128 x 16 inputs
-    unsigned char* p;  // 128 x 64 activations / gradients (two buffers)
-    unsigned char* q;
-    uint32_t mbar;     // shared address of the MMA-completion mbarrier
-    uint32_t tmem;     // tensor-memory base of the tile's columns
-    int bar_id;        // named barrier of the warpgroup
-};
-
-__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
-
-// Shared-memory writes of this warpgroup's threads become operands of an MMA issued next:
-// make them visible to the tensor cores, order earlier TMEM reads, and meet.
-__device__ __forceinline__ void tc_publish(const TcTile& t)
-{
-    tc::fence_smem_async();
-    tc::fence_before();
-    wg_sync(t.bar_id);
-}
-
-// One thread issues `steps` K = 16 MMAs D(tmem col) = A * B and commits them; then every
-// thread waits for the completion. Returns false if the wait gave up.
-__device__ __forceinline__ bool tc_gemm(const TcTile& t, uint32_t& phase, uint32_t dcol, const unsigned char* A,
-                                        int a_rows, const unsigned char* B, int b_rows, int n, int steps,
-                                        bool first_acc)
-{
-    if ((threadIdx.x & 127) == 0) {
-        tc::fence_after();
-        const uint32_t sa = tc::smem_addr(A), sb = tc::smem_addr(B), id = tc::idesc_bf16(128, n);
-        for (int j = 0; j < steps; ++j)
-            tc::mma(t.tmem + dcol, tc::op_desc(sa, a_rows, j), tc::op_desc(sb, b_rows, j), id,
-                    (first_acc || j > 0) ? 1u : 0u);
-        tc::commit(t.mbar);
-    }
-    const bool ok = tc::mbar_wait(t.mbar, phase);
-    phase ^= 1u;
-    tc::fence_after();
-    return ok;
-}
-
-__device__ __forceinline__ float silu_d(float z, float& h)
-{
-    const float sg = 1.f / (1.f + __expf(-z));
-    h = z * sg;
-    return sg * (1.f + z * (1.f - sg));
-}
-
-__device__ __forceinline__ void st_bf16(unsigned char* base, uint32_t off, float v)
-{
-    *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(v);
-}
-
-// This thread's row of D (64 columns from col) plus the bias: z; writes silu(z) as the
-// row of the next A operand (dst, if set) and as this row's column of a transposed
-// operand with tr_rows rows (dstT, if set).
-__device__ __forceinline__ void tc_bias_silu_row(uint32_t lane_t, uint32_t col, const float* b, unsigned char* dst,
-                                                 int row, unsigned char* dstT = nullptr, int tr_rows = 80)
-{
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        float z[16], h[16];
-        tc::ld16(lane_t + col + 16 * c, z);
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-            (void)silu_d(z[e] + b[16 * c + e], h[e]);
-            if (dstT) st_bf16(dstT, tc::kmaj_off(tr_rows, 16 * c + e, row), h[e]);
-        }
-        if (dst) {
-            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c), h);
-            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c + 8), h + 8);
-        }
-    }
-}
-
-// dz = g * silu'(z) for this row: g from D4, z from the forward accumulator at zcol plus
-// the bias; written as the row of an A operand (dst, if set) and as this row's column of
-// a transposed operand of 128 rows (dstT, if set).
-__device__ __forceinline__ void tc_backprop_row(uint32_t lane_t, uint32_t zcol, const float* b, unsigned char* dst,
-                                                int row, unsigned char* dstT = nullptr)
-{
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        float g[16], z[16], dz[16];
-        tc::ld16(lane_t + 192 + 16 * c, g);
-        tc::ld16(lane_t + zcol + 16 * c, z);
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-            float h;
-            dz[e] = g[e] * silu_d(z[e] + b[16 * c + e], h);
-            if (dstT) st_bf16(dstT, tc::kmaj_off(128, 16 * c + e, row), dz[e]);
-        }
-        if (dst) {
-            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c), dz);
-            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c + 8), dz + 8);
-        }
-    }
-}
-
-// Energy and input gradient of 128 rows: x (this thread's row, 7 normalised features;
-// zeros for an unused row) -> y and dy/dx'. Returns false if an MMA wait gave up.
-__device__ bool tc_rows128(const TcTile& t, uint32_t& phase, const MlpVec& V, const float* x, float& y, float* dydx)
-{
-    const int row = threadIdx.x & 127;
-    const uint32_t lane_t = t.tmem + ((uint32_t)(((threadIdx.x >> 5) & 3) * 32) << 16);
-    bool ok = true;
-    {
-        float xr[16];
-#pragma unroll
-        for (int f = 0; f < 16; ++f) xr[f] = f < kMlpIn ? x[f] : 0.f;
-        tc::st_row8(t.x, tc::kmaj_off(128, row, 0), xr);
-        tc::st_row8(t.x, tc::kmaj_off(128, row, 8), xr + 8);
-    }
-    tc_publish(t);
-    ok &= tc_gemm(t, phase, 0, t.x, 128, t.w + tc::kImgF1, 64, 64, 1, false);     // D1 = X F1
-    tc_bias_silu_row(lane_t, 0, V.b1, t.p, row);
-    tc_publish(t);
-    ok &= tc_gemm(t, phase, 64, t.p, 128, t.w + tc::kImgF2, 64, 64, 4, false);    // D2 = H1 F2
-    tc_bias_silu_row(lane_t, 64, V.b2, t.q, row);
-    tc_publish(t);
-    ok &= tc_gemm(t, phase, 128, t.q, 128, t.w + tc::kImgF3, 64, 64, 4, false);   // D3 = H2 F3
-    // output and dy/dz3 = w4 * silu'(z3)
-    float yy = V.b4;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        float z[16], dz[16];
-        tc::ld16(lane_t + 128 + 16 * c, z);
-#pragma unroll
-        for (int e = 0; e < 16; ++e) {
-            float h;
-            const float sp = silu_d(z[e] + V.b3[16 * c + e], h);
-            yy += h * V.w4[16 * c + e];
-            dz[e] = sp * V.w4[16 * c + e];
-        }
-        tc::st_row8(t.p, tc::kmaj_off(128, row, 16 * c), dz);
-        tc::st_row8(t.p, tc::kmaj_off(128, row, 16 * c + 8), dz + 8);
-    }
-    y = yy;
-    tc_publish(t);
-    ok &= tc_gemm(t, phase, 192, t.p, 128, t.w + tc::kImgG3, 64, 64, 4, false);   // dH2 = dZ3 G3
-    tc_backprop_row(lane_t, 64, V.b2, t.q, row);                                  // dZ2
-    tc_publish(t);
-    ok &= tc_gemm(t, phase, 192, t.q, 128, t.w + tc::kImgG2, 64, 64, 4, false);   // dH1 = dZ2 G2
-    tc_backprop_row(lane_t, 0, V.b1, t.p, row);                                   // dZ1
-    tc_publish(t);
-    ok &= tc_gemm(t, phase, 0, t.p, 128, t.w + tc::kImgG1, 16, 16, 4, false);     // dX = dZ1 G1
-    float dx[16];
-    tc::ld16(lane_t, dx);
-#pragma unroll
-    for (int f = 0; f < kMlpIn; ++f) dydx[f] = dx[f];
-    tc::fence_before();  // the next tile's MMAs overwrite these columns after a barrier
-    return ok;
-}
-
-// The class's weight image into shared memory (all threads of the block, 16-byte loads),
-// made visible to the tensor cores.
-__device__ __forceinline__ void tc_load_weights(unsigned char* dst, const unsigned char* src)
-{
-    for (int k = threadIdx.x; k < (int)(tc::kImgBytes / 16); k += blockDim.x)
-        reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(src)[k];
-    tc::fence_smem_async();
 }
 
 // ------------------------------------------------------------------ training (tcgen05)
@@ -373,10 +174,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
         // forward, keeping the activations' transposes for the weight gradients
         tc_publish(t);
         ok &= tc_gemm(t, phase, 0, t.x, 128, t.w + tc::kImgF1, 64, 64, 1, false);
-        tc_bias_silu_row(lane_t, 0, V.b1, t.p, tid, sm + kTrH1T, 80);
+        tc_forward_row(lane_t, 0, V.b1, t.p, tid, sm + kTrH1T, 80);
         tc_publish(t);
         ok &= tc_gemm(t, phase, 64, t.p, 128, t.w + tc::kImgF2, 64, 64, 4, false);
-        tc_bias_silu_row(lane_t, 64, V.b2, t.q, tid, sm + kTrH2T, 80);
+        tc_forward_row(lane_t, 64, V.b2, t.q, tid, sm + kTrH2T, 80);
         tc_publish(t);
         ok &= tc_gemm(t, phase, 128, t.q, 128, t.w + tc::kImgF3, 64, 64, 4, false);
         // output, loss, dL/dy (first pass over z3); dz3 = dL/dy * w4 * silu'(z3) and the
@@ -390,7 +191,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
 #pragma unroll
                 for (int e = 0; e < 16; ++e) {
                     float h;
-                    (void)silu_d(z[e] + V.b3[16 * c + e], h);
+                    (void)tc::silu_and_grad(z[e] + V.b3[16 * c + e], h);
                     y += h * V.w4[16 * c + e];
                 }
             }
@@ -406,7 +207,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
                 for (int e = 0; e < 16; ++e) {
                     const int j = 16 * c + e;
                     float h;
-                    const float sp = silu_d(z[e] + V.b3[j], h);
+                    const float sp = tc::silu_and_grad(z[e] + V.b3[j], h);
                     dz[e] = dy * V.w4[j] * sp;
                     st_bf16(sm + kTrDZT, tc::kmaj_off(128, j, tid), dz[e]);
                     float v = dy * h;
@@ -433,7 +234,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
         ok &= tc::mbar_wait(t.mbar, phase);
         phase ^= 1u;
         tc::fence_after();
-        tc_backprop_row(lane_t, 64, V.b2, t.q, tid, sm + kTrDZT);  // dZ2 into Q and dZ2^T
+        tc_backward_row(lane_t, 64, t.q, tid, sm + kTrDZT);  // dZ2 into Q and dZ2^T
         tc_publish(t);
         // dH1 = dZ2 G2 and DW2 += dZ2^T H1
         if (tid == 0) {
@@ -449,7 +250,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
         ok &= tc::mbar_wait(t.mbar, phase);
         phase ^= 1u;
         tc::fence_after();
-        tc_backprop_row(lane_t, 0, V.b1, nullptr, tid, sm + kTrDZT);  // dZ1^T only (DW1 += dZ1^T X)
+        tc_backward_row(lane_t, 0, nullptr, tid, sm + kTrDZT);  // dZ1^T only (DW1 += dZ1^T X)
         tc_publish(t);
         if (tid == 0) {
             tc::fence_after();
@@ -623,8 +424,6 @@ int mlp_check_err(oxg_mlp* m)
 
 int mlp_repack(oxg_mlp* m, cudaStream_t st)
 {
-    const int n = kMlpClasses * kFragTiles * 32;
-    k_mlp_pack<<<(n + 255) / 256, 256, 0, st>>>(m->P, m->dev);
     const int nt = kMlpClasses * (1024 + 4 * 4096 + 1024);
     k_mlp_pack_tc<<<(nt + 255) / 256, 256, 0, st>>>(m->P, m->dev);
     k_mlp_pack_vec<<<1, kMlpClasses * kMlpHid, 0, st>>>(m->P, m->dev);

@@ -1,5 +1,6 @@
 // oxg_mlp.cuh - the learned surrogate of the fused hydrogen-bonding + cross-stacking
-// pair term: a 7 -> 64 -> 64 -> 64 -> 1 SiLU MLP on BF16 tensor cores (FP32 accumulate).
+// pair term: a 7 -> 64 -> 64 -> 64 -> 1 SiLU MLP on the fifth-generation tensor cores
+// (tcgen05: BF16 operands, FP32 accumulation in tensor memory).
 //
 // Inputs (the base-base geometry the plain evaluator computes, bb_geometry): the BASE-BASE
 // distance and the cosines c1, c2, c3, c4, c7, c8; output: the pair energy. There is one
@@ -7,27 +8,26 @@
 // only cross-stack). Forces and torques come from the analytic input gradient of the
 // network (its backward pass), mapped onto positions and orientations.
 //
-// The warp is the unit of work: 16 pairs are the 16 rows of mma.m16n8k16 tiles, and the
-// activations never leave registers. The C fragment of two neighbouring n-tiles of one
-// layer, packed to BF16, is exactly the A fragment of one k-tile of the next layer, so
-// the forward pass (3 GEMMs) and the input-gradient pass (3 more) chain in registers;
-// the weights are pre-arranged on the device in per-lane fragment order (one 64-bit
-// load per lane per tile).
+// The tile is the unit of work: a warpgroup (128 threads) runs 128 rows (pairs or
+// training samples), a row per thread. Every GEMM has M = 128 rows: the layer's input
+// rows are written as BF16 into shared memory in the canonical K-major layout, one
+// thread issues the MMAs (weights in shared memory as the B operand), the FP32
+// accumulator lands in tensor memory and comes back a row per thread for the bias /
+// SiLU epilogue, which writes the next layer's operand. The SiLU derivatives of the
+// forward pass are written back into tensor memory over the pre-activations, so the
+// backward (input-gradient) GEMMs need no recomputation.
 #pragma once
 #include <cuda_bf16.h>
 #include <stdint.h>
 
 #include "oxg_device.cuh"
+#include "oxg_tc.cuh"
 
 namespace oxg {
 
 constexpr int kMlpIn = 7;      // r, c1, c2, c3, c4, c7, c8
 constexpr int kMlpHid = 64;
 constexpr int kMlpClasses = 2; // 0: non-complementary (cross-stacking only), 1: complementary
-// fragment tiles per class: forward W1 (K16 x N64: 8), W2, W3 (K64 x N64: 32 each),
-// backward W3^T, W2^T (32 each), W1^T (K64 x N16: 8)
-constexpr int kFragF1 = 0, kFragF2 = 8, kFragF3 = 40, kFragG3 = 72, kFragG2 = 104, kFragG1 = 136;
-constexpr int kFragTiles = 144;
 
 // FP32 vectors of one class
 struct MlpVec {
@@ -38,185 +38,174 @@ struct MlpVec {
     float pad[11];
 };
 
-// Device image of the surrogate (both classes): the mma fragments of the in-kernel
-// warp pass, the vectors, and the tcgen05 weight images (B operands of the six GEMMs
-// in the canonical K-major layout, oxg_tc.cuh).
+// Device image of the surrogate (both classes): the FP32 vectors and the BF16 weight
+// images (the B operands of the six GEMMs in the canonical K-major layout, oxg_tc.cuh).
 struct MlpDev {
-    uint2 frag[kMlpClasses][kFragTiles][32];  // BF16x2 pairs (b0, b1) per lane
     MlpVec vec[kMlpClasses];
-    alignas(16) unsigned char tcw[kMlpClasses][36864];
+    alignas(16) unsigned char tcw[kMlpClasses][tc::kImgBytes];
 };
 
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+// ---------------------------------------------------------------- a 128-row tile
+constexpr int kTcRows = 128;
+constexpr uint32_t kTcX = 4096, kTcAct = 16384;  // A buffers: 128 x 16 and 128 x 64 BF16
+
+struct TcTile {
+    unsigned char* w;  // weight image of the class (tc::kImgBytes)
+    unsigned char* x;  // 128 x 16 inputs
+    unsigned char* p;  // 128 x 64 activations / gradients (two buffers)
+    unsigned char* q;
+    uint32_t mbar;     // shared address of the MMA-completion mbarrier
+    uint32_t tmem;     // tensor-memory base of the tile's 256 columns: D1 [0, 64), D2 [64,
+                       // 128), D3 [128, 192), D4 [192, 256); the input gradient in [0, 16)
+    int bar_id;        // named barrier of the warpgroup
+};
+
+__device__ __forceinline__ void wg_sync(int id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+
+__device__ __forceinline__ void st_bf16(unsigned char* base, uint32_t off, float v)
 {
-    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<const uint32_t*>(&v);
+    *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16_rn(v);
 }
 
-// D = A(16x16, bf16, row) * B(16x8, bf16, col) + C (fp32)
-__device__ __forceinline__ void mma_bf16(float* d, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint2 b)
+// Shared-memory writes of this warpgroup become operands of the MMAs issued next: make
+// them visible to the tensor cores, order earlier tensor-memory accesses, and meet.
+__device__ __forceinline__ void tc_publish(const TcTile& t)
 {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b.x), "r"(b.y));
+    tc::fence_smem_async();
+    tc::fence_before();
+    wg_sync(t.bar_id);
 }
 
-__device__ __forceinline__ float sigmoidf_fast(float z) { return 1.f / (1.f + __expf(-z)); }
-
-// One dense layer of 64 outputs over K = 16 * KT inputs given as A fragments:
-// out[nt][0..3] (C fragments of n-tile nt) = sum_kt A[kt] * B[kt][nt].
-template <int KT>
-__device__ __forceinline__ void mlp_layer(const uint2* frag, const uint32_t (*A)[4], float (*out)[4],
-                                          int lane)
+// One thread issues `steps` K = 16 MMAs D(col) = A * B (+ D) and commits them; every
+// thread then waits for their completion. Returns false if the wait gave up.
+__device__ __forceinline__ bool tc_gemm(const TcTile& t, uint32_t& phase, uint32_t dcol, const unsigned char* A,
+                                        int a_rows, const unsigned char* B, int b_rows, int n, int steps,
+                                        bool first_acc)
 {
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) out[nt][0] = out[nt][1] = out[nt][2] = out[nt][3] = 0.f;
-#pragma unroll
-    for (int kt = 0; kt < KT; ++kt)
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-            mma_bf16(out[nt], A[kt][0], A[kt][1], A[kt][2], A[kt][3], frag[(kt * 8 + nt) * 32 + lane]);
-}
-
-// A fragments of the next layer from the 64-column C fragments of this one.
-__device__ __forceinline__ void c_to_a(const float (*c)[4], uint32_t (*A)[4])
-{
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-        A[kt][0] = pack_bf16(c[2 * kt][0], c[2 * kt][1]);
-        A[kt][1] = pack_bf16(c[2 * kt][2], c[2 * kt][3]);
-        A[kt][2] = pack_bf16(c[2 * kt + 1][0], c[2 * kt + 1][1]);
-        A[kt][3] = pack_bf16(c[2 * kt + 1][2], c[2 * kt + 1][3]);
+    if ((threadIdx.x & 127) == 0) {
+        tc::fence_after();
+        const uint32_t sa = tc::smem_addr(A), sb = tc::smem_addr(B), id = tc::idesc_bf16(128, n);
+        for (int j = 0; j < steps; ++j)
+            tc::mma(t.tmem + dcol, tc::op_desc(sa, a_rows, j), tc::op_desc(sb, b_rows, j), id,
+                    (first_acc || j > 0) ? 1u : 0u);
+        tc::commit(t.mbar);
     }
+    const bool ok = tc::mbar_wait(t.mbar, phase);
+    phase ^= 1u;
+    tc::fence_after();
+    return ok;
 }
 
-// Column of C-fragment element e of n-tile nt for this lane (rows: g for e < 2, g + 8 else).
-__device__ __forceinline__ int frag_col(int nt, int e, int lane) { return nt * 8 + 2 * (lane & 3) + (e & 1); }
-
-// z <- z + b; h = silu(z) (in place into z); s = silu'(z).
-__device__ __forceinline__ void bias_silu(float (*z)[4], float (*s)[4], const float* b, int lane)
+// Forward epilogue of this thread's row: z = D (64 columns from col) + b; silu(z) as the
+// row of the next A operand (dst, if set) and as this row's column of a transposed
+// operand with tr_rows rows (dstT, if set); silu'(z) written back over z.
+__device__ __forceinline__ void tc_forward_row(uint32_t lane_t, uint32_t col, const float* b, unsigned char* dst,
+                                               int row, unsigned char* dstT = nullptr, int tr_rows = 80)
 {
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt)
+    for (int c = 0; c < 4; ++c) {
+        float z[16], h[16];
+        tc::ld16(lane_t + col + 16 * c, z);
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const float x = z[nt][e] + b[frag_col(nt, e, lane)];
-            const float sg = sigmoidf_fast(x);
-            z[nt][e] = x * sg;
-            s[nt][e] = sg * (1.f + x * (1.f - sg));
+        for (int e = 0; e < 16; ++e) {
+            z[e] = tc::silu_and_grad(z[e] + b[16 * c + e], h[e]);
+            if (dstT) st_bf16(dstT, tc::kmaj_off(tr_rows, 16 * c + e, row), h[e]);
         }
-}
-
-// silu'(z) of a layer kept as BF16 pairs (in the C-fragment order) for the backward pass.
-__device__ __forceinline__ void pack_frags(const float (*c)[4], uint32_t (*p)[2])
-{
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-        p[nt][0] = pack_bf16(c[nt][0], c[nt][1]);
-        p[nt][1] = pack_bf16(c[nt][2], c[nt][3]);
-    }
-}
-__device__ __forceinline__ void mul_packed(float (*c)[4], const uint32_t (*p)[2])
-{
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-        const float2 lo = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&p[nt][0]));
-        const float2 hi = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&p[nt][1]));
-        c[nt][0] *= lo.x;
-        c[nt][1] *= lo.y;
-        c[nt][2] *= hi.x;
-        c[nt][3] *= hi.y;
+        tc::st16(lane_t + col + 16 * c, z);
+        if (dst) {
+            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c), h);
+            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c + 8), h + 8);
+        }
     }
 }
 
-// Energy and input gradient of 16 pairs (rows) of one class for a warp. x[f] holds the
-// normalised features of row (lane & 15) in lanes 0..15 (any values in lanes 16..31).
-// Returns, in lanes 0..15 for row (lane & 15): y (network output) and dy/dx'[0..6].
-// The SiLU derivatives of the first two layers are kept as BF16 (they multiply values
-// that are rounded to BF16 as the next MMA operand anyway), which keeps the pass within
-// the register budget of the force kernels.
-__device__ __forceinline__ void mlp_rows16(const MlpDev& M, int cls, const float* x, float& y,
-                                           float* dydx)
+// Backward epilogue of this thread's row: dz = g * silu'(z), g from D4 and silu'(z) from
+// the forward columns scol; written as the row of an A operand (dst, if set) and as this
+// row's column of a transposed operand of 128 rows (dstT, if set).
+__device__ __forceinline__ void tc_backward_row(uint32_t lane_t, uint32_t scol, unsigned char* dst, int row,
+                                                unsigned char* dstT = nullptr)
 {
-    const int lane = threadIdx.x & 31;
-    const int g = lane >> 2, t = lane & 3;
-    const uint2* F = &M.frag[cls][0][0];
-    const MlpVec& V = M.vec[cls];
-    // A fragment of the inputs: rows g, g + 8; columns 2t, 2t + 1 (columns >= 7 are 0)
-    float xg[kMlpIn], xg8[kMlpIn];
 #pragma unroll
-    for (int f = 0; f < kMlpIn; ++f) {
-        xg[f] = __shfl_sync(0xffffffffu, x[f], g);
-        xg8[f] = __shfl_sync(0xffffffffu, x[f], g + 8);
+    for (int c = 0; c < 4; ++c) {
+        float g[16], sp[16], dz[16];
+        tc::ld16(lane_t + 192 + 16 * c, g);
+        tc::ld16(lane_t + scol + 16 * c, sp);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            dz[e] = g[e] * sp[e];
+            if (dstT) st_bf16(dstT, tc::kmaj_off(128, 16 * c + e, row), dz[e]);
+        }
+        if (dst) {
+            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c), dz);
+            tc::st_row8(dst, tc::kmaj_off(128, row, 16 * c + 8), dz + 8);
+        }
     }
-    auto pick = [&](const float* v, int f) {
-        float r = 0.f;
+}
+
+// Energy and input gradient of 128 rows: x (this thread's row, 7 normalised features;
+// zeros for an unused row) -> y and dy/dx'. All 128 threads of the warpgroup call it.
+// Returns false if an MMA wait gave up.
+__device__ __forceinline__ bool tc_rows128(const TcTile& t, uint32_t& phase, const MlpVec& V, const float* x,
+                                           float& y, float* dydx)
+{
+    const int row = threadIdx.x & 127;
+    const uint32_t lane_t = t.tmem + ((uint32_t)(((threadIdx.x >> 5) & 3) * 32) << 16);
+    bool ok = true;
+    {
+        float xr[16];
 #pragma unroll
-        for (int k = 0; k < kMlpIn; ++k) r = (k == f) ? v[k] : r;
-        return r;
-    };
-    uint32_t A0[1][4];
-    A0[0][0] = pack_bf16(pick(xg, 2 * t), pick(xg, 2 * t + 1));
-    A0[0][1] = pack_bf16(pick(xg8, 2 * t), pick(xg8, 2 * t + 1));
-    A0[0][2] = 0u;
-    A0[0][3] = 0u;
-    float z[8][4], s[8][4];
-    uint32_t sp1[8][2], sp2[8][2];
-    uint32_t A[4][4];
-    mlp_layer<1>(F + kFragF1 * 32, A0, z, lane);
-    bias_silu(z, s, V.b1, lane);
-    pack_frags(s, sp1);
-    c_to_a(z, A);
-    mlp_layer<4>(F + kFragF2 * 32, A, z, lane);
-    bias_silu(z, s, V.b2, lane);
-    pack_frags(s, sp2);
-    c_to_a(z, A);
-    mlp_layer<4>(F + kFragF3 * 32, A, z, lane);
-    bias_silu(z, s, V.b3, lane);
-    // output: y[row] = h3[row] . w4 + b4 (rows g and g + 8; reduce over the 4 lanes of a
-    // group); dy/dz3 = w4 * silu'(z3)
-    float yg = 0.f, yg8 = 0.f;
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-        const float w0 = V.w4[frag_col(nt, 0, lane)], w1 = V.w4[frag_col(nt, 1, lane)];
-        yg += z[nt][0] * w0 + z[nt][1] * w1;
-        yg8 += z[nt][2] * w0 + z[nt][3] * w1;
-        s[nt][0] *= w0;
-        s[nt][1] *= w1;
-        s[nt][2] *= w0;
-        s[nt][3] *= w1;
+        for (int f = 0; f < 16; ++f) xr[f] = f < kMlpIn ? x[f] : 0.f;
+        tc::st_row8(t.x, tc::kmaj_off(128, row, 0), xr);
+        tc::st_row8(t.x, tc::kmaj_off(128, row, 8), xr + 8);
     }
-    yg += __shfl_xor_sync(0xffffffffu, yg, 1);
-    yg += __shfl_xor_sync(0xffffffffu, yg, 2);
-    yg8 += __shfl_xor_sync(0xffffffffu, yg8, 1);
-    yg8 += __shfl_xor_sync(0xffffffffu, yg8, 2);
-    // back through W3, W2 and W1
-    c_to_a(s, A);
-    mlp_layer<4>(F + kFragG3 * 32, A, z, lane);  // dy/dh2
-    mul_packed(z, sp2);                          // dy/dz2
-    c_to_a(z, A);
-    mlp_layer<4>(F + kFragG2 * 32, A, z, lane);  // dy/dh1
-    mul_packed(z, sp1);                          // dy/dz1
-    c_to_a(z, A);
-    // dy/dx' = dz1 * W1 (N = 16: two n-tiles; only n-tile 0, columns 0..6, are inputs)
-    float dx[4] = {0.f, 0.f, 0.f, 0.f};
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 0, t.x, 128, t.w + tc::kImgF1, 64, 64, 1, false);    // D1 = X F1
+    tc_forward_row(lane_t, 0, V.b1, t.p, row);
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 64, t.p, 128, t.w + tc::kImgF2, 64, 64, 4, false);   // D2 = H1 F2
+    tc_forward_row(lane_t, 64, V.b2, t.q, row);
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 128, t.q, 128, t.w + tc::kImgF3, 64, 64, 4, false);  // D3 = H2 F3
+    // output and dy/dz3 = w4 * silu'(z3)
+    float yy = V.b4;
 #pragma unroll
-    for (int kt = 0; kt < 4; ++kt) mma_bf16(dx, A[kt][0], A[kt][1], A[kt][2], A[kt][3], F[(kFragG1 + kt * 2) * 32 + lane]);
-    // gather to the lane owning the row: row r lives in lanes (r & 7) * 4 + t, elements
-    // (0, 1) for r < 8 and (2, 3) for r >= 8; columns 2t, 2t + 1
-    const int r = lane & 15, src0 = (r & 7) * 4;
-    const float ya = __shfl_sync(0xffffffffu, yg, src0), yb = __shfl_sync(0xffffffffu, yg8, src0);
-    y = (r < 8 ? ya : yb) + V.b4;
+    for (int c = 0; c < 4; ++c) {
+        float z[16], dz[16];
+        tc::ld16(lane_t + 128 + 16 * c, z);
 #pragma unroll
-    for (int tt = 0; tt < 4; ++tt) {
-        const float v0 = __shfl_sync(0xffffffffu, dx[0], src0 + tt), v1 = __shfl_sync(0xffffffffu, dx[1], src0 + tt);
-        const float v2 = __shfl_sync(0xffffffffu, dx[2], src0 + tt), v3 = __shfl_sync(0xffffffffu, dx[3], src0 + tt);
-        if (2 * tt < kMlpIn) dydx[2 * tt] = r < 8 ? v0 : v2;
-        if (2 * tt + 1 < kMlpIn) dydx[2 * tt + 1] = r < 8 ? v1 : v3;
+        for (int e = 0; e < 16; ++e) {
+            float h;
+            const float sp = tc::silu_and_grad(z[e] + V.b3[16 * c + e], h);
+            yy += h * V.w4[16 * c + e];
+            dz[e] = sp * V.w4[16 * c + e];
+        }
+        tc::st_row8(t.p, tc::kmaj_off(128, row, 16 * c), dz);
+        tc::st_row8(t.p, tc::kmaj_off(128, row, 16 * c + 8), dz + 8);
     }
+    y = yy;
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 192, t.p, 128, t.w + tc::kImgG3, 64, 64, 4, false);  // dH2 = dZ3 G3
+    tc_backward_row(lane_t, 64, t.q, row);                                       // dZ2
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 192, t.q, 128, t.w + tc::kImgG2, 64, 64, 4, false);  // dH1 = dZ2 G2
+    tc_backward_row(lane_t, 0, t.p, row);                                        // dZ1
+    tc_publish(t);
+    ok &= tc_gemm(t, phase, 0, t.p, 128, t.w + tc::kImgG1, 16, 16, 4, false);    // dX = dZ1 G1
+    float dx[16];
+    tc::ld16(lane_t, dx);
+#pragma unroll
+    for (int f = 0; f < kMlpIn; ++f) dydx[f] = dx[f];
+    tc::fence_before();  // the next tile's MMAs overwrite these columns after a barrier
+    return ok;
+}
+
+// The class's weight image into shared memory (every thread of the block, 16-byte
+// loads), made visible to the tensor cores.
+__device__ __forceinline__ void tc_load_weights(unsigned char* dst, const unsigned char* src)
+{
+    for (int k = threadIdx.x; k < (int)(tc::kImgBytes / 16); k += blockDim.x)
+        reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(src)[k];
+    tc::fence_smem_async();
 }
 
 // Features of a base-base geometry: r, c1, c2, c3, c4, c7, c8.

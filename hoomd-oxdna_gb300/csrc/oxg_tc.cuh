@@ -120,6 +120,31 @@ __device__ __forceinline__ void ld16(uint32_t taddr, float* v)
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// 16 consecutive FP32 columns of this thread's TMEM lane written from registers, waited
+// for in the same statement.
+__device__ __forceinline__ void st16(uint32_t taddr, const float* v)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n\t"
+        "tcgen05.wait::st.sync.aligned;" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+        : "memory");
+}
+
+// SiLU h = z sigmoid(z) and its derivative sigmoid(z) (1 + z (1 - sigmoid(z))), with the
+// sigmoid as 1/2 + tanh(z / 2) / 2: one special-function instruction per value.
+__device__ __forceinline__ float silu_and_grad(float z, float& h)
+{
+    float th;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(th) : "f"(0.5f * z));
+    const float sg = fmaf(0.5f, th, 0.5f);
+    h = z * sg;
+    return sg * fmaf(z, 1.f - sg, 1.f);
+}
+
 __device__ __forceinline__ uint32_t pack2(float lo, float hi)
 {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);

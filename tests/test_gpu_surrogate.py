@@ -79,12 +79,11 @@ def test_inference_matches_oracle(native):
 
 @pytest.fixture(scope="module")
 def trained():
-    """A network trained on pair geometries of a 1600-nt duplex system at 300 and 340 K
-    (the plain evaluator's samples), with a held-out tenth."""
+    """A network trained on 2M pair geometries the plain evaluator samples along
+    8000-nt duplex trajectories at 280-360 K, with a held-out tenth."""
     import torch
     from oxdna import surrogate
-    f, e = surrogate.training_set(n_target=240_000, temperatures=(300, 340), n_dup=40, box=60.0,
-                                  equil=400, every=50, seed=21)
+    f, e = surrogate.training_set(n_target=2_000_000, seed=21)
     g = torch.Generator(device="cuda")
     g.manual_seed(0)
     perm = torch.randperm(f.shape[0], generator=g, device="cuda")
@@ -93,7 +92,8 @@ def trained():
     net = surrogate.Network(seed=0)
     net.fit_normalization(f[train], e[train])
     rms0 = float(torch.sqrt(((net.energies(f[hold]) - e[hold]) ** 2).mean()))
-    hist = net.train(f[train].contiguous(), e[train].contiguous(), epochs=12, batch=2048, lr=3e-3)
+    hist = net.train(f[train].contiguous(), e[train].contiguous(), epochs=15, batch=4096, lr=3e-3,
+                     lr_end=3e-5)
     rms1 = float(torch.sqrt(((net.energies(f[hold]) - e[hold]) ** 2).mean()))
     shifts = net.calibrate(f[train], e[train])
     d = net.energies(f[hold]) - e[hold]
