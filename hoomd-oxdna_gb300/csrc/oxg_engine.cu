@@ -470,6 +470,11 @@ struct oxg_system {
     GridBarrier* bar = nullptr;
     int grid_run = 0;
     bool lists_valid = false;  // pair lists built for the current positions' reference
+    // the force / torque arrays hold the forces of the current state (a persistent run
+    // ended and nothing changed since: no state, parameter, integrator or surrogate
+    // change, no read-out that reused the arrays); the next run start reuses them
+    bool forces_current = false;
+    uint64_t forces_version = 0;  // ctx->version they were computed with
     cudaEvent_t ev_run[2] = {nullptr, nullptr};  // around each run-kernel launch
     double run_kernel_ms = 0.0;
     long long run_kernel_launches = 0, run_kernel_bodies = 0;
@@ -932,6 +937,7 @@ int oxg_system_set_state(oxg_system* s, const float* pos_type, const float* pos_
                          const float* charge)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    s->forces_current = false;  // the next run start evaluates the forces again
     const size_t b4 = sizeof(float4) * s->N;
     if (pos_type) {
         for (int i = 0; i < s->N; ++i) {
@@ -962,6 +968,7 @@ int oxg_system_device_state(oxg_system* s, float** pos_type, float** pos_lo, flo
                             float** vel, float** angmom, float** charge)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    s->forces_current = false;  // the caller may write the state through these pointers
     if (pos_type) *pos_type = reinterpret_cast<float*>(s->pos);
     if (pos_lo) *pos_lo = reinterpret_cast<float*>(s->pos_lo);
     if (quat) *quat = reinterpret_cast<float*>(s->quat);
@@ -988,6 +995,7 @@ int oxg_system_set_timestep(oxg_system* s, uint64_t step)
 
 static int system_compute_impl(oxg_system* s, uint32_t mask, int bonded)
 {
+    s->forces_current = false;  // the read-out reuses the force and torque arrays
     int rc = sys_setup_nlist(s, mask, false);
     if (rc) return rc;
     for (int attempt = 0; attempt < 8; ++attempt) {
@@ -1040,6 +1048,7 @@ int oxg_system_set_integrator(oxg_system* s, double dt, double kT, double gamma,
     s->run_mask = mask;
     s->run_bonded = bonded;
     s->integ_set = true;
+    s->forces_current = false;
     s->graph_key = ~0ull;
     return OXG_OK;
 }
@@ -1137,7 +1146,7 @@ static int copy_state_async(oxg_system* s, float4* const* host, bool to_device)
 
 // The persistent run kernel: one cooperative launch of `bodies` step bodies, preceded
 // by the run start (prepRun) when `prologue` (see k_run).
-static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = false,
+static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
                       unsigned long long step0 = 0, bool rebuild0 = false)
 {
     const int block_bytes = s->ctx->block_bytes;
@@ -1156,7 +1165,7 @@ static int launch_run(oxg_system* s, int bodies, bool closing, bool prologue = f
     ra.bar = s->bar;
     ra.bodies = bodies;
     ra.closing = closing ? 1 : 0;
-    ra.prologue = prologue ? 1 : 0;
+    ra.prologue = prologue;
     ra.rebuild0 = rebuild0 ? 1u : 0u;
     ra.step0 = step0;
     ra.ck[0] = s->ck_pos;
@@ -1190,6 +1199,9 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
         OXG_CUDA(cudaEventCreate(&s->ev_run[0]));
         OXG_CUDA(cudaEventCreate(&s->ev_run[1]));
     }
+    // the run start may reuse the last step's forces only for an unchanged state
+    const bool reuse = s->forces_current && s->forces_version == s->ctx->version && s->lists_valid && !hin;
+    s->forces_current = false;
     if (hin && (rc = copy_state_async(s, const_cast<float4* const*>(hin), true))) return rc;
     while (done < nsteps) {
         const int todo = (int)std::min<long>(chunk, nsteps - done);
@@ -1200,7 +1212,8 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
         const bool first = done == 0;
         if (!first && (rc = checkpoint(s, false))) return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[0], s->stream));
-        if ((rc = launch_run(s, todo, closing, first, step0, !s->lists_valid))) return rc;
+        const int prologue = first ? ((reuse && retries == 0) ? 2 : 1) : 0;
+        if ((rc = launch_run(s, todo, closing, prologue, step0, !s->lists_valid))) return rc;
         if (closing && hout && (rc = copy_state_async(s, hout, false))) return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
         if ((rc = read_status(s, &d))) return rc;
@@ -1232,6 +1245,8 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
         s->lists_valid = true;
     }
     s->timestep = d.step;
+    s->forces_current = true;  // the closing body left the final state's forces
+    s->forces_version = s->ctx->version;
     return OXG_OK;
 }
 
@@ -1284,6 +1299,7 @@ int oxg_system_run(oxg_system* s, long nsteps)
         OXG_CUDA(cudaStreamSynchronize(s->stream));
         return OXG_OK;
     }
+    s->forces_current = false;  // the per-step path keeps no such record
     // the RNG counter continues from the system's timestep
     OXG_CUDA(cudaMemcpyAsync(&s->st->step, &s->timestep, sizeof(unsigned long long),
                              cudaMemcpyHostToDevice, s->stream));
@@ -1418,6 +1434,7 @@ int oxg_system_hbx_samples(oxg_system* s, int max_n, float* feats, float* energy
     if (!s || max_n < 0 || (max_n > 0 && (!feats || !energy)) || !n_out)
         return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
     if (!s->ctx->hbx.any) return set_err(OXG_ERR_NO_PARAMS, "no fused HB + cross-stacking parameters");
+    s->forces_current = false;  // the sampling evaluation reuses the force arrays
     const uint32_t mask = 1u << kHBCross;
     int rc = sys_setup_nlist(s, mask | s->run_mask, false);
     if (rc) return rc;
@@ -1519,6 +1536,7 @@ int oxg_system_set_surrogate(oxg_system* s, const oxg_mlp* mlp, int flags, int a
     s->audit_mod = (uint32_t)audit_mod;
     s->audit_tol = (float)audit_tol;
     s->graph_key = ~0ull;  // the captured steps launch the surrogate kernel or not
+    s->forces_current = false;
     OXG_CUDA(cudaMemsetAsync(s->audit, 0, sizeof(SurrogateAudit), s->stream));
     OXG_CUDA(cudaStreamSynchronize(s->stream));
     return OXG_OK;

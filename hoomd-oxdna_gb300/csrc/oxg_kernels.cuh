@@ -1705,7 +1705,9 @@ struct RunArgs {
     int bodies;   // step bodies in this launch
     int closing;  // the last body is the run's last step (step two only)
     unsigned long long step0;  // the system's timestep at the launch (RNG counter), every launch
-    // run start in the same launch (the first launch of a run() call):
+    // run start in the same launch (the first launch of a run() call): 0 none, 1 full
+    // (list check, forces of the current state), 2 with the forces of the last step (the
+    // state has not changed since a run ended: the force arrays hold its final forces)
     int prologue;
     uint32_t rebuild0;         // the lists are new: rebuild whatever the displacements
     float4* ck[5];             // checkpoint of pos, pos_lo, quat, vel, angmom for a replay
@@ -1761,6 +1763,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     }
     for (int body = a.prologue ? -1 : 0; body < a.bodies; ++body) {
         const bool pro = body < 0;
+        const bool reuse = pro && a.prologue == 2;  // the last step's forces are this state's
         bool rebuild;
         if (pro) {
             if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1781,6 +1784,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 a.ck[2][i] = a.g.quat[i];
                 a.ck[3][i] = a.g.vel[i];
                 a.ck[4][i] = a.g.angmom[i];
+                if (reuse) continue;  // forces kept; the lists are valid for this state
                 a.g.force[i] = zero;
                 a.g.torque[i] = zero;
                 const float4 r = a.g.pos_ref[i];
@@ -1788,8 +1792,8 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 far |= !(dot(d, d) <= a.g.half_buf2);
             }
             if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->moved, 1u);
-            if (!grid_barrier(a.bar)) break;
-            rebuild = a.rebuild0 != 0u || ld_volatile(&st->moved) != 0u;
+            if (!grid_barrier(a.bar)) break;  // the counters above are reset for every block
+            rebuild = !reuse && (a.rebuild0 != 0u || ld_volatile(&st->moved) != 0u);
         } else {
             // rebuild requests: body 0 reads the one left by the run start or the previous
             // launch, body b > 0 the one the step phase of body b - 1 left in rb[b & 1]
@@ -1827,7 +1831,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         const unsigned long long step = step_base + (unsigned long long)(body + 1);
         LangevinNoise nz;
         const bool have_nz = !pro && gthread < a.g.N;
-        {
+        if (!reuse) {
             // phase B on the block's own queues: a block barrier, not a grid barrier
             forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type, ns_known, nl_known, first_pair);
             forces_b_local<false>(a.f, P, eacc, bad_type, bonds_here);

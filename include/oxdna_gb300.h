@@ -242,7 +242,11 @@ int oxg_system_set_state(oxg_system* sys, const float* pos_type, const float* po
                          const float* charge);
 int oxg_system_get_state(oxg_system* sys, float* pos_type, float* pos_lo, float* quat,
                          float* vel, float* angmom);
-/* Device pointers of the resident state (4*N floats each; charge N floats). */
+/* Device pointers of the resident state (4*N floats each; charge N floats). A run
+ * starts from the forces the previous run left for its final state when nothing has
+ * changed since (as HOOMD's prepRun would recompute them); this call counts as a change.
+ * After writing the state through these pointers later on, call oxg_system_set_state
+ * with every array NULL so that the next run evaluates the forces again. */
 int oxg_system_device_state(oxg_system* sys, float** pos_type, float** pos_lo, float** quat,
                             float** vel, float** angmom, float** charge);
 /* Neighbour-list skin (HOOMD Cell nlist buffer, default 0.4). */

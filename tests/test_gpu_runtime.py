@@ -113,3 +113,28 @@ def test_changed_parameters_rebuild_with_state_kept(native):
     L = s["box"][0]
     assert a.timestep == b.timestep == 40
     assert _pos_diff(a.state.get_snapshot(), b.state.get_snapshot(), L) < 2e-3
+
+
+def test_run_start_reuses_the_last_steps_forces(native):
+    """A run that follows another with nothing changed in between starts from the forces
+    the previous run left for its final state instead of evaluating them again (HOOMD's
+    prepRun recomputes the same forces); the trajectory equals one whose run start does
+    evaluate them (the state marked as changed through the C ABI), up to the order of
+    the FP32 force sums."""
+    import ctypes as C
+
+    from oxdna import _abi, io
+    from oxdna.model import dna2
+    s = _system()
+    ends = []
+    for mark_changed in (False, True):
+        sim, _ = _sim(io.system_snapshot(s), dna2.forces()[0])
+        sim.run(15)
+        if mark_changed:
+            _abi.check(native.oxg_system_set_state(sim._sys, None, None, None, None, None, None),
+                       "oxg_system_set_state")
+        sim.run(15)
+        ends.append(sim.state.get_snapshot())
+    L = s["box"][0]
+    assert _pos_diff(ends[0], ends[1], L) < 1e-4
+    assert np.abs(ends[0].particles.velocity - ends[1].particles.velocity).max() < 1e-3
