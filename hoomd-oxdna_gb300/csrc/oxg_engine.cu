@@ -468,7 +468,7 @@ struct oxg_system {
     int grid_forces = 0;
     // persistent run kernel
     GridBarrier* bar = nullptr;
-    int grid_run = 0;
+    int grid_run = 0, grid_run_host = 0;
     bool lists_valid = false;  // pair lists built for the current positions' reference
     // the force / torque arrays hold the forces of the current state (a persistent run
     // ended and nothing changed since: no state, parameter, integrator or surrogate
@@ -1128,32 +1128,18 @@ static int checkpoint(oxg_system* s, bool restore)
     return OXG_OK;
 }
 
-// Host-driven runs: the five state arrays between the device and mapped page-locked host
-// arrays (device aliases) in one kernel on the system's stream.
-static int copy_state_async(oxg_system* s, float4* const* host, bool to_device)
-{
-    StateCopy c;
-    c.N = s->N;
-    float4* const dev[5] = {s->pos, s->pos_lo, s->quat, s->vel, s->angmom};
-    for (int k = 0; k < 5; ++k) {
-        c.src[k] = to_device ? host[k] : dev[k];
-        c.dst[k] = to_device ? dev[k] : host[k];
-    }
-    k_state_copy<<<(s->N + 255) / 256, 256, 0, s->stream>>>(c);
-    OXG_CUDA(cudaGetLastError());
-    return OXG_OK;
-}
-
 // The persistent run kernel: one cooperative launch of `bodies` step bodies, preceded
 // by the run start (prepRun) when `prologue` (see k_run).
 static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
-                      unsigned long long step0 = 0, bool rebuild0 = false)
+                      unsigned long long step0 = 0, bool rebuild0 = false,
+                      const float4* const* hin = nullptr, float4* const* hout = nullptr, bool reuse_ok = false)
 {
     const int block_bytes = s->ctx->block_bytes;
     RunArgs ra;
     ra.f = force_args(s, s->run_mask, s->run_bonded);  // plain evaluators only
-    const void* fn = (const void*)k_run;
-    int& grid = s->grid_run;
+    const bool host_io = hin || hout;
+    const void* fn = host_io ? (const void*)k_run<true> : (const void*)k_run<false>;
+    int& grid = host_io ? s->grid_run_host : s->grid_run;
     if (grid == 0) {
         int per_sm = 0;
         OXG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRunThreads, block_bytes));
@@ -1173,6 +1159,11 @@ static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
     ra.ck[2] = s->ck_quat;
     ra.ck[3] = s->ck_vel;
     ra.ck[4] = s->ck_angmom;
+    for (int k = 0; k < 5; ++k) {
+        ra.hin[k] = hin ? hin[k] : nullptr;
+        ra.hout[k] = hout ? hout[k] : nullptr;
+    }
+    ra.reuse_ok = reuse_ok ? 1 : 0;
     // the barrier word needs no reset between launches: every completed barrier adds
     // exactly 2^31 (it is cleared at allocation and after a launch that gave up)
     void* kargs[] = {&ra};
@@ -1199,10 +1190,10 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
         OXG_CUDA(cudaEventCreate(&s->ev_run[0]));
         OXG_CUDA(cudaEventCreate(&s->ev_run[1]));
     }
-    // the run start may reuse the last step's forces only for an unchanged state
-    const bool reuse = s->forces_current && s->forces_version == s->ctx->version && s->lists_valid && !hin;
+    // the run start may reuse the last step's forces only for an unchanged state (from
+    // host arrays: the kernel compares them with the device state and decides)
+    const bool reuse = s->forces_current && s->forces_version == s->ctx->version && s->lists_valid;
     s->forces_current = false;
-    if (hin && (rc = copy_state_async(s, const_cast<float4* const*>(hin), true))) return rc;
     while (done < nsteps) {
         const int todo = (int)std::min<long>(chunk, nsteps - done);
         const bool closing = done + todo == nsteps;
@@ -1212,9 +1203,13 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
         const bool first = done == 0;
         if (!first && (rc = checkpoint(s, false))) return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[0], s->stream));
-        const int prologue = first ? ((reuse && retries == 0) ? 2 : 1) : 0;
-        if ((rc = launch_run(s, todo, closing, prologue, step0, !s->lists_valid))) return rc;
-        if (closing && hout && (rc = copy_state_async(s, hout, false))) return rc;
+        // the host state goes in with the run start (not on a replay: the checkpoint holds
+        // it) and comes back with the closing body
+        const bool read_host = first && hin && retries == 0;
+        const int prologue = first ? (read_host ? 3 : ((reuse && retries == 0) ? 2 : 1)) : 0;
+        if ((rc = launch_run(s, todo, closing, prologue, step0, !s->lists_valid, read_host ? hin : nullptr,
+                             closing ? hout : nullptr, reuse)))
+            return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
         if ((rc = read_status(s, &d))) return rc;
         float ms = 0.f;

@@ -44,7 +44,7 @@ struct DevStatus {
     uint32_t qcount[8];    // deferred-term queue lengths, kNQ used (k_forces_a -> k_forces_b)
     uint32_t qspill;       // run kernel: a block's shared-memory queue overflowed this step
     uint32_t rb[2];        // run kernel: rebuild requests of the next bodies, by body parity
-    uint32_t pad2;
+    uint32_t changed;      // run start from host state: it differs from the device state
 };
 
 // ------------------------------------------------------------ parameter view
@@ -1707,10 +1707,17 @@ struct RunArgs {
     unsigned long long step0;  // the system's timestep at the launch (RNG counter), every launch
     // run start in the same launch (the first launch of a run() call): 0 none, 1 full
     // (list check, forces of the current state), 2 with the forces of the last step (the
-    // state has not changed since a run ended: the force arrays hold its final forces)
+    // state has not changed since a run ended: the force arrays hold its final forces),
+    // 3 from host state (hin): kind 2 if it equals the device state and reuse_ok, else 1
     int prologue;
     uint32_t rebuild0;         // the lists are new: rebuild whatever the displacements
     float4* ck[5];             // checkpoint of pos, pos_lo, quat, vel, angmom for a replay
+    // host-state runs (the k_run<true> instantiation): mapped page-locked host arrays of
+    // pos, pos_lo, quat, vel, angmom read at the run start (hin) and written by the run's
+    // closing body (hout); null when not used by this launch
+    const float4* hin[5];
+    float4* hout[5];
+    int reuse_ok;              // kind 3: the force arrays hold the device state's forces
 };
 
 
@@ -1731,6 +1738,7 @@ struct RunArgs {
 // of the current state, no step advance | a = F/m and step one of the first step.
 constexpr int kRunThreads = OXG_RUN_THREADS;  // threads per block of the run kernel
 constexpr int kBondStage = 512;               // bonds a block stages in shared memory
+template <bool HOST_IO>
 __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunArgs a)
 {
     const ParamView P = stage_params(a.f.params, a.f.param_bytes);
@@ -1763,7 +1771,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     }
     for (int body = a.prologue ? -1 : 0; body < a.bodies; ++body) {
         const bool pro = body < 0;
-        const bool reuse = pro && a.prologue == 2;  // the last step's forces are this state's
+        bool reuse = pro && a.prologue == 2;  // the last step's forces are this state's
         bool rebuild;
         if (pro) {
             if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1776,23 +1784,55 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             }
             if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
             const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-            bool far = false;
+            const bool from_host = HOST_IO && a.prologue == 3;
+            bool far = false, diff = false;
             for (int i = gthread; i < a.g.N; i += nthreads) {
-                const float4 x = a.g.pos[i];
-                a.ck[0][i] = x;
-                a.ck[1][i] = a.g.pos_lo[i];
-                a.ck[2][i] = a.g.quat[i];
-                a.ck[3][i] = a.g.vel[i];
-                a.ck[4][i] = a.g.angmom[i];
+                float4 v[5];
+                if (from_host) {
+                    // the host's state (mapped memory) into the device arrays; compared
+                    // bit for bit with what they held
+                    float4* const dv[5] = {a.g.pos, a.g.pos_lo, a.g.quat, a.g.vel, a.g.angmom};
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) {
+                        v[k] = a.hin[k][i];
+                        const float4 o = dv[k][i];
+                        diff |= __float_as_uint(v[k].x) != __float_as_uint(o.x) ||
+                                __float_as_uint(v[k].y) != __float_as_uint(o.y) ||
+                                __float_as_uint(v[k].z) != __float_as_uint(o.z) ||
+                                __float_as_uint(v[k].w) != __float_as_uint(o.w);
+                        dv[k][i] = v[k];
+                    }
+                } else {
+                    v[0] = a.g.pos[i];
+                    v[1] = a.g.pos_lo[i];
+                    v[2] = a.g.quat[i];
+                    v[3] = a.g.vel[i];
+                    v[4] = a.g.angmom[i];
+                }
+#pragma unroll
+                for (int k = 0; k < 5; ++k) a.ck[k][i] = v[k];
                 if (reuse) continue;  // forces kept; the lists are valid for this state
-                a.g.force[i] = zero;
-                a.g.torque[i] = zero;
+                if (!from_host) {     // (from host state: zeroed below once it is known to differ)
+                    a.g.force[i] = zero;
+                    a.g.torque[i] = zero;
+                }
                 const float4 r = a.g.pos_ref[i];
-                const float3 d = min_image(mk3(x.x - r.x, x.y - r.y, x.z - r.z), a.g.L, a.g.invL);
+                const float3 d = min_image(mk3(v[0].x - r.x, v[0].y - r.y, v[0].z - r.z), a.g.L, a.g.invL);
                 far |= !(dot(d, d) <= a.g.half_buf2);
             }
             if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->moved, 1u);
+            if (from_host && __syncthreads_or(diff) && threadIdx.x == 0) atomicOr(&st->changed, 1u);
             if (!grid_barrier(a.bar)) break;  // the counters above are reset for every block
+            if (from_host) {
+                reuse = a.reuse_ok != 0 && ld_volatile(&st->changed) == 0u;  // the same in every block
+                if (!reuse) {
+                    for (int i = gthread; i < a.g.N; i += nthreads) {
+                        a.g.force[i] = zero;
+                        a.g.torque[i] = zero;
+                    }
+                    if (!grid_barrier(a.bar)) break;  // zeroed before any block scatters forces
+                }
+            }
             rebuild = !reuse && (a.rebuild0 != 0u || ld_volatile(&st->moved) != 0u);
         } else {
             // rebuild requests: body 0 reads the one left by the run start or the previous
@@ -1856,7 +1896,8 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         const bool last = a.closing && body == a.bodies - 1;
         if (blockIdx.x == 0) {
             if (threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
-            if (pro && threadIdx.x == 32) st->moved = 0u;  // read two barriers ago
+            if (pro && threadIdx.x == 32) st->moved = 0u;    // read two barriers ago
+            if (pro && threadIdx.x == 64) st->changed = 0u;  // read two barriers ago
         }
         bool far = false, bad = false;
         for (int i = gthread; i < a.g.N; i += nthreads) {
@@ -1878,6 +1919,13 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 a.g.angmom[i] = s.p;
                 a.g.accel[i] = ac;
                 a.g.tnet[i] = tn;
+                if (HOST_IO && a.hout[0]) {  // the run's final state to the host (mapped)
+                    a.hout[0][i] = s.x;
+                    a.hout[1][i] = s.xl;
+                    a.hout[2][i] = s.q;
+                    a.hout[3][i] = s.v;
+                    a.hout[4][i] = s.p;
+                }
             } else {
                 bool f1 = false, b1 = false;
                 particle_step_one(a.g, i, s, ac, tn, f1, b1);

@@ -207,8 +207,11 @@ def test_state_push_pull_pinned_and_pageable(native):
 def test_run_state_arrays_matches_push_run_pull(native, memory):
     """oxg_system_run_host (one call: state in, n steps, state out) against
     push_state_arrays + run + pull_state_arrays on a twin system (same seed and
-    timestep): with page-locked arrays copy kernels on either side of the run launch
-    move the state, with pageable arrays the call falls back to the three steps."""
+    timestep): with page-locked arrays the run kernel itself reads the host state at the
+    run start (reusing the last step's forces when it equals the device state, as in
+    the second and fourth calls here) and writes the final state back; with pageable
+    arrays the call falls back to the three steps. The first and third calls bring a
+    host-side change of the velocities."""
     import torch
     from oxdna import io
     from oxdna.model import dna1, dna2
@@ -229,7 +232,10 @@ def test_run_state_arrays_matches_push_run_pull(native, memory):
     rng = np.random.Generator(np.random.PCG64(2))
     st_a[3][:, :3] += rng.normal(0, 0.05, (n, 3)).astype(np.float32)  # a host-side change
     st_b = [x.copy() for x in st_a]
-    for _ in range(3):
+    for it in range(4):
+        if it == 2:  # another host-side change between calls
+            st_a[3][:, :3] *= np.float32(0.9)
+            st_b[3][:, :3] *= np.float32(0.9)
         a.run_state_arrays(4, *st_a)
         b.push_state_arrays(*st_b)
         b.run(4)
