@@ -753,7 +753,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--quick", action="store_true",
                     help="resident timing only (no fused / e2e / CPU legs); for profiling runs")
-    ap.add_argument("--leg", choices=["batched", "rna", "surrogate", "nt100k", "tiled"],
+    ap.add_argument("--leg", choices=["batched", "rna", "surrogate", "nt100k", "tiled", "dropin"],
                     help="run one extension leg alone and print its numbers (profiling runs)")
     ap.add_argument("--hairpin-fraction", type=float, default=0.0,
                     help="--leg batched: fraction of the replicas that are hairpins")
@@ -777,6 +777,8 @@ def run_leg(args):
         out = bench_rna(stream, steps=args.steps, warmup=args.warmup)
     elif args.leg == "tiled":
         out = bench_tiled(stream, steps=args.steps, warmup=args.warmup)
+    elif args.leg == "dropin":
+        out = bench_dropin(stream, build_system(), calls=args.steps)
     elif args.leg == "nt100k":
         big = build_system(n_dup=2500, n_bp=20, box=230.0, seed=5)
         sim, _ = make_sim(big, fused=False, stream=stream.cuda_stream)

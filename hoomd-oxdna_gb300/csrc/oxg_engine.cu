@@ -358,6 +358,7 @@ int oxg_pair_forces(oxg_context* c, uint32_t mask, int N, const double* pos_type
     a.nlist = nlist;
     a.head_list = reinterpret_cast<const unsigned long long*>(head_list);
     a.L = make_double3(box[0], box[1], box[2]);
+    a.invL = make_float3(1.f / box[0], 1.f / box[1], 1.f / box[2]);
     a.force = reinterpret_cast<float4*>(force);
     a.torque = reinterpret_cast<float4*>(torque);
     a.virial = virial;
@@ -394,6 +395,7 @@ int oxg_bonded_forces(oxg_context* c, int N, const double* pos_type, const doubl
     a.quat = reinterpret_cast<const double4_32a*>(quat);
     a.bonds = bonds;
     a.L = make_double3(box[0], box[1], box[2]);
+    a.invL = make_float3(1.f / box[0], 1.f / box[1], 1.f / box[2]);
     a.force = reinterpret_cast<float4*>(force);
     a.torque = reinterpret_cast<float4*>(torque);
     a.virial = virial;

@@ -885,6 +885,17 @@ __global__ void __launch_bounds__(kSurrThreads) k_surrogate(ForceArgs a)
 }
 
 // --------------------------------------------------- drop-in: HOOMD full nlist
+// Minimum image of a difference of HOOMD's FP64 positions: the image count from an FP32
+// estimate (an integer; either choice at exactly half a box is a valid image), the shift
+// applied in FP64 by one fused multiply-add, so the FP32 result is the rounded exact
+// difference. FP64 division, which costs tens of FP64 operations on this GPU's reduced
+// FP64 pipe, is avoided.
+__device__ __forceinline__ float min_image_d(double d, double L, float invL)
+{
+    const float n = rintf((float)d * invL);
+    return (float)fma(-(double)n, L, d);
+}
+
 struct HoomdPairArgs {
     const unsigned char* params;
     int param_bytes;
@@ -897,6 +908,7 @@ struct HoomdPairArgs {
     const uint32_t* nlist;
     const unsigned long long* head_list;
     double3 L;
+    float3 invL;
     float4* force;
     float4* torque;
     float* virial;  // 6 * N, component-major pitch N (may be null)
@@ -931,11 +943,8 @@ __global__ void __launch_bounds__(256) k_pairs_hoomd(HoomdPairArgs a)
             continue;
         }
         const double4_32a pj = a.pos[j];
-        double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-        dx -= a.L.x * rint(dx / a.L.x);
-        dy -= a.L.y * rint(dy / a.L.y);
-        dz -= a.L.z * rint(dz / a.L.z);
-        const float3 dr = mk3((float)dx, (float)dy, (float)dz);
+        const float3 dr = mk3(min_image_d(pi.x - pj.x, a.L.x, a.invL.x), min_image_d(pi.y - pj.y, a.L.y, a.invL.y),
+                              min_image_d(pi.z - pj.z, a.L.z, a.invL.z));
         const float rsq = dot(dr, dr);
         const double4_32a qjd = a.quat[j];
         const float4 qj = make_float4((float)qjd.x, (float)qjd.y, (float)qjd.z, (float)qjd.w);
@@ -1011,6 +1020,7 @@ struct BondDropinArgs {
     const double4_32a* quat;
     const int* bonds;  // 3 per bond
     double3 L;
+    float3 invL;
     float4* force;
     float4* torque;
     float* virial;
@@ -1038,10 +1048,9 @@ __global__ void __launch_bounds__(256) k_bonds_dropin(BondDropinArgs a)
             bad = (unsigned)tA >= (unsigned)P.h().n_types || (unsigned)tB >= (unsigned)P.h().n_types;
         }
         if (!bad) {
-            double dx = pB.x - pA.x, dy = pB.y - pA.y, dz = pB.z - pA.z;
-            dx -= a.L.x * rint(dx / a.L.x);
-            dy -= a.L.y * rint(dy / a.L.y);
-            dz -= a.L.z * rint(dz / a.L.z);
+            const double dx = min_image_d(pB.x - pA.x, a.L.x, a.invL.x);
+            const double dy = min_image_d(pB.y - pA.y, a.L.y, a.invL.y);
+            const double dz = min_image_d(pB.z - pA.z, a.L.z, a.invL.z);
             BondAcc acc;
             bonded_pair(P.bonded(bt), make_double3(dx, dy, dz), a.quat[A], a.quat[B], tA, tB, acc);
             const float eh = (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2]));
@@ -1722,6 +1731,14 @@ struct RunArgs {
 
 
 
+// L2 prefetch of `bytes` from p, one 128-byte line per thread in turn (fire and forget).
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes, int tid, int nthreads)
+{
+    const char* c = static_cast<const char*>(p);
+    for (size_t off = (size_t)tid * 128; off < bytes; off += (size_t)nthreads * 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(c + off));
+}
+
 #ifndef OXG_DEVICE_FUNCTIONS_ONLY
 // Each body: [neighbour-list rebuild if flagged: bin | pairs] | forces: each block's
 // phase A, then (a block barrier) its phase B on the pairs it queued and its slice of
@@ -1786,6 +1803,16 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
             const bool from_host = HOST_IO && a.prologue == 3;
             bool far = false, diff = false;
+            {
+                // the first body's reads into L2 while the run start works (after an idle
+                // period L2 may hold none of them): pair lists, bonds, charges
+                const size_t ns = min(ld_volatile(&st->n_short), (uint32_t)a.f.cap_short);
+                const size_t nl = min(ld_volatile(&st->n_long), (uint32_t)a.f.cap_long);
+                prefetch_l2(a.f.pairs_short, ns * sizeof(int2), gthread, nthreads);
+                prefetch_l2(a.f.pairs_long, nl * sizeof(int2), gthread, nthreads);
+                if (a.f.bonded) prefetch_l2(a.f.bonds, (size_t)a.f.n_bonds * sizeof(int4), gthread, nthreads);
+                if (a.f.charge) prefetch_l2(a.f.charge, (size_t)a.g.N * sizeof(float), gthread, nthreads);
+            }
             for (int i = gthread; i < a.g.N; i += nthreads) {
                 float4 v[5];
                 if (from_host) {
