@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -1089,7 +1090,18 @@ int oxg_batch_tune(oxg_batch* b, int trial_steps, int* tile_out, int* threads_ou
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int cap : {64, 128, 192, 256, 384, 512}) {
+    // fixed capacities, plus the ones that pack the particles into whole waves of one
+    // tile per SM (1, 2 or 3 waves; 4% slack for the packing), rounded up to 16
+    std::vector<int> caps = {64, 128, 192, 256, 384, 512};
+    const int sms = internal_num_sms();
+    for (int w = 1; w <= 3; ++w) {
+        const double per = 1.04 * (double)b->N / (double)(w * sms);
+        const int cap = ((int)std::ceil(per / 16.0)) * 16;
+        if (cap >= max_n && cap <= kBatchMaxTile) caps.push_back(cap);
+    }
+    std::sort(caps.begin(), caps.end());
+    caps.erase(std::unique(caps.begin(), caps.end()), caps.end());
+    for (int cap : caps) {
         if (cap < max_n) continue;
         for (int th : {64, 128, 256}) {
             if (th > 2 * cap) continue;

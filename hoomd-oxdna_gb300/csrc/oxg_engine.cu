@@ -111,6 +111,8 @@ struct oxg_context {
     uint32_t* d_status = nullptr;
     cudaStream_t last_stream = nullptr;
     int first_error = OXG_OK;
+    float4* conv = nullptr;  // oxg_pair_forces: FP32 copies of HOOMD's arrays (3 x conv_cap)
+    int conv_cap = 0;
 };
 
 namespace {
@@ -294,6 +296,7 @@ int oxg_destroy(oxg_context* c)
     if (!c) return OXG_OK;
     dfree(c->d_block);
     dfree(c->d_status);
+    dfree(c->conv);
     delete c;
     return OXG_OK;
 }
@@ -346,25 +349,42 @@ int oxg_pair_forces(oxg_context* c, uint32_t mask, int N, const double* pos_type
     if (!(box[0] > 0.f && box[1] > 0.f && box[2] > 0.f)) return set_err(OXG_ERR_INVALID_ARG, "bad box");
     int rc = build_block(c);
     if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (N > c->conv_cap) {  // grows with the largest N seen (HOOMD's N is fixed per run)
+        if (c->conv) {
+            OXG_CUDA(cudaStreamSynchronize(s));
+            dfree(c->conv);
+        }
+        if ((rc = dalloc(&c->conv, (size_t)3 * N))) return rc;
+        c->conv_cap = N;
+    }
+    HoomdConvertArgs cv;
+    cv.N = N;
+    cv.pos = reinterpret_cast<const double4_32a*>(pos_type);
+    cv.quat = reinterpret_cast<const double4_32a*>(quat);
+    cv.charge = charge;
+    cv.hi = c->conv;
+    cv.lo = c->conv + c->conv_cap;
+    cv.q = c->conv + 2 * (size_t)c->conv_cap;
+    k_hoomd_convert<<<(N + 255) / 256, 256, 0, s>>>(cv);
     HoomdPairArgs a;
     a.params = c->d_block;
     a.param_bytes = c->block_bytes;
     a.mask = mask;
     a.N = N;
-    a.pos = reinterpret_cast<const double4_32a*>(pos_type);
-    a.quat = reinterpret_cast<const double4_32a*>(quat);
-    a.charge = charge;
+    a.hi = cv.hi;
+    a.lo = cv.lo;
+    a.q = cv.q;
     a.n_neigh = n_neigh;
     a.nlist = nlist;
     a.head_list = reinterpret_cast<const unsigned long long*>(head_list);
-    a.L = make_double3(box[0], box[1], box[2]);
+    a.Lf = make_float3(box[0], box[1], box[2]);
     a.invL = make_float3(1.f / box[0], 1.f / box[1], 1.f / box[2]);
     a.force = reinterpret_cast<float4*>(force);
     a.torque = reinterpret_cast<float4*>(torque);
     a.virial = virial;
     a.energy = term_energy;
     a.status = c->d_status;
-    cudaStream_t s = (cudaStream_t)stream;
     const int threads = 256;
     const int blocks = (int)(((long long)N * 32 + threads - 1) / threads);
     if (term_energy) k_pairs_hoomd<true><<<blocks, threads, c->block_bytes, s>>>(a);
@@ -402,7 +422,7 @@ int oxg_bonded_forces(oxg_context* c, int N, const double* pos_type, const doubl
     a.energy = split_energy;
     a.status = c->d_status;
     cudaStream_t s = (cudaStream_t)stream;
-    const int threads = 256;
+    const int threads = 64;  // a thread per bond: small blocks spread a few thousand bonds over every SM
     k_bonds_dropin<<<(n_bonds + threads - 1) / threads, threads, c->block_bytes, s>>>(a);
     OXG_CUDA(cudaGetLastError());
     c->last_stream = s;
@@ -452,6 +472,7 @@ struct oxg_system {
     uint64_t nlist_version = ~0ull;
     DevStatus* st = nullptr;
     DevStatus* st_host = nullptr;  // pinned
+    DevStatus* st_mirror = nullptr;  // its device alias (the run kernel writes the status there)
     double* energy = nullptr;      // 9 doubles
     // integrator
     double dt = 0.003, kT = 0.1, gamma = 1.0, gamma_r = 1.0;
@@ -478,6 +499,10 @@ struct oxg_system {
     bool forces_current = false;
     uint64_t forces_version = 0;  // ctx->version they were computed with
     cudaEvent_t ev_run[2] = {nullptr, nullptr};  // around each run-kernel launch
+    // the surrogate's tile kernel runs beside forces B on a second stream (fork / join
+    // by events, captured as graph edges)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double run_kernel_ms = 0.0;
     long long run_kernel_launches = 0, run_kernel_bodies = 0;
     bool persistent = true;
@@ -671,6 +696,12 @@ int forces_grid(oxg_system* s)
         cudaFuncSetAttribute(k_surrogate<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         cudaFuncSetAttribute(k_surrogate<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     }
+    if (!s->side) {  // outside any stream capture, like the attributes above
+        if (cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming) != cudaSuccess)
+            s->side = nullptr;
+    }
     return s->grid_forces;
 }
 
@@ -692,15 +723,21 @@ int launch_nlist_forces(oxg_system* s, uint32_t mask, int bonded, bool energy, b
     // the surrogate's tiles on the tensor cores between the phases (two blocks per SM)
     const uint32_t surr_smem = surrogate_smem(s->ctx->block_bytes);
     const int surr_grid = 2 * num_sms();
-    if (energy) {
-        k_forces_a<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-        if (surr) k_surrogate<true><<<surr_grid, kSurrThreads, surr_smem, s->stream>>>(fa);
-        k_forces_b<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-    } else {
-        k_forces_a<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
-        if (surr) k_surrogate<false><<<surr_grid, kSurrThreads, surr_smem, s->stream>>>(fa);
-        k_forces_b<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    if (energy) k_forces_a<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    else k_forces_a<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    if (surr) {
+        // forces B and the surrogate tiles touch different queues and add into the
+        // accumulators with atomics: they run side by side
+        if (!s->side) return set_err(OXG_ERR_CUDA, "could not create the side stream");  // made by forces_grid
+        OXG_CUDA(cudaEventRecord(s->ev_fork, s->stream));
+        OXG_CUDA(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+        if (energy) k_surrogate<true><<<surr_grid, kSurrThreads, surr_smem, s->side>>>(fa);
+        else k_surrogate<false><<<surr_grid, kSurrThreads, surr_smem, s->side>>>(fa);
+        OXG_CUDA(cudaEventRecord(s->ev_join, s->side));
     }
+    if (energy) k_forces_b<true><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    else k_forces_b<false><<<grid, 256, s->ctx->block_bytes, s->stream>>>(fa);
+    if (surr) OXG_CUDA(cudaStreamWaitEvent(s->stream, s->ev_join, 0));
     OXG_CUDA(cudaGetLastError());
     return OXG_OK;
 }
@@ -801,7 +838,12 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
     if (const char* m = std::getenv("OXG_RUN_MODE")) s->persistent = std::string(m) != "graph";
     // test hook: a smaller per-block queue in phase A exercises the spill path
     if (const char* m = std::getenv("OXG_BLOCK_QUEUE")) s->block_q = std::max(0, std::min(kBlockQ, std::atoi(m)));
-    if (cudaMallocHost((void**)&s->st_host, sizeof(DevStatus)) != cudaSuccess)
+    if (cudaMallocHost((void**)&s->st_host, sizeof(DevStatus)) == cudaSuccess &&
+        cudaHostGetDevicePointer((void**)&s->st_mirror, s->st_host, 0) != cudaSuccess) {
+        cudaGetLastError();
+        s->st_mirror = nullptr;
+    }
+    if (!s->st_host)
         return fail(set_err(OXG_ERR_CUDA, "cudaMallocHost failed"));
     cudaMemcpy(s->bonds, bnd.data(), sizeof(int4) * bnd.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(s->excl, excl.data(), sizeof(int4) * N, cudaMemcpyHostToDevice);
@@ -840,6 +882,9 @@ int oxg_system_destroy(oxg_system* s)
     dfree(s->audit);
     for (int k = 0; k < 2; ++k)
         if (s->ev_run[k]) cudaEventDestroy(s->ev_run[k]);
+    if (s->side) cudaStreamDestroy(s->side);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
     if (s->st_host) cudaFreeHost(s->st_host);
     delete s;
     return OXG_OK;
@@ -1166,6 +1211,7 @@ static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
         ra.hout[k] = hout ? hout[k] : nullptr;
     }
     ra.reuse_ok = reuse_ok ? 1 : 0;
+    ra.st_mirror = s->st_mirror;
     // the barrier word needs no reset between launches: every completed barrier adds
     // exactly 2^31 (it is cleared at allocation and after a launch that gave up)
     void* kargs[] = {&ra};
@@ -1213,7 +1259,12 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
                              closing ? hout : nullptr, reuse)))
             return rc;
         OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
-        if ((rc = read_status(s, &d))) return rc;
+        if (s->st_mirror) {  // the launch's last block wrote the status to host memory
+            OXG_CUDA(cudaStreamSynchronize(s->stream));
+            d = *s->st_host;  // read after the synchronisation (an opaque call)
+        } else if ((rc = read_status(s, &d))) {
+            return rc;
+        }
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, s->ev_run[0], s->ev_run[1]) == cudaSuccess) {
             s->run_kernel_ms += ms;
@@ -1225,6 +1276,10 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
             return set_err(OXG_ERR_TIMEOUT, "a grid barrier wait of the run kernel gave up");
         }
         if (d.flags & kStNonFinite) return set_err(OXG_ERR_NONFINITE, "non-finite positions or orientations");
+        if (d.flags & kStBadIndex) {
+            clear_flags(s);
+            return set_err(OXG_ERR_BAD_INDEX, "a particle type is outside the context's types");
+        }
         if (d.flags & (kStCellOverflow | kStPairOverflow)) {
             if (++retries > 8) return set_err(OXG_ERR_NLIST_OVERFLOW, "neighbour list kept overflowing");
             bool grew = false;
@@ -1482,17 +1537,10 @@ int oxg_system_run_host(oxg_system* s, long nsteps, float* pos_type, float* pos_
     if (!s || nsteps < 1 || !pos_type || !pos_lo || !quat || !vel || !angmom)
         return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
     if (!s->integ_set) return set_err(OXG_ERR_INVALID_ARG, "integrator not set");
-    for (int i = 0; i < s->N; ++i) {
-        int t;
-        std::memcpy(&t, pos_type + 4 * (size_t)i + 3, sizeof(int));
-        if (t < 0 || t >= s->ctx->n_types)
-            return set_err(OXG_ERR_BAD_INDEX, "particle " + std::to_string(i) + " has type " +
-                                                  std::to_string(t) + " outside the context's types");
-    }
     const float* const host[5] = {pos_type, pos_lo, quat, vel, angmom};
     float4* dev[5];
     int rc;
-    if (!s->persistent || !mapped_state(host, dev)) {  // per-call transfers
+    if (!s->persistent || !mapped_state(host, dev)) {  // per-call transfers (types checked there)
         if ((rc = oxg_system_set_state(s, pos_type, pos_lo, quat, vel, angmom, nullptr))) return rc;
         if ((rc = oxg_system_run(s, nsteps))) return rc;
         return oxg_system_get_state(s, pos_type, pos_lo, quat, vel, angmom);

@@ -896,19 +896,48 @@ __device__ __forceinline__ float min_image_d(double d, double L, float invL)
     return (float)fma(-(double)n, L, d);
 }
 
+// HOOMD's FP64 particle arrays converted once per call (a thread per particle), so the
+// pair loop reads FP32 only: hi = (x, y, z high parts, type bits), lo = (x, y, z low
+// parts, charge), q = the quaternion. Positions are double-float (hi + lo = the FP64
+// value to ~1e-14 relative), differences taken with image_delta as in the engine.
+struct HoomdConvertArgs {
+    int N;
+    const double4_32a* pos;
+    const double4_32a* quat;
+    const double* charge;  // may be null: unit charges
+    float4* hi;
+    float4* lo;
+    float4* q;
+};
+
+#ifndef OXG_DEVICE_FUNCTIONS_ONLY
+__global__ void k_hoomd_convert(HoomdConvertArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.N) return;
+    const double4_32a p = a.pos[i];
+    const double4_32a qd = a.quat[i];
+    const float hx = (float)p.x, hy = (float)p.y, hz = (float)p.z;
+    const int t = (int)(__double_as_longlong(p.w) & 0xffffffffLL);
+    a.hi[i] = make_float4(hx, hy, hz, __int_as_float(t));
+    a.lo[i] = make_float4((float)(p.x - (double)hx), (float)(p.y - (double)hy), (float)(p.z - (double)hz),
+                          a.charge ? (float)a.charge[i] : 1.f);
+    a.q[i] = make_float4((float)qd.x, (float)qd.y, (float)qd.z, (float)qd.w);
+}
+#endif
+
 struct HoomdPairArgs {
     const unsigned char* params;
     int param_bytes;
     uint32_t mask;
     int N;
-    const double4_32a* pos;
-    const double4_32a* quat;
-    const double* charge;
+    const float4* hi;  // k_hoomd_convert's arrays
+    const float4* lo;
+    const float4* q;
     const uint32_t* n_neigh;
     const uint32_t* nlist;
     const unsigned long long* head_list;
-    double3 L;
-    float3 invL;
+    float3 Lf, invL;
     float4* force;
     float4* torque;
     float* virial;  // 6 * N, component-major pitch N (may be null)
@@ -923,12 +952,11 @@ __global__ void __launch_bounds__(256) k_pairs_hoomd(HoomdPairArgs a)
     const int lane = threadIdx.x & 31;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= a.N) return;  // whole warp exits together
-    const double4_32a pi = a.pos[i];
-    const double4_32a qid = a.quat[i];
-    const float4 qi = make_float4((float)qid.x, (float)qid.y, (float)qid.z, (float)qid.w);
-    const int ti = (int)(__double_as_longlong(pi.w) & 0xffffffffLL);
+    const float4 hi_i = a.hi[i], lo_i = a.lo[i];
+    const float4 qi = a.q[i];
+    const int ti = __float_as_int(hi_i.w);
     const int n_types = P.h().n_types;
-    const float ci = a.charge ? (float)a.charge[i] : 1.f;
+    const float ci = lo_i.w;
     const int nn = (int)a.n_neigh[i];
     const unsigned long long head = a.head_list[i];
     float3 f = mk3(0.f, 0.f, 0.f), tq = mk3(0.f, 0.f, 0.f);
@@ -942,18 +970,16 @@ __global__ void __launch_bounds__(256) k_pairs_hoomd(HoomdPairArgs a)
             bad = true;
             continue;
         }
-        const double4_32a pj = a.pos[j];
-        const float3 dr = mk3(min_image_d(pi.x - pj.x, a.L.x, a.invL.x), min_image_d(pi.y - pj.y, a.L.y, a.invL.y),
-                              min_image_d(pi.z - pj.z, a.L.z, a.invL.z));
+        const float4 hi_j = a.hi[j], lo_j = a.lo[j];
+        const float3 dr = image_delta(hi_i, lo_i, hi_j, lo_j, a.Lf, a.invL);
         const float rsq = dot(dr, dr);
-        const double4_32a qjd = a.quat[j];
-        const float4 qj = make_float4((float)qjd.x, (float)qjd.y, (float)qjd.z, (float)qjd.w);
-        const int tj = (int)(__double_as_longlong(pj.w) & 0xffffffffLL);
+        const float4 qj = a.q[j];
+        const int tj = __float_as_int(hi_j.w);
         if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
             bad = true;
             continue;
         }
-        const float cj = a.charge ? (float)a.charge[j] : 1.f;
+        const float cj = lo_j.w;
         PairAcc acc;
         acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
         float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1642,7 +1668,8 @@ __global__ void k_prep_accel(IntegArgs a)
 struct GridBarrier {
     uint32_t arrive;  // bit 31 flips each time every block has arrived
     uint32_t abort;   // set by a block whose wait gave up: the others leave too
-    uint32_t pad[30]; // a line of its own
+    uint32_t exits;   // blocks that have left the launch (the last one resets it)
+    uint32_t pad[29]; // a line of its own
 };
 
 constexpr long long kBarrierSpinLimit = 1LL << 22;  // polls of an L2 round trip: ~1 s on a GB300 (0.23 us a poll)
@@ -1727,6 +1754,8 @@ struct RunArgs {
     const float4* hin[5];
     float4* hout[5];
     int reuse_ok;              // kind 3: the force arrays hold the device state's forces
+    DevStatus* st_mirror;      // host-mapped copy of the status written by the last block
+                               // to leave (null: the host copies the status itself)
 };
 
 
@@ -1822,6 +1851,8 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
 #pragma unroll
                     for (int k = 0; k < 5; ++k) {
                         v[k] = a.hin[k][i];
+                        if (k == 0 && (unsigned)__float_as_int(v[0].w) >= (unsigned)P.h().n_types)
+                            bad_type = true;  // reported after the run (the kernels skip the particle)
                         const float4 o = dv[k][i];
                         diff |= __float_as_uint(v[k].x) != __float_as_uint(o.x) ||
                                 __float_as_uint(v[k].y) != __float_as_uint(o.y) ||
@@ -1974,6 +2005,19 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     }
     if (__syncthreads_or(bad_type) && threadIdx.x == 0) atomicOr(&st->flags, kStBadIndex);
     if (threadIdx.x == 0 && ld_volatile(&a.bar->abort)) atomicOr(&st->flags, kStBarrierTimeout);
+    // the last block to leave mirrors the final status into host memory, so the host
+    // reads it after the launch without a copy of its own
+    if (a.st_mirror && threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&a.bar->exits, 1u) == gridDim.x - 1u) {
+            __threadfence();
+            const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(st);
+            volatile uint32_t* dst = reinterpret_cast<volatile uint32_t*>(a.st_mirror);
+            for (int k = 0; k < (int)(sizeof(DevStatus) / sizeof(uint32_t)); ++k) dst[k] = src[k];
+            __threadfence_system();
+            a.bar->exits = 0u;
+        }
+    }
 }
 #endif
 

@@ -198,6 +198,10 @@ int oxg_set_bonded_params(oxg_context* ctx, int bond_type, const oxg_bonded_para
  * neighbours, warp-shuffle reductions, no atomics on force/torque.
  * term_energy (device, OXG_N_PAIR_TERMS doubles, may be NULL) receives the per-term
  * FP64 totals (ADDED). virial may be NULL. box = orthorhombic edge lengths.
+ * HOOMD's FP64 positions, orientations and charges are first converted, a thread per
+ * particle, into FP32 copies (positions as high + low parts, so differences keep FP64
+ * accuracy) in a device buffer the context owns: allocated on the first call and grown
+ * to the largest N seen (that growth synchronises `stream`).
  * The call is asynchronous on `stream`. A neighbour index outside [0, N) is skipped
  * and recorded; oxg_context_status() reports it (OXG_ERR_BAD_INDEX). */
 int oxg_pair_forces(oxg_context* ctx, uint32_t term_mask, int N,
@@ -267,19 +271,26 @@ int oxg_system_compute(oxg_system* sys, uint32_t term_mask, int bonded,
 int oxg_system_set_integrator(oxg_system* sys, double dt, double kT, double gamma,
                               double gamma_r, uint64_t seed, uint32_t term_mask,
                               int bonded);
-/* Advance nsteps steps (HOOMD run(): forces of the current state first, as prepRun).
- * By default one cooperative launch of the persistent run kernel per 2000 steps, one
- * synchronisation per launch; with OXG_RUN_MODE=graph in the environment at system
- * creation, per-step kernels replayed from captured CUDA graphs. On a neighbour-list
- * overflow the lists grow and the launch is replayed from its checkpoint. */
+/* Advance nsteps steps (HOOMD run(): forces of the current state first, as prepRun; a
+ * run that follows another run with nothing changed in between starts from the forces
+ * that run left for the same state instead of evaluating them again). By default one
+ * cooperative launch of the persistent run kernel per 2000 steps, one synchronisation
+ * per launch; with OXG_RUN_MODE=graph in the environment at system creation, or while
+ * a surrogate replaces the fused HB + cross-stacking term in MD steps, per-step kernels
+ * replayed from captured CUDA graphs. On a neighbour-list overflow the lists grow and
+ * the launch is replayed from its checkpoint. */
 int oxg_system_run(oxg_system* sys, long nsteps);
 /* One call for host-driven loops: load the state from the host arrays (pos_type,
  * pos_lo, quat, vel, angmom: float[4*N] each, as oxg_system_set_state), run nsteps >= 1
  * steps, and write the final state back into the same arrays. With page-locked, mapped
- * host arrays (cudaHostAlloc, torch pin_memory) on the persistent run kernel, one copy
- * kernel on each side of the run launch reads and writes the host arrays directly (one
- * synchronisation per call); otherwise set_state, run and get_state. No counterpart in
- * the reference (HOOMD keeps the state on the device between calls). */
+ * host arrays (cudaHostAlloc, torch pin_memory) on the persistent run kernel, the run
+ * kernel itself reads the host arrays at its start (comparing them with the device
+ * state: when they are equal and the last run left that state's forces, those are
+ * reused) and its closing step writes the final state back: one launch and one
+ * synchronisation per call. A particle type outside the context's types is then
+ * reported after the run (OXG_ERR_BAD_INDEX; the kernels skip the particle). Otherwise
+ * set_state, run and get_state. No counterpart in the reference (HOOMD keeps the state
+ * on the device between calls). */
 int oxg_system_run_host(oxg_system* sys, long nsteps, float* pos_type, float* pos_lo, float* quat,
                         float* vel, float* angmom);
 /* Per-term energies at the current state (device reduction, FP64) into host arrays. */

@@ -252,6 +252,12 @@ def test_run_state_arrays_matches_push_run_pull(native, memory):
     b.pull_state_arrays(*pb)
     for x, y in zip(pa, pb):
         assert np.allclose(x, y, rtol=1e-5, atol=1e-5)
+    # a particle type outside the context's types is an error (found by the run kernel
+    # on page-locked arrays, before any GPU work on pageable ones)
+    from oxdna import _abi
+    st_a[0][7, 3] = np.array([99], np.int32).view(np.float32)[0]
+    with pytest.raises(_abi.OxgError, match="status 4"):
+        a.run_state_arrays(1, *st_a)
 
 
 @pytest.mark.parametrize("fused", [False, True])
