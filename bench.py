@@ -534,6 +534,42 @@ def cpu_baseline(sysarr, seconds=12.0, max_steps=400, threads=None):
                       f"{threads} threads, run() call per {chunk} steps)"}
 
 
+def cpu_arithmetic(sysarr, reps=3):
+    """Forces of the 8000-nt workload on one host core: the C restatement (its own cell
+    list included) beside the reference's own evaluator and bonded headers compiled
+    unchanged (oracle/_ref, HOOMD CPU driver semantics over a prebuilt half list) where
+    that build exists (the reference source tree is needed to compile it)."""
+    from oracle import oracle as O
+    from oxdna import io
+    from oxdna.model import dna2
+    forces, _ = dna2.forces(fused=False)
+    model = O.Model(forces, io.DNA_BASES)
+    s = O.System(sysarr["pos"], sysarr["quat"], sysarr["typeid"], sysarr["box"], sysarr["bonds"])
+    out = {"workload": "forces of the 8000-nt workload (every term, bonds), FP64, one host core"}
+    O.forces(model, s)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.forces(model, s)
+    out["port_ms"] = (time.perf_counter() - t0) / reps * 1e3
+    if O.ref_lib(64) is not None:
+        pair = forces[1:]
+        rl = max(f.rcut_for(a, b) for f in pair for a in io.DNA_BASES for b in io.DNA_BASES)
+        pairs = O.half_pairs(s, rl * (1 + 1e-9))
+        O.ref_system_forces(model, s, pairs)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            O.ref_system_forces(model, s, pairs)
+        out["reference_headers_ms"] = (time.perf_counter() - t0) / reps * 1e3
+        out["reference_headers_over_port"] = out["reference_headers_ms"] / out["port_ms"]
+        out["note"] = ("reference_headers: src/EvaluatorPairOxDNA*.h and src/OxDNABondedKernel.h "
+                       "compiled unchanged at -O3 (g++), pair list prebuilt; port: "
+                       "oracle/oxdna_oracle.c at -O3 (gcc), its cell list built per call")
+    else:
+        out["reference_headers_ms"] = None
+        out["note"] = "the reference source tree is absent here: only the port is timed"
+    return out
+
+
 def run_reference(args):
     rank, world, _ = _dist_env()
     if rank != 0:
@@ -753,7 +789,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--quick", action="store_true",
                     help="resident timing only (no fused / e2e / CPU legs); for profiling runs")
-    ap.add_argument("--leg", choices=["batched", "rna", "surrogate", "nt100k", "tiled", "dropin"],
+    ap.add_argument("--leg", choices=["batched", "rna", "surrogate", "nt100k", "tiled", "dropin",
+                                      "cpu"],
                     help="run one extension leg alone and print its numbers (profiling runs)")
     ap.add_argument("--hairpin-fraction", type=float, default=0.0,
                     help="--leg batched: fraction of the replicas that are hairpins")
@@ -769,6 +806,9 @@ def main():
 
 
 def run_leg(args):
+    if args.leg == "cpu":
+        print(json.dumps({"leg": "cpu", **cpu_arithmetic(build_system())}), flush=True)
+        return
     import torch
     stream = torch.cuda.Stream()
     if args.leg == "batched":

@@ -42,7 +42,7 @@ def build_oracle(force=False):
             os.path.join(HERE, "..", "include", "oxdna_gb300.h")]
     if force or _stale(ORACLE_SO, [src] + hdrs):
         tmp = ORACLE_SO + ".tmp%d" % os.getpid()
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-Wall",
+        _run(["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-Wall",
               "-o", tmp, src, "-lm"])
         os.replace(tmp, ORACLE_SO)
     return ORACLE_SO
@@ -66,14 +66,15 @@ def build_ref(force=False):
     src = os.path.join(HERE, "ref_wrap.cpp")
     shim = os.path.join(HERE, "ref_shim")
     deps = [src, os.path.join(shim, "hoomd", "HOOMDMath.h"),
-            os.path.join(shim, "hoomd", "VectorMath.h"), os.path.join(shim, "oxref_count.h")]
+            os.path.join(shim, "hoomd", "VectorMath.h"), os.path.join(shim, "oxref_count.h"),
+            os.path.join(HERE, "oxdna_oracle.h")]
     out = []
     for tag, defs in (("64", []), ("32", ["-DHOOMD_HAS_FORCEREAL"]),
                       ("count", ["-DHOOMD_HAS_FORCEREAL", "-DOXREF_COUNTING"])):
         so = os.path.join(REF_DIR, "libref%s.so" % tag)
         if force or _stale(so, deps):
             tmp = so + ".tmp%d" % os.getpid()
-            _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w", *defs,
+            _run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-w", *defs,
                   "-I", shim, "-I", REF_SRC, "-I", pyb, "-I", pyinc, "-o", tmp, src])
             os.replace(tmp, so)
         out.append(so)

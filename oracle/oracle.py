@@ -242,3 +242,46 @@ def langevin(model, system, vel, angmom, steps, dt, kT, gamma=1.0, gamma_r=1.0, 
                                 int(bonded), dt, kT, gamma, gamma_r, seed, step0, steps, buffer,
                                 threads)
     return builds, vel, angmom
+
+
+def half_pairs(system, r_list):
+    """Half neighbour list (i < j) within r_list under the minimum image, bonded pairs
+    excluded (HOOMD's bond exclusions): int32 array (n, 2)."""
+    from scipy.spatial import cKDTree
+    box = np.asarray(system.box, float)
+    p = np.mod(system.pos + 0.5 * box, box)
+    p = np.where(p >= box, p - box, p)
+    pairs = cKDTree(p, boxsize=box).query_pairs(r_list, output_type="ndarray")
+    pairs = np.sort(pairs, axis=1)
+    if system.nb:
+        b = np.sort(system.bonds[:system.nb, :2], axis=1).astype(np.int64)
+        n = len(system.pos)
+        keep = ~np.isin(pairs[:, 0].astype(np.int64) * n + pairs[:, 1], b[:, 0] * n + b[:, 1])
+        pairs = pairs[keep]
+    order = np.lexsort((pairs[:, 1], pairs[:, 0]))
+    return np.ascontiguousarray(pairs[order], dtype=np.int32)
+
+
+def ref_system_forces(model, system, pairs, mask=None, bonded=None, precision=64):
+    """The system's forces through the reference's own evaluators and bonded kernel with
+    HOOMD's CPU driver semantics (``ref_system_forces`` in ref_wrap.cpp), over the given
+    half pair list. Same outputs as :func:`forces`; None when the reference build is
+    unavailable."""
+    L = ref_lib(precision)
+    if L is None:
+        return None
+    fn = L.ref_system_forces
+    fn.argtypes = [C.POINTER(OxoModel), C.POINTER(OxoSystem), C.c_uint32, C.c_int, C.c_int, ip,
+                   dp, dp, dp, dp]
+    fn.restype = C.c_int
+    n = system.s.N
+    f = np.zeros((n, 4))
+    t = np.zeros((n, 3))
+    pe = np.zeros(6)
+    be = np.zeros(3)
+    mask = model.mask if mask is None else mask
+    bonded = model.has_bonded if bonded is None else bonded
+    pairs = np.ascontiguousarray(pairs, dtype=np.int32)
+    fn(C.byref(model.s), C.byref(system.s), mask, int(bonded), len(pairs), pairs.ctypes.data_as(ip),
+       f.ctypes.data_as(dp), t.ctypes.data_as(dp), pe.ctypes.data_as(dp), be.ctypes.data_as(dp))
+    return dict(force=f[:, :3], energy_pp=f[:, 3], torque=t, pair_energy=pe, bonded_energy=be)

@@ -24,6 +24,10 @@
 #include "OxDNABondedKernel.h"
 
 #include "../include/oxdna_gb300.h"
+#include "oxdna_oracle.h"
+
+#include <cmath>
+#include <vector>
 
 using namespace hoomd;
 using namespace hoomd::md;
@@ -383,5 +387,147 @@ void ref_bonded(const oxg_bonded_params* pp, const double Rc[3], const double qA
     e[2] = r.e_stack;
     for (int k = 0; k < 6; ++k)
         vir[k] = r.vir[k];
+}
+
+// A whole system's forces through the reference's own evaluators, with HOOMD's CPU
+// driver semantics (hoomd/md/AnisoPotentialPair.h: half neighbour list and the third
+// law; src/OxDNABondedForceCompute.cc:55-134 for the bonds): for each listed pair (i, j)
+// dr = r_i - r_j (minimum image), every selected term within its cutoff adds F to i and
+// -F to j, its torques to each end and half its energy to each; each bond (A, B) takes
+// Rc = r_B - r_A. Parameters are converted to the reference param_type once per call.
+// It times the reference's arithmetic on the host beside the C restatement.
+// pairs: 2 * n_pairs particle indices (the caller's half list); outputs as oxo_forces
+// (force[4N] with the per-particle energy, torque[3N], pair_energy[6], bonded_energy[3]).
+int ref_system_forces(const oxo_model* m, const oxo_system* s, uint32_t mask, int bonded,
+                      int n_pairs, const int32_t* pairs, double* force, double* torque,
+                      double* pair_energy, double* bonded_energy)
+{
+    const int nt = m->n_types, np = nt * nt, N = s->N;
+    std::vector<OxDNAExcVolParams> pe(np);
+    std::vector<OxDNAHBondParams> ph(np);
+    std::vector<OxDNACrossStackingParams> pc(np);
+    std::vector<OxDNAHBondCrossParams> px(np);
+    std::vector<OxDNACoaxStackingParams> pk(np);
+    std::vector<OxDNADebyeParams> pd(np);
+    std::vector<double> rc2(6 * np, -1.0);
+    for (int k = 0; k < np; ++k) {
+        if (m->excvol) pe[k] = cvt(&m->excvol[k]);
+        if (m->hbond) ph[k] = cvt(&m->hbond[k]);
+        if (m->cross) pc[k] = cvt(&m->cross[k]);
+        if (m->hbondcross) px[k] = cvt(&m->hbondcross[k]);
+        if (m->coax) pk[k] = cvt(&m->coax[k]);
+        if (m->debye) pd[k] = cvt(&m->debye[k]);
+        for (int t = 0; t < 6; ++t)
+            if (((mask >> t) & 1u) && m->r_cut[t]) rc2[t * np + k] = m->r_cut[t][k] * m->r_cut[t][k];
+    }
+    for (int k = 0; k < 4 * N; ++k) force[k] = 0.0;
+    for (int k = 0; k < 3 * N; ++k) torque[k] = 0.0;
+    for (int t = 0; t < 6; ++t) pair_energy[t] = 0.0;
+    for (int t = 0; t < 3; ++t) bonded_energy[t] = 0.0;
+    auto wrap = [&](double d, int k) { return d - s->box[k] * std::rint(d / s->box[k]); };
+    for (int n = 0; n < n_pairs; ++n) {
+        const int i = pairs[2 * n], j = pairs[2 * n + 1];
+        ForceReal3 d;
+        d.x = ForceReal(wrap(s->pos[3 * i] - s->pos[3 * j], 0));
+        d.y = ForceReal(wrap(s->pos[3 * i + 1] - s->pos[3 * j + 1], 1));
+        d.z = ForceReal(wrap(s->pos[3 * i + 2] - s->pos[3 * j + 2], 2));
+        const double rsq = double(d.x) * d.x + double(d.y) * d.y + double(d.z) * d.z;
+        const int k = s->type[i] * nt + s->type[j];
+        const double* qa = s->quat + 4 * i;
+        const double* qb = s->quat + 4 * j;
+        const Scalar4 a = make_scalar4(qa[0], qa[1], qa[2], qa[3]);
+        const Scalar4 b = make_scalar4(qb[0], qb[1], qb[2], qb[3]);
+        const double ci = s->charge ? s->charge[i] : 1.0, cj = s->charge ? s->charge[j] : 1.0;
+        for (int t = 0; t < 6; ++t) {
+            const double r2 = rc2[t * np + k];
+            if (!(rsq < r2)) continue;
+            ForceReal3 F, Ti, Tj;
+            ForceReal E = 0;
+            bool ok = false;
+            switch (t) {
+            case OXG_EXCVOL: {
+                EvaluatorPairOxDNAExcVol ev(d, a, b, ForceReal(r2), pe[k]);
+                ok = ev.evaluate(F, E, false, Ti, Tj);
+                break;
+            }
+            case OXG_HBOND: {
+                EvaluatorPairOxDNAHBond ev(d, a, b, ForceReal(r2), ph[k]);
+                ok = ev.evaluate(F, E, false, Ti, Tj);
+                break;
+            }
+            case OXG_CROSS: {
+                EvaluatorPairOxDNACrossStacking ev(d, a, b, ForceReal(r2), pc[k]);
+                ok = ev.evaluate(F, E, false, Ti, Tj);
+                break;
+            }
+            case OXG_HBONDCROSS: {
+                EvaluatorPairOxDNAHBondCross ev(d, a, b, ForceReal(r2), px[k]);
+                ok = ev.evaluate(F, E, false, Ti, Tj);
+                break;
+            }
+            case OXG_COAX: {
+                EvaluatorPairOxDNACoaxStacking ev(d, a, b, ForceReal(r2), pk[k]);
+                ok = ev.evaluate(F, E, false, Ti, Tj);
+                break;
+            }
+            default: {
+                EvaluatorPairOxDNADebye ev(d, a, b, ForceReal(r2), pd[k]);
+                ev.setCharge(ci, cj);
+                ok = ev.evaluate(F, E, false, Ti, Tj);
+                break;
+            }
+            }
+            if (!ok) continue;
+            const double f[3] = {double(F.x), double(F.y), double(F.z)};
+            for (int c = 0; c < 3; ++c) {
+                force[4 * i + c] += f[c];
+                force[4 * j + c] -= f[c];
+            }
+            force[4 * i + 3] += 0.5 * double(E);
+            force[4 * j + 3] += 0.5 * double(E);
+            torque[3 * i] += Ti.x;
+            torque[3 * i + 1] += Ti.y;
+            torque[3 * i + 2] += Ti.z;
+            torque[3 * j] += Tj.x;
+            torque[3 * j + 1] += Tj.y;
+            torque[3 * j + 2] += Tj.z;
+            pair_energy[t] += E;
+        }
+    }
+    if (bonded && m->bonded) {
+        std::vector<oxdna_bonded_params> pb(m->n_bond_types);
+        for (int k = 0; k < m->n_bond_types; ++k) pb[k] = cvt(&m->bonded[k]);
+        for (int n = 0; n < s->n_bonds; ++n) {
+            const int A = s->bonds[3 * n], B = s->bonds[3 * n + 1], bt = s->bonds[3 * n + 2];
+            const vec3<Scalar> Rc(wrap(s->pos[3 * B] - s->pos[3 * A], 0),
+                                  wrap(s->pos[3 * B + 1] - s->pos[3 * A + 1], 1),
+                                  wrap(s->pos[3 * B + 2] - s->pos[3 * A + 2], 2));
+            const double* qa = s->quat + 4 * A;
+            const double* qb = s->quat + 4 * B;
+            quat<Scalar> a(make_scalar4(qa[0], qa[1], qa[2], qa[3]));
+            quat<Scalar> b(make_scalar4(qb[0], qb[1], qb[2], qb[3]));
+            oxdna::BondedResult r;
+            oxdna::oxdna_bonded_pair(pb[bt], Rc, a, b, (unsigned)s->type[A], (unsigned)s->type[B], r);
+            const double e = r.e_fene + r.e_bexc + r.e_stack;
+            force[4 * B] += r.FB.x;
+            force[4 * B + 1] += r.FB.y;
+            force[4 * B + 2] += r.FB.z;
+            force[4 * A] -= r.FB.x;
+            force[4 * A + 1] -= r.FB.y;
+            force[4 * A + 2] -= r.FB.z;
+            force[4 * A + 3] += 0.5 * e;
+            force[4 * B + 3] += 0.5 * e;
+            torque[3 * A] += r.tauA.x;
+            torque[3 * A + 1] += r.tauA.y;
+            torque[3 * A + 2] += r.tauA.z;
+            torque[3 * B] += r.tauB.x;
+            torque[3 * B + 1] += r.tauB.y;
+            torque[3 * B + 2] += r.tauB.z;
+            bonded_energy[0] += r.e_fene;
+            bonded_energy[1] += r.e_bexc;
+            bonded_energy[2] += r.e_stack;
+        }
+    }
+    return 0;
 }
 } // extern "C"

@@ -75,6 +75,34 @@ def test_system_driver_matches_reference(oracle):
         assert maxrel(r["torque"], g["bonded/torque"]) < TOL_ORACLE
 
 
+def test_reference_system_driver_matches_oracle(oracle):
+    """The reference's own evaluators and bonded kernel driven over a whole system with
+    HOOMD's CPU semantics (the timed reference-arithmetic CPU baseline) give the
+    oracle's forces, torques and energies (every term, fused and not)."""
+    if oracle.ref_lib(64) is None:
+        pytest.skip("reference source tree not present")
+    from oxdna import io
+    g = golden("system_dna2.npz")
+    for fused in (False, True):
+        pair, bonded = model_forces("dna2") if not fused else _fused_dna2()
+        model = oracle.Model(pair + [bonded], io.DNA_BASES)
+        sysm = oracle.System(g["pos"], g["quat"], g["typeid"], g["box"], g["bonds"], g["charge"])
+        rl = max(f.rcut_for(a, b) for f in pair for a in io.DNA_BASES for b in io.DNA_BASES)
+        pairs = oracle.half_pairs(sysm, rl * (1 + 1e-9))
+        want = oracle.forces(model, sysm)
+        got = oracle.ref_system_forces(model, sysm, pairs)
+        for k in ("force", "torque", "energy_pp"):
+            assert maxrel(got[k], want[k]) < TOL_ORACLE, (fused, k)
+        assert np.allclose(got["pair_energy"], want["pair_energy"], rtol=1e-10, atol=1e-10)
+        assert np.allclose(got["bonded_energy"], want["bonded_energy"], rtol=1e-10, atol=1e-10)
+
+
+def _fused_dna2():
+    from oxdna.model import dna2
+    forces, _ = dna2.forces(fused=True)
+    return forces[1:], forces[0]
+
+
 def test_parameter_structs_match_the_reference_constructors():
     """This build's route from a parameter dict to the evaluators' param_type (dict ->
     POD struct -> field copy in oracle/ref_wrap.cpp) against the reference's own
