@@ -311,6 +311,50 @@ __device__ __forceinline__ void scatter(const ForceArgs& a, int i, int j, const 
     atomicAdd(a.torque + j, make_float4(acc.tj.x, acc.tj.y, acc.tj.z, 0.f));
 }
 
+// The forces of a unit's pairs with the i side summed over each run of adjacent lanes
+// with equal i (the lists hold a particle's pairs mostly contiguously) by a segmented
+// suffix sum over the warp: the run's first lane adds the run's total with one atomic
+// per array, instead of one per pair; the j side is added per pair. A particle whose
+// pairs are split over runs that are not adjacent (list appends of other warps in
+// between) is added once per run. key: the pair's i, or -1 for a lane outside the list;
+// has: the lane's pair contributed (acc, e valid). All lanes call it.
+// (8000 nt: phase A 6.0 -> 5.45 us, 59.5k -> 61.0k steps/s; 100k nt: 11.5k -> 12.1k.)
+template <bool ENERGY>
+__device__ __forceinline__ void scatter_seg(const ForceArgs& a, int key, bool has, int i, int j,
+                                            const PairAcc& acc, float e)
+{
+    const int lane = threadIdx.x & 31;
+    const float eh = ENERGY ? 0.5f * e : 0.f;
+    // force, energy half, torque, and the count of contributing pairs of the run
+    float v[8] = {acc.fi.x, acc.fi.y, acc.fi.z, eh, acc.ti.x, acc.ti.y, acc.ti.z, 1.f};
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+        if (!has) v[c] = 0.f;
+    // run heads: lanes whose left neighbour has another key; a run ends before the next head
+    const int kp = __shfl_up_sync(0xffffffffu, key, 1);
+    const bool head = lane == 0 || kp != key;
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const unsigned above = heads & ~((2u << lane) - 1u);  // heads right of this lane
+    const int end = above ? __ffs(above) - 2 : 31;       // last lane of this lane's run
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const bool add = lane + off <= end;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const float o = __shfl_down_sync(0xffffffffu, v[c], off);
+            if (add) v[c] += o;
+        }
+    }
+    if (head && key >= 0 && v[7] > 0.f) {
+        atomicAdd(a.force + i, make_float4(v[0], v[1], v[2], v[3]));
+        atomicAdd(a.torque + i, make_float4(v[4], v[5], v[6], 0.f));
+    }
+    if (has) {
+        atomicAdd(a.force + j, make_float4(-acc.fi.x, -acc.fi.y, -acc.fi.z, eh));
+        atomicAdd(a.torque + j, make_float4(acc.tj.x, acc.tj.y, acc.tj.z, 0.f));
+    }
+}
+
 // Full evaluation of one deferred term for short pair w (warp-uniform q). part (fused
 // HB + CS pairs only): 0 both terms, 1 the HB term, 2 the CS term.
 template <bool ENERGY>
@@ -449,12 +493,12 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
         if (w + stride < n_short) next_pr = __ldcg(a.pairs_short + w + stride);
         bool want[kNQ] = {};
         PairIn p;
+        PairAcc acc;
+        acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
+        float e_inline = 0.f;
+        bool inl = false;
         if (w < n_short && load_pair(a, pr, n_types, p, bad_type) && p.rsq < H.rcutsq_max) {
             const Frame fi = quat_frame(p.qi), fj = quat_frame(p.qj);
-            PairAcc acc;
-            acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
-            float e_inline = 0.f;
-            bool inl = false;
             if (mask & (1u << kExcVol)) {
                 const DExcVol& pe = P.term<DExcVol>(kExcVol, p.pidx);
                 if (p.rsq < pe.rcutsq) {
@@ -473,7 +517,6 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
                     inl = true;
                 }
             }
-            if (inl) scatter<ENERGY>(a, p.i, p.j, acc, e_inline);
             BBGeom g;
             bool gv = false;
             if (mask & (1u << kHBond)) {
@@ -508,6 +551,7 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
                 want[kQCX] = p.rsq < pc.rcutsq && coax_support(pc, p.rc, fi, fj);
             }
         }
+        scatter_seg<ENERGY>(a, w < n_short ? pr.x : -1, inl, p.i, p.j, acc, e_inline);
 #pragma unroll
         for (int q = 0; q < kNQ; ++q) {
             const unsigned m = __ballot_sync(0xffffffffu, want[q]);
@@ -547,26 +591,26 @@ __device__ __forceinline__ void forces_a_body(const ForceArgs& a, const ParamVie
         const int w = v * 32 + lane;
         const int2 pr = next_lp;
         if (w + vstride * 32 < n_long) next_lp = __ldcg(a.pairs_long + w + vstride * 32);
-        if (w >= n_long) continue;
         const int i = pr.x, j = pr.y;
+        const bool in_range = w < n_long;
         // every load of the pair issued at once (one L2 round trip)
         const float4 pi = __ldcg(a.pos + i), pj = __ldcg(a.pos + j);
         const float4 li = __ldcg(a.pos_lo + i), lj = __ldcg(a.pos_lo + j);
         const float4 qi = __ldcg(a.quat + i), qj = __ldcg(a.quat + j);
         const float ci = a.charge ? a.charge[i] : 1.f, cj = a.charge ? a.charge[j] : 1.f;
         const int ti = type_of(pi), tj = type_of(pj);
-        if ((unsigned)ti >= (unsigned)n_types || (unsigned)tj >= (unsigned)n_types) {
-            bad_type = true;
-            continue;
-        }
+        const bool tok = (unsigned)ti < (unsigned)n_types && (unsigned)tj < (unsigned)n_types;
+        if (in_range && !tok) bad_type = true;
         const float3 dr = image_delta(pi, li, pj, lj, a.L, a.invL);
         PairAcc acc;
         acc.fi = acc.ti = acc.tj = mk3(0.f, 0.f, 0.f);
         float E[kNTerms] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), qi, qj, ci, cj, acc, E)) {
+        bool has = false;
+        if (in_range && tok && eval_pair(P, long_mask, ti * kMaxTypes + tj, dr, dot(dr, dr), qi, qj, ci, cj, acc, E)) {
             if (ENERGY) eacc[kDebye] += (double)E[kDebye];
-            scatter<ENERGY>(a, i, j, acc, E[kDebye]);
+            has = true;
         }
+        scatter_seg<ENERGY>(a, in_range ? i : -1, has, i, j, acc, E[kDebye]);
     }
     __syncthreads();
     if (LOCAL) {  // the entries written, for forces_b_local after the block's barrier
