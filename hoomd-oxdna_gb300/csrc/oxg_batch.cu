@@ -239,19 +239,20 @@ __device__ __noinline__ void batch_heavy(const Smem& s, const BatchArgs& a, int 
 }
 
 // Phase-A work of one pair (pi < pj) of replica r: the cheap terms (excluded volume,
-// Debye) inline, the zero-factor tests of the heavy ones, which are queued.
+// Debye) inline, the zero-factor tests of the heavy ones; returns the heavy terms the
+// pair needs (bit q: queue q), which the caller appends warp by warp.
 template <bool ENERGY>
-__device__ __forceinline__ void pair_a(const Smem& s, const BatchArgs& a, int r, int pi, int pj)
+__device__ __forceinline__ uint32_t pair_a(const Smem& s, const BatchArgs& a, int r, int pi, int pj)
 {
     const TileRep& R = s.reps[r];
     const int4 ex = s.ex[pi];
-    if (ex.x == pj || ex.y == pj || ex.z == pj || ex.w == pj) return;
+    if (ex.x == pj || ex.y == pj || ex.z == pj || ex.w == pj) return 0u;
     const float3 dr = rep_delta(s, R, pi, pj);
     const float rsq = dot(dr, dr);
     ParamView P;
     P.b = s.params + (size_t)r * a.param_bytes;
     const ParamHeader& H = P.h();
-    if (!(rsq < H.rcutsq_max)) return;
+    if (!(rsq < H.rcutsq_max)) return 0u;
     const int pidx = __float_as_int(s.x[pi].w) * kMaxTypes + __float_as_int(s.x[pj].w);
     const Frame fi = frame_of(s, pi), fj = frame_of(s, pj);
     const float3 rc = -dr;
@@ -314,11 +315,35 @@ __device__ __forceinline__ void pair_a(const Smem& s, const BatchArgs& a, int r,
         const DCoax& pc = P.term<DCoax>(kCoax, pidx);
         want[kQCX] = rsq < pc.rcutsq && coax_support(pc, rc, fi, fj);
     }
+    uint32_t bits = 0u;
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q)
+        if (want[q]) bits |= 1u << q;
+    return bits;
+}
+
+// Append the warp's heavy-term pairs to the tile's queues: one shared atomic per warp and
+// queue (all lanes call it; bits 0: nothing to append). A pair that does not fit is
+// evaluated at once.
+template <bool ENERGY>
+__device__ __forceinline__ void queue_warp(const Smem& s, const BatchArgs& a, uint32_t bits, int r, int pi, int pj)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
     for (int q = 0; q < kNQ; ++q) {
-        if (!want[q]) continue;
-        const int slot = atomicAdd(&s.qcnt[q], 1);
-        if (slot < a.qcap) s.queue[q * a.qcap + slot] = (pi << 16) | pj;
-        else batch_heavy<ENERGY>(s, a, q, pi, pj, r);  // queue full: evaluate here
+        const bool w = (bits >> q) & 1u;
+        const unsigned m = __ballot_sync(0xffffffffu, w);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&s.qcnt[q], __popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (w) {
+            const int slot = base + __popc(m & lt);
+            if (slot < a.qcap) s.queue[q * a.qcap + slot] = (pi << 16) | pj;
+            else batch_heavy<ENERGY>(s, a, q, pi, pj, r);  // queue full: evaluate here
+        }
     }
 }
 
@@ -381,53 +406,77 @@ __device__ void tile_forces(const Smem& s, const BatchArgs& a, int nrep, int np,
     __syncthreads();
     // phase A: the tile's pair list (or every pair of every replica of the tile)
     const int npl = s.nl[0];
+    // (loops run in whole warps: the queue appends are warp-wide)
+    const int wbase0 = tid & ~31;
     if (npl >= 0) {
-        for (int k = tid; k < npl; k += nt) {
-            const int v = s.plist[k];
-            const int pi = v >> 16, pj = v & 0xffff;
-            pair_a<ENERGY>(s, a, s.rep_of[pi], pi, pj);
+        for (int kb = wbase0; kb < npl; kb += nt) {
+            const int k = kb + (tid & 31);
+            uint32_t bits = 0u;
+            int r = 0, pi = 0, pj = 0;
+            if (k < npl) {
+                const int v = s.plist[k];
+                pi = v >> 16;
+                pj = v & 0xffff;
+                r = s.rep_of[pi];
+                bits = pair_a<ENERGY>(s, a, r, pi, pj);
+            }
+            queue_warp<ENERGY>(s, a, bits, r, pi, pj);
         }
     } else {
-        for (int k = tid; k < total_pairs; k += nt) {
-            int r, pi, pj;
-            tri_pair(s, nrep, k, r, pi, pj);
-            pair_a<ENERGY>(s, a, r, pi, pj);
+        for (int kb = wbase0; kb < total_pairs; kb += nt) {
+            const int k = kb + (tid & 31);
+            uint32_t bits = 0u;
+            int r = 0, pi = 0, pj = 0;
+            if (k < total_pairs) {
+                tri_pair(s, nrep, k, r, pi, pj);
+                bits = pair_a<ENERGY>(s, a, r, pi, pj);
+            }
+            queue_warp<ENERGY>(s, a, bits, r, pi, pj);
         }
     }
     __syncthreads();
-    // phase B: queued heavy terms, all lanes busy
-    for (int q = 0; q < kNQ; ++q) {
-        const int cnt = min(s.qcnt[q], a.qcap);
-        for (int e = tid; e < cnt; e += nt) {
+    // phase B: the queued heavy terms and the bonds as segments [HB | CS | HB+CS | coax |
+    // bonds], each padded to whole warps, so that every warp evaluates 32 items of one
+    // kind (term-uniform warps, no lane idle but in a segment's last warp)
+    int cnt[kNQ + 1], seg[kNQ + 2];
+    seg[0] = 0;
+#pragma unroll
+    for (int q = 0; q < kNQ; ++q) cnt[q] = min(s.qcnt[q], a.qcap);
+    cnt[kNQ] = a.bonded ? nb : 0;
+#pragma unroll
+    for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
+    const int lane = tid & 31;
+    for (int wbase = (tid >> 5) * 32; wbase < seg[kNQ + 1]; wbase += nt) {
+        int q = 0;
+        while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
+        const int e = wbase - seg[q] + lane;
+        if (e >= cnt[q]) continue;
+        if (q < kNQ) {
             const int v = s.queue[q * a.qcap + e];
             const int pi = v >> 16, pj = v & 0xffff;
             batch_heavy<ENERGY>(s, a, q, pi, pj, s.rep_of[pi]);
+            continue;
         }
-    }
-    // bonds
-    if (a.bonded) {
-        for (int b = tid; b < nb; b += nt) {
-            const int4 bd = s.bd[b];
-            const int A = bd.x, B = bd.y, r = s.rep_of[A];
-            const TileRep& R = s.reps[r];
-            ParamView P;
-            P.b = s.params + (size_t)r * a.param_bytes;
-            const float3 Rcf = rep_delta(s, R, B, A);
-            const float4 qA = s.q[A], qB = s.q[B];
-            BondAcc acc;
-            bonded_pair<false>(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
-                        make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
-                        __float_as_int(s.x[A].w), __float_as_int(s.x[B].w), acc);
-            const float eh = ENERGY ? (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2])) : 0.f;
-            sm_add(s.f, A, -acc.fB, eh);
-            sm_add(s.f, B, acc.fB, eh);
-            sm_add(s.t, A, acc.tA, 0.f);
-            sm_add(s.t, B, acc.tB, 0.f);
-            if (ENERGY) {
-                atomicAdd(&s.eacc[r * 9 + kNTerms + 0], acc.e[0]);
-                atomicAdd(&s.eacc[r * 9 + kNTerms + 1], acc.e[1]);
-                atomicAdd(&s.eacc[r * 9 + kNTerms + 2], acc.e[2]);
-            }
+        const int4 bd = s.bd[e];
+        const int A = bd.x, B = bd.y, r = s.rep_of[A];
+        const TileRep& R = s.reps[r];
+        ParamView P;
+        P.b = s.params + (size_t)r * a.param_bytes;
+        const float3 Rcf = rep_delta(s, R, B, A);
+        const float4 qA = s.q[A], qB = s.q[B];
+        BondAcc acc;
+        bonded_pair<false>(P.bonded(bd.z), make_double3(Rcf.x, Rcf.y, Rcf.z),
+                    make_double4_32a(qA.x, qA.y, qA.z, qA.w), make_double4_32a(qB.x, qB.y, qB.z, qB.w),
+                    __float_as_int(s.x[A].w), __float_as_int(s.x[B].w), acc);
+        const float eh = ENERGY ? (float)(0.5 * (acc.e[0] + acc.e[1] + acc.e[2])) : 0.f;
+        sm_add(s.f, A, -acc.fB, eh);
+        sm_add(s.f, B, acc.fB, eh);
+        sm_add(s.t, A, acc.tA, 0.f);
+        sm_add(s.t, B, acc.tB, 0.f);
+        if (ENERGY) {
+            atomicAdd(&s.eacc[r * 9 + kNTerms + 0], acc.e[0]);
+            atomicAdd(&s.eacc[r * 9 + kNTerms + 1], acc.e[1]);
+            atomicAdd(&s.eacc[r * 9 + kNTerms + 2], acc.e[2]);
         }
     }
     __syncthreads();
