@@ -483,9 +483,9 @@ class Simulation:
     def run_state_arrays(self, steps, pos_type, pos_lo, quat, vel, angmom):
         """push_state_arrays + run(steps) + pull_state_arrays in one call: the state is
         read from the host float32 (N, 4) arrays and the final state written back into
-        them. With page-locked arrays (torch ``pin_memory()``) a copy kernel on each side
-        of the run launch moves the state over the host link: one synchronisation per
-        call."""
+        them. With page-locked arrays (torch ``pin_memory()``) the run kernel itself reads
+        them at its start and writes them in its last step, over the host link: one
+        launch and one synchronisation per call."""
         self._sync()
         self._cache = {}
         L = _abi.lib()
