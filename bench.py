@@ -741,8 +741,9 @@ def run_ours(args):
     e2e3_s = replicas.max_over_ranks(time.perf_counter() - t0, dist)
     e2e = {"value": world * e2e_steps / e2e_s, "unit": "steps/s",
            "h2d_bytes_per_step": 5 * 16 * n, "d2h_bytes_per_step": 5 * 16 * n,
-           "path": "Simulation.run_state_arrays(1, pinned host arrays) (oxg_system_run_host: a copy "
-                   "kernel reads the host state, the run kernel steps, a copy kernel writes it back)",
+           "path": "Simulation.run_state_arrays(1, pinned host arrays) (oxg_system_run_host: one "
+                   "launch of the run kernel, which reads the mapped host state at its start and "
+                   "writes it back in its last step; one synchronisation)",
            "three_calls_steps_per_s": world * e2e_steps / e2e3_s,
            "three_calls_path": "push_state_arrays -> run(1) -> pull_state_arrays"}
 

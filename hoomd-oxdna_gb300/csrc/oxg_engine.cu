@@ -1548,11 +1548,9 @@ int oxg_system_run_host(oxg_system* s, long nsteps, float* pos_type, float* pos_
     for (int t = 0; t < s->ctx->n_bond_types && s->run_bonded; ++t)
         if (!s->ctx->bonded_set[t]) return set_err(OXG_ERR_NO_PARAMS, "bond type without parameters");
     if ((rc = sys_setup_nlist(s, s->run_mask, false))) return rc;
-    // copy kernels move the state from the host arrays before the run launch and back
-    // after it, all on the stream, then one synchronisation
-    if ((rc = run_persistent(s, nsteps, dev, dev))) return rc;
-    OXG_CUDA(cudaStreamSynchronize(s->stream));
-    return OXG_OK;
+    // the run kernel reads the mapped host arrays at its start and writes them in its
+    // closing body; run_persistent synchronises after every launch
+    return run_persistent(s, nsteps, dev, dev);
 }
 
 int oxg_system_run_timing(oxg_system* s, double* out, int n, int reset)

@@ -1891,17 +1891,23 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 if (from_host) {
                     // the host's state (mapped memory) into the device arrays; compared
                     // bit for bit with what they held
+                    // every load issued before any store: a store to a device array
+                    // could alias a later host load for the compiler, which would then
+                    // serialise the five host round trips
                     float4* const dv[5] = {a.g.pos, a.g.pos_lo, a.g.quat, a.g.vel, a.g.angmom};
+                    float4 o[5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) v[k] = a.hin[k][i];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) o[k] = dv[k][i];
+                    if ((unsigned)__float_as_int(v[0].w) >= (unsigned)P.h().n_types)
+                        bad_type = true;  // reported after the run (the kernels skip the particle)
 #pragma unroll
                     for (int k = 0; k < 5; ++k) {
-                        v[k] = a.hin[k][i];
-                        if (k == 0 && (unsigned)__float_as_int(v[0].w) >= (unsigned)P.h().n_types)
-                            bad_type = true;  // reported after the run (the kernels skip the particle)
-                        const float4 o = dv[k][i];
-                        diff |= __float_as_uint(v[k].x) != __float_as_uint(o.x) ||
-                                __float_as_uint(v[k].y) != __float_as_uint(o.y) ||
-                                __float_as_uint(v[k].z) != __float_as_uint(o.z) ||
-                                __float_as_uint(v[k].w) != __float_as_uint(o.w);
+                        diff |= __float_as_uint(v[k].x) != __float_as_uint(o[k].x) ||
+                                __float_as_uint(v[k].y) != __float_as_uint(o[k].y) ||
+                                __float_as_uint(v[k].z) != __float_as_uint(o[k].z) ||
+                                __float_as_uint(v[k].w) != __float_as_uint(o[k].w);
                         dv[k][i] = v[k];
                     }
                 } else {
