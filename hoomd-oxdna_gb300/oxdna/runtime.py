@@ -18,6 +18,8 @@ from . import _abi
 from . import forces as _forces_mod
 from .forces import OxDNABonded, _PairForce
 
+_F32 = np.dtype(np.float32)  # native float32 (a singleton: compared by identity)
+
 
 # --------------------------------------------------------------------- snapshot
 class _Particles:
@@ -473,12 +475,36 @@ class Simulation:
         if getattr(self, "_surrogate_args", None) is not None:
             self._apply_surrogate(*self._surrogate_args)
 
+    def _host_state_ptrs(self, arrays, allow_none=False):
+        """Addresses of the five host state arrays, each checked to be a C-contiguous
+        float32 (N, 4) array (the engine reads and writes 16 * N bytes at each). Reading
+        an array's address through numpy costs ~2 µs, a sizeable part of a one-step call,
+        so the addresses of the last arrays seen are kept (with a reference to each
+        array, so that an address is never taken for another array's)."""
+        n = self._snap.particles.N
+        cache = self.__dict__.setdefault("_addr_cache", {})
+        out = []
+        for a in arrays:
+            if a is None and allow_none:
+                out.append(None)
+                continue
+            if (not isinstance(a, np.ndarray) or a.dtype is not _F32 or a.shape != (n, 4)
+                    or not a.flags.c_contiguous):
+                raise ValueError("state arrays must be C-contiguous float32 arrays of shape "
+                                 f"({n}, 4)")
+            hit = cache.get(id(a))
+            if hit is None or hit[0] is not a:
+                if len(cache) >= 32:
+                    cache.clear()
+                hit = (a, a.__array_interface__["data"][0])
+                cache[id(a)] = hit
+            out.append(hit[1])
+        return out
+
     def push_state_arrays(self, pos_type, pos_lo, quat, vel, angmom):
         """Copy host float32 (N, 4) arrays (pinned or not) into the device state."""
-        L = _abi.lib()
-        ptr = lambda a: C.c_void_p(a.ctypes.data) if a is not None else None  # noqa: E731
-        _abi.check(L.oxg_system_set_state(self._sys, ptr(pos_type), ptr(pos_lo), ptr(quat),
-                                          ptr(vel), ptr(angmom), None), "oxg_system_set_state")
+        ptrs = self._host_state_ptrs((pos_type, pos_lo, quat, vel, angmom), allow_none=True)
+        _abi.check(_abi.lib().oxg_system_set_state(self._sys, *ptrs, None), "oxg_system_set_state")
 
     def run_state_arrays(self, steps, pos_type, pos_lo, quat, vel, angmom):
         """push_state_arrays + run(steps) + pull_state_arrays in one call: the state is
@@ -488,21 +514,19 @@ class Simulation:
         launch and one synchronisation per call."""
         self._sync()
         self._cache = {}
-        L = _abi.lib()
         steps = int(steps)
         if steps < 1 or self._langevin is None:
             raise ValueError("run_state_arrays needs steps >= 1 and a Langevin method")
-        ptr = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
-        _abi.check(L.oxg_system_run_host(self._sys, steps, ptr(pos_type), ptr(pos_lo), ptr(quat),
-                                         ptr(vel), ptr(angmom)), "oxg_system_run_host")
+        ptrs = self._host_state_ptrs((pos_type, pos_lo, quat, vel, angmom))
+        rc = _abi.lib().oxg_system_run_host(self._sys, steps, *ptrs)
+        if rc:
+            _abi.check(rc, "oxg_system_run_host")
         self.timestep += steps
 
     def pull_state_arrays(self, pos_type, pos_lo, quat, vel, angmom):
         """Copy the device state into host float32 (N, 4) arrays."""
-        L = _abi.lib()
-        ptr = lambda a: C.c_void_p(a.ctypes.data) if a is not None else None  # noqa: E731
-        _abi.check(L.oxg_system_get_state(self._sys, ptr(pos_type), ptr(pos_lo), ptr(quat),
-                                          ptr(vel), ptr(angmom)), "oxg_system_get_state")
+        ptrs = self._host_state_ptrs((pos_type, pos_lo, quat, vel, angmom), allow_none=True)
+        _abi.check(_abi.lib().oxg_system_get_state(self._sys, *ptrs), "oxg_system_get_state")
 
     def _push_state(self):
         L = _abi.lib()

@@ -221,3 +221,25 @@ def test_surrogate_is_reapplied_after_a_rebuild(fake):
     forces[1].params[("A", "A")] = dict(forces[1].params[("A", "A")])
     sim.run(1)
     assert "set_surrogate" not in _kinds(fake, n0)  # switched off: not reapplied
+
+
+def test_state_arrays_are_checked_before_the_engine_sees_them(fake):
+    """The host state arrays go to the engine as raw addresses of 16 * N bytes each: an
+    array of another dtype, shape or layout is a ValueError, raised before any call."""
+    sim, forces, lang = _sim()
+    sim.run(1)
+    n = sim.state.get_snapshot().particles.N
+    good = [np.zeros((n, 4), np.float32) for _ in range(5)]
+    sim.pull_state_arrays(*good)
+    sim.push_state_arrays(*good)
+    sim.run_state_arrays(1, *good)
+    bad_cases = [np.zeros((n, 4), np.float64), np.zeros((n, 3), np.float32),
+                 np.zeros((n + 1, 4), np.float32), np.zeros((4, n), np.float32).T,
+                 list(np.zeros((n, 4), np.float32))]
+    for bad in bad_cases:
+        n0 = len(fake.calls)
+        for call in (sim.push_state_arrays, sim.pull_state_arrays,
+                     lambda *a: sim.run_state_arrays(1, *a)):
+            with pytest.raises(ValueError):
+                call(bad, *good[1:])
+        assert len(fake.calls) == n0
