@@ -1847,6 +1847,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     // once after each list build (they change only there)
     int ns_known = -1, nl_known = -1;
     int2 first_pair[2];
+    bool completed = false;  // the launch's last body ran to its end
     // the block's slice of the (constant) bond table, staged once per launch when it fits
     __shared__ int4 bond_stage[kBondStage];
     const int4* bonds_here = nullptr;
@@ -2045,26 +2046,33 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         // body b's to rb[(b + 1) & 1] (cleared by body b - 1 after its force barrier)
         if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(pro ? &st->rebuild : &st->rb[(body + 1) & 1], 1u);
         if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
-        if (!grid_barrier(a.bar)) break;
-        if (body == a.bodies - 1 && blockIdx.x == 0 && threadIdx.x == 0) {
-            // completed: hand the pending request to the next launch (or per-step kernels)
-            st->rebuild = ld_volatile(&st->rb[a.bodies & 1]);
-            st->rb[0] = 0u;
-            st->rb[1] = 0u;
+        if (body == a.bodies - 1) {  // the launch's last body: no barrier after it (below)
+            completed = true;
+            break;
         }
+        if (!grid_barrier(a.bar)) break;
     }
     if (__syncthreads_or(bad_type) && threadIdx.x == 0) atomicOr(&st->flags, kStBadIndex);
     if (threadIdx.x == 0 && ld_volatile(&a.bar->abort)) atomicOr(&st->flags, kStBarrierTimeout);
-    // the last block to leave mirrors the final status into host memory, so the host
-    // reads it after the launch without a copy of its own
-    if (a.st_mirror && threadIdx.x == 0) {
+    // the last block to leave: after a completed launch it hands the pending rebuild
+    // request to the next launch (or the per-step kernels) — every block has written its
+    // part by then, so the last body needs no grid barrier of its own — and it mirrors
+    // the final status into host memory, so the host reads it without a copy of its own
+    if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(&a.bar->exits, 1u) == gridDim.x - 1u) {
             __threadfence();
-            const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(st);
-            volatile uint32_t* dst = reinterpret_cast<volatile uint32_t*>(a.st_mirror);
-            for (int k = 0; k < (int)(sizeof(DevStatus) / sizeof(uint32_t)); ++k) dst[k] = src[k];
-            __threadfence_system();
+            if (completed) {  // the same in every block (all complete, or all left early)
+                st->rebuild = ld_volatile(&st->rb[a.bodies & 1]);
+                st->rb[0] = 0u;
+                st->rb[1] = 0u;
+            }
+            if (a.st_mirror) {
+                const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(st);
+                volatile uint32_t* dst = reinterpret_cast<volatile uint32_t*>(a.st_mirror);
+                for (int k = 0; k < (int)(sizeof(DevStatus) / sizeof(uint32_t)); ++k) dst[k] = src[k];
+                __threadfence_system();
+            }
             a.bar->exits = 0u;
         }
     }
