@@ -784,20 +784,31 @@ __device__ __forceinline__ void forces_b_local(const ForceArgs& a, const ParamVi
     const int nb = a.bonded ? a.n_bonds : 0;
     const int b0 = (int)((long long)nb * blockIdx.x / gridDim.x);
     const int b1 = (int)((long long)nb * (blockIdx.x + 1) / gridDim.x);
-    int cnt[kNQ + 1], seg[kNQ + 2];
+    // segments: the kNQ queues, then the cross-stacking halves of the fused HB + CS pairs
+    // of complementary bases (their queue segment takes the HB halves: two items of one
+    // term each instead of one of both), then the bonds; the fused pairs of the other
+    // class take the CS half only (their HB factor is zero: the half adds exactly zero)
+    int cnt[kNQ + 2], seg[kNQ + 3];
     seg[0] = 0;
 #pragma unroll
     for (int q = 0; q < kNQ; ++q) cnt[q] = (int)bq.count[q];
-    cnt[kNQ] = b1 - b0;
+    cnt[kNQ] = cnt[kQHBX];
+    cnt[kNQ + 1] = b1 - b0;
 #pragma unroll
-    for (int q = 0; q <= kNQ; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
-    for (int wbase = w * 32; wbase < seg[kNQ + 1]; wbase += nw * 32) {
+    for (int q = 0; q <= kNQ + 1; ++q) seg[q + 1] = seg[q] + ((cnt[q] + 31) & ~31);
+    for (int wbase = w * 32; wbase < seg[kNQ + 2]; wbase += nw * 32) {
         int q = 0;
-        while (q < kNQ && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
+        while (q < kNQ + 1 && wbase >= seg[q + 1]) ++q;  // warp-uniform segment
         const int k = wbase - seg[q] + lane;
         if (k >= cnt[q]) continue;
-        if (q < kNQ) eval_deferred<ENERGY>(a, P, q, bq.buf[q][k], eacc);
-        else eval_bond<ENERGY>(a, P, bond_stage ? bond_stage[k] : a.bonds[b0 + k], n_types, eacc, bad_type, 0);
+        if (q < kNQ) {
+            const int part = q == kQHBX ? 1 : (q == kQHBX0 ? 2 : 0);
+            eval_deferred<ENERGY>(a, P, q, bq.buf[q][k], eacc, part);
+        } else if (q == kNQ) {
+            eval_deferred<ENERGY>(a, P, kQHBX, bq.buf[kQHBX][k], eacc, 2);
+        } else {
+            eval_bond<ENERGY>(a, P, bond_stage ? bond_stage[k] : a.bonds[b0 + k], n_types, eacc, bad_type, 0);
+        }
     }
 }
 
