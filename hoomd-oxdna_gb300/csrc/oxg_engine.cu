@@ -1250,7 +1250,9 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
         // new or a particle moved half the buffer since they were built)
         const bool first = done == 0;
         if (!first && (rc = checkpoint(s, false))) return rc;
-        OXG_CUDA(cudaEventRecord(s->ev_run[0], s->stream));
+        // the launch's device time (oxg_system_run_timing); host-state runs go untimed
+        const bool timed = hin == nullptr;
+        if (timed) OXG_CUDA(cudaEventRecord(s->ev_run[0], s->stream));
         // the host state goes in with the run start (not on a replay: the checkpoint holds
         // it) and comes back with the closing body
         const bool read_host = first && hin && retries == 0;
@@ -1258,7 +1260,7 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
         if ((rc = launch_run(s, todo, closing, prologue, step0, !s->lists_valid, read_host ? hin : nullptr,
                              closing ? hout : nullptr, reuse)))
             return rc;
-        OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
+        if (timed) OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
         if (s->st_mirror) {  // the launch's last block wrote the status to host memory
             OXG_CUDA(cudaStreamSynchronize(s->stream));
             d = *s->st_host;  // read after the synchronisation (an opaque call)
@@ -1266,7 +1268,7 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
             return rc;
         }
         float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, s->ev_run[0], s->ev_run[1]) == cudaSuccess) {
+        if (timed && cudaEventElapsedTime(&ms, s->ev_run[0], s->ev_run[1]) == cudaSuccess) {
             s->run_kernel_ms += ms;
             s->run_kernel_launches += 1;
             s->run_kernel_bodies += todo;

@@ -299,8 +299,9 @@ int oxg_system_energies(oxg_system* sys, double* pair_energy, double* bonded_ene
  * 3 pair-list entries (long), 4 kernels launched per step. */
 int oxg_system_stats(oxg_system* sys, int64_t* out, int n);
 /* Device time of the persistent run kernel measured with CUDA events around each of its
- * launches on the system's stream: out[0] milliseconds, out[1] launches, out[2] step
- * bodies, accumulated since the last reset (reset != 0 clears after reading). */
+ * launches on the system's stream (those of oxg_system_run; oxg_system_run_host calls
+ * are not timed): out[0] milliseconds, out[1] launches, out[2] step bodies, accumulated
+ * since the last reset (reset != 0 clears after reading). */
 int oxg_system_run_timing(oxg_system* sys, double* out, int n, int reset);
 
 /* ---- learned surrogate of the fused HB + cross-stacking term -------------------
