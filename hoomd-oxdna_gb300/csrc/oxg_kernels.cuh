@@ -45,6 +45,8 @@ struct DevStatus {
     uint32_t qspill;       // run kernel: a block's shared-memory queue overflowed this step
     uint32_t rb[2];        // run kernel: rebuild requests of the next bodies, by body parity
     uint32_t changed;      // run start from host state: it differs from the device state
+    uint32_t spec_far;     // run start: a particle's first step one (taken in the run start's
+                           // pass) moved it half the buffer since the last build
 };
 
 // ------------------------------------------------------------ parameter view
@@ -1855,9 +1857,20 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     // first increment in a block that starts late
     const unsigned long long step_base = a.step0;
     // the stored pair counts and this thread's first short- and long-pair entries, read
-    // once after each list build (they change only there)
-    int ns_known = -1, nl_known = -1;
+    // at the launch's start (issued here, they arrive while the run start works) and
+    // again after each list build (they change only there)
+    int ns_known, nl_known;
     int2 first_pair[2];
+    auto load_known = [&]() {
+        ns_known = (int)min(ld_volatile(&st->n_short), (uint32_t)a.f.cap_short);
+        nl_known = (int)min(ld_volatile(&st->n_long), (uint32_t)a.f.cap_long);
+        first_pair[0] = gwarp * 32 + lane < ns_known ? __ldcg(a.f.pairs_short + gwarp * 32 + lane) : make_int2(0, 0);
+        int v0, vstride;
+        long_units(gwarp, nwarps, ns_known, nl_known, v0, vstride);
+        first_pair[1] = (v0 >= 0 && v0 * 32 + lane < nl_known) ? __ldcg(a.f.pairs_long + v0 * 32 + lane)
+                                                               : make_int2(0, 0);
+    };
+    load_known();
     bool completed = false;  // the launch's last body ran to its end
     // the block's slice of the (constant) bond table, staged once per launch when it fits
     __shared__ int4 bond_stage[kBondStage];
@@ -1871,6 +1884,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             bonds_here = bond_stage;  // read after phase A's first block barrier
         }
     }
+    bool spec_used = false;  // the run start took the first step one in its own pass
     for (int body = a.prologue ? -1 : 0; body < a.bodies; ++body) {
         const bool pro = body < 0;
         bool reuse = pro && a.prologue == 2;  // the last step's forces are this state's
@@ -1887,19 +1901,24 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
             const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
             const bool from_host = HOST_IO && a.prologue == 3;
-            bool far = false, diff = false;
+            // When the force arrays may hold this state's forces (kind 2; kind 3 with
+            // reuse_ok, which is only known once every block has compared its particles),
+            // this pass also takes the first step's step one (a = F/m from those forces),
+            // saving the run start's own step pass and its grid barrier. If the host state
+            // turns out to differ, the pass after the barrier restores the state from the
+            // checkpoint and the run start continues as kind 1 does.
+            const bool spec = a.prologue == 2 || (from_host && a.reuse_ok != 0);
+            bool far = false, diff = false, sfar = false, sbad = false;
             {
                 // the first body's reads into L2 while the run start works (after an idle
                 // period L2 may hold none of them): pair lists, bonds, charges
-                const size_t ns = min(ld_volatile(&st->n_short), (uint32_t)a.f.cap_short);
-                const size_t nl = min(ld_volatile(&st->n_long), (uint32_t)a.f.cap_long);
-                prefetch_l2(a.f.pairs_short, ns * sizeof(int2), gthread, nthreads);
-                prefetch_l2(a.f.pairs_long, nl * sizeof(int2), gthread, nthreads);
+                prefetch_l2(a.f.pairs_short, (size_t)ns_known * sizeof(int2), gthread, nthreads);
+                prefetch_l2(a.f.pairs_long, (size_t)nl_known * sizeof(int2), gthread, nthreads);
                 if (a.f.bonded) prefetch_l2(a.f.bonds, (size_t)a.f.n_bonds * sizeof(int4), gthread, nthreads);
                 if (a.f.charge) prefetch_l2(a.f.charge, (size_t)a.g.N * sizeof(float), gthread, nthreads);
             }
             for (int i = gthread; i < a.g.N; i += nthreads) {
-                float4 v[5];
+                float4 v[5], F = zero, T = zero, r;
                 if (from_host) {
                     // the host's state (mapped memory) into the device arrays; compared
                     // bit for bit with what they held
@@ -1912,6 +1931,11 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                     for (int k = 0; k < 5; ++k) v[k] = a.hin[k][i];
 #pragma unroll
                     for (int k = 0; k < 5; ++k) o[k] = dv[k][i];
+                    r = a.g.pos_ref[i];
+                    if (spec) {
+                        F = __ldcg(a.g.force + i);
+                        T = __ldcg(a.g.torque + i);
+                    }
                     if ((unsigned)__float_as_int(v[0].w) >= (unsigned)P.h().n_types)
                         bad_type = true;  // reported after the run (the kernels skip the particle)
 #pragma unroll
@@ -1928,18 +1952,41 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                     v[2] = a.g.quat[i];
                     v[3] = a.g.vel[i];
                     v[4] = a.g.angmom[i];
+                    r = a.g.pos_ref[i];
+                    if (spec) {
+                        F = __ldcg(a.g.force + i);
+                        T = __ldcg(a.g.torque + i);
+                    }
                 }
 #pragma unroll
                 for (int k = 0; k < 5; ++k) a.ck[k][i] = v[k];
-                if (reuse) continue;  // forces kept; the lists are valid for this state
-                if (!from_host) {     // (from host state: zeroed below once it is known to differ)
+                if (!spec && reuse) continue;  // forces kept; the lists are valid for this state
+                if (!from_host && !spec) {     // (from host state: zeroed below once it is known to differ)
                     a.g.force[i] = zero;
                     a.g.torque[i] = zero;
                 }
-                const float4 r = a.g.pos_ref[i];
-                const float3 d = min_image(mk3(v[0].x - r.x, v[0].y - r.y, v[0].z - r.z), a.g.L, a.g.invL);
-                far |= !(dot(d, d) <= a.g.half_buf2);
+                if (!reuse) {  // the state's own displacement since the last list build
+                    const float3 d = min_image(mk3(v[0].x - r.x, v[0].y - r.y, v[0].z - r.z), a.g.L, a.g.invL);
+                    far |= !(dot(d, d) <= a.g.half_buf2);
+                }
+                if (spec) {
+                    // the first step one (writes the stepped state, zeroes the accumulators)
+                    PState ps;
+                    ps.x = v[0];
+                    ps.xl = v[1];
+                    ps.q = v[2];
+                    ps.v = v[3];
+                    ps.p = v[4];
+                    ps.ref = r;
+                    const float minv = 1.f / ps.v.w;
+                    bool f1 = false, b1 = false;
+                    particle_step_one(a.g, i, ps, make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f),
+                                      make_float4(T.x, T.y, T.z, 0.f), f1, b1);
+                    sfar |= f1;
+                    sbad |= b1;
+                }
             }
+            if (spec && __syncthreads_or(sfar) && threadIdx.x == 0) atomicOr(&st->spec_far, 1u);
             if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->moved, 1u);
             if (from_host && __syncthreads_or(diff) && threadIdx.x == 0) atomicOr(&st->changed, 1u);
             if (!grid_barrier(a.bar)) break;  // the counters above are reset for every block
@@ -1947,17 +1994,32 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 reuse = a.reuse_ok != 0 && ld_volatile(&st->changed) == 0u;  // the same in every block
                 if (!reuse) {
                     for (int i = gthread; i < a.g.N; i += nthreads) {
+                        if (spec) {  // undo the first step one: the state from the checkpoint
+                            a.g.pos[i] = a.ck[0][i];
+                            a.g.pos_lo[i] = a.ck[1][i];
+                            a.g.quat[i] = a.ck[2][i];
+                            a.g.vel[i] = a.ck[3][i];
+                            a.g.angmom[i] = a.ck[4][i];
+                        }
                         a.g.force[i] = zero;
                         a.g.torque[i] = zero;
                     }
                     if (!grid_barrier(a.bar)) break;  // zeroed before any block scatters forces
                 }
             }
+            if (spec && reuse) {
+                // the first step one is done: its forces (body 0) come next; its
+                // displacement test is read there from spec_far
+                if (__syncthreads_or(sbad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
+                spec_used = true;
+                continue;
+            }
             rebuild = !reuse && (a.rebuild0 != 0u || ld_volatile(&st->moved) != 0u);
         } else {
             // rebuild requests: body 0 reads the one left by the run start or the previous
             // launch, body b > 0 the one the step phase of body b - 1 left in rb[b & 1]
             rebuild = ld_volatile(body == 0 ? &st->rebuild : &st->rb[body & 1]) != 0u;
+            if (body == 0 && spec_used) rebuild = rebuild || ld_volatile(&st->spec_far) != 0u;
         }
         if (rebuild) {
             const uint32_t par = ld_volatile(&st->gen) & 1u;
@@ -1973,15 +2035,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             if (!grid_barrier(a.bar)) break;
             if (ld_volatile(&st->flags) & (kStCellOverflow | kStPairOverflow)) break;
         }
-        if (rebuild || ns_known < 0) {
-            ns_known = (int)min(ld_volatile(&st->n_short), (uint32_t)a.f.cap_short);
-            nl_known = (int)min(ld_volatile(&st->n_long), (uint32_t)a.f.cap_long);
-            first_pair[0] = gwarp * 32 + lane < ns_known ? __ldcg(a.f.pairs_short + gwarp * 32 + lane) : make_int2(0, 0);
-            int v0, vstride;
-            long_units(gwarp, nwarps, ns_known, nl_known, v0, vstride);
-            first_pair[1] = (v0 >= 0 && v0 * 32 + lane < nl_known) ? __ldcg(a.f.pairs_long + v0 * 32 + lane)
-                                                                   : make_int2(0, 0);
-        }
+        if (rebuild) load_known();
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             if (rebuild) st->gen += 1u;
             if (!pro) st->step += 1ull;
@@ -2008,8 +2062,16 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
         }
         // every block read this body's rebuild request before the last barrier
         if (blockIdx.x == 0 && threadIdx.x == 0) {
-            if (body == 0) st->rebuild = 0u;
-            else if (body > 0) st->rb[body & 1] = 0u;
+            if (body == 0) {
+                st->rebuild = 0u;
+                st->spec_far = 0u;
+                if (spec_used) {  // the run start's step pass, which clears these, was skipped
+                    st->moved = 0u;
+                    st->changed = 0u;
+                }
+            } else if (body > 0) {
+                st->rb[body & 1] = 0u;
+            }
         }
         // step two of this step (+ step one of the next); at run start a = F/m and
         // step one of the first step

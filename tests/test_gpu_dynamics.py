@@ -203,15 +203,18 @@ def test_state_push_pull_pinned_and_pageable(native):
     assert not np.array_equal(out[0][0], pinned[0])
 
 
+@pytest.mark.parametrize("steps", [1, 4])
 @pytest.mark.parametrize("memory", ["pinned", "pageable"])
-def test_run_state_arrays_matches_push_run_pull(native, memory):
+def test_run_state_arrays_matches_push_run_pull(native, memory, steps):
     """oxg_system_run_host (one call: state in, n steps, state out) against
     push_state_arrays + run + pull_state_arrays on a twin system (same seed and
     timestep): with page-locked arrays the run kernel itself reads the host state at the
     run start (reusing the last step's forces when it equals the device state, as in
-    the second and fourth calls here) and writes the final state back; with pageable
-    arrays the call falls back to the three steps. The first and third calls bring a
-    host-side change of the velocities."""
+    the second and fourth calls here: it then takes the first step one in the same pass
+    as the host read) and writes the final state back; with pageable arrays the call
+    falls back to the three steps. The first and third calls bring a host-side change of
+    the velocities (the step one taken with the host read is undone from the
+    checkpoint)."""
     import torch
     from oxdna import io
     from oxdna.model import dna1, dna2
@@ -236,9 +239,9 @@ def test_run_state_arrays_matches_push_run_pull(native, memory):
         if it == 2:  # another host-side change between calls
             st_a[3][:, :3] *= np.float32(0.9)
             st_b[3][:, :3] *= np.float32(0.9)
-        a.run_state_arrays(4, *st_a)
+        a.run_state_arrays(steps, *st_a)
         b.push_state_arrays(*st_b)
-        b.run(4)
+        b.run(steps)
         b.pull_state_arrays(*st_b)
     assert a.timestep == b.timestep
     for x, y in zip(st_a, st_b):
