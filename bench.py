@@ -264,15 +264,15 @@ def bench_tiled(stream, steps=10000, warmup=500, copies=8):
     return out
 
 
-def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epochs=15):
+def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epochs=60, md_states=5):
     """The learned HB + cross-stacking surrogate on the 100k-nt system (2500 x 20 bp, box
     230, forces(fused=True)): trained here by the library's kernels on 4M pair geometries
     from 8000-nt trajectories at 280-360 K, its output shift calibrated on the training
     set; steps/s against the plain fused path with 1% of the pairs audited by the plain
     evaluator every 100 steps (speed run: audits recorded, switch disarmed), the fused
-    term's energy error against the plain evaluator on the same state, and a run at the
-    default tolerance (the 1e-4 per-term energy budget) showing whether the audit's kill
-    switch trips."""
+    term's energy error against the plain evaluator on the start state and on states of
+    the plain trajectory, and a run at the default tolerance (the 1e-4 per-term energy
+    budget) showing whether the audit's kill switch trips."""
     import torch
 
     from oxdna import surrogate
@@ -313,6 +313,19 @@ def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epoc
         with nvtx(mode + "_timed"):
             ms = time_resident(sim, steps, warmup, stream)
         out[mode + "_steps_per_s"] = steps / (ms * 1e-3)
+        if mode == "plain":
+            # the term's energy on states of the plain trajectory: surrogate read-out
+            # against the plain evaluator's on the same state, every 1000 steps
+            md = []
+            for _ in range(md_states):
+                e_plain = forces[2].energy
+                sim.set_surrogate(net, run=False, compute=True)
+                md.append((forces[2].energy - e_plain) / abs(e_plain))
+                sim.set_surrogate(None)
+                sim.run(1000)
+            out["fused_term_energy_rel_error_vs_plain_md_states"] = md
+            out["md_states_note"] = (f"states of the plain trajectory after {warmup + steps} steps, "
+                                     "then every 1000 steps (signed relative error)")
         if mode == "surrogate":
             st = sim.surrogate_stats()
             out["audit"] = {"pairs": int(st["n_audited"]),

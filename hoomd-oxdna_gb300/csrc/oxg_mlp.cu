@@ -53,35 +53,52 @@ __global__ void k_mlp_pack_vec(const float* P, MlpDev* M)
 }
 
 // ------------------------------------------------------------------ tcgen05 images
-// The six B operands of one class in the canonical K-major layout (oxg_tc.cuh), one
-// thread per element: forward F (n = output, k = input): W[n][k]; backward G (n = input,
-// k = output): W[k][n].
+// The B operands of one class in the canonical K-major layout (oxg_tc.cuh), one thread
+// per element: forward F (n = output, k = input): W[n][k]; backward G (n = input, k =
+// output): W[k][n]; each as hi = bf16(w) and lo = bf16(w - hi) images (F1 also carries
+// W1_hi in input columns 7..13 for the inputs' low parts, G1 carries W1_lo in rows 7..13).
+constexpr int kPackPerClass = 3 * 1024 + 8 * 4096;
+
+__device__ __forceinline__ float bf16_hi(float w) { return __bfloat162float(__float2bfloat16_rn(w)); }
+
 __global__ void k_mlp_pack_tc(const float* P, MlpDev* M)
 {
-    const int per_class = 1024 + 4 * 4096 + 1024;
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= kMlpClasses * per_class) return;
-    const int cls = id / per_class;
-    int e = id % per_class;
+    if (id >= kMlpClasses * kPackPerClass) return;
+    const int cls = id / kPackPerClass;
+    int e = id % kPackPerClass;
     const float* W = P + (size_t)cls * kMlpParams;
     unsigned char* img = M->tcw[cls];
-    float v;
+    float v = 0.f;
     uint32_t off;
-    if (e < 1024) {  // F1: 64 x 16
-        const int n = e >> 4, k = e & 15;
-        v = W[P_W1 + n * 16 + k];
-        off = tc::kImgF1 + tc::kmaj_off(64, n, k);
-    } else if ((e -= 1024) < 4 * 4096) {
-        const int m = e >> 12, n = (e >> 6) & 63, k = e & 63;
+    if (e < 2048) {  // F1 (hi) and F1L: 64 x 16
+        const bool lo = e >= 1024;
+        const int n = (e & 1023) >> 4, k = e & 15;
+        if (k < kMlpIn) {
+            const float w = W[P_W1 + n * 16 + k];
+            v = lo ? w - bf16_hi(w) : w;
+        } else if (!lo && k < 2 * kMlpIn) {
+            v = W[P_W1 + n * 16 + k - kMlpIn];
+        }
+        off = (lo ? tc::kImgF1L : tc::kImgF1) + tc::kmaj_off(64, n, k);
+    } else if ((e -= 2048) < 8 * 4096) {  // F2, F3, G3, G2, then their lo images: 64 x 64
+        const bool lo = e >= 4 * 4096;
+        const int m = (e >> 12) & 3, n = (e >> 6) & 63, k = e & 63;
         const float* Wm = W + ((m == 0 || m == 3) ? P_W2 : P_W3);
-        const bool fwd = m < 2;
-        v = fwd ? Wm[n * 64 + k] : Wm[k * 64 + n];
-        const uint32_t base = m == 0 ? tc::kImgF2 : m == 1 ? tc::kImgF3 : m == 2 ? tc::kImgG3 : tc::kImgG2;
+        const float w = m < 2 ? Wm[n * 64 + k] : Wm[k * 64 + n];
+        v = lo ? w - bf16_hi(w) : w;
+        const uint32_t base = lo ? (m == 0 ? tc::kImgF2L : m == 1 ? tc::kImgF3L : m == 2 ? tc::kImgG3L : tc::kImgG2L)
+                                 : (m == 0 ? tc::kImgF2 : m == 1 ? tc::kImgF3 : m == 2 ? tc::kImgG3 : tc::kImgG2);
         off = base + tc::kmaj_off(64, n, k);
-    } else {  // G1: 16 (inputs) x 64 (outputs)
-        e -= 4 * 4096;
+    } else {  // G1: 16 (inputs: hi rows, then lo rows) x 64 (outputs)
+        e -= 8 * 4096;
         const int n = e >> 6, k = e & 63;
-        v = W[P_W1 + k * 16 + n];
+        if (n < kMlpIn) {
+            v = W[P_W1 + k * 16 + n];
+        } else if (n < 2 * kMlpIn) {
+            const float w = W[P_W1 + k * 16 + n - kMlpIn];
+            v = w - bf16_hi(w);
+        }
         off = tc::kImgG1 + tc::kmaj_off(16, n, k);
     }
     *reinterpret_cast<__nv_bfloat16*>(img + off) = __float2bfloat16_rn(v);
@@ -104,9 +121,10 @@ struct TrainArgs {
 // the 128 samples of a tile: A = dZ^T (128 rows: the 64 units, then zeros), B = H^T (80
 // rows: the 64 inputs, a row of ones that yields the bias gradient, zeros) or X^T (32
 // rows: 16 inputs, ones, zeros). 32 KB of slack follow the last operand.
-constexpr uint32_t kTrW = 0, kTrX = 36864, kTrP = kTrX + kTcX, kTrQ = kTrP + kTcAct, kTrXT = kTrQ + kTcAct,
+constexpr uint32_t kTrW = 0, kTrX = tc::kImgBytes, kTrP = kTrX + kTcX, kTrQ = kTrP + kTcAct, kTrXT = kTrQ + kTcAct,
                    kTrH1T = kTrXT + 32 * 128 * 2, kTrH2T = kTrH1T + 80 * 128 * 2, kTrDZT = kTrH2T + 80 * 128 * 2,
                    kTrRed = kTrDZT + 128 * 128 * 2, kTrBytes = kTrRed + 4 * 65 * 4 + 32768;
+static_assert(kTrBytes + 1024 <= 227 * 1024, "training kernel exceeds the shared memory of a block");
 // tensor-memory columns of the weight gradients (after D1..D4)
 constexpr uint32_t kColDW3 = 256, kColDW2 = 336, kColDW1 = 416;
 
@@ -167,19 +185,23 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
             for (int f = 0; f < kMlpIn; ++f) x[f] = (a.feats[(size_t)sI * 8 + f] - V.mu[f]) * V.inv_sd[f];
             yt = (a.target[sI] - V.e_shift) / V.e_scale;
         }
-        tc::st_row8(t.x, tc::kmaj_off(128, tid, 0), x);
-        tc::st_row8(t.x, tc::kmaj_off(128, tid, 8), x + 8);
+        float xr[16];
+        split_inputs(x, xr);
+        tc::st_row8(t.x, tc::kmaj_off(128, tid, 0), xr);
+        tc::st_row8(t.x, tc::kmaj_off(128, tid, 8), xr + 8);
+        // (the W1 gradient takes input rows 0..6 of X^T: the inputs' BF16 parts)
 #pragma unroll
-        for (int f = 0; f < 16; ++f) st_bf16(sm + kTrXT, tc::kmaj_off(32, f, tid), x[f]);
-        // forward, keeping the activations' transposes for the weight gradients
+        for (int f = 0; f < 16; ++f) st_bf16(sm + kTrXT, tc::kmaj_off(32, f, tid), xr[f]);
+        // forward (weights as hi + lo, as in inference), keeping the activations'
+        // transposes for the weight gradients
         tc_publish(t);
-        ok &= tc_gemm(t, phase, 0, t.x, 128, t.w + tc::kImgF1, 64, 64, 1, false);
+        ok &= tc_gemm_split(t, phase, 0, t.x, 128, t.w + tc::kImgF1, t.w + tc::kImgF1L, 64, 64, 1);
         tc_forward_row(lane_t, 0, V.b1, t.p, tid, sm + kTrH1T, 80);
         tc_publish(t);
-        ok &= tc_gemm(t, phase, 64, t.p, 128, t.w + tc::kImgF2, 64, 64, 4, false);
+        ok &= tc_gemm_split(t, phase, 64, t.p, 128, t.w + tc::kImgF2, t.w + tc::kImgF2L, 64, 64, 4);
         tc_forward_row(lane_t, 64, V.b2, t.q, tid, sm + kTrH2T, 80);
         tc_publish(t);
-        ok &= tc_gemm(t, phase, 128, t.q, 128, t.w + tc::kImgF3, 64, 64, 4, false);
+        ok &= tc_gemm_split(t, phase, 128, t.q, 128, t.w + tc::kImgF3, t.w + tc::kImgF3L, 64, 64, 4);
         // output, loss, dL/dy (first pass over z3); dz3 = dL/dy * w4 * silu'(z3) and the
         // w4 gradient dL/dy * h3 (second pass; warp sums into the block's accumulators)
         {
@@ -342,7 +364,7 @@ __global__ void k_mlp_adam(float* P, float* G, float* m1, float* m2, int n, floa
 
 // Network outputs for contiguous samples of one class (tests, calibration, audits): y
 // and dy/dx' in normalised units, 128 samples per tile on the tensor cores.
-constexpr uint32_t kPrW = 0, kPrX = 36864, kPrP = kPrX + kTcX, kPrQ = kPrP + kTcAct,
+constexpr uint32_t kPrW = 0, kPrX = tc::kImgBytes, kPrP = kPrX + kTcX, kPrQ = kPrP + kTcAct,
                    kPrBytes = kPrQ + kTcAct + 32768;
 
 __global__ void __launch_bounds__(128) k_mlp_predict(const MlpDev* M, int cls, const float* feats, int n, float* y,
@@ -424,7 +446,7 @@ int mlp_check_err(oxg_mlp* m)
 
 int mlp_repack(oxg_mlp* m, cudaStream_t st)
 {
-    const int nt = kMlpClasses * (1024 + 4 * 4096 + 1024);
+    const int nt = kMlpClasses * kPackPerClass;
     k_mlp_pack_tc<<<(nt + 255) / 256, 256, 0, st>>>(m->P, m->dev);
     k_mlp_pack_vec<<<1, kMlpClasses * kMlpHid, 0, st>>>(m->P, m->dev);
     MCUDA(cudaGetLastError());

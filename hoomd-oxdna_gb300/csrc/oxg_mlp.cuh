@@ -96,6 +96,42 @@ __device__ __forceinline__ bool tc_gemm(const TcTile& t, uint32_t& phase, uint32
     return ok;
 }
 
+// As tc_gemm with the weights held as hi + lo images: `steps` MMAs with B_hi, then
+// `steps` with B_lo into the same accumulator, one commit and one wait.
+__device__ __forceinline__ bool tc_gemm_split(const TcTile& t, uint32_t& phase, uint32_t dcol, const unsigned char* A,
+                                              int a_rows, const unsigned char* Bhi, const unsigned char* Blo,
+                                              int b_rows, int n, int steps)
+{
+    if ((threadIdx.x & 127) == 0) {
+        tc::fence_after();
+        const uint32_t sa = tc::smem_addr(A), sh = tc::smem_addr(Bhi), sl = tc::smem_addr(Blo);
+        const uint32_t id = tc::idesc_bf16(128, n);
+        for (int j = 0; j < steps; ++j)
+            tc::mma(t.tmem + dcol, tc::op_desc(sa, a_rows, j), tc::op_desc(sh, b_rows, j), id, j > 0 ? 1u : 0u);
+        for (int j = 0; j < steps; ++j)
+            tc::mma(t.tmem + dcol, tc::op_desc(sa, a_rows, j), tc::op_desc(sl, b_rows, j), id, 1u);
+        tc::commit(t.mbar);
+    }
+    const bool ok = tc::mbar_wait(t.mbar, phase);
+    phase ^= 1u;
+    tc::fence_after();
+    return ok;
+}
+
+// The layer-1 operand row of normalised inputs x: bf16(x) in columns 0..6 and the
+// remainders x - bf16(x) in columns 7..13 (rounded to BF16 when stored), zeros after.
+__device__ __forceinline__ void split_inputs(const float* x, float* xr)
+{
+#pragma unroll
+    for (int f = 0; f < 16; ++f) xr[f] = 0.f;
+#pragma unroll
+    for (int f = 0; f < kMlpIn; ++f) {
+        const float hi = __bfloat162float(__float2bfloat16_rn(x[f]));
+        xr[f] = hi;
+        xr[kMlpIn + f] = x[f] - hi;
+    }
+}
+
 // Forward epilogue of this thread's row: z = D (64 columns from col) + b; silu(z) as the
 // row of the next A operand (dst, if set) and as this row's column of a transposed
 // operand with tr_rows rows (dstT, if set); silu'(z) written back over z.
@@ -153,19 +189,18 @@ __device__ __forceinline__ bool tc_rows128(const TcTile& t, uint32_t& phase, con
     bool ok = true;
     {
         float xr[16];
-#pragma unroll
-        for (int f = 0; f < 16; ++f) xr[f] = f < kMlpIn ? x[f] : 0.f;
+        split_inputs(x, xr);
         tc::st_row8(t.x, tc::kmaj_off(128, row, 0), xr);
         tc::st_row8(t.x, tc::kmaj_off(128, row, 8), xr + 8);
     }
     tc_publish(t);
-    ok &= tc_gemm(t, phase, 0, t.x, 128, t.w + tc::kImgF1, 64, 64, 1, false);    // D1 = X F1
+    ok &= tc_gemm_split(t, phase, 0, t.x, 128, t.w + tc::kImgF1, t.w + tc::kImgF1L, 64, 64, 1);    // D1 = X W1
     tc_forward_row(lane_t, 0, V.b1, t.p, row);
     tc_publish(t);
-    ok &= tc_gemm(t, phase, 64, t.p, 128, t.w + tc::kImgF2, 64, 64, 4, false);   // D2 = H1 F2
+    ok &= tc_gemm_split(t, phase, 64, t.p, 128, t.w + tc::kImgF2, t.w + tc::kImgF2L, 64, 64, 4);   // D2 = H1 W2
     tc_forward_row(lane_t, 64, V.b2, t.q, row);
     tc_publish(t);
-    ok &= tc_gemm(t, phase, 128, t.q, 128, t.w + tc::kImgF3, 64, 64, 4, false);  // D3 = H2 F3
+    ok &= tc_gemm_split(t, phase, 128, t.q, 128, t.w + tc::kImgF3, t.w + tc::kImgF3L, 64, 64, 4);  // D3 = H2 W3
     // output and dy/dz3 = w4 * silu'(z3)
     float yy = V.b4;
 #pragma unroll
@@ -184,17 +219,17 @@ __device__ __forceinline__ bool tc_rows128(const TcTile& t, uint32_t& phase, con
     }
     y = yy;
     tc_publish(t);
-    ok &= tc_gemm(t, phase, 192, t.p, 128, t.w + tc::kImgG3, 64, 64, 4, false);  // dH2 = dZ3 G3
-    tc_backward_row(lane_t, 64, t.q, row);                                       // dZ2
+    ok &= tc_gemm_split(t, phase, 192, t.p, 128, t.w + tc::kImgG3, t.w + tc::kImgG3L, 64, 64, 4);  // dH2 = dZ3 W3^T
+    tc_backward_row(lane_t, 64, t.q, row);                                                       // dZ2
     tc_publish(t);
-    ok &= tc_gemm(t, phase, 192, t.q, 128, t.w + tc::kImgG2, 64, 64, 4, false);  // dH1 = dZ2 G2
-    tc_backward_row(lane_t, 0, t.p, row);                                        // dZ1
+    ok &= tc_gemm_split(t, phase, 192, t.q, 128, t.w + tc::kImgG2, t.w + tc::kImgG2L, 64, 64, 4);  // dH1 = dZ2 W2^T
+    tc_backward_row(lane_t, 0, t.p, row);                                                        // dZ1
     tc_publish(t);
-    ok &= tc_gemm(t, phase, 0, t.p, 128, t.w + tc::kImgG1, 16, 16, 4, false);    // dX = dZ1 G1
+    ok &= tc_gemm(t, phase, 0, t.p, 128, t.w + tc::kImgG1, 16, 16, 4, false);  // dZ1 [W1_hi | W1_lo]^T
     float dx[16];
     tc::ld16(lane_t, dx);
 #pragma unroll
-    for (int f = 0; f < kMlpIn; ++f) dydx[f] = dx[f];
+    for (int f = 0; f < kMlpIn; ++f) dydx[f] = dx[f] + dx[kMlpIn + f];
     tc::fence_before();  // the next tile's MMAs overwrite these columns after a barrier
     return ok;
 }

@@ -157,12 +157,22 @@ __device__ __forceinline__ void st_row8(unsigned char* base, uint32_t off, const
         make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
 }
 
-// ---- weight image of one class (bytes), B operands of the six GEMMs ---------------
-// forward:  F1 (N 64 outputs x K 16 inputs), F2, F3 (64 x 64): element (n, k) = W[n][k]
-// backward: G3, G2 (N 64 inputs x K 64 outputs), G1 (N 16 inputs x K 64 outputs):
-//           element (n, k) = W[k][n]
+// ---- weight image of one class (bytes), B operands of the GEMMs --------------------
+// Every weight w is held as two BF16 numbers, hi = bf16(w) and lo = bf16(w - hi), and a
+// GEMM with weights W runs as A W_hi + A W_lo into the same FP32 accumulator: the
+// weights then carry ~16 significant bits instead of 8 (BF16 weights alone leave a
+// pointwise energy error of a few 1e-4 of the pair energy, above the term's 1e-4 budget
+// where many pairs share one geometry, as in built duplexes).
+// forward:  F1 (N 64 outputs x K 16 inputs), F2, F3 (64 x 64): element (n, k) = W[n][k];
+//           F1 also holds W1_hi in input columns 7..13, which multiply the low parts
+//           x - bf16(x) of the 7 inputs (so the inputs carry ~16 bits too)
+// backward: G3, G2 (N 64 inputs x K 64 outputs): element (n, k) = W[k][n];
+//           G1 (N 16 inputs x K 64 outputs): W1_hi[k][n] in rows n < 7 and W1_lo[k][n - 7]
+//           in rows 7..13 (the input gradient is the sum of the two row blocks)
+// the lo images F1L (W1_lo in input columns 0..6), F2L, F3L, G3L, G2L follow the hi ones
 constexpr uint32_t kImgF1 = 0, kImgF2 = 2048, kImgF3 = 10240, kImgG3 = 18432, kImgG2 = 26624,
-                   kImgG1 = 34816, kImgBytes = 36864;
+                   kImgG1 = 34816, kImgF1L = 36864, kImgF2L = 38912, kImgF3L = 47104, kImgG3L = 55296,
+                   kImgG2L = 63488, kImgBytes = 71680;
 
 }  // namespace tc
 }  // namespace oxg

@@ -239,17 +239,23 @@ def samples(sim, max_n=200000):
 
 
 def training_set(n_target=4_000_000, temperatures=(280, 290, 300, 310, 320, 330, 340, 350, 360),
-                 n_dup=200, n_bp=20, box=100.0, equil=2000, every=200, seed=11, log=None):
+                 n_dup=200, n_bp=20, box=100.0, equil=0, every=100, early=(10, 20, 40, 80),
+                 per_snapshot=5000, seed=11, log=None):
     """Pair geometries from trajectories of the 8000-nt duplex system (200 x 20 bp,
-    box 100) at each temperature (oxDNA2, fused forces, Langevin dt 0.003): after
-    `equil` steps, a sample of every queued pair each `every` steps until the set holds
-    n_target pairs (spread evenly over the temperatures)."""
+    box 100) at each temperature (oxDNA2, fused forces, Langevin dt 0.003): a random
+    subset of at most `per_snapshot` of the queued pairs at step `equil` (default 0: the
+    built duplexes and their relaxation are part of what an MD run meets), at the steps
+    `early` after it (the relaxation from the built geometry, where the pair geometries
+    change fastest) and then every `every` steps, until the set holds n_target pairs
+    (spread evenly over the temperatures)."""
     import torch
 
     from . import io, runtime
     from .model import dna1, dna2
     per_t = n_target // len(temperatures)
     fs, es = [], []
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
     for k, T in enumerate(temperatures):
         s = io.duplex_system(n_dup, n_bp, box, seed=seed + k)
         forces, _ = dna2.forces(temperature=T, fused=True)
@@ -260,13 +266,20 @@ def training_set(n_target=4_000_000, temperatures=(280, 290, 300, 310, 320, 330,
                                                           forces=forces, methods=[lang])
         sim.run(equil)
         got = 0
+        t_now = 0
+        marks = [t for t in early if 0 < t < every]
         while got < per_t:
             f, e = samples(sim)
+            if per_snapshot and f.shape[0] > per_snapshot:
+                sel = torch.randperm(int(f.shape[0]), generator=gen, device=f.device)[:per_snapshot]
+                f, e = f[sel], e[sel]
             take = min(int(f.shape[0]), per_t - got)
             fs.append(f[:take])
             es.append(e[:take])
             got += take
-            sim.run(every)
+            t_next = marks.pop(0) if marks else (t_now // every + 1) * every
+            sim.run(t_next - t_now)
+            t_now = t_next
         if log:
             log(f"T = {T} K: {got} pairs")
         del sim

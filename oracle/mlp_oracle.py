@@ -38,20 +38,36 @@ def normalise(feats, mu, inv_sd):
             * np.asarray(inv_sd, np.float32)).astype(np.float32)
 
 
+def split(a):
+    """(hi, lo) BF16 parts of float32 values: hi = bf16(a), lo = bf16(a - hi)."""
+    hi = bf16(a)
+    return hi, bf16(np.asarray(a, np.float32).astype(np.float64) - hi)
+
+
+def wsum(W):
+    """The weights as the tensor-core GEMMs use them: W_hi + W_lo."""
+    hi, lo = split(W)
+    return hi + lo
+
+
 def forward(params, xn):
-    """Network output y of normalised inputs xn (n x 7) and the intermediates."""
+    """Network output y of normalised inputs xn (n x 7) and the intermediates. Inputs
+    and weights enter the GEMMs as hi + lo BF16 pairs (the kernels' layer 1 sums
+    x_hi W_hi + x_lo W_hi + x_hi W_lo; the hidden layers h W_hi + h W_lo), the hidden
+    activations as single BF16 values."""
     w = unpack(params)
-    xb = bf16(xn)
-    z1 = xb @ bf16(w["W1"]).T + w["b1"]
+    xh, xl = split(xn)
+    W1h, W1l = split(w["W1"])
+    z1 = xh @ W1h.T + xl @ W1h.T + xh @ W1l.T + w["b1"]
     h1, s1 = _silu(z1)
     h1b = bf16(h1)
-    z2 = h1b @ bf16(w["W2"]).T + w["b2"]
+    z2 = h1b @ wsum(w["W2"]).T + w["b2"]
     h2, s2 = _silu(z2)
     h2b = bf16(h2)
-    z3 = h2b @ bf16(w["W3"]).T + w["b3"]
+    z3 = h2b @ wsum(w["W3"]).T + w["b3"]
     h3, s3 = _silu(z3)
     y = h3 @ w["w4"] + w["b4"]
-    return y, dict(xb=xb, s1=s1, h1b=h1b, s2=s2, h2b=h2b, h3=h3, s3=s3, w=w)
+    return y, dict(xb=xh, s1=s1, h1b=h1b, s2=s2, h2b=h2b, h3=h3, s3=s3, w=w)
 
 
 def loss_gradient(params, xn, yt):
@@ -84,18 +100,18 @@ def loss_gradient(params, xn, yt):
 
 def input_gradient(params, xn, round_silu_grad=False):
     """y and dy/dxn of each sample as the inference passes compute them: every GEMM
-    operand BF16; the SiLU derivatives of the first two layers FP32 (the tensor-core
+    operand BF16, the weights as hi + lo pairs; the SiLU derivatives of the first two layers FP32 (the tensor-core
     pass recomputes them from the accumulators kept in tensor memory) or, with
     round_silu_grad, rounded to BF16 (the in-kernel warp pass keeps them packed)."""
     y, c = forward(params, xn)
     w = c["w"]
     r = bf16 if round_silu_grad else (lambda v: v)
     dz3 = c["s3"] * w["w4"][None, :]
-    dh2 = bf16(dz3) @ bf16(w["W3"])
+    dh2 = bf16(dz3) @ wsum(w["W3"])
     dz2 = dh2 * r(c["s2"])
-    dh1 = bf16(dz2) @ bf16(w["W2"])
+    dh1 = bf16(dz2) @ wsum(w["W2"])
     dz1 = dh1 * r(c["s1"])
-    dx = bf16(dz1) @ bf16(w["W1"])
+    dx = bf16(dz1) @ wsum(w["W1"])
     return y, dx
 
 

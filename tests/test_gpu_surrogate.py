@@ -79,11 +79,12 @@ def test_inference_matches_oracle(native):
 
 @pytest.fixture(scope="module")
 def trained():
-    """A network trained on 2M pair geometries the plain evaluator samples along
-    8000-nt duplex trajectories at 280-360 K, with a held-out tenth."""
+    """A network trained (60 epochs) on 4M pair geometries the plain evaluator samples
+    along 8000-nt duplex trajectories at 280-360 K from their built start on, with a
+    held-out tenth (the benchmark's recipe)."""
     import torch
     from oxdna import surrogate
-    f, e = surrogate.training_set(n_target=2_000_000, seed=21)
+    f, e = surrogate.training_set(n_target=4_000_000, seed=21)
     g = torch.Generator(device="cuda")
     g.manual_seed(0)
     perm = torch.randperm(f.shape[0], generator=g, device="cuda")
@@ -92,7 +93,7 @@ def trained():
     net = surrogate.Network(seed=0)
     net.fit_normalization(f[train], e[train])
     rms0 = float(torch.sqrt(((net.energies(f[hold]) - e[hold]) ** 2).mean()))
-    hist = net.train(f[train].contiguous(), e[train].contiguous(), epochs=15, batch=4096, lr=3e-3,
+    hist = net.train(f[train].contiguous(), e[train].contiguous(), epochs=60, batch=4096, lr=3e-3,
                      lr_end=3e-5)
     rms1 = float(torch.sqrt(((net.energies(f[hold]) - e[hold]) ** 2).mean()))
     shifts = net.calibrate(f[train], e[train])
@@ -100,7 +101,7 @@ def trained():
     bias1 = float(d.mean())
     bias1_se = float(d.std()) / np.sqrt(d.numel())
     return dict(net=net, hist=hist, rms0=rms0, rms1=rms1, e_sd=float(e.std()), shifts=shifts,
-                bias1=bias1, bias1_se=bias1_se)
+                bias1=bias1, bias1_se=bias1_se, mean_e=float(e[hold].mean()))
 
 
 def test_training_gains_over_untrained(native, trained):
@@ -127,28 +128,42 @@ def _fused_sim(seed=3, T=300.0):
 
 def test_calibration_leaves_no_mean_error(native, trained):
     """After the output shift fitted on the training set, the held-out mean pair-energy
-    error (what adds up over the term's pairs) is zero within three standard errors."""
-    assert abs(trained["bias1"]) <= 3.0 * trained["bias1_se"], trained
+    error (what adds up over the term's pairs) is within the 1e-4 budget of the mean pair
+    energy. (Pairs of one snapshot are not independent samples, those of a built state
+    share a handful of geometries, so the naive standard error is not the yardstick.)"""
+    assert abs(trained["bias1"]) <= 1e-4 * abs(trained["mean_e"]), trained
 
 
 def test_engine_surrogate_energy_audits_and_kill_switch(native, trained):
-    """Inside the engine: the surrogate's fused-term energy close to the plain one,
-    audits counted during MD with the sampled relative error of the term's energy
-    matching the read-out's, and the kill switch tripping at the default tolerance (the
-    1e-4 budget) for a network whose output is planted 1% off, after which the plain
-    evaluator's result is back."""
+    """Inside the engine, against the 1e-4 per-term energy budget: the surrogate's
+    fused-term energy on the built start state (every base pair at one ideal geometry,
+    so the network's pointwise error there does not average out: within 1e-3); then,
+    once the duplexes have relaxed (500 plain steps), 2000 MD steps driven by the
+    surrogate with audits at the default tolerance: the sampled relative error of the
+    term's energy within the budget (two standard errors), the kill switch not tripped,
+    and the read-out on the final state within 3e-4 (about 1,200 pairs: ~7e-5 of random
+    error is expected); then the switch tripping for a network whose output is planted
+    1% off, after which the plain evaluator's result is back."""
     sim, forces = _fused_sim()
     hbx = forces[2]
     e_plain = hbx.energy
     net = trained["net"]
-    sim.set_surrogate(net, run=True, compute=True, audit_every=10, audit_fraction=0.2, tol=1e9)
+    sim.set_surrogate(net, run=False, compute=True)
     e_sur = hbx.energy
-    assert abs(e_sur - e_plain) < 0.02 * abs(e_plain), (e_sur, e_plain)
-    sim.run(50)
+    assert abs(e_sur - e_plain) < 1e-3 * abs(e_plain), (e_sur, e_plain)
+    sim.set_surrogate(None)
+    sim.run(500)
+    sim.set_surrogate(net, run=True, compute=True, audit_every=10, audit_fraction=0.2)
+    sim.run(2000)
     st = sim.surrogate_stats()
-    assert st["n_audited"] > 0 and st["disabled"] == 0 and st["n_over"] == 0
-    assert st["rms_de"] < 0.1 * st["rms_e"], st
-    assert abs(st["rel_energy_error"]) < 0.02 and st["rel_energy_error_se"] > 0.0, st
+    assert st["n_audited"] > 10000 and st["disabled"] == 0 and st["n_over"] == 0, st
+    assert st["rms_de"] < 0.01 * st["rms_e"], st
+    assert st["rel_energy_error_se"] > 0.0, st
+    assert abs(st["rel_energy_error"]) - 2 * st["rel_energy_error_se"] <= 1e-4, st
+    e_sur = hbx.energy
+    sim.set_surrogate(None)
+    e_plain = hbx.energy
+    assert abs(e_sur - e_plain) < 3e-4 * abs(e_plain), (e_sur, e_plain)
     # kill switch at the default tolerance: the class-1 output planted 1% of the energy
     # spread off (a host-side change of the output shift)
     mu, inv, es, sh = net.norm[1]
