@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -473,6 +475,8 @@ struct oxg_system {
     DevStatus* st = nullptr;
     DevStatus* st_host = nullptr;  // pinned
     DevStatus* st_mirror = nullptr;  // its device alias (the run kernel writes the status there)
+    uint32_t run_seq = 0;            // sequence number of the last run-kernel launch (never 0,
+                                     // unique in the process)
     double* energy = nullptr;      // 9 doubles
     // integrator
     double dt = 0.003, kT = 0.1, gamma = 1.0, gamma_r = 1.0;
@@ -692,6 +696,7 @@ int forces_grid(oxg_system* s)
         s->grid_forces = num_sms() * per_sm;
         // the surrogate kernel's shared memory exceeds the default limit (set here, outside
         // any stream capture)
+        static_assert(surrogate_smem(kParamBlockMax) <= 227 * 1024, "surrogate tile exceeds a block's shared memory");
         const int smem = (int)surrogate_smem(kParamBlockMax);
         cudaFuncSetAttribute(k_surrogate<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         cudaFuncSetAttribute(k_surrogate<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -845,6 +850,7 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
     }
     if (!s->st_host)
         return fail(set_err(OXG_ERR_CUDA, "cudaMallocHost failed"));
+    std::memset(s->st_host, 0, sizeof(DevStatus));  // (page-locked memory may be recycled)
     cudaMemcpy(s->bonds, bnd.data(), sizeof(int4) * bnd.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(s->excl, excl.data(), sizeof(int4) * N, cudaMemcpyHostToDevice);
     cudaMemset(s->st, 0, sizeof(DevStatus));
@@ -1212,11 +1218,46 @@ static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
     }
     ra.reuse_ok = reuse_ok ? 1 : 0;
     ra.st_mirror = s->st_mirror;
+    // a sequence number no other launch of the process had (never 0), and the mirror's
+    // word cleared before the launch: a stale word never reads as this launch's end
+    static std::atomic<uint32_t> seq_counter{0};
+    uint32_t seq;
+    do seq = seq_counter.fetch_add(1u) + 1u;
+    while (seq == 0u);
+    s->run_seq = seq;
+    ra.seq = seq;
+    if (s->st_host) *reinterpret_cast<volatile uint32_t*>(&s->st_host->seq) = 0u;
     // the barrier word needs no reset between launches: every completed barrier adds
     // exactly 2^31 (it is cleared at allocation and after a launch that gave up)
     void* kargs[] = {&ra};
     OXG_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kRunThreads), kargs, (size_t)block_bytes, s->stream));
     return OXG_OK;
+}
+
+// The end of a run-kernel launch as the host sees it: its last block stores the status,
+// then the launch's sequence number, into page-locked host memory (system-scope fences
+// between, and after every block's host-array writes). Spinning on that word returns a
+// few microseconds before a stream synchronisation would. Gives up after 2 ms (a longer
+// launch, or one that failed before its end); the caller then synchronises the stream,
+// which also reports any launch error.
+static bool wait_mirror(const oxg_system* s)
+{
+    const volatile uint32_t* seq = &s->st_host->seq;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (long k = 1;; ++k) {
+        if (*seq == s->run_seq) {
+            std::atomic_thread_fence(std::memory_order_acquire);
+            return true;
+        }
+        if ((k & 1023) == 0 && std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(2)) return false;
+    }
+}
+
+static void copy_mirror(const oxg_system* s, DevStatus* d)
+{
+    const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(s->st_host);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(d);
+    for (int k = 0; k < (int)(sizeof(DevStatus) / sizeof(uint32_t)); ++k) dst[k] = src[k];
 }
 
 // A run of n steps on the persistent kernel, in launches of up to `chunk` step bodies.
@@ -1262,8 +1303,9 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
             return rc;
         if (timed) OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
         if (s->st_mirror) {  // the launch's last block wrote the status to host memory
-            OXG_CUDA(cudaStreamSynchronize(s->stream));
-            d = *s->st_host;  // read after the synchronisation (an opaque call)
+            // (a timed launch waits for its end event, which the spin does not see)
+            if (timed || !wait_mirror(s)) OXG_CUDA(cudaStreamSynchronize(s->stream));
+            copy_mirror(s, &d);
         } else if ((rc = read_status(s, &d))) {
             return rc;
         }

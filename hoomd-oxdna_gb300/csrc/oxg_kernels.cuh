@@ -13,6 +13,7 @@
 //  k_step_one / k_step_two       Langevin + NO_SQUISH (Miller et al. 2002).
 #pragma once
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "oxg_device.cuh"
@@ -47,6 +48,8 @@ struct DevStatus {
     uint32_t changed;      // run start from host state: it differs from the device state
     uint32_t spec_far;     // run start: a particle's first step one (taken in the run start's
                            // pass) moved it half the buffer since the last build
+    uint32_t seq;          // host-mapped copy only: the sequence number of the launch that
+                           // wrote it, stored after every other word (never set on the device)
 };
 
 // ------------------------------------------------------------ parameter view
@@ -1813,6 +1816,7 @@ struct RunArgs {
     int reuse_ok;              // kind 3: the force arrays hold the device state's forces
     DevStatus* st_mirror;      // host-mapped copy of the status written by the last block
                                // to leave (null: the host copies the status itself)
+    uint32_t seq;              // this launch's sequence number, stored last into st_mirror->seq
 };
 
 
@@ -2132,7 +2136,12 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     // part by then, so the last body needs no grid barrier of its own — and it mirrors
     // the final status into host memory, so the host reads it without a copy of its own
     if (threadIdx.x == 0) {
-        __threadfence();
+        // a launch that wrote host arrays orders them (its block's writes, by the barrier
+        // above) before its arrival at the system scope: the host, once it sees the
+        // launch's sequence number in the status mirror, reads them without waiting for
+        // the launch to retire
+        if (HOST_IO && a.hout[0]) __threadfence_system();
+        else __threadfence();
         if (atomicAdd(&a.bar->exits, 1u) == gridDim.x - 1u) {
             __threadfence();
             if (completed) {  // the same in every block (all complete, or all left early)
@@ -2143,7 +2152,10 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             if (a.st_mirror) {
                 const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(st);
                 volatile uint32_t* dst = reinterpret_cast<volatile uint32_t*>(a.st_mirror);
-                for (int k = 0; k < (int)(sizeof(DevStatus) / sizeof(uint32_t)); ++k) dst[k] = src[k];
+                constexpr int kSeqWord = (int)(offsetof(DevStatus, seq) / sizeof(uint32_t));
+                for (int k = 0; k < kSeqWord; ++k) dst[k] = src[k];
+                __threadfence_system();
+                dst[kSeqWord] = a.seq;  // after every other word
                 __threadfence_system();
             }
             a.bar->exits = 0u;
