@@ -245,14 +245,14 @@ struct ForceArgs {
 // kill switch the force kernels read. The audited pairs are a hashed sample of the
 // term's pairs, so sum_de / sum_e estimates the relative error of the term's energy;
 // the switch trips when that estimate exceeds the tolerance by more than two standard
-// errors (at least kAuditMinPairs audited pairs): the audit sets `pending`, and the
-// next step's forces A turns it into `disabled`, so every kernel of a step sees the
-// same switch.
+// errors (at least kAuditMinPairs audited pairs), tested by the next step's forces A
+// (audit_decide below), which sets `disabled`, so every kernel of a step sees the same
+// switch.
 struct SurrogateAudit {
-    uint32_t disabled;           // read by the force kernels; set from `pending` at a step start
+    uint32_t disabled;           // read by the force kernels; set at a step start
     uint32_t n_audited;
-    uint32_t n_over;             // audits at which the test failed (the switch tripped)
-    uint32_t pending;            // the test failed during this step
+    uint32_t n_over;             // step starts at which the test failed (at most 1)
+    uint32_t pending;            // the test has failed
     double sum_sq_de, sum_sq_e;  // pair energy error and reference
     double sum_sq_df, sum_sq_f;  // force (on i) error and reference
     double sum_de, sum_e;        // signed sums of the pair energy error and reference
@@ -260,6 +260,29 @@ struct SurrogateAudit {
     float pad2[2];
 };
 constexpr uint32_t kAuditMinPairs = 100;
+
+// The kill switch, decided at a step start (block 0 of the step's first kernel, so that
+// every kernel of the step sees one value) from the complete sums of every audit so far:
+// the sampled relative error of the term's energy above the tolerance by more than two
+// standard errors, over at least kAuditMinPairs pairs (a NaN trips it too). Testing the
+// running sums after each audited pair instead tripped on partial samples: pairs are
+// audited in queue order, class by class, and the first hundreds of one class carry that
+// class's error against its own smaller energy sum.
+__device__ __forceinline__ void audit_decide(SurrogateAudit* au, float tol)
+{
+    if (au->disabled) return;
+    const uint32_t n = au->n_audited;
+    const double se = au->sum_e;
+    if (n < kAuditMinPairs || se == 0.0) return;
+    const double mean = au->sum_de / n;
+    const double se_rel = sqrt(fmax(au->sum_sq_de / n - mean * mean, 0.0) * n) / fabs(se);
+    const double rel = fabs(au->sum_de) / fabs(se);
+    if (!(rel - 2.0 * se_rel <= (double)tol)) {
+        au->disabled = 1u;
+        au->pending = 1u;
+        au->n_over += 1u;
+    }
+}
 
 // The force evaluation is split in two launches so that the acos-heavy terms run with
 // every lane busy (whatever the system size):
@@ -652,8 +675,8 @@ __global__ void __launch_bounds__(256) k_forces_a(ForceArgs a)
             a.st_rw->gen += 1u;
         }
         if (a.advance_step) a.st_rw->step += 1ull;
-        // a failed surrogate audit of the last step switches the surrogate off from here
-        if (a.audit && ld_volatile(&a.audit->pending)) a.audit->disabled = 1u;
+        // the audits so far decide whether the surrogate stays on for this step
+        if (a.audit) audit_decide(a.audit, a.audit_tol);
     }
     double eacc[kNTerms + 3];
 #pragma unroll
@@ -683,26 +706,16 @@ static __device__ __noinline__ void surrogate_audit(const ForceArgs& a, const Pa
     const float3 df = acc_sur.fi - pa.fi;
     const float df2 = dot(df, df);
     SurrogateAudit* au = a.audit;
-    // the running sums including this pair (each field read as it was updated)
-    const uint32_t n = atomicAdd(&au->n_audited, 1u) + 1u;
-    const double sq = atomicAdd(&au->sum_sq_de, (double)de * de) + (double)de * de;
+    atomicAdd(&au->n_audited, 1u);
+    atomicAdd(&au->sum_sq_de, (double)de * de);
     atomicAdd(&au->sum_sq_e, (double)e * e);
     atomicAdd(&au->sum_sq_df, (double)df2);
     atomicAdd(&au->sum_sq_f, (double)dot(pa.fi, pa.fi));
-    const double sde = atomicAdd(&au->sum_de, (double)de) + (double)de;
-    const double se = atomicAdd(&au->sum_e, (double)e) + (double)e;
+    atomicAdd(&au->sum_de, (double)de);
+    atomicAdd(&au->sum_e, (double)e);
     // non-negative floats order like their bit patterns
     atomicMax(reinterpret_cast<int*>(&au->max_abs_de), __float_as_int(fabsf(de)));
     atomicMax(reinterpret_cast<int*>(&au->max_abs_df), __float_as_int(sqrtf(df2)));
-    // kill switch: the sampled relative error of the term's energy over the tolerance by
-    // more than two standard errors (NaN errors trip it too)
-    if (n >= kAuditMinPairs && fabs(se) > 0.0) {
-        const double mean = sde / n;
-        const double se_rel = sqrt(fmax(sq / n - mean * mean, 0.0) * n) / fabs(se);
-        const double rel = fabs(sde) / fabs(se);
-        if (!(rel - 2.0 * se_rel <= (double)a.audit_tol) && atomicExch(&au->pending, 1u) == 0u)
-            atomicAdd(&au->n_over, 1u);
-    }
 }
 
 __device__ __forceinline__ bool audit_pick(int k, unsigned long long step, uint32_t mod)
