@@ -477,6 +477,15 @@ struct oxg_system {
     DevStatus* st_mirror = nullptr;  // its device alias (the run kernel writes the status there)
     uint32_t run_seq = 0;            // sequence number of the last run-kernel launch (never 0,
                                      // unique in the process)
+    // host session (oxg_system_set_host_session): the request block (page-locked, mapped),
+    // the idle time, whether a run kernel is resident and the parameter version it staged
+    HostRequest* req_host = nullptr;
+    HostRequest* req_dev = nullptr;
+    int session_idle_us = 0;
+    bool resident = false;
+    uint32_t resident_version = 0;
+    int64_t session_served = 0;      // host-state runs served by a resident kernel
+    int64_t run_launches = 0;        // launches of the run kernel
     double* energy = nullptr;      // 9 doubles
     // integrator
     double dt = 0.003, kT = 0.1, gamma = 1.0, gamma_r = 1.0;
@@ -520,6 +529,11 @@ struct oxg_system {
     // stats
     long long steps_run = 0;
 };
+
+// (defined with the run path below; every system entry point ends a host session first)
+extern "C" {
+static int end_session(oxg_system* s);
+}
 
 namespace {
 
@@ -877,6 +891,8 @@ int oxg_system_create(oxg_system** out, oxg_context* ctx, int N, const float box
 int oxg_system_destroy(oxg_system* s)
 {
     if (!s) return OXG_OK;
+    end_session(s);
+    if (s->req_host) cudaFreeHost(s->req_host);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     dfree(s->pos); dfree(s->pos_lo); dfree(s->ck_pos_lo); dfree(s->quat); dfree(s->vel); dfree(s->angmom); dfree(s->accel);
     dfree(s->tnet); dfree(s->pos_ref); dfree(s->force); dfree(s->torque); dfree(s->charge);
@@ -980,6 +996,7 @@ extern "C" {
 int oxg_system_set_stream(oxg_system* s, void* stream)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     s->stream = (cudaStream_t)stream;
     s->graph_key = ~0ull;
     return OXG_OK;
@@ -990,6 +1007,7 @@ int oxg_system_set_state(oxg_system* s, const float* pos_type, const float* pos_
                          const float* charge)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     s->forces_current = false;  // the next run start evaluates the forces again
     const size_t b4 = sizeof(float4) * s->N;
     if (pos_type) {
@@ -1012,6 +1030,7 @@ int oxg_system_get_state(oxg_system* s, float* pos_type, float* pos_lo, float* q
                          float* angmom)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     const float* const host[5] = {pos_type, pos_lo, quat, vel, angmom};
     float4* const dev[5] = {s->pos, s->pos_lo, s->quat, s->vel, s->angmom};
     return state_transfer(s, host, dev, false);
@@ -1021,6 +1040,7 @@ int oxg_system_device_state(oxg_system* s, float** pos_type, float** pos_lo, flo
                             float** vel, float** angmom, float** charge)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     s->forces_current = false;  // the caller may write the state through these pointers
     if (pos_type) *pos_type = reinterpret_cast<float*>(s->pos);
     if (pos_lo) *pos_lo = reinterpret_cast<float*>(s->pos_lo);
@@ -1034,6 +1054,7 @@ int oxg_system_device_state(oxg_system* s, float** pos_type, float** pos_lo, flo
 int oxg_system_set_nlist_buffer(oxg_system* s, double buffer)
 {
     if (!s || !(buffer >= 0.0)) return set_err(OXG_ERR_INVALID_ARG, "bad buffer");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     s->buffer = buffer;
     s->nlist_version = ~0ull;
     return OXG_OK;
@@ -1042,6 +1063,7 @@ int oxg_system_set_nlist_buffer(oxg_system* s, double buffer)
 int oxg_system_set_timestep(oxg_system* s, uint64_t step)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     s->timestep = step;  // the next run's RNG steps continue from here
     return OXG_OK;
 }
@@ -1070,6 +1092,7 @@ int oxg_system_compute(oxg_system* s, uint32_t mask, int bonded, float* force, f
                        double* pair_energy, double* bonded_energy)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     if (mask & ~present_mask(s->ctx)) return set_err(OXG_ERR_NO_PARAMS, "a requested term has no parameters");
     if (bonded)
         for (int t = 0; t < s->ctx->n_bond_types; ++t)
@@ -1092,6 +1115,7 @@ int oxg_system_set_integrator(oxg_system* s, double dt, double kT, double gamma,
 {
     if (!s || !(dt > 0.0) || !(kT >= 0.0) || !(gamma >= 0.0) || !(gamma_r >= 0.0))
         return set_err(OXG_ERR_INVALID_ARG, "bad integrator parameters");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     if (mask & ~present_mask(s->ctx)) return set_err(OXG_ERR_NO_PARAMS, "a requested term has no parameters");
     s->dt = dt;
     s->kT = kT;
@@ -1185,7 +1209,8 @@ static int checkpoint(oxg_system* s, bool restore)
 // by the run start (prepRun) when `prologue` (see k_run).
 static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
                       unsigned long long step0 = 0, bool rebuild0 = false,
-                      const float4* const* hin = nullptr, float4* const* hout = nullptr, bool reuse_ok = false)
+                      const float4* const* hin = nullptr, float4* const* hout = nullptr, bool reuse_ok = false,
+                      bool serve = false)
 {
     const int block_bytes = s->ctx->block_bytes;
     RunArgs ra;
@@ -1227,6 +1252,12 @@ static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
     s->run_seq = seq;
     ra.seq = seq;
     if (s->st_host) *reinterpret_cast<volatile uint32_t*>(&s->st_host->seq) = 0u;
+    ra.req = serve ? s->req_dev : nullptr;
+    ra.idle_ns = (unsigned long long)std::max(s->session_idle_us, 0) * 1000ull;
+    if (serve) {  // no request pending: the kernel waits for the next sequence number
+        s->req_host->quit = 0u;
+        __atomic_store_n(&s->req_host->seq, 0u, __ATOMIC_RELEASE);
+    }
     // the barrier word needs no reset between launches: every completed barrier adds
     // exactly 2^31 (it is cleared at allocation and after a launch that gave up)
     void* kargs[] = {&ra};
@@ -1258,6 +1289,61 @@ static void copy_mirror(const oxg_system* s, DevStatus* d)
     const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(s->st_host);
     uint32_t* dst = reinterpret_cast<uint32_t*>(d);
     for (int k = 0; k < (int)(sizeof(DevStatus) / sizeof(uint32_t)); ++k) dst[k] = src[k];
+}
+
+static uint32_t next_seq()
+{
+    static std::atomic<uint32_t> counter{0};
+    uint32_t seq;
+    do seq = counter.fetch_add(1u) + 1u;
+    while (seq == 0u);
+    return seq;
+}
+
+// A host session's request to the resident run kernel: the run's parameters, then its
+// sequence number (a release store). Returns true once the status mirror shows the run's
+// end, false if the kernel had left (idle time out) or failed before it took the request
+// (the caller then synchronises the stream and launches).
+static bool post_request(oxg_system* s, int bodies, unsigned long long step0, const float4* const* hin,
+                         float4* const* hout, bool reuse_ok)
+{
+    HostRequest* r = s->req_host;
+    r->quit = 0u;
+    r->bodies = bodies;
+    r->reuse_ok = reuse_ok ? 1 : 0;
+    r->step0 = step0;
+    for (int k = 0; k < 5; ++k) {
+        r->hin[k] = hin[k];
+        r->hout[k] = hout[k];
+    }
+    const uint32_t seq = next_seq();
+    s->run_seq = seq;
+    __atomic_store_n(&r->seq, seq, __ATOMIC_RELEASE);
+    const volatile uint32_t* done = &s->st_host->seq;
+    for (long k = 1;; ++k) {
+        if (*done == seq) {
+            std::atomic_thread_fence(std::memory_order_acquire);
+            return true;
+        }
+        if ((k & 1023) == 0 && cudaStreamQuery(s->stream) != cudaErrorNotReady) {
+            const bool ok = *done == seq;  // it may have ended the run just before leaving
+            std::atomic_thread_fence(std::memory_order_acquire);
+            return ok;
+        }
+    }
+}
+
+// Ends a host session's resident kernel (a quit request; the kernel leaves at its next
+// poll of the request word, or has left already) and waits for it. Every entry point that
+// touches the system's device state, other than a served host-state run, calls this.
+static int end_session(oxg_system* s)
+{
+    if (!s || !s->resident) return OXG_OK;
+    s->resident = false;
+    s->req_host->quit = 1u;
+    __atomic_store_n(&s->req_host->seq, next_seq(), __ATOMIC_RELEASE);
+    OXG_CUDA(cudaStreamSynchronize(s->stream));
+    return OXG_OK;
 }
 
 // A run of n steps on the persistent kernel, in launches of up to `chunk` step bodies.
@@ -1298,17 +1384,44 @@ static int run_persistent(oxg_system* s, long nsteps, const float4* const* hin =
         // it) and comes back with the closing body
         const bool read_host = first && hin && retries == 0;
         const int prologue = first ? (read_host ? 3 : ((reuse && retries == 0) ? 2 : 1)) : 0;
-        if ((rc = launch_run(s, todo, closing, prologue, step0, !s->lists_valid, read_host ? hin : nullptr,
-                             closing ? hout : nullptr, reuse)))
-            return rc;
-        if (timed) OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
-        if (s->st_mirror) {  // the launch's last block wrote the status to host memory
-            // (a timed launch waits for its end event, which the spin does not see)
-            if (timed || !wait_mirror(s)) OXG_CUDA(cudaStreamSynchronize(s->stream));
-            copy_mirror(s, &d);
-        } else if ((rc = read_status(s, &d))) {
+        // a host session serves one-launch host-state runs with a resident kernel: the
+        // run is posted to it when it is still there (and staged the current parameters)
+        const bool serve = read_host && closing && hout && s->req_host && s->st_mirror && s->session_idle_us > 0;
+        bool served = false;
+        if (serve && s->resident && s->resident_version == s->ctx->version && s->lists_valid) {
+            served = post_request(s, todo, step0, hin, hout, reuse);
+            if (!served) {
+                s->resident = false;
+                OXG_CUDA(cudaStreamSynchronize(s->stream));  // (reports a failed kernel)
+            }
+        } else if ((rc = end_session(s))) {
             return rc;
         }
+        if (served) {
+            copy_mirror(s, &d);
+            s->session_served += 1;
+        } else {
+            s->run_launches += 1;
+            if ((rc = launch_run(s, todo, closing, prologue, step0, !s->lists_valid, read_host ? hin : nullptr,
+                                 closing ? hout : nullptr, reuse, serve)))
+                return rc;
+            if (serve) {
+                s->resident = true;
+                s->resident_version = s->ctx->version;
+            }
+            if (timed) OXG_CUDA(cudaEventRecord(s->ev_run[1], s->stream));
+            if (s->st_mirror) {  // the launch's last block wrote the status to host memory
+                // (a timed launch waits for its end event, which the spin does not see)
+                if (timed || !wait_mirror(s)) OXG_CUDA(cudaStreamSynchronize(s->stream));
+                copy_mirror(s, &d);
+            } else if ((rc = read_status(s, &d))) {
+                return rc;
+            }
+        }
+        // a resident kernel leaves before the host handles a failed or overflowed run
+        if ((d.flags & (kStBarrierTimeout | kStNonFinite | kStBadIndex | kStCellOverflow | kStPairOverflow)) &&
+            (rc = end_session(s)))
+            return rc;
         float ms = 0.f;
         if (timed && cudaEventElapsedTime(&ms, s->ev_run[0], s->ev_run[1]) == cudaSuccess) {
             s->run_kernel_ms += ms;
@@ -1382,6 +1495,7 @@ static bool mapped_state(const float* const host[5], float4* dev[5])
 int oxg_system_run(oxg_system* s, long nsteps)
 {
     if (!s || nsteps < 0) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     if (!s->integ_set) return set_err(OXG_ERR_INVALID_ARG, "integrator not set");
     for (int t = 0; t < s->ctx->n_bond_types && s->run_bonded; ++t)
         if (!s->ctx->bonded_set[t]) return set_err(OXG_ERR_NO_PARAMS, "bond type without parameters");
@@ -1479,6 +1593,7 @@ int oxg_system_run(oxg_system* s, long nsteps)
 int oxg_system_energies(oxg_system* s, double* pair_energy, double* bonded_energy)
 {
     if (!s) return set_err(OXG_ERR_INVALID_ARG, "null system");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     uint32_t mask = s->integ_set ? s->run_mask : present_mask(s->ctx);
     int bonded = s->integ_set ? s->run_bonded : 1;
     return oxg_system_compute(s, mask, bonded, nullptr, nullptr, pair_energy, bonded_energy);
@@ -1529,6 +1644,7 @@ int oxg_system_hbx_samples(oxg_system* s, int max_n, float* feats, float* energy
 {
     if (!s || max_n < 0 || (max_n > 0 && (!feats || !energy)) || !n_out)
         return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     if (!s->ctx->hbx.any) return set_err(OXG_ERR_NO_PARAMS, "no fused HB + cross-stacking parameters");
     s->forces_current = false;  // the sampling evaluation reuses the force arrays
     const uint32_t mask = 1u << kHBCross;
@@ -1584,7 +1700,9 @@ int oxg_system_run_host(oxg_system* s, long nsteps, float* pos_type, float* pos_
     const float* const host[5] = {pos_type, pos_lo, quat, vel, angmom};
     float4* dev[5];
     int rc;
-    if (!s->persistent || !mapped_state(host, dev)) {  // per-call transfers (types checked there)
+    // (MD steps with the surrogate take the per-step path of oxg_system_run)
+    const bool surrogate_md = s->mlp && (s->surr_flags & OXG_SURROGATE_RUN) && ((s->run_mask >> kHBCross) & 1u);
+    if (!s->persistent || surrogate_md || !mapped_state(host, dev)) {  // per-call transfers (types checked there)
         if ((rc = oxg_system_set_state(s, pos_type, pos_lo, quat, vel, angmom, nullptr))) return rc;
         if ((rc = oxg_system_run(s, nsteps))) return rc;
         return oxg_system_get_state(s, pos_type, pos_lo, quat, vel, angmom);
@@ -1595,6 +1713,25 @@ int oxg_system_run_host(oxg_system* s, long nsteps, float* pos_type, float* pos_
     // the run kernel reads the mapped host arrays at its start and writes them in its
     // closing body; run_persistent synchronises after every launch
     return run_persistent(s, nsteps, dev, dev);
+}
+
+int oxg_system_set_host_session(oxg_system* s, int idle_us)
+{
+    if (!s || idle_us < 0 || idle_us > 100000) return set_err(OXG_ERR_INVALID_ARG, "idle time outside [0, 100000] us");
+    if (int rc = end_session(s)) return rc;
+    if (idle_us > 0 && !s->req_host) {
+        if (cudaHostAlloc((void**)&s->req_host, sizeof(HostRequest), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer((void**)&s->req_dev, s->req_host, 0) != cudaSuccess) {
+            cudaGetLastError();
+            if (s->req_host) cudaFreeHost(s->req_host);
+            s->req_host = nullptr;
+            s->req_dev = nullptr;
+            return set_err(OXG_ERR_CUDA, "page-locked request block for the host session");
+        }
+        std::memset(s->req_host, 0, sizeof(HostRequest));
+    }
+    s->session_idle_us = idle_us;
+    return OXG_OK;
 }
 
 int oxg_system_run_timing(oxg_system* s, double* out, int n, int reset)
@@ -1615,6 +1752,7 @@ int oxg_system_set_surrogate(oxg_system* s, const oxg_mlp* mlp, int flags, int a
     if (!s || flags < 0 || flags > (OXG_SURROGATE_RUN | OXG_SURROGATE_COMPUTE) || audit_every < 0 ||
         audit_mod < 1 || !(audit_tol >= 0.0))
         return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     if (mlp && flags && !s->ctx->hbx.any)
         return set_err(OXG_ERR_NO_PARAMS, "the surrogate replaces the fused HB + cross-stacking term, which has no parameters");
     s->mlp = static_cast<const MlpDev*>(internal_mlp_device(mlp));
@@ -1632,6 +1770,7 @@ int oxg_system_set_surrogate(oxg_system* s, const oxg_mlp* mlp, int flags, int a
 int oxg_system_surrogate_stats(oxg_system* s, double* out, int n)
 {
     if (!s || !out) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     SurrogateAudit h;
     OXG_CUDA(cudaMemcpyAsync(&h, s->audit, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
     OXG_CUDA(cudaStreamSynchronize(s->stream));
@@ -1651,11 +1790,13 @@ int oxg_system_surrogate_stats(oxg_system* s, double* out, int n)
 int oxg_system_stats(oxg_system* s, int64_t* out, int n)
 {
     if (!s || !out) return set_err(OXG_ERR_INVALID_ARG, "bad arguments");
+    if (int rc_ = end_session(s)) return rc_;  // a resident kernel leaves first
     DevStatus d;
     int rc = read_status(s, &d);
     if (rc) return rc;
-    const int64_t v[5] = {s->steps_run, (int64_t)d.builds, (int64_t)d.n_short, (int64_t)d.n_long, 5};
-    for (int k = 0; k < n && k < 5; ++k) out[k] = v[k];
+    const int64_t v[7] = {s->steps_run, (int64_t)d.builds, (int64_t)d.n_short, (int64_t)d.n_long, 5,
+                          s->session_served, s->run_launches};
+    for (int k = 0; k < n && k < 7; ++k) out[k] = v[k];
     return OXG_OK;
 }
 

@@ -1738,20 +1738,66 @@ __global__ void k_prep_accel(IntegArgs a)
 #ifndef OXG_RUN_BLOCKS_PER_SM
 #define OXG_RUN_BLOCKS_PER_SM (512 / OXG_RUN_THREADS)
 #endif
+// The parameters of one run of the run kernel: from the launch's arguments for its first
+// run, from the host's request for each further run of a host session (below).
+struct RunCmd {
+    int bodies;                // step bodies of the run
+    int closing;               // the last body is the run's last step (step two only)
+    int prologue;              // run start kind (RunArgs::prologue)
+    int reuse_ok;              // kind 3: the force arrays hold the device state's forces
+    uint32_t rebuild0;         // the lists are new: rebuild whatever the displacements
+    uint32_t seq;              // stored last into the status mirror at the run's end
+    unsigned long long step0;  // the system's timestep at the run's start (RNG counter)
+    const float4* hin[5];      // host state read at the run start (mapped), or null
+    float4* hout[5];           // host arrays written by the closing body (mapped), or null
+};
+
+// A host session (oxg_system_set_host_session): the run kernel stays resident after a
+// host-state run and serves the host's next requests, each a run of the same kind, until
+// the host asks it to leave or no request comes within the idle time. The host writes a
+// request into page-locked memory, its sequence number last; block 0 of the kernel polls
+// that word (bounded by the idle time), copies the request into the barrier's command
+// and the blocks meet at a grid barrier before the run.
+struct HostRequest {
+    uint32_t seq;              // stored last by the host: a request differs from the last one
+    uint32_t quit;             // leave the kernel instead of running
+    int bodies;
+    int reuse_ok;
+    unsigned long long step0;
+    const float4* hin[5];      // device aliases of the caller's page-locked arrays
+    float4* hout[5];
+};
+
 struct GridBarrier {
     uint32_t arrive;  // bit 31 flips each time every block has arrived
     uint32_t abort;   // set by a block whose wait gave up: the others leave too
     uint32_t exits;   // blocks that have left the launch (the last one resets it)
     uint32_t pad[29]; // a line of its own
+    uint32_t go;      // host session: the next command is a run (0: leave)
+    uint32_t pad2;
+    RunCmd cmd;       // host session: the next run, written by block 0 before a grid barrier
+    HostRequest req;  // host session: block 0's copy of the host's request
 };
+static_assert(sizeof(HostRequest) % sizeof(unsigned long long) == 0 && sizeof(HostRequest) <= 32 * 8,
+              "a host request is copied one 8-byte word per lane of a warp");
+static_assert(sizeof(RunCmd) % sizeof(unsigned long long) == 0, "a run command is copied in 8-byte words");
 
-constexpr long long kBarrierSpinLimit = 1LL << 22;  // polls of an L2 round trip: ~1 s on a GB300 (0.23 us a poll)
+constexpr long long kBarrierSpinLimit = 1LL << 22;
+constexpr long long kServeSpinLimit = 1LL << 30;   // polls of a host request (the idle time ends it first)  // polls of an L2 round trip: ~1 s on a GB300 (0.23 us a poll)
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p)
 {
     uint32_t v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
 // Arrive at the grid barrier (the whole block); the returned token (thread 0) is the
@@ -1830,6 +1876,10 @@ struct RunArgs {
     DevStatus* st_mirror;      // host-mapped copy of the status written by the last block
                                // to leave (null: the host copies the status itself)
     uint32_t seq;              // this launch's sequence number, stored last into st_mirror->seq
+    // host session (k_run<true> only): after each run, wait up to idle_ns for the next
+    // request in req (mapped host memory); null: leave after the launch's run
+    const HostRequest* req;
+    unsigned long long idle_ns;
 };
 
 
@@ -1869,10 +1919,6 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     const int gthread = gwarp * 32 + lane, nthreads = nwarps * 32;
     double eacc[kNTerms + 3];  // unused: MD steps evaluate no energies
     bool bad_type = false;
-    // the RNG step of body b is step0 + b + 1 (block 0 advances st->step to match); the
-    // host passes step0 to every launch: reading st->step here would race with block 0's
-    // first increment in a block that starts late
-    const unsigned long long step_base = a.step0;
     // the stored pair counts and this thread's first short- and long-pair entries, read
     // at the launch's start (issued here, they arrive while the run start works) and
     // again after each list build (they change only there)
@@ -1888,7 +1934,6 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                                                                : make_int2(0, 0);
     };
     load_known();
-    bool completed = false;  // the launch's last body ran to its end
     // the block's slice of the (constant) bond table, staged once per launch when it fits
     __shared__ int4 bond_stage[kBondStage];
     const int4* bonds_here = nullptr;
@@ -1901,278 +1946,363 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
             bonds_here = bond_stage;  // read after phase A's first block barrier
         }
     }
-    bool spec_used = false;  // the run start took the first step one in its own pass
-    for (int body = a.prologue ? -1 : 0; body < a.bodies; ++body) {
-        const bool pro = body < 0;
-        bool reuse = pro && a.prologue == 2;  // the last step's forces are this state's
-        bool rebuild;
-        if (pro) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) {
-                st->step = a.step0;
-                st->flags = 0u;
-                st->rebuild = 0u;
-                st->qspill = 0u;
-                st->rb[0] = 0u;
-                st->rb[1] = 0u;
-            }
-            if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
-            const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-            const bool from_host = HOST_IO && a.prologue == 3;
-            // When the force arrays may hold this state's forces (kind 2; kind 3 with
-            // reuse_ok, which is only known once every block has compared its particles),
-            // this pass also takes the first step's step one (a = F/m from those forces),
-            // saving the run start's own step pass and its grid barrier. If the host state
-            // turns out to differ, the pass after the barrier restores the state from the
-            // checkpoint and the run start continues as kind 1 does.
-            const bool spec = a.prologue == 2 || (from_host && a.reuse_ok != 0);
-            bool far = false, diff = false, sfar = false, sbad = false;
-            {
-                // the first body's reads into L2 while the run start works (after an idle
-                // period L2 may hold none of them): pair lists, bonds, charges
-                prefetch_l2(a.f.pairs_short, (size_t)ns_known * sizeof(int2), gthread, nthreads);
-                prefetch_l2(a.f.pairs_long, (size_t)nl_known * sizeof(int2), gthread, nthreads);
-                if (a.f.bonded) prefetch_l2(a.f.bonds, (size_t)a.f.n_bonds * sizeof(int4), gthread, nthreads);
-                if (a.f.charge) prefetch_l2(a.f.charge, (size_t)a.g.N * sizeof(float), gthread, nthreads);
-            }
-            for (int i = gthread; i < a.g.N; i += nthreads) {
-                float4 v[5], F = zero, T = zero, r;
-                if (from_host) {
-                    // the host's state (mapped memory) into the device arrays; compared
-                    // bit for bit with what they held
-                    // every load issued before any store: a store to a device array
-                    // could alias a later host load for the compiler, which would then
-                    // serialise the five host round trips
-                    float4* const dv[5] = {a.g.pos, a.g.pos_lo, a.g.quat, a.g.vel, a.g.angmom};
-                    float4 o[5];
+    // this run's parameters: the launch's; in a host session, each further request's
+    __shared__ RunCmd cmd;
+    __shared__ uint32_t serve_go;
+    if (threadIdx.x == 0) {
+        cmd.bodies = a.bodies;
+        cmd.closing = a.closing;
+        cmd.prologue = a.prologue;
+        cmd.reuse_ok = a.reuse_ok;
+        cmd.rebuild0 = a.rebuild0;
+        cmd.seq = a.seq;
+        cmd.step0 = a.step0;
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) v[k] = a.hin[k][i];
+        for (int k = 0; k < 5; ++k) {
+            cmd.hin[k] = a.hin[k];
+            cmd.hout[k] = a.hout[k];
+        }
+    }
+    __syncthreads();
+    for (;;) {  // one run per pass
+        bool spec_used = false;  // the run start took the first step one in its own pass
+        bool completed = false;  // the run's last body ran to its end
+        bad_type = false;
+        // the RNG step of body b is step0 + b + 1 (block 0 advances st->step to match); the
+        // host passes step0 to every run: reading st->step here would race with block 0's
+        // first increment in a block that starts late
+        const unsigned long long step_base = cmd.step0;
+        for (int body = cmd.prologue ? -1 : 0; body < cmd.bodies; ++body) {
+            const bool pro = body < 0;
+            bool reuse = pro && cmd.prologue == 2;  // the last step's forces are this state's
+            bool rebuild;
+            if (pro) {
+                if (blockIdx.x == 0 && threadIdx.x == 0) {
+                    st->step = cmd.step0;
+                    st->flags = 0u;
+                    st->rebuild = 0u;
+                    st->qspill = 0u;
+                    st->rb[0] = 0u;
+                    st->rb[1] = 0u;
+                }
+                if (blockIdx.x == 0 && threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
+                const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+                const bool from_host = HOST_IO && cmd.prologue == 3;
+                // When the force arrays may hold this state's forces (kind 2; kind 3 with
+                // reuse_ok, which is only known once every block has compared its particles),
+                // this pass also takes the first step's step one (a = F/m from those forces),
+                // saving the run start's own step pass and its grid barrier. If the host state
+                // turns out to differ, the pass after the barrier restores the state from the
+                // checkpoint and the run start continues as kind 1 does.
+                const bool spec = cmd.prologue == 2 || (from_host && cmd.reuse_ok != 0);
+                bool far = false, diff = false, sfar = false, sbad = false;
+                {
+                    // the first body's reads into L2 while the run start works (after an idle
+                    // period L2 may hold none of them): pair lists, bonds, charges
+                    prefetch_l2(a.f.pairs_short, (size_t)ns_known * sizeof(int2), gthread, nthreads);
+                    prefetch_l2(a.f.pairs_long, (size_t)nl_known * sizeof(int2), gthread, nthreads);
+                    if (a.f.bonded) prefetch_l2(a.f.bonds, (size_t)a.f.n_bonds * sizeof(int4), gthread, nthreads);
+                    if (a.f.charge) prefetch_l2(a.f.charge, (size_t)a.g.N * sizeof(float), gthread, nthreads);
+                }
+                for (int i = gthread; i < a.g.N; i += nthreads) {
+                    float4 v[5], F = zero, T = zero, r;
+                    if (from_host) {
+                        // the host's state (mapped memory) into the device arrays; compared
+                        // bit for bit with what they held
+                        // every load issued before any store: a store to a device array
+                        // could alias a later host load for the compiler, which would then
+                        // serialise the five host round trips
+                        float4* const dv[5] = {a.g.pos, a.g.pos_lo, a.g.quat, a.g.vel, a.g.angmom};
+                        float4 o[5];
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) o[k] = dv[k][i];
-                    r = a.g.pos_ref[i];
-                    if (spec) {
-                        F = __ldcg(a.g.force + i);
-                        T = __ldcg(a.g.torque + i);
-                    }
-                    if ((unsigned)__float_as_int(v[0].w) >= (unsigned)P.h().n_types)
-                        bad_type = true;  // reported after the run (the kernels skip the particle)
+                        for (int k = 0; k < 5; ++k) v[k] = cmd.hin[k][i];
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) {
-                        diff |= __float_as_uint(v[k].x) != __float_as_uint(o[k].x) ||
-                                __float_as_uint(v[k].y) != __float_as_uint(o[k].y) ||
-                                __float_as_uint(v[k].z) != __float_as_uint(o[k].z) ||
-                                __float_as_uint(v[k].w) != __float_as_uint(o[k].w);
-                        dv[k][i] = v[k];
-                    }
-                } else {
-                    v[0] = a.g.pos[i];
-                    v[1] = a.g.pos_lo[i];
-                    v[2] = a.g.quat[i];
-                    v[3] = a.g.vel[i];
-                    v[4] = a.g.angmom[i];
-                    r = a.g.pos_ref[i];
-                    if (spec) {
-                        F = __ldcg(a.g.force + i);
-                        T = __ldcg(a.g.torque + i);
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < 5; ++k) a.ck[k][i] = v[k];
-                if (!spec && reuse) continue;  // forces kept; the lists are valid for this state
-                if (!from_host && !spec) {     // (from host state: zeroed below once it is known to differ)
-                    a.g.force[i] = zero;
-                    a.g.torque[i] = zero;
-                }
-                if (!reuse) {  // the state's own displacement since the last list build
-                    const float3 d = min_image(mk3(v[0].x - r.x, v[0].y - r.y, v[0].z - r.z), a.g.L, a.g.invL);
-                    far |= !(dot(d, d) <= a.g.half_buf2);
-                }
-                if (spec) {
-                    // the first step one (writes the stepped state, zeroes the accumulators)
-                    PState ps;
-                    ps.x = v[0];
-                    ps.xl = v[1];
-                    ps.q = v[2];
-                    ps.v = v[3];
-                    ps.p = v[4];
-                    ps.ref = r;
-                    const float minv = 1.f / ps.v.w;
-                    bool f1 = false, b1 = false;
-                    particle_step_one(a.g, i, ps, make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f),
-                                      make_float4(T.x, T.y, T.z, 0.f), f1, b1);
-                    sfar |= f1;
-                    sbad |= b1;
-                }
-            }
-            if (spec && __syncthreads_or(sfar) && threadIdx.x == 0) atomicOr(&st->spec_far, 1u);
-            if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->moved, 1u);
-            if (from_host && __syncthreads_or(diff) && threadIdx.x == 0) atomicOr(&st->changed, 1u);
-            if (!grid_barrier(a.bar)) break;  // the counters above are reset for every block
-            if (from_host) {
-                reuse = a.reuse_ok != 0 && ld_volatile(&st->changed) == 0u;  // the same in every block
-                if (!reuse) {
-                    for (int i = gthread; i < a.g.N; i += nthreads) {
-                        if (spec) {  // undo the first step one: the state from the checkpoint
-                            a.g.pos[i] = a.ck[0][i];
-                            a.g.pos_lo[i] = a.ck[1][i];
-                            a.g.quat[i] = a.ck[2][i];
-                            a.g.vel[i] = a.ck[3][i];
-                            a.g.angmom[i] = a.ck[4][i];
+                        for (int k = 0; k < 5; ++k) o[k] = dv[k][i];
+                        r = a.g.pos_ref[i];
+                        if (spec) {
+                            F = __ldcg(a.g.force + i);
+                            T = __ldcg(a.g.torque + i);
                         }
+                        if ((unsigned)__float_as_int(v[0].w) >= (unsigned)P.h().n_types)
+                            bad_type = true;  // reported after the run (the kernels skip the particle)
+#pragma unroll
+                        for (int k = 0; k < 5; ++k) {
+                            diff |= __float_as_uint(v[k].x) != __float_as_uint(o[k].x) ||
+                                    __float_as_uint(v[k].y) != __float_as_uint(o[k].y) ||
+                                    __float_as_uint(v[k].z) != __float_as_uint(o[k].z) ||
+                                    __float_as_uint(v[k].w) != __float_as_uint(o[k].w);
+                            dv[k][i] = v[k];
+                        }
+                    } else {
+                        v[0] = a.g.pos[i];
+                        v[1] = a.g.pos_lo[i];
+                        v[2] = a.g.quat[i];
+                        v[3] = a.g.vel[i];
+                        v[4] = a.g.angmom[i];
+                        r = a.g.pos_ref[i];
+                        if (spec) {
+                            F = __ldcg(a.g.force + i);
+                            T = __ldcg(a.g.torque + i);
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) a.ck[k][i] = v[k];
+                    if (!spec && reuse) continue;  // forces kept; the lists are valid for this state
+                    if (!from_host && !spec) {     // (from host state: zeroed below once it is known to differ)
                         a.g.force[i] = zero;
                         a.g.torque[i] = zero;
                     }
-                    if (!grid_barrier(a.bar)) break;  // zeroed before any block scatters forces
+                    if (!reuse) {  // the state's own displacement since the last list build
+                        const float3 d = min_image(mk3(v[0].x - r.x, v[0].y - r.y, v[0].z - r.z), a.g.L, a.g.invL);
+                        far |= !(dot(d, d) <= a.g.half_buf2);
+                    }
+                    if (spec) {
+                        // the first step one (writes the stepped state, zeroes the accumulators)
+                        PState ps;
+                        ps.x = v[0];
+                        ps.xl = v[1];
+                        ps.q = v[2];
+                        ps.v = v[3];
+                        ps.p = v[4];
+                        ps.ref = r;
+                        const float minv = 1.f / ps.v.w;
+                        bool f1 = false, b1 = false;
+                        particle_step_one(a.g, i, ps, make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f),
+                                          make_float4(T.x, T.y, T.z, 0.f), f1, b1);
+                        sfar |= f1;
+                        sbad |= b1;
+                    }
                 }
+                if (spec && __syncthreads_or(sfar) && threadIdx.x == 0) atomicOr(&st->spec_far, 1u);
+                if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->moved, 1u);
+                if (from_host && __syncthreads_or(diff) && threadIdx.x == 0) atomicOr(&st->changed, 1u);
+                if (!grid_barrier(a.bar)) break;  // the counters above are reset for every block
+                if (from_host) {
+                    reuse = cmd.reuse_ok != 0 && ld_volatile(&st->changed) == 0u;  // the same in every block
+                    if (!reuse) {
+                        for (int i = gthread; i < a.g.N; i += nthreads) {
+                            if (spec) {  // undo the first step one: the state from the checkpoint
+                                a.g.pos[i] = a.ck[0][i];
+                                a.g.pos_lo[i] = a.ck[1][i];
+                                a.g.quat[i] = a.ck[2][i];
+                                a.g.vel[i] = a.ck[3][i];
+                                a.g.angmom[i] = a.ck[4][i];
+                            }
+                            a.g.force[i] = zero;
+                            a.g.torque[i] = zero;
+                        }
+                        if (!grid_barrier(a.bar)) break;  // zeroed before any block scatters forces
+                    }
+                }
+                if (spec && reuse) {
+                    // the first step one is done: its forces (body 0) come next; its
+                    // displacement test is read there from spec_far
+                    if (__syncthreads_or(sbad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
+                    spec_used = true;
+                    continue;
+                }
+                rebuild = !reuse && (cmd.rebuild0 != 0u || ld_volatile(&st->moved) != 0u);
+            } else {
+                // rebuild requests: body 0 reads the one left by the run start or the previous
+                // launch, body b > 0 the one the step phase of body b - 1 left in rb[b & 1]
+                rebuild = ld_volatile(body == 0 ? &st->rebuild : &st->rb[body & 1]) != 0u;
+                if (body == 0 && spec_used) rebuild = rebuild || ld_volatile(&st->spec_far) != 0u;
             }
-            if (spec && reuse) {
-                // the first step one is done: its forces (body 0) come next; its
-                // displacement test is read there from spec_far
-                if (__syncthreads_or(sbad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
-                spec_used = true;
-                continue;
-            }
-            rebuild = !reuse && (a.rebuild0 != 0u || ld_volatile(&st->moved) != 0u);
-        } else {
-            // rebuild requests: body 0 reads the one left by the run start or the previous
-            // launch, body b > 0 the one the step phase of body b - 1 left in rb[b & 1]
-            rebuild = ld_volatile(body == 0 ? &st->rebuild : &st->rb[body & 1]) != 0u;
-            if (body == 0 && spec_used) rebuild = rebuild || ld_volatile(&st->spec_far) != 0u;
-        }
-        if (rebuild) {
-            const uint32_t par = ld_volatile(&st->gen) & 1u;
-            nlist_zero_other(a.n, gthread, nthreads, par);
-            for (int i = gthread; i < a.n.N; i += nthreads) nlist_bin_particle(a.n, i, par);
-            if (!grid_barrier(a.bar)) break;
-            {
-                __shared__ int2 stage_buf[2][kRunThreads / 32][kPairStage];
-                PairStage sg{stage_buf[0][threadIdx.x >> 5], stage_buf[1][threadIdx.x >> 5], 0, 0};
-                for (int i = gwarp; i < a.n.N; i += nwarps) nlist_pairs_warp(a.n, i, par, &sg);
-                stage_flush_all(a.n, sg);
-            }
-            if (!grid_barrier(a.bar)) break;
-            if (ld_volatile(&st->flags) & (kStCellOverflow | kStPairOverflow)) break;
-        }
-        if (rebuild) load_known();
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            if (rebuild) st->gen += 1u;
-            if (!pro) st->step += 1ull;
-        }
-        // this thread's first particle's bath noise for step two, computed between its
-        // block's arrival at the force barrier and the barrier's release
-        const unsigned long long step = step_base + (unsigned long long)(body + 1);
-        LangevinNoise nz;
-        const bool have_nz = !pro && gthread < a.g.N;
-        if (!reuse) {
-            // phase B on the block's own queues: a block barrier, not a grid barrier
-            forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type, ns_known, nl_known, first_pair);
-            forces_b_local<false>(a.f, P, eacc, bad_type, bonds_here);
-            const uint32_t tok = grid_arrive(a.bar);
-            if (have_nz)
-                nz = langevin_noise((uint32_t)gthread, step, a.g.seed_lo, a.g.seed_hi, a.g.dt, a.g.kT, a.g.gamma,
-                                    a.g.gamma_r);
-            if (!grid_wait(a.bar, tok)) break;
-            if (ld_volatile(&st->qspill)) {  // pairs that did not fit a block's queues
-                forces_b_body<false, false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+            if (rebuild) {
+                const uint32_t par = ld_volatile(&st->gen) & 1u;
+                nlist_zero_other(a.n, gthread, nthreads, par);
+                for (int i = gthread; i < a.n.N; i += nthreads) nlist_bin_particle(a.n, i, par);
                 if (!grid_barrier(a.bar)) break;
-                if (blockIdx.x == 0 && threadIdx.x == 0) st->qspill = 0u;  // read a barrier ago
-            }
-        }
-        // every block read this body's rebuild request before the last barrier
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            if (body == 0) {
-                st->rebuild = 0u;
-                st->spec_far = 0u;
-                if (spec_used) {  // the run start's step pass, which clears these, was skipped
-                    st->moved = 0u;
-                    st->changed = 0u;
+                {
+                    __shared__ int2 stage_buf[2][kRunThreads / 32][kPairStage];
+                    PairStage sg{stage_buf[0][threadIdx.x >> 5], stage_buf[1][threadIdx.x >> 5], 0, 0};
+                    for (int i = gwarp; i < a.n.N; i += nwarps) nlist_pairs_warp(a.n, i, par, &sg);
+                    stage_flush_all(a.n, sg);
                 }
-            } else if (body > 0) {
-                st->rb[body & 1] = 0u;
+                if (!grid_barrier(a.bar)) break;
+                if (ld_volatile(&st->flags) & (kStCellOverflow | kStPairOverflow)) break;
             }
-        }
-        // step two of this step (+ step one of the next); at run start a = F/m and
-        // step one of the first step
-        const bool last = a.closing && body == a.bodies - 1;
-        if (blockIdx.x == 0) {
-            if (threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
-            if (pro && threadIdx.x == 32) st->moved = 0u;    // read two barriers ago
-            if (pro && threadIdx.x == 64) st->changed = 0u;  // read two barriers ago
-        }
-        bool far = false, bad = false;
-        for (int i = gthread; i < a.g.N; i += nthreads) {
-            PState s = load_pstate(a.g, i);
-            float4 ac, tn;
-            if (pro) {
-                const float4 F = __ldcg(a.g.force + i), T = __ldcg(a.g.torque + i);
-                const float minv = 1.f / s.v.w;
-                ac = make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f);
-                tn = make_float4(T.x, T.y, T.z, 0.f);
-            } else if (have_nz && i == gthread) {
-                step_two_noise(s, __ldcg(a.g.force + i), __ldcg(a.g.torque + i), nz, a.g.dt, a.g.gamma,
-                               a.g.gamma_r, a.g.inertia, ac, tn);
-            } else {
-                particle_step_two(a.g, i, step, s, ac, tn);
+            if (rebuild) load_known();
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                if (rebuild) st->gen += 1u;
+                if (!pro) st->step += 1ull;
             }
-            if (last) {
-                a.g.vel[i] = s.v;
-                a.g.angmom[i] = s.p;
-                a.g.accel[i] = ac;
-                a.g.tnet[i] = tn;
-                if (HOST_IO && a.hout[0]) {  // the run's final state to the host (mapped)
-                    a.hout[0][i] = s.x;
-                    a.hout[1][i] = s.xl;
-                    a.hout[2][i] = s.q;
-                    a.hout[3][i] = s.v;
-                    a.hout[4][i] = s.p;
+            // this thread's first particle's bath noise for step two, computed between its
+            // block's arrival at the force barrier and the barrier's release
+            const unsigned long long step = step_base + (unsigned long long)(body + 1);
+            LangevinNoise nz;
+            const bool have_nz = !pro && gthread < a.g.N;
+            if (!reuse) {
+                // phase B on the block's own queues: a block barrier, not a grid barrier
+                forces_a_body<false, true>(a.f, P, gwarp, nwarps, eacc, bad_type, ns_known, nl_known, first_pair);
+                forces_b_local<false>(a.f, P, eacc, bad_type, bonds_here);
+                const uint32_t tok = grid_arrive(a.bar);
+                if (have_nz)
+                    nz = langevin_noise((uint32_t)gthread, step, a.g.seed_lo, a.g.seed_hi, a.g.dt, a.g.kT, a.g.gamma,
+                                        a.g.gamma_r);
+                if (!grid_wait(a.bar, tok)) break;
+                if (ld_volatile(&st->qspill)) {  // pairs that did not fit a block's queues
+                    forces_b_body<false, false>(a.f, P, gwarp, nwarps, eacc, bad_type);
+                    if (!grid_barrier(a.bar)) break;
+                    if (blockIdx.x == 0 && threadIdx.x == 0) st->qspill = 0u;  // read a barrier ago
                 }
-            } else {
-                bool f1 = false, b1 = false;
-                particle_step_one(a.g, i, s, ac, tn, f1, b1);
-                far |= f1;
-                bad |= b1;
+            }
+            // every block read this body's rebuild request before the last barrier
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                if (body == 0) {
+                    st->rebuild = 0u;
+                    st->spec_far = 0u;
+                    if (spec_used) {  // the run start's step pass, which clears these, was skipped
+                        st->moved = 0u;
+                        st->changed = 0u;
+                    }
+                } else if (body > 0) {
+                    st->rb[body & 1] = 0u;
+                }
+            }
+            // step two of this step (+ step one of the next); at run start a = F/m and
+            // step one of the first step
+            const bool last = cmd.closing && body == cmd.bodies - 1;
+            if (blockIdx.x == 0) {
+                if (threadIdx.x < kNQ) st->qcount[threadIdx.x] = 0u;
+                if (pro && threadIdx.x == 32) st->moved = 0u;    // read two barriers ago
+                if (pro && threadIdx.x == 64) st->changed = 0u;  // read two barriers ago
+            }
+            bool far = false, bad = false;
+            for (int i = gthread; i < a.g.N; i += nthreads) {
+                PState s = load_pstate(a.g, i);
+                float4 ac, tn;
+                if (pro) {
+                    const float4 F = __ldcg(a.g.force + i), T = __ldcg(a.g.torque + i);
+                    const float minv = 1.f / s.v.w;
+                    ac = make_float4(F.x * minv, F.y * minv, F.z * minv, 0.f);
+                    tn = make_float4(T.x, T.y, T.z, 0.f);
+                } else if (have_nz && i == gthread) {
+                    step_two_noise(s, __ldcg(a.g.force + i), __ldcg(a.g.torque + i), nz, a.g.dt, a.g.gamma,
+                                   a.g.gamma_r, a.g.inertia, ac, tn);
+                } else {
+                    particle_step_two(a.g, i, step, s, ac, tn);
+                }
+                if (last) {
+                    a.g.vel[i] = s.v;
+                    a.g.angmom[i] = s.p;
+                    a.g.accel[i] = ac;
+                    a.g.tnet[i] = tn;
+                    if (HOST_IO && cmd.hout[0]) {  // the run's final state to the host (mapped)
+                        cmd.hout[0][i] = s.x;
+                        cmd.hout[1][i] = s.xl;
+                        cmd.hout[2][i] = s.q;
+                        cmd.hout[3][i] = s.v;
+                        cmd.hout[4][i] = s.p;
+                    }
+                } else {
+                    bool f1 = false, b1 = false;
+                    particle_step_one(a.g, i, s, ac, tn, f1, b1);
+                    far |= f1;
+                    bad |= b1;
+                }
+            }
+            // the next body's rebuild request: the run start's to st->rebuild (read by body 0),
+            // body b's to rb[(b + 1) & 1] (cleared by body b - 1 after its force barrier)
+            if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(pro ? &st->rebuild : &st->rb[(body + 1) & 1], 1u);
+            if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
+            if (body == cmd.bodies - 1) {  // the launch's last body: no barrier after it (below)
+                completed = true;
+                break;
+            }
+            if (!grid_barrier(a.bar)) break;
+        }
+        if (__syncthreads_or(bad_type) && threadIdx.x == 0) atomicOr(&st->flags, kStBadIndex);
+        if (threadIdx.x == 0 && ld_volatile(&a.bar->abort)) atomicOr(&st->flags, kStBarrierTimeout);
+        // the last block to leave: after a completed launch it hands the pending rebuild
+        // request to the next launch (or the per-step kernels) — every block has written its
+        // part by then, so the last body needs no grid barrier of its own — and it mirrors
+        // the final status into host memory, so the host reads it without a copy of its own
+        if (threadIdx.x == 0) {
+            // a launch that wrote host arrays orders them (its block's writes, by the barrier
+            // above) before its arrival at the system scope: the host, once it sees the
+            // launch's sequence number in the status mirror, reads them without waiting for
+            // the launch to retire
+            if (HOST_IO && cmd.hout[0]) __threadfence_system();
+            else __threadfence();
+            if (atomicAdd(&a.bar->exits, 1u) == gridDim.x - 1u) {
+                a.bar->exits = 0u;  // (every block has counted itself: before the status goes out)
+                __threadfence();
+                if (completed) {  // the same in every block (all complete, or all left early)
+                    st->rebuild = ld_volatile(&st->rb[cmd.bodies & 1]);
+                    st->rb[0] = 0u;
+                    st->rb[1] = 0u;
+                }
+                if (a.st_mirror) {
+                    const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(st);
+                    volatile uint32_t* dst = reinterpret_cast<volatile uint32_t*>(a.st_mirror);
+                    constexpr int kSeqWord = (int)(offsetof(DevStatus, seq) / sizeof(uint32_t));
+                    for (int k = 0; k < kSeqWord; ++k) dst[k] = src[k];
+                    __threadfence_system();
+                    dst[kSeqWord] = cmd.seq;  // after every other word
+                    __threadfence_system();
+                }
             }
         }
-        // the next body's rebuild request: the run start's to st->rebuild (read by body 0),
-        // body b's to rb[(b + 1) & 1] (cleared by body b - 1 after its force barrier)
-        if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(pro ? &st->rebuild : &st->rb[(body + 1) & 1], 1u);
-        if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
-        if (body == a.bodies - 1) {  // the launch's last body: no barrier after it (below)
-            completed = true;
-            break;
+        if (!HOST_IO || a.req == nullptr) break;
+        // host session: warp 0 of block 0 waits (at most idle_ns) for the host's next
+        // request and copies it, one 8-byte word per lane (one round trip over the host
+        // link), into the barrier's command; every block reads it after a grid barrier
+        if (blockIdx.x == 0 && threadIdx.x < 32) {
+            uint32_t go = 0u;
+            if (threadIdx.x == 0 && !ld_volatile(&a.bar->abort)) {
+                const unsigned long long t0 = global_ns();
+                for (long long k = 1;; ++k) {
+                    // (relaxed polls; an acquire at the system scope per poll measured
+                    // several microseconds slower to see the host's store)
+                    const uint32_t v = *(const volatile uint32_t*)&a.req->seq;
+                    if (v != cmd.seq && v != 0u) {
+                        go = v;
+                        break;
+                    }
+                    if ((k & 63) == 0 && (global_ns() - t0 > a.idle_ns || k > kServeSpinLimit)) break;
+                }
+                // the host's stores before its store of the sequence number are visible
+                // to the loads after this fence
+                asm volatile("fence.acq_rel.sys;" ::: "memory");
+            }
+            go = __shfl_sync(0xffffffffu, go, 0);
+            __syncwarp();  // lane 0's fence before every lane's loads of the request
+            constexpr int kReqWords = (int)(sizeof(HostRequest) / sizeof(unsigned long long));
+            if (go && threadIdx.x < kReqWords)
+                reinterpret_cast<unsigned long long*>(&a.bar->req)[threadIdx.x] =
+                    *(reinterpret_cast<const volatile unsigned long long*>(a.req) + threadIdx.x);
+            __syncwarp();
+            if (threadIdx.x == 0) {
+                if (go && a.bar->req.quit) go = 0u;
+                if (go) {
+                    const HostRequest& r = a.bar->req;
+                    RunCmd& c = a.bar->cmd;
+                    c.bodies = r.bodies;
+                    c.closing = 1;
+                    c.prologue = 3;
+                    c.reuse_ok = r.reuse_ok;
+                    c.rebuild0 = 0u;
+                    c.seq = go;
+                    c.step0 = r.step0;
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) {
+                        c.hin[k] = r.hin[k];
+                        c.hout[k] = r.hout[k];
+                    }
+                }
+                *(volatile uint32_t*)&a.bar->go = go;
+            }
         }
         if (!grid_barrier(a.bar)) break;
-    }
-    if (__syncthreads_or(bad_type) && threadIdx.x == 0) atomicOr(&st->flags, kStBadIndex);
-    if (threadIdx.x == 0 && ld_volatile(&a.bar->abort)) atomicOr(&st->flags, kStBarrierTimeout);
-    // the last block to leave: after a completed launch it hands the pending rebuild
-    // request to the next launch (or the per-step kernels) — every block has written its
-    // part by then, so the last body needs no grid barrier of its own — and it mirrors
-    // the final status into host memory, so the host reads it without a copy of its own
-    if (threadIdx.x == 0) {
-        // a launch that wrote host arrays orders them (its block's writes, by the barrier
-        // above) before its arrival at the system scope: the host, once it sees the
-        // launch's sequence number in the status mirror, reads them without waiting for
-        // the launch to retire
-        if (HOST_IO && a.hout[0]) __threadfence_system();
-        else __threadfence();
-        if (atomicAdd(&a.bar->exits, 1u) == gridDim.x - 1u) {
-            __threadfence();
-            if (completed) {  // the same in every block (all complete, or all left early)
-                st->rebuild = ld_volatile(&st->rb[a.bodies & 1]);
-                st->rb[0] = 0u;
-                st->rb[1] = 0u;
-            }
-            if (a.st_mirror) {
-                const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(st);
-                volatile uint32_t* dst = reinterpret_cast<volatile uint32_t*>(a.st_mirror);
-                constexpr int kSeqWord = (int)(offsetof(DevStatus, seq) / sizeof(uint32_t));
-                for (int k = 0; k < kSeqWord; ++k) dst[k] = src[k];
-                __threadfence_system();
-                dst[kSeqWord] = a.seq;  // after every other word
-                __threadfence_system();
-            }
-            a.bar->exits = 0u;
-        }
+        // the command into shared memory, one 8-byte word per thread (L2, after the barrier)
+        if (threadIdx.x == 0) serve_go = __ldcg(&a.bar->go);
+        constexpr int kCmdWords = (int)(sizeof(RunCmd) / sizeof(unsigned long long));
+        if (threadIdx.x < kCmdWords)
+            reinterpret_cast<unsigned long long*>(&cmd)[threadIdx.x] =
+                __ldcg(reinterpret_cast<const unsigned long long*>(&a.bar->cmd) + threadIdx.x);
+        __syncthreads();
+        if (!serve_go || cmd.bodies < 1) break;
     }
 }
 #endif

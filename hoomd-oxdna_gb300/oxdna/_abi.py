@@ -244,7 +244,7 @@ EXPORTS = [
     "oxg_mlp_set_normalization", "oxg_mlp_gradient", "oxg_mlp_train_step", "oxg_mlp_predict",
     "oxg_system_set_surrogate", "oxg_system_surrogate_stats", "oxg_system_hbx_samples",
     "oxg_system_run_timing", "oxg_device_peaks", "oxg_system_run_host", "oxg_selftest_barrier",
-    "oxg_system_set_timestep",
+    "oxg_system_set_timestep", "oxg_system_set_host_session",
 ]
 
 MLP_PARAMS = 9480  # OXG_MLP_PARAMS
@@ -331,6 +331,7 @@ def lib():
         "oxg_device_peaks": ([dp, i32, vp], i32),
         "oxg_selftest_barrier": ([i32, i32, C.POINTER(C.c_int), vp], i32),
         "oxg_system_run_host": ([vp, C.c_long, vp, vp, vp, vp, vp], i32),
+        "oxg_system_set_host_session": ([vp, C.c_int], i32),
         "oxg_last_error": ([], C.c_char_p),
         "oxg_version": ([], C.c_char_p),
         "oxg_status_string": ([i32], C.c_char_p),

@@ -474,6 +474,8 @@ class Simulation:
         self._attached = True
         if getattr(self, "_surrogate_args", None) is not None:
             self._apply_surrogate(*self._surrogate_args)
+        if getattr(self, "_session_idle_us", 0):
+            _abi.check(L.oxg_system_set_host_session(sys_, self._session_idle_us), "oxg_system_set_host_session")
 
     def _host_state_ptrs(self, arrays, allow_none=False):
         """Addresses of the five host state arrays, each checked to be a C-contiguous
@@ -505,6 +507,17 @@ class Simulation:
         """Copy host float32 (N, 4) arrays (pinned or not) into the device state."""
         ptrs = self._host_state_ptrs((pos_type, pos_lo, quat, vel, angmom), allow_none=True)
         _abi.check(_abi.lib().oxg_system_set_state(self._sys, *ptrs, None), "oxg_system_set_state")
+
+    def set_host_session(self, idle_us):
+        """Host session for loops of run_state_arrays calls (page-locked arrays, at most
+        2000 steps a call): with idle_us > 0 the run kernel stays resident between calls,
+        occupying every SM, and serves the next call through page-locked host memory
+        instead of a new launch; it leaves after idle_us microseconds without a call, or
+        at any other call on this simulation. 0 turns the session off (the default)."""
+        self._sync()
+        _abi.check(_abi.lib().oxg_system_set_host_session(self._sys, int(idle_us)),
+                   "oxg_system_set_host_session")
+        self._session_idle_us = int(idle_us)
 
     def run_state_arrays(self, steps, pos_type, pos_lo, quat, vel, angmom):
         """push_state_arrays + run(steps) + pull_state_arrays in one call: the state is
@@ -675,9 +688,10 @@ class Simulation:
 
     def native_stats(self):
         L = _abi.lib()
-        out = (C.c_int64 * 5)()
-        _abi.check(L.oxg_system_stats(self._sys, out, 5), "oxg_system_stats")
-        return dict(steps=out[0], nlist_builds=out[1], pairs_short=out[2], pairs_long=out[3])
+        out = (C.c_int64 * 7)()
+        _abi.check(L.oxg_system_stats(self._sys, out, 7), "oxg_system_stats")
+        return dict(steps=out[0], nlist_builds=out[1], pairs_short=out[2], pairs_long=out[3],
+                    session_served=out[5], run_launches=out[6])
 
 
 def device_peaks(stream=None):

@@ -293,10 +293,24 @@ int oxg_system_run(oxg_system* sys, long nsteps);
  * on the device between calls). */
 int oxg_system_run_host(oxg_system* sys, long nsteps, float* pos_type, float* pos_lo, float* quat,
                         float* vel, float* angmom);
+/* Host session for host-driven loops: with idle_us > 0, the run kernel of a
+ * oxg_system_run_host call that takes one launch (nsteps <= 2000, page-locked arrays)
+ * stays resident after the run, occupying every SM of the device, and serves the next
+ * such call through a request block in page-locked host memory instead of a new launch
+ * (~5 us instead of ~17 us of launch and completion on GB300); it leaves when no
+ * request comes within idle_us microseconds (at most 100000), when any other call on
+ * this system is made (each ends the session first), when the context's parameters
+ * changed, or after a run that failed or overflowed its neighbour list (handled as
+ * without a session). idle_us = 0 ends the session and turns it off (the default).
+ * Other work on the device waits for the resident kernel to leave. No counterpart in
+ * the reference. */
+int oxg_system_set_host_session(oxg_system* sys, int idle_us);
 /* Per-term energies at the current state (device reduction, FP64) into host arrays. */
 int oxg_system_energies(oxg_system* sys, double* pair_energy, double* bonded_energy);
 /* Counters: index 0 steps run, 1 neighbour-list builds, 2 pair-list entries (short),
- * 3 pair-list entries (long), 4 kernels launched per step. */
+ * 3 pair-list entries (long), 4 kernels launched per step, 5 host-state runs served by a
+ * resident run kernel (oxg_system_set_host_session), 6 launches of the persistent run
+ * kernel. */
 int oxg_system_stats(oxg_system* sys, int64_t* out, int n);
 /* Device time of the persistent run kernel measured with CUDA events around each of its
  * launches on the system's stream (those of oxg_system_run; oxg_system_run_host calls

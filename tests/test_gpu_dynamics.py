@@ -263,6 +263,59 @@ def test_run_state_arrays_matches_push_run_pull(native, memory, steps):
         a.run_state_arrays(1, *st_a)
 
 
+def test_host_session_matches_a_launch_per_call(native):
+    """A host session (the run kernel resident between run_state_arrays calls, each call
+    a request in page-locked memory) against the same calls with a launch each, on twin
+    systems driven one after the other (a resident kernel holds every SM, so interleaved
+    calls of another system would wait for it to leave): one-step calls with the host
+    state unchanged and changed between calls, a four-step call, another call on the
+    simulation in between (it ends the session), a pause longer than the idle time (the
+    kernel leaves; the next call launches again) and a parameter change (the native system
+    is rebuilt, the session set again). Most calls were served by the resident kernel."""
+    import time
+
+    import torch
+    from oxdna import io
+    from oxdna.model import dna1, dna2
+    s = io.duplex_system(8, 20, 40.0, seed=4)
+    kT = dna1.kT_from_temperature(296.15)
+    n = len(s["pos"])
+
+    def drive(session_us):
+        forces, _ = dna2.forces()
+        sim = _sim(io.system_snapshot(s), forces, dt=0.003, kT=kT, seed=9)
+        st = [torch.zeros((n, 4), dtype=torch.float32).pin_memory().numpy() for _ in range(5)]
+        sim.pull_state_arrays(*st)
+        sim.set_host_session(session_us)
+        served = 0
+        for it in range(40):
+            if it == 10:  # a host-side change of the velocities
+                st[3][:, :3] *= np.float32(0.9)
+            if it == 20:  # another call on the simulation ends the session
+                sim.native_stats()
+            if it == 25:  # longer than the idle time: a resident kernel has left
+                time.sleep(0.05)
+            if it == 30:  # a parameter change (the counter of the system it replaces first)
+                served = sim.native_stats()["session_served"]
+                for key in list(forces[2].params.keys()):
+                    p = dict(forces[2].params[key])
+                    p["eps"] = 1.1 * p["eps"]
+                    forces[2].params[key] = p
+            sim.run_state_arrays(4 if it == 15 else 1, *st)
+        served += sim.native_stats()["session_served"]
+        assert sim.timestep == 39 + 4
+        sim.set_host_session(0)
+        return st, served
+
+    st_a, served_a = drive(2000)
+    st_b, served_b = drive(0)
+    for x, y in zip(st_a, st_b):
+        assert np.allclose(x, y, rtol=1e-5, atol=1e-5)
+    # launched: the first call and the calls after the stats call, the pause and the
+    # rebuild (36 of the 40 served otherwise)
+    assert served_a >= 30 and served_b == 0, (served_a, served_b)
+
+
 @pytest.mark.parametrize("fused", [False, True])
 def test_run_kernel_forces_match_oracle(native, oracle, fused):
     """The run kernel's own force evaluation (the run start's and the step's: phase A and
