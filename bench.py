@@ -54,7 +54,12 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region: one
+    `nvidia-smi -lms 200` process, started before the region and read by a thread.
+    __enter__ returns once its first sample is in, so the process start (which takes the
+    host and the driver for a while, longer than a 20-step timed region) stays outside
+    the region and only the periodic queries of the running process overlap it. The
+    summary covers the samples taken from just before the region to its end."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -62,42 +67,66 @@ class ClockSampler:
 
     def __init__(self, gpu=0):
         self.gpu = gpu
-        self.rows = []
-        self._stop = threading.Event()
+        self.rows = []  # (time, fields)
+        self._first = threading.Event()
+        self._proc = None
         self._t = None
+        self._t0 = self._t1 = None
 
-    def _loop(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                      "--format=csv,noheader,nounits"], capture_output=True,
-                                     text=True, timeout=5).stdout.strip()
-                if out:
-                    self.rows.append([x.strip() for x in out.split(",")])
-            except Exception:
-                return
-            self._stop.wait(0.2)
+    def _reader(self):
+        try:
+            for line in self._proc.stdout:
+                f = [x.strip() for x in line.strip().split(",")]
+                if len(f) >= 5:
+                    self.rows.append((time.time(), f))
+                    self._first.set()
+        except Exception:
+            pass
+        self._first.set()
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._loop, daemon=True)
-        self._t.start()
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._reader, daemon=True)
+            self._t.start()
+            self._first.wait(timeout=15)
+        except Exception:
+            self._proc = None
+        self._t0 = time.time()
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=6)
+        self._t1 = time.time()
+        if self._proc is not None:
+            self._proc.terminate()  # (the process started above)
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+            self._t.join(timeout=5)
+
+    def _window(self):
+        if self._t0 is None:
+            return [f for _, f in self.rows]
+        before = [f for t, f in self.rows if t < self._t0]
+        inside = [f for t, f in self.rows if self._t0 <= t <= (self._t1 or self._t0)]
+        return (before[-1:] if before else []) + inside
 
     def summary(self):
-        if not self.rows:
+        rows = self._window()
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in self.rows for k in range(4)
+        reasons = sorted({names[k] for r in rows for k in range(4)
                           if len(r) > 5 + k and r[5 + k].lower().startswith("active")})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.rows)}
+                "samples": len(rows)}
 
 
 class nvtx:
@@ -264,7 +293,7 @@ def bench_tiled(stream, steps=10000, warmup=500, copies=8):
     return out
 
 
-def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epochs=60, md_states=5):
+def bench_surrogate(stream, big, steps=1000, warmup=100, n_train=4_000_000, epochs=300, md_states=5):
     """The learned HB + cross-stacking surrogate on the 100k-nt system (2500 x 20 bp, box
     230, forces(fused=True)): trained here by the library's kernels on 4M pair geometries
     from 8000-nt trajectories at 280-360 K, its output shift calibrated on the training

@@ -79,7 +79,7 @@ def test_inference_matches_oracle(native):
 
 @pytest.fixture(scope="module")
 def trained():
-    """A network trained (60 epochs) on 4M pair geometries the plain evaluator samples
+    """A network trained (300 epochs) on 4M pair geometries the plain evaluator samples
     along 8000-nt duplex trajectories at 280-360 K from their built start on, with a
     held-out tenth (the benchmark's recipe)."""
     import torch
@@ -93,7 +93,7 @@ def trained():
     net = surrogate.Network(seed=0)
     net.fit_normalization(f[train], e[train])
     rms0 = float(torch.sqrt(((net.energies(f[hold]) - e[hold]) ** 2).mean()))
-    hist = net.train(f[train].contiguous(), e[train].contiguous(), epochs=60, batch=4096, lr=3e-3,
+    hist = net.train(f[train].contiguous(), e[train].contiguous(), epochs=300, batch=4096, lr=3e-3,
                      lr_end=3e-5)
     rms1 = float(torch.sqrt(((net.energies(f[hold]) - e[hold]) ** 2).mean()))
     shifts = net.calibrate(f[train], e[train])
