@@ -247,8 +247,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
             tc::fence_after();
             const uint32_t id64 = tc::idesc_bf16(128, 64), id80 = tc::idesc_bf16(128, 80);
             const uint32_t sp_ = tc::smem_addr(t.p), sg = tc::smem_addr(t.w + tc::kImgG3);
+            const uint32_t sgl = tc::smem_addr(t.w + tc::kImgG3L);
             const uint32_t sdz = tc::smem_addr(sm + kTrDZT), sh = tc::smem_addr(sm + kTrH2T);
             for (int j = 0; j < 4; ++j) tc::mma(t.tmem + 192, tc::op_desc(sp_, 128, j), tc::op_desc(sg, 64, j), id64, j > 0);
+            for (int j = 0; j < 4; ++j) tc::mma(t.tmem + 192, tc::op_desc(sp_, 128, j), tc::op_desc(sgl, 64, j), id64, 1u);
             for (int j = 0; j < 8; ++j)
                 tc::mma(t.tmem + kColDW3, tc::op_desc(sdz, 128, j), tc::op_desc(sh, 80, j), id80, (!first || j > 0));
             tc::commit(t.mbar);
@@ -263,8 +265,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_train(TrainArgs a)
             tc::fence_after();
             const uint32_t id64 = tc::idesc_bf16(128, 64), id80 = tc::idesc_bf16(128, 80);
             const uint32_t sq = tc::smem_addr(t.q), sg = tc::smem_addr(t.w + tc::kImgG2);
+            const uint32_t sgl = tc::smem_addr(t.w + tc::kImgG2L);
             const uint32_t sdz = tc::smem_addr(sm + kTrDZT), sh = tc::smem_addr(sm + kTrH1T);
             for (int j = 0; j < 4; ++j) tc::mma(t.tmem + 192, tc::op_desc(sq, 128, j), tc::op_desc(sg, 64, j), id64, j > 0);
+            for (int j = 0; j < 4; ++j) tc::mma(t.tmem + 192, tc::op_desc(sq, 128, j), tc::op_desc(sgl, 64, j), id64, 1u);
             for (int j = 0; j < 8; ++j)
                 tc::mma(t.tmem + kColDW2, tc::op_desc(sdz, 128, j), tc::op_desc(sh, 80, j), id80, (!first || j > 0));
             tc::commit(t.mbar);

@@ -85,11 +85,11 @@ def loss_gradient(params, xn, yt):
     dz3 = dy[:, None] * w["w4"][None, :] * c["s3"]
     g[9344:9408] = bf16(dz3).sum(0)
     g[5248:9344] = (bf16(dz3).T @ c["h2b"]).ravel()
-    dh2 = bf16(dz3) @ bf16(w["W3"])
+    dh2 = bf16(dz3) @ wsum(w["W3"])
     dz2 = dh2 * c["s2"]
     g[5184:5248] = bf16(dz2).sum(0)
     g[1088:5184] = (bf16(dz2).T @ c["h1b"]).ravel()
-    dh1 = bf16(dz2) @ bf16(w["W2"])
+    dh1 = bf16(dz2) @ wsum(w["W2"])
     dz1 = dh1 * c["s1"]
     g[1024:1088] = bf16(dz1).sum(0)
     gw1 = np.zeros((64, 16))
