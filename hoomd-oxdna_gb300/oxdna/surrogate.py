@@ -239,7 +239,8 @@ def samples(sim, max_n=200000):
 
 
 def training_set(n_target=4_000_000, temperatures=(280, 290, 300, 310, 320, 330, 340, 350, 360),
-                 n_dup=200, n_bp=20, box=100.0, equil=0, every=100, early=(10, 20, 40, 80),
+                 n_dup=200, n_bp=20, box=100.0, equil=0, every=200,
+                 early=(5, 10, 15, 20, 30, 40, 50, 60, 70, 80, 90),
                  per_snapshot=5000, built_weight=0.08, seed=11, log=None):
     """Pair geometries from trajectories of the 8000-nt duplex system (200 x 20 bp,
     box 100) at each temperature (oxDNA2, fused forces, Langevin dt 0.003): a random
