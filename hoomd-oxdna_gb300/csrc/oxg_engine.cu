@@ -1205,6 +1205,17 @@ static int checkpoint(oxg_system* s, bool restore)
     return OXG_OK;
 }
 
+// Sequence numbers of run-kernel launches and host-session requests: one counter for
+// both, so that the status mirror never holds a number a later launch or request gets.
+static uint32_t next_seq()
+{
+    static std::atomic<uint32_t> counter{0};
+    uint32_t seq;
+    do seq = counter.fetch_add(1u) + 1u;
+    while (seq == 0u);
+    return seq;
+}
+
 // The persistent run kernel: one cooperative launch of `bodies` step bodies, preceded
 // by the run start (prepRun) when `prologue` (see k_run).
 static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
@@ -1243,12 +1254,10 @@ static int launch_run(oxg_system* s, int bodies, bool closing, int prologue = 0,
     }
     ra.reuse_ok = reuse_ok ? 1 : 0;
     ra.st_mirror = s->st_mirror;
-    // a sequence number no other launch of the process had (never 0), and the mirror's
-    // word cleared before the launch: a stale word never reads as this launch's end
-    static std::atomic<uint32_t> seq_counter{0};
-    uint32_t seq;
-    do seq = seq_counter.fetch_add(1u) + 1u;
-    while (seq == 0u);
+    // a sequence number no other launch or host-session request of the process had
+    // (never 0), and the mirror's word cleared before the launch: a stale word never
+    // reads as this launch's end
+    const uint32_t seq = next_seq();
     s->run_seq = seq;
     ra.seq = seq;
     if (s->st_host) *reinterpret_cast<volatile uint32_t*>(&s->st_host->seq) = 0u;
@@ -1289,15 +1298,6 @@ static void copy_mirror(const oxg_system* s, DevStatus* d)
     const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(s->st_host);
     uint32_t* dst = reinterpret_cast<uint32_t*>(d);
     for (int k = 0; k < (int)(sizeof(DevStatus) / sizeof(uint32_t)); ++k) dst[k] = src[k];
-}
-
-static uint32_t next_seq()
-{
-    static std::atomic<uint32_t> counter{0};
-    uint32_t seq;
-    do seq = counter.fetch_add(1u) + 1u;
-    while (seq == 0u);
-    return seq;
 }
 
 // A host session's request to the resident run kernel: the run's parameters, then its

@@ -1782,8 +1782,8 @@ static_assert(sizeof(HostRequest) % sizeof(unsigned long long) == 0 && sizeof(Ho
               "a host request is copied one 8-byte word per lane of a warp");
 static_assert(sizeof(RunCmd) % sizeof(unsigned long long) == 0, "a run command is copied in 8-byte words");
 
-constexpr long long kBarrierSpinLimit = 1LL << 22;
-constexpr long long kServeSpinLimit = 1LL << 30;   // polls of a host request (the idle time ends it first)  // polls of an L2 round trip: ~1 s on a GB300 (0.23 us a poll)
+constexpr long long kBarrierSpinLimit = 1LL << 22;  // polls of an L2 round trip: ~1 s on a GB300 (0.23 us a poll)
+constexpr long long kServeSpinLimit = 1LL << 30;    // polls of a host request (the idle time ends it first)
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p)
 {
