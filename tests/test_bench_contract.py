@@ -62,3 +62,24 @@ def test_compute_roofline_arithmetic(monkeypatch):
     assert sp["ops_per_step"] == sum(census["special_per_step"].values())
     assert abs(sp["frac"] - sp["achieved"] / 8_000.0) < 1e-15
     assert 0.0 < r["frac"] < 1.0 and 0.0 < sp["frac"] < 1.0
+
+
+def test_clock_sampler_summarises_the_timed_window():
+    """The clock record covers the sample taken just before the timed region and those
+    inside it (a process-start sample long before it and samples after it are left out);
+    throttle reasons are read from the flags; without nvidia-smi the record says
+    'unsampled' instead of failing."""
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.ClockSampler(0)
+    row = lambda mhz, hw="Not Active", pc="Not Active": ["0", str(mhz), "2070", "900", "0x0", hw,  # noqa: E731
+                                                          "Not Active", "Not Active", pc]
+    c.rows = [(1.0, row(1200)), (9.5, row(2070)), (10.1, row(2070, pc="Active")), (10.3, row(2070)),
+              (20.0, row(800, hw="Active"))]
+    c._t0, c._t1 = 10.0, 10.5
+    s = c.summary()
+    assert s["samples"] == 3 and s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    none = bench.ClockSampler(0)
+    none._t0, none._t1 = 1.0, 2.0
+    assert none.summary()["reasons"] == ["unsampled"]
