@@ -286,8 +286,10 @@ int oxg_system_run(oxg_system* sys, long nsteps);
  * host arrays (cudaHostAlloc, torch pin_memory) on the persistent run kernel, the run
  * kernel itself reads the host arrays at its start (comparing them with the device
  * state: when they are equal and the last run left that state's forces, those are
- * reused) and its closing step writes the final state back: one launch and one
- * synchronisation per call. A particle type outside the context's types is then
+ * reused) and its closing step writes the final state back: one launch per call, whose
+ * end the host reads from a status word the launch writes into page-locked memory (or,
+ * in a host session, no launch: see oxg_system_set_host_session). A particle type
+ * outside the context's types is then
  * reported after the run (OXG_ERR_BAD_INDEX; the kernels skip the particle). Otherwise
  * set_state, run and get_state. No counterpart in the reference (HOOMD keeps the state
  * on the device between calls). */
