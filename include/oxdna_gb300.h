@@ -440,10 +440,10 @@ int oxg_batch_compute(oxg_batch* b, uint32_t term_mask, int bonded, float* force
  * call waits for its work on `stream` to finish before returning).
  *
  * The call copies its parameter block from host memory and reads its status back, so
- * it synchronises `stream` before returning. The first call on a device looks up the
- * array's device address (once per device, with that device current, and again after
- * the device's context was replaced, e.g. by cudaDeviceReset); make that first call
- * before any stream capture. Every call uses the same array and leaves its contents
+ * it synchronises `stream` before returning and cannot be captured into a CUDA graph.
+ * The first call on a device looks up the array's device address (once per device,
+ * with that device current, and again after the device's context was replaced, e.g.
+ * by cudaDeviceReset). Every call uses the same array and leaves its contents
  * behind; the call clears what must start empty. Calls whose GPU work overlaps
  * (several streams or threads) race on the shared array. */
 #define OXG_NOALLOC_MAX_PARTICLES 8192
