@@ -138,3 +138,58 @@ def test_run_start_reuses_the_last_steps_forces(native):
     L = s["box"][0]
     assert _pos_diff(ends[0], ends[1], L) < 1e-4
     assert np.abs(ends[0].particles.velocity - ends[1].particles.velocity).max() < 1e-3
+
+
+@pytest.mark.parametrize("path", ["run", "host", "session"])
+def test_non_finite_state_is_reported_and_the_system_recovers(native, path):
+    """A NaN coordinate in the state handed to the engine (through push_state_arrays and
+    run(), or page-locked host arrays and run_state_arrays, with and without a host
+    session) is reported as a non-finite state after the run, the timestep is left where
+    it was, and the system then runs on from a finite state as a twin that never saw the
+    NaN does. The NaN is made on the host: its pairs fail every cutoff test, its cell
+    index is clamped, and the integrator's check raises the flag."""
+    import torch
+
+    from oxdna import _abi, io
+    from oxdna.model import dna2
+    s = _system()
+    n = len(s["pos"])
+    a, _ = _sim(io.system_snapshot(s), dna2.forces()[0])
+    b, _ = _sim(io.system_snapshot(s), dna2.forces()[0])
+    a.run(5)
+    b.run(5)
+    good = [torch.zeros((n, 4), dtype=torch.float32).pin_memory().numpy() for _ in range(5)]
+    a.pull_state_arrays(*good)
+    bad = [torch.zeros((n, 4), dtype=torch.float32).pin_memory().numpy() for _ in range(5)]
+    for x, y in zip(bad, good):
+        x[:] = y
+    bad[0][3, 0] = np.nan
+    if path == "session":
+        a.set_host_session(2000)
+    with pytest.raises(_abi.OxgError) as err:
+        if path == "run":
+            a.push_state_arrays(*bad)
+            a.run(10)
+        else:
+            a.run_state_arrays(10, *bad)
+    assert err.value.code == _abi.ERR_NONFINITE
+    assert a.timestep == 5
+    if path == "run":
+        a.push_state_arrays(*good)
+        a.run(10)
+        end_a = a.state.get_snapshot()
+        pos_a, vel_a = end_a.particles.position, end_a.particles.velocity
+    else:
+        a.run_state_arrays(10, *good)
+        pos_a = good[0][:, :3].astype(np.float64) + good[1][:, :3]
+        vel_a = good[3][:, :3]
+    a.set_host_session(0)
+    b.run(10)
+    end_b = b.state.get_snapshot()
+    assert a.timestep == b.timestep == 15
+    assert np.isfinite(pos_a).all()
+    d = pos_a - end_b.particles.position
+    L = s["box"][0]
+    d -= L * np.round(d / L)
+    assert np.abs(d).max() < 1e-3
+    assert np.abs(vel_a - end_b.particles.velocity).max() < 1e-2
