@@ -141,13 +141,16 @@ def test_run_start_reuses_the_last_steps_forces(native):
 
 
 @pytest.mark.parametrize("path", ["run", "host", "session"])
-def test_non_finite_state_is_reported_and_the_system_recovers(native, path):
-    """A NaN coordinate in the state handed to the engine (through push_state_arrays and
-    run(), or page-locked host arrays and run_state_arrays, with and without a host
-    session) is reported as a non-finite state after the run, the timestep is left where
-    it was, and the system then runs on from a finite state as a twin that never saw the
-    NaN does. The NaN is made on the host: its pairs fail every cutoff test, its cell
-    index is clamped, and the integrator's check raises the flag."""
+@pytest.mark.parametrize("kind", ["nan", "type"])
+def test_bad_state_is_reported_and_the_system_recovers(native, path, kind):
+    """A NaN coordinate, or a particle type outside the context's types, in the state
+    handed to the engine (through push_state_arrays and run(), or page-locked host arrays
+    and run_state_arrays, with and without a host session) is reported after the run
+    (non-finite state; bad index), the timestep is left where it was, and the system then
+    runs on from a valid state as a twin that never saw the bad one does. Both are made
+    on the host: a NaN position fails every cutoff test and its cell coordinate is
+    clamped, the integrator's check raises the flag; every pair and bond evaluation
+    checks both types before it reads a parameter and skips the pair."""
     import torch
 
     from oxdna import _abi, io
@@ -163,7 +166,10 @@ def test_non_finite_state_is_reported_and_the_system_recovers(native, path):
     bad = [torch.zeros((n, 4), dtype=torch.float32).pin_memory().numpy() for _ in range(5)]
     for x, y in zip(bad, good):
         x[:] = y
-    bad[0][3, 0] = np.nan
+    if kind == "nan":
+        bad[0][3, 0] = np.nan
+    else:
+        bad[0][3, 3] = np.array([99], dtype=np.int32).view(np.float32)[0]
     if path == "session":
         a.set_host_session(2000)
     with pytest.raises(_abi.OxgError) as err:
@@ -172,7 +178,7 @@ def test_non_finite_state_is_reported_and_the_system_recovers(native, path):
             a.run(10)
         else:
             a.run_state_arrays(10, *bad)
-    assert err.value.code == _abi.ERR_NONFINITE
+    assert err.value.code == (_abi.ERR_NONFINITE if kind == "nan" else _abi.ERR_BAD_INDEX)
     assert a.timestep == 5
     if path == "run":
         a.push_state_arrays(*good)
