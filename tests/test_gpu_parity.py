@@ -257,4 +257,52 @@ def test_dropin_full_nlist_and_bonds(native, oracle):
                                  ptr(bad), ptr(hd_d), ptr(force), ptr(torque), None, None, None),
                "pair_forces")
     assert L.oxg_context_status(ctx, 1) == _abi.ERR_BAD_INDEX
+    # empty calls (no particles, no terms, no bonds) return at once and leave the
+    # outputs as they were
+    force.fill_(7.0)
+    energy = torch.full((6,), 7.0, dtype=torch.float64, device=dev)
+    for N_, mask in ((0, 0x3f), (n, 0)):
+        _abi.check(L.oxg_pair_forces(ctx, mask, N_, ptr(pos_d), ptr(quat_d), ptr(ch_d), box,
+                                     ptr(nn_d), ptr(fl_d), ptr(hd_d), ptr(force), ptr(torque),
+                                     None, ptr(energy), None), "pair_forces (empty)")
+    _abi.check(L.oxg_bonded_forces(ctx, n, ptr(pos_d), ptr(quat_d), box, 0, ptr(bonds),
+                                   ptr(force), ptr(torque), None, ptr(split), None), "bonded (empty)")
+    torch.cuda.synchronize()
+    assert (force == 7.0).all() and (energy == 7.0).all()
+    # a ragged list: every other particle keeps its neighbours (HOOMD's head offsets
+    # unchanged, so the used runs are not contiguous), the rest have none; the
+    # particles with neighbours get the oracle's full-list excluded-volume forces, the
+    # others nothing
+    keep = np.arange(n) % 2 == 0
+    nn_r = np.where(keep, nn, 0).astype(np.int64)
+    nn_rd = torch.tensor(nn_r, device=dev).to(torch.int32)
+    force = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    torque = torch.zeros((n, 4), dtype=torch.float32, device=dev)
+    energy = torch.zeros(6, dtype=torch.float64, device=dev)
+    _abi.check(L.oxg_pair_forces(ctx, 1, n, ptr(pos_d), ptr(quat_d), ptr(ch_d), box, ptr(nn_rd),
+                                 ptr(fl_d), ptr(hd_d), ptr(force), ptr(torque), None, ptr(energy),
+                                 None), "pair_forces (ragged)")
+    _abi.check(L.oxg_context_status(ctx, 1), "status")
+    Fo = np.zeros((n, 3))
+    To = np.zeros((n, 3))
+    Eo = 0.0
+    f = pair[0]
+    for i in np.nonzero(keep)[0]:
+        for j in flat[head[i]:head[i] + nn[i]]:
+            d = g["pos"][i] - g["pos"][j]
+            d -= g["box"] * np.round(d / g["box"])
+            key = (io.DNA_BASES[g["typeid"][i]], io.DNA_BASES[g["typeid"][j]])
+            p = _abi.FROM_DICT[0](f.params[key])
+            ok, fi, e, ti, _ = oracle.eval_pair(oracle.oracle_lib(), "oxo", 0, p, d, g["quat"][i],
+                                                g["quat"][j], f.rcut_for(*key) ** 2,
+                                                g["charge"][i], g["charge"][j])
+            Fo[i] += fi
+            To[i] += ti
+            Eo += 0.5 * e
+    assert np.abs(Fo).max() > 0
+    Fg = force.cpu().numpy()
+    assert maxrel(Fg[:, :3], Fo) < TOL_GPU
+    assert maxrel(torque.cpu().numpy()[:, :3], To) < TOL_GPU
+    assert not Fg[~keep].any()
+    assert abs(energy[0].item() - Eo) <= TOL_GPU * max(abs(Eo), 1e-6)
     L.oxg_destroy(ctx)
