@@ -57,7 +57,7 @@ class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region: one
     `nvidia-smi -lms 200` process, started before the region and read by a thread.
     __enter__ returns once its first sample is in, so the process start (which takes the
-    host and the driver for a while, longer than a 20-step timed region) stays outside
+    host and the NVIDIA kernel driver for a while, longer than a 20-step timed region) stays outside
     the region and only the periodic queries of the running process overlap it. The
     summary covers the samples taken from just before the region to its end."""
 
