@@ -482,8 +482,17 @@ class Simulation:
         float32 (N, 4) array (the engine reads and writes 16 * N bytes at each). Reading
         an array's address through numpy costs ~2 µs, a sizeable part of a one-step call,
         so the addresses of the last arrays seen are kept (with a reference to each
-        array, so that an address is never taken for another array's)."""
+        array, so that an address is never taken for another array's). A call with the
+        same five arrays as the last one, for the same N, takes their addresses without
+        checking them again (~0.2 against ~2.4 µs): the references kept make numpy refuse
+        to resize them, so each still spans the 16 * N bytes it was checked to span."""
         n = self._snap.particles.N
+        last = self.__dict__.get("_last_state")
+        if last is not None and last[0] == n:
+            p = last[1]
+            if (arrays[0] is p[0] and arrays[1] is p[1] and arrays[2] is p[2] and arrays[3] is p[3]
+                    and arrays[4] is p[4]):
+                return last[2]
         cache = self.__dict__.setdefault("_addr_cache", {})
         out = []
         for a in arrays:
@@ -501,6 +510,8 @@ class Simulation:
                 hit = (a, a.__array_interface__["data"][0])
                 cache[id(a)] = hit
             out.append(hit[1])
+        if len(arrays) == 5 and all(a is not None for a in arrays):
+            self.__dict__["_last_state"] = (n, tuple(arrays), out)
         return out
 
     def push_state_arrays(self, pos_type, pos_lo, quat, vel, angmom):

@@ -243,3 +243,24 @@ def test_state_arrays_are_checked_before_the_engine_sees_them(fake):
             with pytest.raises(ValueError):
                 call(bad, *good[1:])
         assert len(fake.calls) == n0
+
+
+def test_repeated_state_arrays_skip_the_checks_but_not_other_arrays(fake):
+    """Calls with the same five arrays as the last call take the kept addresses without
+    checking the arrays again; any other array is checked (and its address taken), and
+    numpy refuses to resize an array whose address is kept."""
+    sim, forces, lang = _sim()
+    sim.run(1)
+    n = sim.state.get_snapshot().particles.N
+    good = [np.zeros((n, 4), np.float32) for _ in range(5)]
+    first = sim._host_state_ptrs(good)
+    again = sim._host_state_ptrs(good)
+    assert again == first == [a.ctypes.data for a in good]
+    sim.run_state_arrays(1, *good)
+    with pytest.raises(ValueError):
+        good[0].resize((n + 1, 4))
+    other = np.zeros((n, 4), np.float32)
+    assert sim._host_state_ptrs([other] + good[1:]) == [other.ctypes.data] + first[1:]
+    with pytest.raises(ValueError):
+        sim._host_state_ptrs([np.zeros((n, 3), np.float32)] + good[1:])
+    assert sim._host_state_ptrs(good) == first
