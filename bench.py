@@ -25,7 +25,7 @@ import json
 import os
 import subprocess
 import sys
-import threading
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -55,11 +55,15 @@ def _peaks():
 
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region: one
-    `nvidia-smi -lms 200` process, started before the region and read by a thread.
-    __enter__ returns once its first sample is in, so the process start (which takes the
-    host and the NVIDIA kernel driver for a while, longer than a 20-step timed region) stays outside
-    the region and only the periodic queries of the running process overlap it. The
-    summary covers the samples taken from just before the region to its end."""
+    `nvidia-smi -lms 200` process, started before the region, writing its samples (each
+    with nvidia-smi's own timestamp) to a temporary file that is read after the region.
+    The bench runs no reader thread during the region, so a timed call never waits for
+    the interpreter lock on its return. __enter__ returns as soon as the second sample is
+    in: the process start (which takes the host and the NVIDIA kernel driver for a while,
+    longer than a 20-step timed region) and the catch-up query that can follow a slow
+    first one stay outside the region, which starts a whole period before the next
+    query. The summary covers the samples taken from just before the region to its end,
+    with their times relative to its start."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -68,31 +72,48 @@ class ClockSampler:
     def __init__(self, gpu=0):
         self.gpu = gpu
         self.rows = []  # (time, fields)
-        self._first = threading.Event()
         self._proc = None
-        self._t = None
+        self._path = None
         self._t0 = self._t1 = None
 
-    def _reader(self):
+    @staticmethod
+    def parse(line):
+        """(seconds since the epoch, the FIELDS values) of one output line, whose first
+        value is nvidia-smi's local timestamp 'YYYY/MM/DD HH:MM:SS.mmm'; None if the line
+        is incomplete. A timestamp that does not parse gives time None."""
+        f = [x.strip() for x in line.strip().split(",")]
+        if len(f) < 6:
+            return None
         try:
-            for line in self._proc.stdout:
-                f = [x.strip() for x in line.strip().split(",")]
-                if len(f) >= 5:
-                    self.rows.append((time.time(), f))
-                    self._first.set()
-        except Exception:
-            pass
-        self._first.set()
+            day, frac = (f[0].split(".") + ["0"])[:2]
+            t = time.mktime(time.strptime(day, "%Y/%m/%d %H:%M:%S")) + float("0." + frac)
+        except (ValueError, OverflowError):
+            t = None
+        return t, f[1:]
+
+    def _lines(self):
+        try:
+            with open(self._path) as fh:
+                return fh.read().split("\n")
+        except (OSError, TypeError):
+            return []
 
     def __enter__(self):
         try:
-            self._proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self._t = threading.Thread(target=self._reader, daemon=True)
-            self._t.start()
-            self._first.wait(timeout=15)
+            fd, self._path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+            with os.fdopen(fd, "w") as out:
+                self._proc = subprocess.Popen(
+                    ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=timestamp," + self.FIELDS,
+                     "--format=csv,noheader,nounits", "-lms", "200"],
+                    stdout=out, stderr=subprocess.DEVNULL)
+            # a busy wait: a host core that slept through it would run the first timed
+            # call at its idle clock (a call right after a 200-ms sleep took ~25 µs longer)
+            deadline = time.time() + 15
+            polls = 0
+            while time.time() < deadline and self._proc.poll() is None:
+                polls += 1
+                if polls % 1000 == 0 and len(self._lines()) > 2:  # two complete lines
+                    break
         except Exception:
             self._proc = None
         self._t0 = time.time()
@@ -106,7 +127,15 @@ class ClockSampler:
                 self._proc.wait(timeout=5)
             except Exception:
                 self._proc.kill()
-            self._t.join(timeout=5)
+        for line in self._lines():
+            r = self.parse(line)
+            if r is not None:
+                self.rows.append((self._t0 if r[0] is None else r[0], r[1]))
+        if self._path:
+            try:
+                os.unlink(self._path)
+            except OSError:
+                pass
 
     def _window(self):
         if self._t0 is None:
@@ -124,9 +153,15 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4)
                           if len(r) > 5 + k and r[5 + k].lower().startswith("active")})
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows)}
+        out = {"sm_mhz": float(np.median(sm)) if sm else None,
+               "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+               "samples": len(rows)}
+        if self._t0 is not None:
+            lo = [t for t, _ in self.rows if t < self._t0][-1:]
+            inside = [t for t, _ in self.rows if self._t0 <= t <= (self._t1 or self._t0)]
+            out["sample_ms_from_start"] = [round((t - self._t0) * 1e3, 1) for t in lo + inside]
+            out["region_ms"] = round(((self._t1 or self._t0) - self._t0) * 1e3, 1)
+        return out
 
 
 class nvtx:
@@ -164,28 +199,61 @@ def make_sim(sysarr, fused=False, seed=1, stream=None):
     return sim, forces
 
 
+class no_gc:
+    """The interpreter's cyclic garbage collector off inside a timed loop (as timeit
+    does), so no collection pause lands in a timed call."""
+
+    def __enter__(self):
+        import gc
+        self._was = gc.isenabled()
+        gc.disable()
+
+    def __exit__(self, *a):
+        import gc
+        if self._was:
+            gc.enable()
+
+
+_FLUSH = []
+
+
+def l2_flush_buffer(stream):
+    """The 256 MB buffer whose write flushes L2 between timed blocks, allocated and
+    written once beforehand, so that neither the allocation nor the first load of the
+    fill kernel falls into a timed region."""
+    import torch
+    if not _FLUSH:
+        buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        with torch.cuda.stream(stream):
+            buf.fill_(-1.0)
+        torch.cuda.synchronize()
+        _FLUSH.append(buf)
+    return _FLUSH[0]
+
+
 def time_resident(sim, steps, warmup, stream, block=1000):
     """K steps in blocks of `block` (one run() call each, as a HOOMD user would call
     sim.run), each timed with CUDA events on the engine stream; L2 is flushed (256 MB
     write) before every block, outside the timed events."""
     import torch
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    flush = l2_flush_buffer(stream)
     sim.run(warmup)
     torch.cuda.synchronize()
     total_ms = 0.0
     done = 0
-    while done < steps:
-        n = min(block, steps - done)
-        with torch.cuda.stream(stream):
-            flush.fill_(float(done))
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        sim.run(n)
-        b.record(stream)
-        b.synchronize()
-        total_ms += a.elapsed_time(b)
-        done += n
+    with no_gc():
+        while done < steps:
+            n = min(block, steps - done)
+            with torch.cuda.stream(stream):
+                flush.fill_(float(done))
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sim.run(n)
+            b.record(stream)
+            b.synchronize()
+            total_ms += a.elapsed_time(b)
+            done += n
     return total_ms
 
 
@@ -687,9 +755,11 @@ def run_ours(args):
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
-    sim.run(args.warmup)
-    sim.run_kernel_timing(reset=True)
+    l2_flush_buffer(stream)
     with ClockSampler(local) as clk:
+        # the W warm-up steps directly before the timed block, after the sampler's wait
+        sim.run(args.warmup)
+        sim.run_kernel_timing(reset=True)
         with nvtx("timed"):
             ms = time_resident(sim, args.steps, 0, stream)
     k_ms, k_launches, k_steps = sim.run_kernel_timing(reset=True)
@@ -774,11 +844,12 @@ def run_ours(args):
             sim.run_state_arrays(1, hp, hl, hq, hv, ha)
         sim.set_host_session(session_us)  # (ends the warm-up's resident kernel)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            # H2D: this step's inputs, one MD step, D2H: this step's result, in one call
-            sim.run_state_arrays(1, hp, hl, hq, hv, ha)
-        sim.set_host_session(0)
+        with no_gc():
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                # H2D: this step's inputs, one MD step, D2H: this step's result, in one call
+                sim.run_state_arrays(1, hp, hl, hq, hv, ha)
+            sim.set_host_session(0)
         torch.cuda.synchronize()
         return replicas.max_over_ranks(time.perf_counter() - t0, dist)
 
@@ -786,12 +857,13 @@ def run_ours(args):
     e2e_launch_s = e2e_loop(0)
     # the same through three calls (state push, run, state pull)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        sim.push_state_arrays(hp, hl, hq, hv, ha)
-        sim.run(1)
-        sim.pull_state_arrays(hp, hl, hq, hv, ha)
-    torch.cuda.synchronize()
+    with no_gc():
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            sim.push_state_arrays(hp, hl, hq, hv, ha)
+            sim.run(1)
+            sim.pull_state_arrays(hp, hl, hq, hv, ha)
+        torch.cuda.synchronize()
     e2e3_s = replicas.max_over_ranks(time.perf_counter() - t0, dist)
     e2e = {"value": world * e2e_steps / e2e_s, "unit": "steps/s",
            "h2d_bytes_per_step": 5 * 16 * n, "d2h_bytes_per_step": 5 * 16 * n,

@@ -83,3 +83,27 @@ def test_clock_sampler_summarises_the_timed_window():
     none = bench.ClockSampler(0)
     none._t0, none._t1 = 1.0, 2.0
     assert none.summary()["reasons"] == ["unsampled"]
+
+
+def test_clock_sampler_reads_its_file_after_the_region():
+    """The sampler's output lines (nvidia-smi's local timestamp first) parse into the
+    sample time and the clock fields; an incomplete line is skipped and a timestamp that
+    does not parse gives no time. Where nvidia-smi cannot be started, the region still
+    runs and the record says 'unsampled'."""
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    t, f = bench.ClockSampler.parse("2026/12/04 23:01:02.250, 0, 2070, 2070, 901.5, 0x0000000000000000, "
+                                    "Not Active, Not Active, Not Active, Not Active\n")
+    assert abs(t - (time.mktime(time.strptime("2026/12/04 23:01:02", "%Y/%m/%d %H:%M:%S")) + 0.25)) < 1e-9
+    assert f[:3] == ["0", "2070", "2070"] and len(f) == 9
+    assert bench.ClockSampler.parse("2026/12/04 23:01:02.250, 0, 20") is None
+    assert bench.ClockSampler.parse("garbled, 0, 2070, 2070, 900, 0x0, Active")[0] is None
+    env_path = os.environ.get("PATH", "")
+    os.environ["PATH"] = ""
+    try:
+        with bench.ClockSampler(0) as c:
+            pass
+    finally:
+        os.environ["PATH"] = env_path
+    assert c.summary()["reasons"] == ["unsampled"]
