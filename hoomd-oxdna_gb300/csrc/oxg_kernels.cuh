@@ -1966,6 +1966,7 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
     __syncthreads();
     for (;;) {  // one run per pass
         bool spec_used = false;  // the run start took the first step one in its own pass
+        uint32_t spec_rebuild = 0u;  // then: body 0's rebuild request, read by the run start
         bool completed = false;  // the run's last body ran to its end
         bad_type = false;
         // the RNG step of body b is step0 + b + 1 (block 0 advances st->step to match); the
@@ -2077,8 +2078,15 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                 if (__syncthreads_or(far) && threadIdx.x == 0) atomicOr(&st->moved, 1u);
                 if (from_host && __syncthreads_or(diff) && threadIdx.x == 0) atomicOr(&st->changed, 1u);
                 if (!grid_barrier(a.bar)) break;  // the counters above are reset for every block
+                // the words the run start's pass left, read together (one L2 round trip, not
+                // one after another): whether the host state differed, the first step one's
+                // displacement test and the rebuild request body 0 would read (nothing writes
+                // either of the last two between this barrier and body 0's force barrier)
+                const uint32_t v_changed = from_host ? ld_volatile(&st->changed) : 0u;
+                const uint32_t v_sfar = spec ? ld_volatile(&st->spec_far) : 0u;
+                const uint32_t v_rebuild = spec ? ld_volatile(&st->rebuild) : 0u;
                 if (from_host) {
-                    reuse = cmd.reuse_ok != 0 && ld_volatile(&st->changed) == 0u;  // the same in every block
+                    reuse = cmd.reuse_ok != 0 && v_changed == 0u;  // the same in every block
                     if (!reuse) {
                         for (int i = gthread; i < a.g.N; i += nthreads) {
                             if (spec) {  // undo the first step one: the state from the checkpoint
@@ -2095,18 +2103,19 @@ __global__ void __launch_bounds__(kRunThreads, OXG_RUN_BLOCKS_PER_SM) k_run(RunA
                     }
                 }
                 if (spec && reuse) {
-                    // the first step one is done: its forces (body 0) come next; its
-                    // displacement test is read there from spec_far
+                    // the first step one is done: its forces (body 0) come next; body 0
+                    // takes its rebuild request from the words read above
                     if (__syncthreads_or(sbad) && threadIdx.x == 0) atomicOr(&st->flags, kStNonFinite);
                     spec_used = true;
+                    spec_rebuild = v_rebuild | v_sfar;
                     continue;
                 }
                 rebuild = !reuse && (cmd.rebuild0 != 0u || ld_volatile(&st->moved) != 0u);
             } else {
                 // rebuild requests: body 0 reads the one left by the run start or the previous
                 // launch, body b > 0 the one the step phase of body b - 1 left in rb[b & 1]
-                rebuild = ld_volatile(body == 0 ? &st->rebuild : &st->rb[body & 1]) != 0u;
-                if (body == 0 && spec_used) rebuild = rebuild || ld_volatile(&st->spec_far) != 0u;
+                if (body == 0 && spec_used) rebuild = spec_rebuild != 0u;
+                else rebuild = ld_volatile(body == 0 ? &st->rebuild : &st->rb[body & 1]) != 0u;
             }
             if (rebuild) {
                 const uint32_t par = ld_volatile(&st->gen) & 1u;
